@@ -1,0 +1,154 @@
+"""TEST INFRASTRUCTURE: Python access to the CPU oracles.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may use
+this package, and only as the checker (or the timed CPU baseline); the
+product never imports it.
+
+Libraries (built by oracle/Makefile):
+  port         _build/liboracle.so          project C restatement, parity math
+  port_native  _build/liboracle_native.so   same, glibc float math
+  ref          _ref/libref_rjmcmc.so        the reference sampler, parity math
+  ref_native   _ref/libref_rjmcmc_native.so the reference sampler, glibc math
+The `ref` variants exist only where the reference tree could be compiled.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from bamf_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.environ.get("BAMF_REFERENCE_DIR", "/root/reference")
+PATHS = {
+    "port": os.path.join(HERE, "_build", "liboracle.so"),
+    "port_native": os.path.join(HERE, "_build", "liboracle_native.so"),
+    "ref": os.path.join(HERE, "_ref", "libref_rjmcmc.so"),
+    "ref_native": os.path.join(HERE, "_ref", "libref_rjmcmc_native.so"),
+}
+PREFIX = {"port": "oracle", "port_native": "oracle", "ref": "ref", "ref_native": "ref"}
+_libs: dict = {}
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the port (always) and the reference oracle (when its sources exist)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref is None:
+        ref = os.path.isfile(os.path.join(REF_DIR, "source", "c", "LibRJMCMC.cpp"))
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={REF_DIR}"], check=True)
+
+
+def available(kind: str) -> bool:
+    return os.path.exists(PATHS[kind])
+
+
+def load(kind: str = "port") -> C.CDLL:
+    if kind in _libs:
+        return _libs[kind]
+    if not os.path.exists(PATHS[kind]):
+        if kind.startswith("port"):
+            build(ref=False)
+        else:
+            raise FileNotFoundError(f"{PATHS[kind]} not built (reference sources unavailable)")
+    L = C.CDLL(PATHS[kind])
+    p = PREFIX[kind]
+    pf = C.POINTER(C.c_float)
+    run = getattr(L, f"{p}_rjmcmc_run")
+    run.restype = C.c_void_p
+    run.argtypes = [pf, C.c_int, C.c_int, C.POINTER(abi.Emitters), C.POINTER(abi.McmcParams),
+                    pf, C.c_int, pf, C.c_int, pf, C.c_int, pf, C.POINTER(abi.Rng)]
+    getattr(L, f"{p}_result_sizes").argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
+    getattr(L, f"{p}_result_chain").argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.Chain)]
+    getattr(L, f"{p}_result_grids").argtypes = [C.c_void_p, pf, pf]
+    getattr(L, f"{p}_result_counters").argtypes = [C.c_void_p, C.POINTER(abi.Counters)]
+    getattr(L, f"{p}_result_free").argtypes = [C.c_void_p]
+    if kind.startswith("port"):
+        pi = C.POINTER(C.c_int32)
+        L.oracle_rjmcmc_batch.argtypes = [
+            pf, C.POINTER(C.c_int64), pi, pi, C.c_int, C.POINTER(abi.McmcParams),
+            pf, C.c_int, pf, C.c_int, pf, C.c_int, C.c_float, C.c_uint32, C.c_int, pi, pi, pi]
+        L.oracle_findroi_filter.argtypes = [pf, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                            C.c_int, C.c_float, pf, C.c_int]
+        L.oracle_gaussmle_xynb.argtypes = [pf, C.c_int, C.c_int, C.c_float, C.c_int, pf, pf, pf,
+                                           C.c_int]
+        pd = C.POINTER(C.c_double)
+        L.oracle_gaussmle_xynb_f64.argtypes = [pf, C.c_int, C.c_int, C.c_double, C.c_int, pd, pd,
+                                               pd, C.c_int]
+    _libs[kind] = L
+    return L
+
+
+def run_chain(kind: str, roi: np.ndarray, params: abi.McmcParams, off: np.ndarray,
+              sig: np.ndarray, back: np.ndarray, e0=None, rng=(0, 0, 0),
+              scmos: np.ndarray | None = None) -> dict:
+    """One cRJMCMC run on a (Ysize, Xsize) ROI; returns the raw outputs.
+
+    e0 = (I, X, Y, BG) or None for the empty start of rjmcmc.m (BG taken
+    from the offset prior's maximum by the caller)."""
+    L = load(kind)
+    p = PREFIX[kind]
+    ysize, xsize = roi.shape
+    data = np.ascontiguousarray(roi.ravel(order="F"), dtype=np.float32)
+    if e0 is None:
+        e0 = ([], [], [], 0.0)
+    I, X, Y, BG = e0
+    em, keep = abi.make_emitters(len(I), I, X, Y, BG)
+    off = np.ascontiguousarray(off, np.float32)
+    sig = np.ascontiguousarray(sig, np.float32)
+    back = np.ascontiguousarray(back, np.float32)
+    sc = None if scmos is None else np.ascontiguousarray(np.asarray(scmos).ravel(order="F"),
+                                                         np.float32)
+    r = abi.Rng(*rng)
+    h = getattr(L, f"{p}_rjmcmc_run")(abi.fptr(data), xsize, ysize, C.byref(em), C.byref(params),
+                                      abi.fptr(off), off.size, abi.fptr(sig), sig.size,
+                                      abi.fptr(back), back.size,
+                                      abi.fptr(sc) if sc is not None else None, C.byref(r))
+    if not h:
+        raise ValueError("oracle rejected the arguments")
+    try:
+        sizes = (C.c_int64 * 7)()
+        getattr(L, f"{p}_result_sizes")(h, sizes)
+        out = {"uniforms_used": int(sizes[5]), "messages": int(sizes[6])}
+        for w, name in ((0, "chain"), (1, "chain_test")):
+            ne, nr = int(sizes[2 * w]), int(sizes[2 * w + 1])
+            ch, arrs = abi.alloc_chain(ne, nr)
+            abi.check(getattr(L, f"{p}_result_chain")(h, w, C.byref(ch)), "result_chain")
+            out[name] = abi.chain_to_dict(ch, arrs)
+        g = int(sizes[4])
+        pg = np.zeros(g, np.float32)
+        pb = np.zeros(g, np.float32)
+        getattr(L, f"{p}_result_grids")(h, abi.fptr(pg), abi.fptr(pb))
+        Z = params.Grid_Zoom
+        out["pgrid"] = pg.reshape(xsize * Z, ysize * Z).T.copy()
+        out["pback"] = pb.reshape(xsize * Z, ysize * Z).T.copy()
+        c = abi.Counters()
+        getattr(L, f"{p}_result_counters")(h, C.byref(c))
+        out["counters"] = c.as_dict()
+    finally:
+        getattr(L, f"{p}_result_free")(h)
+    return out
+
+
+def run_batch(batch, params: abi.McmcParams, off, sig, back, bg0: float, seed: int,
+              threads: int = 1, kind: str = "port_native") -> dict:
+    """Per-ROI summaries (final N, MAP N, accepted moves) on host threads."""
+    L = load(kind)
+    n = batch.n
+    fn = np.zeros(n, np.int32)
+    mn = np.zeros(n, np.int32)
+    na = np.zeros(n, np.int32)
+    off = np.ascontiguousarray(off, np.float32)
+    sig = np.ascontiguousarray(sig, np.float32)
+    back = np.ascontiguousarray(back, np.float32)
+    pi = C.POINTER(C.c_int32)
+    abi.check(L.oracle_rjmcmc_batch(
+        abi.fptr(batch.data), batch.offsets.ctypes.data_as(C.POINTER(C.c_int64)),
+        batch.xsize.ctypes.data_as(pi), batch.ysize.ctypes.data_as(pi), n, C.byref(params),
+        abi.fptr(off), off.size, abi.fptr(sig), sig.size, abi.fptr(back), back.size,
+        float(bg0), int(seed), int(threads), fn.ctypes.data_as(pi), mn.ctypes.data_as(pi),
+        na.ctypes.data_as(pi)), "oracle_rjmcmc_batch")
+    return {"final_n": fn, "map_n": mn, "n_accepted": na}
