@@ -1,0 +1,568 @@
+/*
+ * api_sampler.cu - host side of the sampler C ABI (include/bamf.h): prior
+ * tables, device buffers, launches, the MAP-count reduction.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bamf.h"
+#include "sampler_common.h"
+
+namespace bamf {
+cudaError_t launch_rjmcmc_exact(const SamplerConsts &K, const SamplerBatch &B, int side_max,
+                                int blocks, int warps_per_block, cudaStream_t stream);
+cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, int side_max,
+                               int blocks, int warps_per_block, cudaStream_t stream);
+int blocks_per_sm_exact(int side_max, int warps_per_block);
+int blocks_per_sm_fast(int side_max, int warps_per_block);
+}  // namespace bamf
+
+using namespace bamf;
+
+static thread_local std::string g_last_error;
+
+static bamf_status cuda_fail(cudaError_t e, const char *where)
+{
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    return BAMF_ERR_CUDA;
+}
+
+#define CU(call)                                                     \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);          \
+    } while (0)
+
+extern "C" const char *bamf_version(void) { return "bamf_gb300 0.1.0 (sm_103a)"; }
+
+extern "C" int bamf_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+extern "C" const char *bamf_last_error(void) { return g_last_error.c_str(); }
+
+/* ------------------------------------------------------------ prior tables */
+/* The reference's Stat construction (LibRJMCMC.cpp:176-217) in float, plus
+ * the checks the device lookups rely on: the grid and the unique CDF must be
+ * strictly increasing (binary search stands in for the linear scans). */
+struct HostStat {
+    std::vector<float> x, pdf, ux, uc;
+};
+
+static bamf_status build_stat(const float *in, int L, float DX, HostStat &s)
+{
+    if (!in || L < 1) return BAMF_ERR_INVALID_ARG;
+    if (!(DX > 0.0f)) return BAMF_ERR_BAD_PRIOR;
+    for (int i = 0; i < L; ++i)
+        if (!(in[i] >= 0.0f) || std::isinf(in[i])) return BAMF_ERR_BAD_PRIOR;
+    std::vector<float> cdf(L), xm(L);
+    s.x.assign(L, 0.0f);
+    s.pdf.assign(in, in + L);
+    cdf[0] = 0.0f;
+    xm[0] = 0.0f;
+    for (int i = 1; i < L; ++i) {
+        cdf[i] = cdf[i - 1] + (s.pdf[i] + s.pdf[i - 1]) * DX / 2.0f;
+        if (cdf[i] > 1.0f) cdf[i] = 1.0f;
+        xm[i] = cdf[i];
+        s.x[i] = s.x[i - 1] + DX;
+        if (!(s.x[i] > s.x[i - 1])) return BAMF_ERR_BAD_PRIOR;
+    }
+    for (int i = L - 2; i >= 0; --i)
+        if (cdf[i] == cdf[i + 1]) xm[i + 1] = -1.0f;
+    s.ux.clear();
+    s.uc.clear();
+    for (int i = 0; i < L; ++i)
+        if (xm[i] != -1.0f) {
+            s.ux.push_back(s.x[i]);
+            s.uc.push_back(cdf[i]);
+        }
+    if (s.uc.back() != 1.0f) s.uc.back() = 1.0f;
+    if (s.uc[0] != 0.0f) s.uc[0] = 0.0f;
+    for (size_t i = 1; i < s.uc.size(); ++i)
+        if (!(s.uc[i] > s.uc[i - 1])) return BAMF_ERR_BAD_PRIOR;
+    return BAMF_OK;
+}
+
+static void cumulative(const float *P, float *PV)
+{
+    for (int ii = 0; ii < 8; ii++) {
+        float t = 0.0f;
+        for (int mm = 0; mm <= ii; mm++) t = t + P[mm];
+        PV[ii] = t;
+    }
+}
+
+/* ---------------------------------------------------------------- workspace */
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    bamf_status ensure(size_t bytes)
+    {
+        if (bytes <= n) return BAMF_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t b = std::max<size_t>(bytes, 256);
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+        n = b;
+        return BAMF_OK;
+    }
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
+struct bamf_workspace {
+    DevBuf tables;   /* the three prior tables                       */
+    DevBuf queue;    /* work-queue counter                             */
+    DevBuf trace;    /* per-ROI Signal==1 count per chain entry        */
+    DevBuf entries;  /* per-ROI entry count when the caller wants none */
+    DevBuf order;    /* ROI ids largest first                           */
+    DevBuf hostin;   /* staging for the host entry point                */
+};
+
+extern "C" bamf_status bamf_workspace_create(bamf_workspace **ws)
+{
+    if (!ws) return BAMF_ERR_INVALID_ARG;
+    *ws = new bamf_workspace();
+    return BAMF_OK;
+}
+
+extern "C" void bamf_workspace_destroy(bamf_workspace *ws) { delete ws; }
+
+/* Copies the three tables into one device buffer and fills the DevStats. */
+static bamf_status upload_tables(bamf_workspace *ws, const HostStat st[3], DevStat out[3],
+                                 cudaStream_t s)
+{
+    size_t total = 0;
+    for (int k = 0; k < 3; ++k)
+        total += st[k].x.size() * 2 + st[k].ux.size() * 2;
+    bamf_status r = ws->tables.ensure(total * sizeof(float));
+    if (r) return r;
+    std::vector<float> h;
+    h.reserve(total);
+    size_t off[3][4];
+    for (int k = 0; k < 3; ++k) {
+        off[k][0] = h.size(); h.insert(h.end(), st[k].x.begin(), st[k].x.end());
+        off[k][1] = h.size(); h.insert(h.end(), st[k].pdf.begin(), st[k].pdf.end());
+        off[k][2] = h.size(); h.insert(h.end(), st[k].ux.begin(), st[k].ux.end());
+        off[k][3] = h.size(); h.insert(h.end(), st[k].uc.begin(), st[k].uc.end());
+    }
+    /* synchronous: h is a temporary */
+    CU(cudaMemcpyAsync(ws->tables.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    CU(cudaStreamSynchronize(s));
+    float *base = (float *)ws->tables.p;
+    for (int k = 0; k < 3; ++k) {
+        out[k].x = base + off[k][0];
+        out[k].pdf = base + off[k][1];
+        out[k].ux = base + off[k][2];
+        out[k].uc = base + off[k][3];
+        out[k].L = (int)st[k].x.size();
+        out[k].nu = (int)st[k].ux.size();
+    }
+    return BAMF_OK;
+}
+
+static bamf_status make_consts(bamf_workspace *ws, const bamf_mcmc_params *p,
+                               const bamf_priors *pri, uint32_t seed, float bg0,
+                               SamplerConsts &K, cudaStream_t s)
+{
+    if (!p || !pri) return BAMF_ERR_INVALID_ARG;
+    if (p->N_Burnin < 0 || p->N_Trials < 0 || p->Grid_Zoom < 0) return BAMF_ERR_INVALID_ARG;
+    HostStat st[3];
+    bamf_status r;
+    if ((r = build_stat(pri->offset_pdf, pri->offset_len, p->DX, st[0]))) return r;
+    if ((r = build_stat(pri->signal_pdf, pri->signal_len, p->DX, st[1]))) return r;
+    if ((r = build_stat(pri->back_pdf, pri->back_len, p->DX, st[2]))) return r;
+    DevStat ds[3];
+    if ((r = upload_tables(ws, st, ds, s))) return r;
+    std::memset(&K, 0, sizeof K);
+    K.p = *p;
+    cumulative(p->P_Burnin, K.PVB);
+    cumulative(p->P_Trials, K.PVT);
+    K.off = ds[0];
+    K.sig = ds[1];
+    K.back = ds[2];
+    K.seed = seed;
+    K.bg0 = bg0;
+    return BAMF_OK;
+}
+
+static int sm_count()
+{
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+/* Launch the chains of batch B as a persistent grid: as many CTAs as fit
+ * on the GPU at once (or fewer for small batches); warps pull ROI ids from
+ * the work queue until it runs dry. */
+static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, SamplerBatch B,
+                                int arith, cudaStream_t s)
+{
+    bamf_status r;
+    if ((r = ws->queue.ensure(sizeof(int32_t)))) return r;
+    B.queue = (int32_t *)ws->queue.p;
+    CU(cudaMemsetAsync(ws->queue.p, 0, sizeof(int32_t), s));
+    bool exact = arith == BAMF_ARITH_EXACT;
+    int wpb = 4;
+    int per_sm = exact ? blocks_per_sm_exact(B.side_max, wpb) : blocks_per_sm_fast(B.side_max, wpb);
+    if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
+    int need = (B.n_rois + wpb - 1) / wpb;
+    int blocks = std::min(need, per_sm * sm_count());
+    if (blocks < 1) return BAMF_OK;
+    cudaError_t e = exact ? launch_rjmcmc_exact(K, B, B.side_max, blocks, wpb, s)
+                          : launch_rjmcmc_fast(K, B, B.side_max, blocks, wpb, s);
+    if (e != cudaSuccess) return cuda_fail(e, "rjmcmc kernel launch");
+    return BAMF_OK;
+}
+
+/* MAP emitter count per ROI (findMap.m:29-45): the MEX output drops the
+ * last chain entry (cRJMCMC.cpp:174), so Iter = entries - 1; the mode of the
+ * Signal==1 count over entries round(Iter/2)..Iter (1-based), smallest on
+ * ties.  One warp per ROI. */
+__global__ void map_n_kernel(const uint8_t *__restrict__ trace, int trace_cap,
+                             const int32_t *__restrict__ n_entries, int n_rois,
+                             int32_t *__restrict__ map_n)
+{
+    __shared__ int hist[8][BAMF_NMAX + 1];
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int roi = blockIdx.x * 8 + warp;
+    for (int k = lane; k <= BAMF_NMAX; k += 32) hist[warp][k] = 0;
+    __syncwarp();
+    if (roi >= n_rois) return;
+    int iter = min(n_entries[roi], trace_cap) - 1;
+    if (iter < 1) {
+        if (lane == 0) map_n[roi] = 0;
+        return;
+    }
+    int start = (iter + 1) / 2;
+    const uint8_t *t = trace + (int64_t)roi * trace_cap;
+    for (int k = start + lane; k <= iter; k += 32) atomicAdd(&hist[warp][min((int)t[k - 1], BAMF_NMAX)], 1);
+    __syncwarp();
+    if (lane == 0) {
+        int best = 0;
+        for (int v = 1; v <= BAMF_NMAX; ++v)
+            if (hist[warp][v] > hist[warp][best]) best = v;
+        map_n[roi] = best;
+    }
+}
+
+/* Counting sort of ROI ids by side, largest first (one block): the longest
+ * chains start first so the persistent warps finish together. */
+__global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__restrict__ ys,
+                            int n, int32_t *__restrict__ order)
+{
+    __shared__ int cnt[BAMF_MAX_ROI_SIDE + 2];
+    __shared__ int pos[BAMF_MAX_ROI_SIDE + 2];
+    for (int k = threadIdx.x; k < BAMF_MAX_ROI_SIDE + 2; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int s = min(max(max(xs[i], ys[i]), 0), BAMF_MAX_ROI_SIDE + 1);
+        atomicAdd(&cnt[s], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int s = BAMF_MAX_ROI_SIDE + 1; s >= 0; --s) {
+            pos[s] = acc;
+            acc += cnt[s];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int s = min(max(max(xs[i], ys[i]), 0), BAMF_MAX_ROI_SIDE + 1);
+        order[atomicAdd(&pos[s], 1)] = i;
+    }
+}
+
+extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_roi_batch *rois,
+                                                const bamf_mcmc_params *p,
+                                                const bamf_priors *priors, uint32_t seed,
+                                                int arith, const bamf_batch_results *out,
+                                                void *stream)
+{
+    if (!ws || !rois || !p || !priors || !out) return BAMF_ERR_INVALID_ARG;
+    if (arith != BAMF_ARITH_EXACT && arith != BAMF_ARITH_FAST) return BAMF_ERR_INVALID_ARG;
+    if (rois->n_rois < 0) return BAMF_ERR_INVALID_ARG;
+    if (rois->n_rois == 0) return BAMF_OK;
+    if (!rois->data || !rois->offsets || !rois->xsize || !rois->ysize) return BAMF_ERR_INVALID_ARG;
+    if ((rois->init_n != nullptr) != (rois->init_ixy != nullptr)) return BAMF_ERR_INVALID_ARG;
+    int side_max = rois->side_max > 0 ? rois->side_max : BAMF_MAX_ROI_SIDE;
+    if (side_max > BAMF_MAX_ROI_SIDE) return BAMF_ERR_TOO_LARGE;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    cudaStream_t s = (cudaStream_t)stream;
+    SamplerConsts K;
+    bamf_status r = make_consts(ws, p, priors, seed, rois->bg0, K, s);
+    if (r) return r;
+    int n = rois->n_rois;
+    int64_t steps = (int64_t)p->N_Burnin + p->N_Trials;
+    int trace_cap = (int)std::min<int64_t>(steps, INT32_MAX);
+    SamplerBatch B;
+    std::memset(&B, 0, sizeof B);
+    B.n_rois = n;
+    B.side_max = side_max;
+    B.data = rois->data;
+    B.offsets = rois->offsets;
+    B.xsize = rois->xsize;
+    B.ysize = rois->ysize;
+    B.psf_sigma = rois->psf_sigma;
+    B.scmos = rois->scmos;
+    B.init_n = rois->init_n;
+    B.init_bg = rois->init_bg;
+    B.init_ixy = rois->init_ixy;
+    B.final_n = out->final_n;
+    B.final_state = out->final_state;
+    B.counters = out->counters;
+    B.status = out->status;
+    B.overflow = out->overflow;
+    if ((r = ws->order.ensure((size_t)n * sizeof(int32_t)))) return r;
+    B.order = (int32_t *)ws->order.p;
+    order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)ws->order.p);
+    CU(cudaGetLastError());
+    if (out->map_n) {
+        if ((r = ws->trace.ensure((size_t)n * trace_cap))) return r;
+        B.nsig_trace = (uint8_t *)ws->trace.p;
+        B.trace_cap = trace_cap;
+    }
+    int32_t *entries = out->n_entries;
+    if (!entries && out->map_n) {
+        if ((r = ws->entries.ensure((size_t)n * sizeof(int32_t)))) return r;
+        entries = (int32_t *)ws->entries.p;
+    }
+    B.n_entries = entries;
+    if ((r = launch_batch(ws, K, B, arith, s))) return r;
+    if (out->map_n) {
+        map_n_kernel<<<(n + 7) / 8, 256, 0, s>>>(B.nsig_trace, trace_cap, entries, n, out->map_n);
+        CU(cudaGetLastError());
+    }
+    return BAMF_OK;
+}
+
+/* ------------------------------------------------------- host entry points */
+template <typename T>
+static bamf_status dalloc(std::vector<void *> &owned, T **p, size_t count)
+{
+    *p = nullptr;
+    if (count == 0) return BAMF_OK;
+    cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    owned.push_back(*p);
+    return BAMF_OK;
+}
+
+struct Owned {
+    std::vector<void *> v;
+    ~Owned()
+    {
+        for (void *p : v) cudaFree(p);
+    }
+};
+
+template <typename T>
+static bamf_status upload(Owned &o, T **dst, const T *src, size_t count)
+{
+    *dst = nullptr;
+    if (!src || count == 0) return BAMF_OK;
+    bamf_status r = dalloc(o.v, dst, count);
+    if (r) return r;
+    CU(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+    return BAMF_OK;
+}
+
+template <typename T>
+static bamf_status download(T *dst, const T *src, size_t count)
+{
+    if (!dst || !src || count == 0) return BAMF_OK;
+    CU(cudaMemcpy(dst, src, count * sizeof(T), cudaMemcpyDeviceToHost));
+    return BAMF_OK;
+}
+
+extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi_batch *rois,
+                                              const bamf_mcmc_params *p,
+                                              const bamf_priors *priors, uint32_t seed,
+                                              int arith, const bamf_batch_results *out)
+{
+    if (!ws || !rois || !p || !priors || !out) return BAMF_ERR_INVALID_ARG;
+    int n = rois->n_rois;
+    if (n < 0) return BAMF_ERR_INVALID_ARG;
+    if (n == 0) return BAMF_OK;
+    if (!rois->data || !rois->offsets || !rois->xsize || !rois->ysize) return BAMF_ERR_INVALID_ARG;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    int64_t npix = 0;
+    int side_max = 0;
+    for (int k = 0; k < n; ++k) {
+        if (rois->xsize[k] < 1 || rois->ysize[k] < 1 || rois->offsets[k] < 0) return BAMF_ERR_INVALID_ARG;
+        npix = std::max<int64_t>(npix, rois->offsets[k] + (int64_t)rois->xsize[k] * rois->ysize[k]);
+        side_max = std::max(side_max, (int)std::max(rois->xsize[k], rois->ysize[k]));
+    }
+    if (side_max > BAMF_MAX_ROI_SIDE) return BAMF_ERR_TOO_LARGE;
+    Owned o;
+    bamf_roi_batch d = *rois;
+    d.side_max = side_max;
+    bamf_status r;
+    if ((r = upload(o, (float **)&d.data, rois->data, (size_t)npix))) return r;
+    if ((r = upload(o, (int64_t **)&d.offsets, rois->offsets, (size_t)n))) return r;
+    if ((r = upload(o, (int32_t **)&d.xsize, rois->xsize, (size_t)n))) return r;
+    if ((r = upload(o, (int32_t **)&d.ysize, rois->ysize, (size_t)n))) return r;
+    if ((r = upload(o, (float **)&d.psf_sigma, rois->psf_sigma, (size_t)n))) return r;
+    if ((r = upload(o, (float **)&d.scmos, rois->scmos, (size_t)npix))) return r;
+    if ((r = upload(o, (int32_t **)&d.init_n, rois->init_n, (size_t)n))) return r;
+    if ((r = upload(o, (float **)&d.init_bg, rois->init_bg, (size_t)n))) return r;
+    if ((r = upload(o, (float **)&d.init_ixy, rois->init_ixy, (size_t)n * 3 * BAMF_NMAX))) return r;
+    bamf_batch_results dout;
+    std::memset(&dout, 0, sizeof dout);
+    const size_t fs = 4 + 4 * BAMF_NMAX;
+    if (out->map_n && (r = dalloc(o.v, &dout.map_n, n))) return r;
+    if (out->final_n && (r = dalloc(o.v, &dout.final_n, n))) return r;
+    if (out->final_state && (r = dalloc(o.v, &dout.final_state, n * fs))) return r;
+    if (out->counters && (r = dalloc(o.v, &dout.counters, (size_t)n * 30))) return r;
+    if (out->n_entries && (r = dalloc(o.v, &dout.n_entries, n))) return r;
+    if (out->status && (r = dalloc(o.v, &dout.status, n))) return r;
+    if (out->overflow && (r = dalloc(o.v, &dout.overflow, n))) return r;
+    if ((r = bamf_rjmcmc_batch_device(ws, &d, p, priors, seed, arith, &dout, nullptr))) return r;
+    CU(cudaDeviceSynchronize());
+    if ((r = download(out->map_n, dout.map_n, n))) return r;
+    if ((r = download(out->final_n, dout.final_n, n))) return r;
+    if ((r = download(out->final_state, dout.final_state, n * fs))) return r;
+    if ((r = download(out->counters, dout.counters, (size_t)n * 30))) return r;
+    if ((r = download(out->n_entries, dout.n_entries, n))) return r;
+    if ((r = download(out->status, dout.status, n))) return r;
+    if ((r = download(out->overflow, dout.overflow, n))) return r;
+    return BAMF_OK;
+}
+
+extern "C" bamf_status bamf_crjmcmc_host(const float *data, int xsize, int ysize,
+                                         const bamf_emitters *e0, const bamf_mcmc_params *p,
+                                         const float *off, int off_len, const float *sig,
+                                         int sig_len, const float *back, int back_len,
+                                         const float *scmos, const bamf_rng *rng, int arith,
+                                         float *pgrid, float *pback, bamf_chain *chain,
+                                         bamf_chain *chain_test, bamf_counters *counters)
+{
+    if (!data || !e0 || !p || !off || !sig || !back || !rng) return BAMF_ERR_INVALID_ARG;
+    if (xsize < 1 || ysize < 1 || off_len < 1 || sig_len < 1 || back_len < 1) return BAMF_ERR_INVALID_ARG;
+    if (arith != BAMF_ARITH_EXACT && arith != BAMF_ARITH_FAST) return BAMF_ERR_INVALID_ARG;
+    if ((pgrid == nullptr) != (pback == nullptr)) return BAMF_ERR_INVALID_ARG;
+    if ((chain == nullptr) != (chain_test == nullptr)) return BAMF_ERR_INVALID_ARG;
+    if (e0->N < 0 || (e0->N > 0 && (!e0->I || !e0->X || !e0->Y))) return BAMF_ERR_INVALID_ARG;
+    if (xsize > BAMF_MAX_ROI_SIDE || ysize > BAMF_MAX_ROI_SIDE || e0->N > BAMF_NMAX) return BAMF_ERR_TOO_LARGE;
+    if (p->N_Burnin < 0 || p->N_Trials < 0 || p->Grid_Zoom < 0) return BAMF_ERR_INVALID_ARG;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+
+    bamf_workspace ws;
+    bamf_priors pri = {off, off_len, sig, sig_len, back, back_len};
+    SamplerConsts K;
+    bamf_status r = make_consts(&ws, p, &pri, rng->seed, e0->BG, K, nullptr);
+    if (r) return r;
+    Owned o;
+    int npix = xsize * ysize;
+    SamplerBatch B;
+    std::memset(&B, 0, sizeof B);
+    B.n_rois = 1;
+    B.side_max = std::max(xsize, ysize);
+    int64_t zero = 0;
+    int32_t xs = xsize, ys = ysize;
+    if ((r = upload(o, (float **)&B.data, data, (size_t)npix))) return r;
+    if ((r = upload(o, (int64_t **)&B.offsets, &zero, 1))) return r;
+    if ((r = upload(o, (int32_t **)&B.xsize, &xs, 1))) return r;
+    if ((r = upload(o, (int32_t **)&B.ysize, &ys, 1))) return r;
+    if ((r = upload(o, (float **)&B.scmos, scmos, (size_t)npix))) return r;
+    std::vector<float> ixy(3 * BAMF_NMAX, 0.0f);
+    for (int k = 0; k < e0->N; ++k) {
+        ixy[k] = e0->I[k];
+        ixy[BAMF_NMAX + k] = e0->X[k];
+        ixy[2 * BAMF_NMAX + k] = e0->Y[k];
+    }
+    int32_t n0 = e0->N;
+    float bg = e0->BG;
+    if ((r = upload(o, (int32_t **)&B.init_n, &n0, 1))) return r;
+    if ((r = upload(o, (float **)&B.init_bg, &bg, 1))) return r;
+    if ((r = upload(o, (float **)&B.init_ixy, ixy.data(), ixy.size()))) return r;
+    uint32_t cid = rng->chain_id, roff = rng->offset;
+    if ((r = upload(o, (uint32_t **)&B.chain_ids, &cid, 1))) return r;
+    if ((r = upload(o, (uint32_t **)&B.rng_offset, &roff, 1))) return r;
+    int32_t *d_counters = nullptr, *d_status = nullptr, *d_entries = nullptr;
+    if ((r = dalloc(o.v, &d_counters, 30))) return r;
+    if ((r = dalloc(o.v, &d_status, 1))) return r;
+    if ((r = dalloc(o.v, &d_entries, 1))) return r;
+    B.counters = d_counters;
+    B.status = d_status;
+    B.n_entries = d_entries;
+    size_t gsz = (size_t)npix * p->Grid_Zoom * p->Grid_Zoom;
+    if (pgrid) {
+        if ((r = dalloc(o.v, &B.pgrid, gsz))) return r;
+        if ((r = dalloc(o.v, &B.pback, gsz))) return r;
+        CU(cudaMemset(B.pgrid, 0, gsz * sizeof(float)));
+        CU(cudaMemset(B.pback, 0, gsz * sizeof(float)));
+        B.grid_stride = (int64_t)gsz;
+    }
+    bamf_chain dch[2];
+    bamf_chain *hch[2] = {chain, chain_test};
+    if (chain) {
+        for (int w = 0; w < 2; ++w) {
+            bamf_chain &c = dch[w];
+            std::memset(&c, 0, sizeof c);
+            c.capacity_entries = hch[w]->capacity_entries;
+            c.capacity_records = hch[w]->capacity_records;
+            size_t ce = (size_t)std::max(c.capacity_entries, 1), cr = (size_t)std::max(c.capacity_records, 1);
+            if ((r = dalloc(o.v, &c.N, ce)) || (r = dalloc(o.v, &c.LLR, ce)) || (r = dalloc(o.v, &c.PR, ce)) ||
+                (r = dalloc(o.v, &c.JumpType, ce)) || (r = dalloc(o.v, &c.Accepted, ce)) ||
+                (r = dalloc(o.v, &c.BG, ce)) || (r = dalloc(o.v, &c.ABG, ce)) || (r = dalloc(o.v, &c.BBG, ce)) ||
+                (r = dalloc(o.v, &c.Index, cr)) || (r = dalloc(o.v, &c.Photons, cr)) || (r = dalloc(o.v, &c.X, cr)) ||
+                (r = dalloc(o.v, &c.Y, cr)) || (r = dalloc(o.v, &c.Signal, cr)))
+                return r;
+        }
+        bamf_chain *dchains = nullptr;
+        if ((r = upload(o, &dchains, dch, 2))) return r;
+        B.chains = dchains;
+    }
+    if ((r = launch_batch(&ws, K, B, arith, nullptr))) return r;
+    CU(cudaDeviceSynchronize());
+    int32_t st = 0, ne = 0;
+    if ((r = download(&st, d_status, 1))) return r;
+    if (st != BAMF_OK) return st;
+    if ((r = download(&ne, d_entries, 1))) return r;
+    if (counters) {
+        if ((r = download((int32_t *)counters, d_counters, 30))) return r;
+    }
+    if (pgrid) {
+        if ((r = download(pgrid, B.pgrid, gsz))) return r;
+        if ((r = download(pback, B.pback, gsz))) return r;
+    }
+    if (chain) {
+        bamf_chain got[2];
+        CU(cudaMemcpy(got, B.chains, sizeof got, cudaMemcpyDeviceToHost));
+        for (int w = 0; w < 2; ++w) {
+            bamf_chain *h = hch[w];
+            if (ne > h->capacity_entries || got[w].n_records > h->capacity_records) return BAMF_ERR_CAPACITY;
+            size_t e = (size_t)ne, rc = (size_t)got[w].n_records;
+            if ((r = download(h->N, dch[w].N, e)) || (r = download(h->LLR, dch[w].LLR, e)) ||
+                (r = download(h->PR, dch[w].PR, e)) || (r = download(h->JumpType, dch[w].JumpType, e)) ||
+                (r = download(h->Accepted, dch[w].Accepted, e)) || (r = download(h->BG, dch[w].BG, e)) ||
+                (r = download(h->ABG, dch[w].ABG, e)) || (r = download(h->BBG, dch[w].BBG, e)) ||
+                (r = download(h->Index, dch[w].Index, rc)) || (r = download(h->Photons, dch[w].Photons, rc)) ||
+                (r = download(h->X, dch[w].X, rc)) || (r = download(h->Y, dch[w].Y, rc)) ||
+                (r = download(h->Signal, dch[w].Signal, rc)))
+                return r;
+            h->n_entries = ne;
+            h->n_records = got[w].n_records;
+        }
+    }
+    return BAMF_OK;
+}

@@ -1,0 +1,73 @@
+/*
+ * sampler_common.h - device-side data layout shared by the sampler kernels
+ * and their host launcher.
+ */
+#ifndef BAMF_SAMPLER_COMMON_H
+#define BAMF_SAMPLER_COMMON_H
+
+#include <stdint.h>
+
+#include "bamf.h"
+
+namespace bamf {
+
+/* A prior table after the reference's Stat construction
+ * (source/c/LibRJMCMC.cpp:176-217): grid x[L] and pdf[L] for findPDF,
+ * unique CDF uc[nu] and its grid ux[nu] for genRand. */
+struct DevStat {
+    const float *x;
+    const float *pdf;
+    const float *ux;
+    const float *uc;
+    int L;
+    int nu;
+};
+
+/* Everything uniform over a batch of chains. */
+struct SamplerConsts {
+    bamf_mcmc_params p;
+    float PVB[8];   /* cumulative P_Burnin (cRJMCMC.cpp:37-47) */
+    float PVT[8];   /* cumulative P_Trials                      */
+    DevStat off, sig, back;
+    uint32_t seed;
+    float bg0;      /* starting BG when no per-ROI start state is given */
+};
+
+/* Per-ROI inputs and outputs of a batch.  Arrays indexed by ROI id. */
+struct SamplerBatch {
+    int n_rois;
+    int side_max;                 /* max(xsize, ysize) over the batch      */
+    const float *data;            /* ROI pixels, column-major, y fastest   */
+    const int64_t *offsets;       /* pixel offset of each ROI in data      */
+    const int32_t *xsize;
+    const int32_t *ysize;
+    const float *psf_sigma;       /* per-ROI sigma, or null: p.PSFsigma    */
+    const float *scmos;           /* same layout as data, or null: zeros   */
+    const int32_t *order;         /* work-queue order (ROI ids), or null   */
+    /* optional start states: n, then BG, then I/X/Y rows of BAMF_NMAX */
+    const int32_t *init_n;
+    const float *init_bg;
+    const float *init_ixy;        /* [roi][3][BAMF_NMAX]                   */
+    const uint32_t *chain_ids;    /* Philox chain id per ROI, or null: id  */
+    const uint32_t *rng_offset;   /* first stream index per ROI, or null   */
+    /* outputs (any may be null) */
+    int32_t *final_n;             /* [roi]                                 */
+    float *final_state;           /* [roi][4 + 4*BAMF_NMAX]: BG ABG BBG -, I[], X[], Y[], S[] */
+    int32_t *counters;            /* [roi][30] bamf_counters order          */
+    uint8_t *nsig_trace;          /* [roi][trace_cap] Signal==1 count per entry */
+    int32_t trace_cap;
+    int32_t *n_entries;           /* [roi] recorded chain entries          */
+    uint32_t *uniforms_used;      /* [roi]                                 */
+    int32_t *status;              /* [roi] 0 ok, else BAMF_ERR_*           */
+    int32_t *overflow;            /* [roi] proposals rejected at BAMF_NMAX */
+    float *pgrid;                 /* [roi][grid_stride] or null            */
+    float *pback;
+    int64_t grid_stride;
+    /* full chain recording (exact cRJMCMC outputs), or null */
+    bamf_chain *chains;           /* device array [roi][2] of bamf_chain with device pointers */
+    int32_t *queue;               /* work-queue counter (device int)       */
+};
+
+}  // namespace bamf
+
+#endif

@@ -1,0 +1,1259 @@
+/*
+ * sampler_kernel.cuh - the batched RJMCMC sampler (cRJMCMC's algorithm,
+ * source/c/LibRJMCMC.cpp) as a persistent CUDA kernel for sm_103a.
+ *
+ * Layout of the work:
+ *   - one warp runs one ROI chain from burn-in to the last trial, then pulls
+ *     the next ROI id from a device work queue (atomic counter);
+ *   - lane j holds emitter slot j (I, X, Y, Signal) of the current state A
+ *     and of the proposed state T in registers (BAMF_NMAX = 32 slots), so
+ *     emitter edits are register moves and neighbour searches are ballots;
+ *   - the ROI pixels D, the current model M, the proposed model Mt and the
+ *     per-pixel work buffer live in shared memory; pixel p = y + x*Ysize is
+ *     handled by lane p mod 32;
+ *   - the scalar move logic (proposal, priors, Hastings ratio, accept) runs
+ *     warp-uniformly: every lane evaluates it on the same values, so no
+ *     broadcasts are needed and the warp never diverges there;
+ *   - uniforms come from the chain's Philox stream (include/bamf_philox.h):
+ *     each lane generates one 4-word block, 32 blocks = 128 uniforms per
+ *     refill, and a draw is one shuffle.
+ *
+ * Two instantiations (template parameter EXACT):
+ *   EXACT = true  (sampler_exact.cu, built with -fmad=false): the reference's
+ *     float operation order, parity erf/log/exp, full model rebuild per
+ *     proposal and serial pixel sums, so the chain is the reference chain
+ *     bit for bit given the same uniforms.
+ *   EXACT = false (sampler_fast.cu): hardware math, incremental model
+ *     updates (only changed emitters' stencils are evaluated), cached
+ *     log-model and warp-tree reductions; same moves and acceptance rule.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bamf.h"
+#include "bamf_parity_math.h"
+#include "bamf_philox.h"
+#include "sampler_common.h"
+
+namespace bamf {
+
+#define BAMF_FULL 0xffffffffu
+
+/* counter slots, in bamf_counters order */
+enum {
+    C_N_jump, C_N_split, C_N_merge, C_N_birth, C_N_death,
+    C_A_jump, C_A_split, C_A_merge, C_A_birth, C_A_death,
+    C_N_jumpFg, C_N_splitFg, C_N_mergeFg, C_N_birthFg, C_N_deathFg,
+    C_A_jumpFg, C_A_splitFg, C_A_mergeFg, C_A_birthFg, C_A_deathFg,
+    C_N_jumpBg, C_N_splitBg, C_N_mergeBg, C_N_birthBg, C_N_deathBg,
+    C_A_jumpBg, C_A_splitBg, C_A_mergeBg, C_A_birthBg, C_A_deathBg,
+    C_COUNT
+};
+
+template <bool EXACT>
+struct SMath;
+
+template <>
+struct SMath<true> {
+    static __device__ __forceinline__ float erf_(float x) { return bamf_pm_erff(x); }
+    static __device__ __forceinline__ float log_(float x) { return bamf_pm_logf(x); }
+    static __device__ __forceinline__ float exp_(float x) { return bamf_pm_expf(x); }
+    static __device__ __forceinline__ float powf_(float x, float y) { return bamf_pm_powf(x, y); }
+};
+
+template <>
+struct SMath<false> {
+    static __device__ __forceinline__ float erf_(float x) { return erff(x); }
+    static __device__ __forceinline__ float log_(float x) { return __logf(x); }
+    static __device__ __forceinline__ float exp_(float x) { return __expf(x); }
+    static __device__ __forceinline__ float powf_(float x, float y) { return powf(x, y); }
+};
+
+/* Per-warp shared-memory carve-out, in floats: D, M, Mt, E, sCMOS,
+ * stencils NX/NY of the proposal, counters, pick list; fast mode adds A's
+ * stencil cache NXa/NYa and log2 M. */
+__host__ __device__ inline int warp_smem_floats(int side_max, bool exact)
+{
+    int npix = side_max * side_max;
+    int base = 5 * npix + 2 * BAMF_NMAX * side_max + C_COUNT + BAMF_NMAX + 2;
+    return exact ? base : base + 2 * BAMF_NMAX * side_max + npix;
+}
+
+/* double helpers that nvcc may not contract */
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+
+template <bool EXACT>
+struct ChainWarp {
+    typedef SMath<EXACT> MT;
+    const SamplerConsts *K;
+    const SamplerBatch *B;
+    int lane;
+    int roi;
+    /* geometry */
+    int X, Y, npix;
+    float sigma, Cst, MeanN;
+    /* shared memory */
+    float *D, *M, *Mt, *E, *scm, *NX, *NY, *NXa, *NYa, *logM;
+    int *cnt, *cl;
+    int rec_n[2];
+    /* current state A (lane j = slot j) */
+    int an;
+    float aI, aX, aY;
+    int aS;
+    float aBG, aABG, aBBG;
+    /* proposed state T */
+    int tn;
+    float tI, tX, tY;
+    int tS;
+    float tBG, tABG, tBBG;
+    bool t_overflow;
+    /* uniform stream */
+    uint32_t seed, chain, idx, base;
+    uint32_t r0, r1, r2, r3;
+    /* phase */
+    int is_burnin;
+    float P[8];
+    int entries;
+    int overflow;
+    /* incremental-model bookkeeping (fast mode) */
+    uint32_t a_dirty, t_dirty;
+    int removed;
+
+    /* ---------------------------------------------------------- RNG */
+    __device__ __forceinline__ void refill()
+    {
+        bamf_philox_block b = bamf_philox4x32_10(base + (uint32_t)lane, 0u, 0u, 0u, seed, chain);
+        r0 = b.v[0]; r1 = b.v[1]; r2 = b.v[2]; r3 = b.v[3];
+    }
+    __device__ __forceinline__ float urand()
+    {
+        uint32_t blk = idx >> 2;
+        if (blk - base >= 32u) {
+            base = blk;
+            refill();
+        }
+        uint32_t c = idx & 3u;
+        uint32_t v = c == 0 ? r0 : (c == 1 ? r1 : (c == 2 ? r2 : r3));
+        v = __shfl_sync(BAMF_FULL, v, (int)(blk - base));
+        idx++;
+        return bamf_u31_to_float(v >> 1);
+    }
+    /* Irwin-Hall sum of 12 uniforms (LibRJMCMCreturn.hpp:23-26). */
+    __device__ __forceinline__ float randn()
+    {
+        float t = 0;
+        for (int k = 0; k < 12; ++k) t = t + urand();
+        return t - 6.0f;
+    }
+
+    /* ------------------------------------------------------ lane access */
+    __device__ __forceinline__ float A_I(int k) const { return __shfl_sync(BAMF_FULL, aI, k); }
+    __device__ __forceinline__ float A_X(int k) const { return __shfl_sync(BAMF_FULL, aX, k); }
+    __device__ __forceinline__ float A_Y(int k) const { return __shfl_sync(BAMF_FULL, aY, k); }
+    __device__ __forceinline__ int A_S(int k) const { return __shfl_sync(BAMF_FULL, aS, k); }
+    __device__ __forceinline__ float T_I(int k) const { return __shfl_sync(BAMF_FULL, tI, k); }
+    __device__ __forceinline__ int T_S(int k) const { return __shfl_sync(BAMF_FULL, tS, k); }
+
+    __device__ __forceinline__ void setT(int k, float I, float x, float y)
+    {
+        if (lane == k) {
+            tI = I;
+            tX = x;
+            tY = y;
+        }
+        if (!EXACT) t_dirty |= 1u << k;
+    }
+    __device__ __forceinline__ void addT(float I, float x, float y, int s)
+    {
+        if (tn >= BAMF_NMAX) {
+            t_overflow = true;
+            return;
+        }
+        if (lane == tn) {
+            tI = I;
+            tX = x;
+            tY = y;
+            tS = s;
+        }
+        if (!EXACT) t_dirty |= 1u << tn;
+        tn++;
+    }
+    /* Emitters::remove (LibRJMCMC.cpp:478-490) */
+    __device__ __forceinline__ void removeT(int id)
+    {
+        float vI = __shfl_down_sync(BAMF_FULL, tI, 1);
+        float vX = __shfl_down_sync(BAMF_FULL, tX, 1);
+        float vY = __shfl_down_sync(BAMF_FULL, tY, 1);
+        int vS = __shfl_down_sync(BAMF_FULL, tS, 1);
+        if (lane >= id) {
+            tI = vI; tX = vX; tY = vY; tS = vS;
+        }
+        if (!EXACT) {
+            uint32_t lo = t_dirty & ((1u << id) - 1u);
+            uint32_t hi = id < 31 ? (t_dirty >> (id + 1)) << id : 0u;
+            t_dirty = lo | hi;
+            removed = id;
+        }
+        tn--;
+    }
+    __device__ __forceinline__ void copyA2T()
+    {
+        tn = an; tI = aI; tX = aX; tY = aY; tS = aS;
+        tBG = aBG; tABG = aABG; tBBG = aBBG;
+        t_overflow = false;
+        if (!EXACT) {
+            a_dirty = 0u;
+            t_dirty = 0u;
+            removed = -1;
+        }
+    }
+    __device__ __forceinline__ void cinc(int k)
+    {
+        if (lane == 0) cnt[k]++;
+    }
+
+    /* Emitters::test (:492-514) with Bnd_out cast to int. */
+    __device__ __forceinline__ bool testT() const
+    {
+        int bnd = (int)K->p.Bnd_out;
+        bool bad = false;
+        if (lane < tn)
+            bad = (tI < 0.0f) || (tX < (float)(-bnd)) || (tY < (float)(-bnd)) ||
+                  (tX > (float)(X + bnd)) || (tY > (float)(Y + bnd));
+        return !__any_sync(BAMF_FULL, bad);
+    }
+
+    __device__ __forceinline__ float nsignalA() const
+    {
+        return (float)__popc(__ballot_sync(BAMF_FULL, lane < an && aS == 1));
+    }
+
+    /* ---------------------------------------------------- prior tables */
+    /* Stat::findPDF (:219-246): first grid node strictly above I. */
+    __device__ float findPDF(const DevStat &s, float I) const
+    {
+        const float *x = s.x;
+        float xl = __ldg(&x[s.L - 1]);
+        if (I >= xl || I <= 0.0f || I != I) return 0.0f;
+        int lo = 0, hi = s.L - 1;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (__ldg(&x[mid]) > I) hi = mid; else lo = mid;
+        }
+        int j = hi;
+        float xj = __ldg(&x[j]), xj1 = __ldg(&x[j - 1]);
+        return (__ldg(&s.pdf[j]) * (I - xj1) + __ldg(&s.pdf[j - 1]) * (xj - I)) /
+               (__ldg(&x[1]) - __ldg(&x[0]));
+    }
+    /* Stat::genRand (:248-282). */
+    __device__ float genRand(const DevStat &s)
+    {
+        float R = urand();
+        if (R <= 0.0f) return 0.0f;
+        if (R >= 1.0f) return __ldg(&s.ux[s.nu - 1]);
+        if (s.nu < 2) return 0.0f;
+        int lo = 0, hi = s.nu - 1;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (__ldg(&s.uc[mid]) > R) hi = mid; else lo = mid;
+        }
+        int si = hi;
+        float uc1 = __ldg(&s.uc[si]), uc0 = __ldg(&s.uc[si - 1]);
+        return (__ldg(&s.ux[si - 1]) * (uc1 - R) + __ldg(&s.ux[si]) * (R - uc0)) / (uc1 - uc0);
+    }
+    __device__ __forceinline__ float sob(int signal, float I) const
+    {
+        return signal == 1 ? findPDF(K->sig, I) : findPDF(K->back, I);
+    }
+    /* normpdf (LibRJMCMCreturn.hpp:19-21); sq2pi = (float)sqrt(2.0f*pi). */
+    __device__ __forceinline__ float normpdf(float x, float u, float s) const
+    {
+        const float sq2pi = (float)sqrt(2.0 * 3.141592);
+        float d = x - u;
+        return 1.0f / (sq2pi * s) * MT::exp_(-d * d / (2.0f * s * s));
+    }
+
+    /* ------------------------------------------------ neighbour search */
+    __device__ __forceinline__ uint32_t near_mask(int jj, float dmin) const
+    {
+        float xj = A_X(jj), yj = A_Y(jj);
+        bool in = false;
+        if (lane < an && lane != jj) {
+            float dx = aX - xj, dy = aY - yj;
+            float d = (float)sqrt(dadd(dmul((double)dx, (double)dx), dmul((double)dy, (double)dy)));
+            in = d < dmin;
+        }
+        return __ballot_sync(BAMF_FULL, in);
+    }
+    static __device__ __forceinline__ int nth_bit(uint32_t m, int q)
+    {
+        for (int t = 0; t < q; ++t) m &= m - 1u;
+        return __ffs(m) - 1;
+    }
+    /* Emitters::closest (:525-558). */
+    __device__ int closest(int jj, float dmin)
+    {
+        uint32_t m = near_mask(jj, dmin);
+        int num = __popc(m);
+        if (num > 0) {
+            float Ua = urand();
+            int mm = min((int)(Ua * (float)num), num - 1);
+            return nth_bit(m, mm);
+        }
+        uint32_t others = (an >= 32 ? BAMF_FULL : ((1u << an) - 1u)) & ~(1u << jj);
+        float Ua = urand();
+        int mm = min((int)(Ua * (float)(an - 1)), an - 2);
+        return nth_bit(others, mm);
+    }
+    /* Emitters::closestMulti (:615-650); picks go to cl[] in pick order. */
+    __device__ int closestMulti(int jj, float dmin)
+    {
+        uint32_t m = near_mask(jj, dmin);
+        int num = __popc(m);
+        int np = 0;
+        if (num > 0) {
+            float Ua = urand();
+            int Np;
+            if (Ua < 1.0f / (float)num) Np = num;
+            else Np = min((int)(Ua * (float)num), num - 1);
+            for (int n = 0; n < Np; ++n) {
+                Ua = urand();
+                int q = min((int)(Ua * (float)(num - n)), num - n - 1);
+                int b = nth_bit(m, q);
+                m &= ~(1u << b);
+                if (lane == 0) cl[np] = b;
+                np++;
+            }
+        }
+        __syncwarp();
+        return np;
+    }
+
+    /* ------------------------------------------------------------ model */
+    /* Stencil + Model (:15-59) of a lane-distributed state, into out[]. */
+    __device__ void model_full(int n, float I, float Xv, float Yv, float BG, float ABG, float BBG,
+                               float *out, float *nx, float *ny)
+    {
+        int totx = n * X, toty = n * Y;
+        for (int b0 = 0; b0 < totx; b0 += 32) {
+            int item = b0 + lane;
+            int k = min(item / X, n - 1);
+            int x = item - k * X;
+            float Ik = __shfl_sync(BAMF_FULL, I, k);
+            float Xk = __shfl_sync(BAMF_FULL, Xv, k);
+            if (item < totx)
+                nx[k * X + x] = Ik * 0.5f * (MT::erf_(((float)x - Xk + 1.0f) * Cst) -
+                                             MT::erf_(((float)x - Xk) * Cst));
+        }
+        for (int b0 = 0; b0 < toty; b0 += 32) {
+            int item = b0 + lane;
+            int k = min(item / Y, n - 1);
+            int y = item - k * Y;
+            float Yk = __shfl_sync(BAMF_FULL, Yv, k);
+            if (item < toty)
+                ny[k * Y + y] = 0.5f * (MT::erf_(((float)y - Yk + 1.0f) * Cst) -
+                                        MT::erf_(((float)y - Yk) * Cst));
+        }
+        __syncwarp();
+        for (int p = lane; p < npix; p += 32) {
+            int x = p / Y, y = p - x * Y;
+            float m = BG + ABG * (float)x + BBG * (float)y + scm[p];
+            for (int k = 0; k < n; ++k) m += nx[k * X + x] * ny[k * Y + y];
+            out[p] = m;
+        }
+        __syncwarp();
+    }
+
+    /* Stencil rows of the dirty T slots into NX/NY (fast mode). */
+    __device__ void stencils_dirty(uint32_t mask)
+    {
+        int nd = __popc(mask);
+        int totx = nd * X, toty = nd * Y;
+        for (int b0 = 0; b0 < totx; b0 += 32) {
+            int item = b0 + lane;
+            int q = min(item / X, nd - 1);
+            int x = item - q * X;
+            int k = nth_bit(mask, q);
+            float Ik = __shfl_sync(BAMF_FULL, tI, k);
+            float Xk = __shfl_sync(BAMF_FULL, tX, k);
+            if (item < totx)
+                NX[k * X + x] = Ik * 0.5f * (MT::erf_(((float)x - Xk + 1.0f) * Cst) -
+                                             MT::erf_(((float)x - Xk) * Cst));
+        }
+        for (int b0 = 0; b0 < toty; b0 += 32) {
+            int item = b0 + lane;
+            int q = min(item / Y, nd - 1);
+            int y = item - q * Y;
+            int k = nth_bit(mask, q);
+            float Yk = __shfl_sync(BAMF_FULL, tY, k);
+            if (item < toty)
+                NY[k * Y + y] = 0.5f * (MT::erf_(((float)y - Yk + 1.0f) * Cst) -
+                                        MT::erf_(((float)y - Yk) * Cst));
+        }
+        __syncwarp();
+    }
+
+    /* likelihood_ratio (:1650-1686).  M always holds Model(A). */
+    __device__ float llr()
+    {
+        if (EXACT) {
+            model_full(tn, tI, tX, tY, tBG, tABG, tBBG, Mt, NX, NY);
+            for (int p = lane; p < npix; p += 32)
+                E[p] = M[p] - Mt[p] + D[p] * MT::log_(Mt[p] / M[p]);
+            __syncwarp();
+            float tmp = 0.0f;
+            if (lane == 0)
+                for (int p = 0; p < npix; ++p) tmp += E[p];
+            tmp = __shfl_sync(BAMF_FULL, tmp, 0);
+            return MT::exp_(tmp);
+        } else {
+            /* Mt = M - sum(old stencils of A's dirty/removed slots)
+             *        + sum(new stencils of T's dirty slots) + background delta */
+            stencils_dirty(t_dirty);
+            float dBG = tBG - aBG, dABG = tABG - aABG, dBBG = tBBG - aBBG;
+            uint32_t am = a_dirty, tm = t_dirty;
+            float acc = 0.0f;
+            for (int p = lane; p < npix; p += 32) {
+                int x = p / Y, y = p - x * Y;
+                float d = dBG + dABG * (float)x + dBBG * (float)y;
+                uint32_t m1 = am;
+                while (m1) {
+                    int k = __ffs(m1) - 1;
+                    m1 &= m1 - 1u;
+                    d -= NXa[k * X + x] * NYa[k * Y + y];
+                }
+                uint32_t m2 = tm;
+                while (m2) {
+                    int k = __ffs(m2) - 1;
+                    m2 &= m2 - 1u;
+                    d += NX[k * X + x] * NY[k * Y + y];
+                }
+                float mt = M[p] + d;
+                float lmt = __log2f(mt);
+                Mt[p] = mt;
+                E[p] = lmt;
+                acc += D[p] * (lmt - logM[p]) * 0.69314718f - d;
+            }
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(BAMF_FULL, acc, o);
+            return MT::exp_(acc);
+        }
+    }
+
+    /* fast mode: fold the accepted proposal into M, log2 M and the
+     * stencil cache of A */
+    __device__ void commit_fast()
+    {
+        for (int p = lane; p < npix; p += 32) {
+            M[p] = Mt[p];
+            logM[p] = E[p];
+        }
+        /* stencil cache: drop the removed slot, then take T's dirty rows */
+        if (removed >= 0) {
+            for (int k = removed; k < an - 1; ++k) {
+                for (int x = lane; x < X; x += 32) NXa[k * X + x] = NXa[(k + 1) * X + x];
+                for (int y = lane; y < Y; y += 32) NYa[k * Y + y] = NYa[(k + 1) * Y + y];
+            }
+        }
+        uint32_t m = t_dirty;
+        while (m) {
+            int k = __ffs(m) - 1;
+            m &= m - 1u;
+            for (int x = lane; x < X; x += 32) NXa[k * X + x] = NX[k * X + x];
+            for (int y = lane; y < Y; y += 32) NYa[k * Y + y] = NY[k * Y + y];
+        }
+        __syncwarp();
+    }
+
+    __device__ void accept_T()
+    {
+        if (!EXACT) commit_fast();
+        an = tn; aI = tI; aX = tX; aY = tY; aS = tS;
+        aBG = tBG; aABG = tABG; aBBG = tBBG;
+        if (EXACT) {
+            float *t = M;
+            M = Mt;
+            Mt = t;
+        }
+    }
+
+    /* Full rebuild of M (and, in fast mode, log2 M and A's stencil cache). */
+    __device__ void rebuild_model()
+    {
+        if (EXACT) {
+            model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NX, NY);
+        } else {
+            model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NXa, NYa);
+            for (int p = lane; p < npix; p += 32) logM[p] = __log2f(M[p]);
+            __syncwarp();
+        }
+    }
+
+    /* ------------------------------------------------------- recording */
+    __device__ void record_one(int w, int n, float I, float x, float y, int s, float BG, float ABG,
+                               float BBG, float LLR, float PR, int type, int acc)
+    {
+        bamf_chain *ch = &B->chains[2 * roi + w];
+        int e = entries;
+        if (e >= ch->capacity_entries) return;
+        if (lane == 0) {
+            ch->N[e] = n; ch->LLR[e] = LLR; ch->PR[e] = PR; ch->JumpType[e] = type;
+            ch->Accepted[e] = acc; ch->BG[e] = BG; ch->ABG[e] = ABG; ch->BBG[e] = BBG;
+        }
+        int rc = rec_n[w];
+        int nrec = n < 1 ? 1 : n;
+        if (rc + nrec <= ch->capacity_records) {
+            if (n < 1) {
+                if (lane == 0) {
+                    ch->Index[rc] = e + 1; ch->Photons[rc] = 0.0f; ch->X[rc] = -100.0f;
+                    ch->Y[rc] = -100.0f; ch->Signal[rc] = -1;
+                }
+            } else if (lane < n) {
+                ch->Index[rc + lane] = e + 1;
+                ch->Photons[rc + lane] = I;
+                ch->X[rc + lane] = x + K->p.DriftX;
+                ch->Y[rc + lane] = y + K->p.DriftY;
+                ch->Signal[rc + lane] = s;
+            }
+        }
+        rec_n[w] = rc + nrec;
+    }
+
+    /* RJMCMCChain::addEmitters on Chain (A) and Chain_Test (T). */
+    __device__ void record2(float LLR, float PR, int type, int acc)
+    {
+        if (B->nsig_trace && entries < B->trace_cap) {
+            int ns = __popc(__ballot_sync(BAMF_FULL, lane < an && aS == 1));
+            if (lane == 0) B->nsig_trace[(int64_t)roi * B->trace_cap + entries] = (uint8_t)(an < 1 ? 0 : ns);
+        }
+        if (B->chains) {
+            record_one(0, an, aI, aX, aY, aS, aBG, aABG, aBBG, LLR, PR, type, acc);
+            record_one(1, tn, tI, tX, tY, tS, tBG, tABG, tBBG, LLR, PR, type, acc);
+        }
+        entries++;
+    }
+
+    /* RJMCMC::update_grids (:1629-1648). */
+    __device__ void update_grids()
+    {
+        if (is_burnin || !B->pgrid) return;
+        int Z = K->p.Grid_Zoom;
+        if (lane < an) {
+            int x = (int)floor(dadd((double)((float)Z * (aX + K->p.DriftX)), 0.5));
+            int y = (int)floor(dadd((double)((float)Z * (aY + K->p.DriftY)), 0.5));
+            if (x >= 0 && x < X * Z && y >= 0 && y < Y * Z && aI > K->p.Icutoff) {
+                float *g = (aS == 1 ? B->pgrid : B->pback) + (int64_t)roi * B->grid_stride;
+                atomicAdd(&g[x * Y * Z + y], 1.0f);
+            }
+        }
+    }
+
+    __device__ __forceinline__ void reject_record(int type)
+    {
+        record2(0.0f, 0.0f, type, 0);
+        update_grids();
+    }
+
+    /* ------------------------------------------------------------ moves */
+    /* RJMCMC::jump (:752-970). */
+    __device__ void mv_jump()
+    {
+        cinc(C_N_jump);
+        int type = 1;
+        float PrI = 1.0f, IPDF, IPDFtest;
+        copyA2T();
+        if (an < 1) return;
+        float Ua = urand();
+        int nn = min((int)(Ua * (float)tn), tn - 1);
+        float Ub = urand();
+        const bamf_mcmc_params &p = K->p;
+        if ((double)Ub < 0.25) {
+            type = 2;
+            tBG = tBG + p.BG_std * randn();
+            tABG = tABG + p.ABBG_std * randn();
+            tBBG = tBBG + p.ABBG_std * randn();
+        } else if ((double)Ub < 0.50 && (double)Ub >= 0.25) {
+            if (an < 2) return;
+            type = 10;
+            int Np = closestMulti(nn, 2 * sigma);
+            if (Np == 0) return;
+            float I0 = A_I(nn);
+            for (int i = 0; i < Np; ++i) I0 = I0 + A_I(cl[i]);
+            float II0 = 0, XI0 = 0, YI0 = 0, XII0 = 0, YII0 = 0;
+            for (int i = 0; i < Np; ++i) {
+                int c = cl[i];
+                float aIc = A_I(c), aXc = A_X(c), aYc = A_Y(c);
+                int aSc = A_S(c);
+                float nX, nY, nI;
+                if (aSc == 1) {
+                    nX = aXc + p.X_stdFg * randn();
+                    nY = aYc + p.X_stdFg * randn();
+                    nI = (I0 / (float)(Np + 1)) * (0.15f * randn() + 1.0f);
+                    IPDFtest = findPDF(K->sig, nI);
+                    IPDF = findPDF(K->sig, aIc);
+                } else {
+                    nX = aXc + p.X_stdBg * randn();
+                    nY = aYc + p.X_stdBg * randn();
+                    nI = (I0 / (float)(Np + 1)) * (0.15f * randn() + 1.0f);
+                    IPDFtest = findPDF(K->back, nI);
+                    IPDF = findPDF(K->back, aIc);
+                }
+                PrI = PrI * IPDFtest / IPDF;
+                setT(c, nI, nX, nY);
+                if (!EXACT) a_dirty |= 1u << c;
+                XI0 = XI0 + aIc * aXc;
+                YI0 = YI0 + aIc * aYc;
+                XII0 = XII0 + nI * nX;
+                YII0 = YII0 + nI * nY;
+                II0 = II0 + nI;
+            }
+            float aIn = A_I(nn), aXn = A_X(nn), aYn = A_Y(nn);
+            int aSn = A_S(nn);
+            float tIn = I0 - II0;
+            float tXn = (XI0 + aIn * aXn - XII0) / tIn;
+            float tYn = (YI0 + aIn * aYn - YII0) / tIn;
+            setT(nn, tIn, tXn, tYn);
+            if (!EXACT) a_dirty |= 1u << nn;
+            IPDFtest = sob(aSn, tIn);
+            IPDF = sob(aSn, aIn);
+            PrI = PrI * IPDFtest / IPDF;
+        } else if ((double)Ub >= 0.5 && (double)Ub < 0.75) {
+            type = 3;
+            int NN = closestMulti(nn, 2 * sigma);
+            if (lane == 0) cl[NN] = nn;
+            __syncwarp();
+            NN++;
+            for (int i = 0; i < NN; ++i) {
+                int c = cl[i];
+                float aIc = A_I(c);
+                int aSc = A_S(c);
+                float cI = T_I(c);
+                float cX = __shfl_sync(BAMF_FULL, tX, c), cY = __shfl_sync(BAMF_FULL, tY, c);
+                float nI, nX, nY;
+                if (aSc == 1) {
+                    cinc(C_N_jumpFg);
+                    nI = cI + p.I_stdFg * randn();
+                    nX = cX + p.X_stdFg * randn();
+                    nY = cY + p.X_stdFg * randn();
+                    IPDFtest = findPDF(K->sig, nI);
+                    IPDF = findPDF(K->sig, aIc);
+                } else {
+                    cinc(C_N_jumpBg);
+                    nI = cI + p.I_stdBg * randn();
+                    nX = cX + p.X_stdBg * randn();
+                    nY = cY + p.X_stdBg * randn();
+                    IPDFtest = findPDF(K->back, nI);
+                    IPDF = findPDF(K->back, aIc);
+                }
+                PrI = PrI * IPDFtest / IPDF;
+                setT(c, nI, nX, nY);
+                if (!EXACT) a_dirty |= 1u << c;
+            }
+        } else {
+            float aIn = A_I(nn), aXn = A_X(nn), aYn = A_Y(nn);
+            int aSn = A_S(nn);
+            float nI, nX, nY;
+            if (aSn == 1) {
+                cinc(C_N_jumpFg);
+                nI = aIn + p.I_stdFg * randn();
+                nX = aXn + p.X_stdFg * randn();
+                nY = aYn + p.X_stdFg * randn();
+                IPDFtest = findPDF(K->sig, nI);
+                IPDF = findPDF(K->sig, aIn);
+            } else {
+                cinc(C_N_jumpBg);
+                nI = aIn + p.I_stdBg * randn();
+                nX = aXn + p.X_stdBg * randn();
+                nY = aYn + p.X_stdBg * randn();
+                IPDFtest = findPDF(K->back, nI);
+                IPDF = findPDF(K->back, aIn);
+            }
+            PrI = IPDFtest / IPDF;
+            setT(nn, nI, nX, nY);
+            if (!EXACT) a_dirty |= 1u << nn;
+        }
+        if (!testT()) {
+            reject_record(type);
+            return;
+        }
+        float LLR = llr();
+        float BgPDF = findPDF(K->off, aBG);
+        float BgPDFtest = findPDF(K->off, tBG);
+        float PrBg = (BgPDFtest / BgPDF) * MT::exp_(-(tBBG * tBBG - aBBG * aBBG) / 2.0f) *
+                     MT::exp_(-(tABG * tABG - aABG * aABG) / 2.0f);
+        float PR = LLR * PrI * PrBg;
+        int accept = (urand() < PR);
+        if (accept) {
+            cinc(C_A_jump);
+            cinc(A_S(nn) == 1 ? C_A_jumpFg : C_A_jumpBg);
+            accept_T();
+        }
+        record2(LLR, PR, type, accept);
+        update_grids();
+    }
+
+    /* RJMCMC::split (:972-1109). */
+    __device__ void mv_split()
+    {
+        const int type = 4;
+        cinc(C_N_split);
+        copyA2T();
+        if (an < 1) return;
+        const bamf_mcmc_params &p = K->p;
+        float Ua = urand();
+        int jj = min((int)floorf((float)an * Ua), an - 1);
+        float Ijp = A_I(jj), mux = A_X(jj), muy = A_Y(jj);
+        int BF = A_S(jj);
+        cinc(BF == 1 ? C_N_splitFg : C_N_splitBg);
+        float u1 = urand();
+        float u2 = p.Split_std * randn();
+        float u3 = p.Split_std * randn();
+        setT(jj, u1 * Ijp, mux + u2, muy + u3);
+        if (!EXACT) a_dirty |= 1u << jj;
+        addT((1.0f - u1) * Ijp, mux - u1 * u2 / (1.0f - u1), muy - u1 * u3 / (1.0f - u1), BF);
+        if (t_overflow) {
+            overflow++;
+            reject_record(type);
+            return;
+        }
+        if (!testT()) {
+            reject_record(type);
+            return;
+        }
+        float LLR = llr();
+        float tmp1 = 1.0f, tmp2 = 1.0f;
+        tmp1 = tmp1 * sob(A_S(jj), A_I(jj));
+        tmp2 = tmp2 * sob(T_S(jj), T_I(jj));
+        tmp2 = tmp2 * sob(T_S(tn - 1), T_I(tn - 1));
+        float Norm1 = normpdf(u2, 0.0f, p.Split_std);
+        float Norm2 = normpdf(u3, 0.0f, p.Split_std);
+        float NEm = nsignalA();
+        float PrM = MeanN / (NEm + 1.0f);
+        float PrI = tmp2 / tmp1;
+        float Area = (float)(((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out));
+        float PrX = 1.0f / Area;
+        float Us = 1.0f / (Norm1 * Norm2);
+        float om = 1.0f - u1;
+        float Jacob = (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om)));
+        float PR = LLR * PrI * PrX * Us * Jacob * (P[1] / P[2]) * PrM;
+        int accept = (urand() < PR);
+        if (accept) {
+            cinc(C_A_split);
+            cinc(BF == 1 ? C_A_splitFg : C_A_splitBg);
+            accept_T();
+        }
+        record2(LLR, PR, type, accept);
+        update_grids();
+    }
+
+    /* RJMCMC::merge (:1111-1255). */
+    __device__ void mv_merge()
+    {
+        const int type = 5;
+        cinc(C_N_merge);
+        copyA2T();
+        if (an < 2) {
+            update_grids();
+            return;
+        }
+        const bamf_mcmc_params &p = K->p;
+        float Ua = urand();
+        int jj = min((int)floorf((float)an * Ua), an - 1);
+        int ii = closest(jj, 3 * sigma);
+        int aSj = A_S(jj);
+        cinc(aSj == 1 ? C_N_mergeFg : C_N_mergeBg);
+        float aIj = A_I(jj), aXj = A_X(jj), aYj = A_Y(jj);
+        float aIi = A_I(ii), aXi = A_X(ii), aYi = A_Y(ii);
+        {
+            float dx = aXj - aXi, dy = aYj - aYi;
+            float d2 = (float)dadd(dmul((double)dx, (double)dx), dmul((double)dy, (double)dy));
+            if (sqrtf(d2) > 3 * sigma) {
+                update_grids();
+                return;
+            }
+        }
+        float Ijp = aIj + aIi;
+        float muxjp = (aIj * aXj + aIi * aXi) / Ijp;
+        float muyjp = (aIj * aYj + aIi * aYi) / Ijp;
+        float u1 = aIj / Ijp;
+        float u2 = aXj - muxjp;
+        float u3 = aYj - muyjp;
+        setT(jj, Ijp, muxjp, muyjp);
+        float PDFfg = findPDF(K->sig, Ijp);
+        float PDFbg = findPDF(K->back, Ijp);
+        if (lane == jj) tS = (PDFbg > PDFfg) ? 0 : 1;
+        if (!EXACT) a_dirty |= (1u << jj) | (1u << ii);
+        removeT(ii);
+        if (!testT()) {
+            reject_record(type);
+            return;
+        }
+        float LLR = llr();
+        float tmp1 = 1.0f, tmp2 = 1.0f;
+        tmp1 = tmp1 * sob(aSj, aIj);
+        tmp1 = tmp1 * sob(A_S(ii), aIi);
+        int jt = ii > jj ? jj : jj - 1;
+        tmp2 = tmp2 * sob(T_S(jt), T_I(jt));
+        float Norm1 = normpdf(u2, 0.0f, p.Split_std);
+        float Norm2 = normpdf(u3, 0.0f, p.Split_std);
+        float NEm = nsignalA();
+        float PrI = tmp1 / tmp2;
+        float Area = (float)(((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out));
+        float PrX = 1.0f / Area;
+        float Us = 1.0f / (Norm1 * Norm2);
+        float om = 1.0f - u1;
+        float Jacob = (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om)));
+        float PrM = MeanN / NEm;
+        float PR = LLR / (PrI * PrX * Jacob * Us * PrM * P[1] / P[2]);
+        int accept = (urand() < PR);
+        if (accept) {
+            cinc(aSj == 1 ? C_A_mergeFg : C_A_mergeBg);
+            cinc(C_A_merge);
+            accept_T();
+        }
+        record2(LLR, PR, type, accept);
+        update_grids();
+    }
+
+    /* RJMCMC::find_Birth (:1688-1736); PixProb is overwritten with 1. */
+    __device__ void find_birth(float *bx, float *by)
+    {
+        float total;
+        if (EXACT) {
+            for (int p = lane; p < npix; p += 32) {
+                float v = D[p] - M[p];
+                E[p] = (0.0f > v) ? 0.0f : v;
+            }
+            __syncwarp();
+            if (lane == 0)
+                for (int p = 1; p < npix; ++p) E[p] += E[p - 1];
+            __syncwarp();
+            total = E[npix - 1];
+        } else {
+            /* contiguous chunk per lane, lane-local serial sum, warp scan */
+            int per = (npix + 31) >> 5;
+            int p0 = min(lane * per, npix), p1 = min(p0 + per, npix);
+            float s = 0.0f;
+            for (int p = p0; p < p1; ++p) {
+                float v = D[p] - M[p];
+                s += v > 0.0f ? v : 0.0f;
+                E[p] = s;
+            }
+            float incl = s;
+            for (int o = 1; o < 32; o <<= 1) {
+                float t = __shfl_up_sync(BAMF_FULL, incl, o);
+                if (lane >= o) incl += t;
+            }
+            float excl = incl - s;
+            for (int p = p0; p < p1; ++p) E[p] += excl;
+            __syncwarp();
+            total = __shfl_sync(BAMF_FULL, incl, 31);
+        }
+        float rr = total * urand();
+        int first = npix;
+        for (int p = lane; p < npix; p += 32)
+            if (rr <= E[p]) {
+                first = p;
+                break;
+            }
+        for (int o = 16; o > 0; o >>= 1) first = min(first, __shfl_xor_sync(BAMF_FULL, first, o));
+        int ii = first;
+        *by = (float)(ii - Y * (ii / Y)) + urand() - 0.5f;
+        *bx = (float)(int)floorf((float)ii / (float)Y) + urand() - 0.5f;
+        __syncwarp();
+    }
+
+    /* RJMCMC::birth (:1258-1330). */
+    __device__ void mv_birth()
+    {
+        const int type = 6;
+        cinc(C_N_birth);
+        copyA2T();
+        const bamf_mcmc_params &p = K->p;
+        float bx, by;
+        find_birth(&bx, &by);
+        int BF;
+        if (p.IsBackg == 1) BF = (int)floor(dadd((double)urand(), 0.5));
+        else BF = 1;
+        float I_new;
+        if (BF == 1) {
+            cinc(C_N_birthFg);
+            I_new = genRand(K->sig);
+        } else {
+            cinc(C_N_birthBg);
+            I_new = genRand(K->back);
+        }
+        addT(I_new, bx, by, BF);
+        if (t_overflow) {
+            overflow++;
+            reject_record(type);
+            return;
+        }
+        if (!testT()) {
+            reject_record(type);
+            return;
+        }
+        float LLR = llr();
+        float NEm = nsignalA();
+        float PrM = MeanN / (NEm + 1.0f);
+        const float PixProb = 1.0f;
+        float PR = LLR * P[3] / (P[4] * ((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out) * PixProb) * PrM;
+        int accept = (urand() < PR);
+        if (accept) {
+            cinc(BF == 1 ? C_A_birthFg : C_A_birthBg);
+            cinc(C_A_birth);
+            accept_T();
+        }
+        record2(LLR, PR, type, accept);
+        update_grids();
+    }
+
+    /* RJMCMC::death (:1332-1387). */
+    __device__ void mv_death()
+    {
+        const int type = 7;
+        cinc(C_N_death);
+        copyA2T();
+        if (an < 1) return;
+        float Ua = urand();
+        int jj = min((int)floorf((float)an * Ua), an - 1);
+        int aSj = A_S(jj);
+        cinc(aSj == 1 ? C_N_deathFg : C_N_deathBg);
+        if (!EXACT) a_dirty |= 1u << jj;
+        removeT(jj);
+        float LLR = llr();
+        float NEm = nsignalA();
+        float PrM = NEm / MeanN;
+        float PR = LLR * (P[4] / P[3]) * PrM;
+        int accept = (urand() < PR);
+        if (accept) {
+            cinc(C_A_death);
+            cinc(aSj == 1 ? C_A_deathFg : C_A_deathBg);
+            accept_T();
+        }
+        record2(LLR, PR, type, accept);
+        update_grids();
+    }
+
+    /* RJMCMC::gSplit (:1389-1485). */
+    __device__ void mv_gsplit()
+    {
+        const int type = 8;
+        if (an < 2) return;
+        copyA2T();
+        float Ua = urand();
+        int jj = min((int)floorf((float)an * Ua), an - 1);
+        int Np = closestMulti(jj, 2 * sigma);
+        if (lane == 0) cl[Np] = jj;
+        __syncwarp();
+        Np++;
+        if (Np == 1) return;
+        float I0 = 0.0f, X0 = 0.0f, Y0 = 0.0f;
+        for (int n = 0; n < Np; ++n) {
+            int c = cl[n];
+            I0 = I0 + A_I(c);
+            X0 = X0 + A_X(c);
+            Y0 = Y0 + A_Y(c);
+        }
+        float u1 = 0.3f * randn();
+        float u2 = 0.3f * randn();
+        float u3 = (1.0f / (float)Np) * urand();
+        for (int n = 0; n < Np; ++n) {
+            int c = cl[n];
+            float aXc = A_X(c), aYc = A_Y(c), aIc = A_I(c);
+            setT(c, (1.0f - u3) * aIc, (aXc - u3 * (X0 / (float)Np + u1)) / (1.0f - u3),
+                 (aYc - u3 * (Y0 / (float)Np + u2)) / (1.0f - u3));
+            if (!EXACT) a_dirty |= 1u << c;
+        }
+        addT(u3 * I0, X0 / (float)Np + u1, Y0 / (float)Np + u2, 1);
+        if (t_overflow) {
+            overflow++;
+            reject_record(type);
+            return;
+        }
+        float LLR = llr();
+        float PrI = 1.0f, tmpCurrent, tmpProposed;
+        for (int n = 0; n < Np; ++n) {
+            int c = cl[n];
+            tmpCurrent = sob(A_S(c), A_I(c));
+            tmpProposed = sob(T_S(n), T_I(c));
+            PrI = PrI * tmpProposed / tmpCurrent;
+        }
+        tmpProposed = sob(T_S(tn - 1), T_I(tn - 1));
+        PrI = PrI * (tmpProposed);
+        float PDFu1 = normpdf(u1, 0.0f, 0.4f);
+        float PDFu2 = normpdf(u2, 0.0f, 0.4f);
+        float PDFu3 = (float)Np;
+        float Us = 1.0f / (PDFu1 * PDFu2 * PDFu3);
+        float NEm = nsignalA();
+        float PrM = MeanN / (NEm + 1.0f);
+        const bamf_mcmc_params &p = K->p;
+        float Area = (float)(((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out));
+        float PrX = 1.0f / Area;
+        float Jacob = I0 / MT::powf_(1.0f - u3, (float)(Np + 1));
+        float PR = LLR * PrI * PrX * Us * Jacob * PrM * (P[5] / P[6]);
+        int accept = (urand() < PR);
+        if (accept) accept_T();
+        record2(LLR, PR, type, accept);
+        update_grids();
+    }
+
+    /* RJMCMC::gMerge (:1487-1584). */
+    __device__ void mv_gmerge()
+    {
+        const int type = 9;
+        if (an < 3) return;
+        copyA2T();
+        float Ua = urand();
+        int jj = min((int)floorf((float)an * Ua), an - 1);
+        int Np = closestMulti(jj, 3 * sigma);
+        if (Np == 0) return;
+        float aIj = A_I(jj), aXj = A_X(jj), aYj = A_Y(jj);
+        float I0 = aIj;
+        for (int n = 0; n < Np; ++n) I0 = I0 + A_I(cl[n]);
+        float XX0 = 0.0f, YY0 = 0.0f;
+        float U3 = aIj / I0;
+        for (int n = 0; n < Np; ++n) {
+            int c = cl[n];
+            float aIc = A_I(c), aXc = A_X(c), aYc = A_Y(c);
+            float nX = U3 * aXj + (1.0f - U3) * aXc;
+            XX0 = XX0 + U3 * aXj + (1.0f - U3) * aXc;
+            float nY = U3 * aYj + (1.0f - U3) * aYc;
+            YY0 = YY0 + U3 * aYj + (1.0f - U3) * aYc;
+            setT(c, aIc / (1.0f - U3), nX, nY);
+            if (!EXACT) a_dirty |= 1u << c;
+        }
+        float U1 = aXj - XX0 / (float)Np;
+        float U2 = aYj - YY0 / (float)Np;
+        float PrI = 1.0f, tmpProposed, tmpCurrent;
+        for (int n = 0; n < Np; ++n) {
+            int c = cl[n];
+            tmpProposed = sob(T_S(c), T_I(c));
+            tmpCurrent = sob(A_S(c), A_I(c));
+            PrI = PrI * (tmpCurrent / tmpProposed);
+        }
+        tmpCurrent = sob(A_S(jj), aIj);
+        PrI = PrI * tmpCurrent;
+        if (!EXACT) a_dirty |= 1u << jj;
+        removeT(jj);
+        float LLR = llr();
+        float PDFu1 = normpdf(U1, 0.0f, 0.4f);
+        float PDFu2 = normpdf(U2, 0.0f, 0.4f);
+        float PDFu3 = (float)Np;
+        float Us = 1.0f / (PDFu1 * PDFu2 * PDFu3);
+        float NEm = nsignalA();
+        float PrM = NEm / MeanN;
+        const bamf_mcmc_params &p = K->p;
+        float Area = (float)(((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out));
+        float PrX = 1.0f / Area;
+        float Jacob = I0 / MT::powf_(1.0f - U3, (float)(Np + 1));
+        float PR = LLR / (PrI * PrX * Us * Jacob * PrM * (P[5] / P[6]));
+        if (PDFu1 == 0.0f || PDFu2 == 0.0f) PR = -1.0f;
+        int accept = (urand() < PR);
+        if (accept) accept_T();
+        record2(LLR, PR, type, accept);
+        update_grids();
+    }
+
+    /* RJMCMC::backFore (:1586-1627). */
+    __device__ void mv_backfore()
+    {
+        if (an == 0) return;
+        if (K->p.IsBackg == 0) return;
+        float Ua = urand();
+        int nn = min((int)floorf((float)an * Ua), an - 1);
+        float In = A_I(nn);
+        int Sn = A_S(nn);
+        float BackP = findPDF(K->back, In);
+        float SignalP = findPDF(K->sig, In);
+        int ns = Sn;
+        if (Sn == 1) {
+            if (SignalP != 0.0f) {
+                float PrSig = BackP / SignalP;
+                if (PrSig > urand()) ns = 0;
+            } else {
+                ns = 0;
+            }
+        } else {
+            if (BackP != 0.0f) {
+                float PrSig = SignalP / BackP;
+                if (PrSig > urand()) ns = 1;
+            } else {
+                ns = 1;
+            }
+        }
+        if (lane == nn) aS = ns;
+    }
+
+    __device__ void step(const float *V, const float *W, float t)
+    {
+        /* dispatch of start_Chain (:693-717, :725-748); W = this phase's
+         * cumulative vector, V = PV_Burnin for the gSplit/gMerge slots */
+        if (t < W[0]) mv_jump();
+        else if (t >= W[0] && t < W[1]) mv_split();
+        else if (t >= W[1] && t < W[2]) mv_merge();
+        else if (t >= W[2] && t < W[3]) mv_birth();
+        else if (t >= W[3] && t < W[4]) mv_death();
+        else if (t >= V[4] && t < V[5]) mv_gsplit();
+        else if (t >= V[5] && t < V[6]) mv_gmerge();
+        else mv_backfore();
+    }
+
+    /* RJMCMC::start_Chain (:685-750). */
+    __device__ void run_chain()
+    {
+        const bamf_mcmc_params &p = K->p;
+        is_burnin = 1;
+        for (int k = 0; k < 8; ++k) P[k] = p.P_Burnin[k];
+        int since_rebuild = 0;
+        for (int n = 0; n < p.N_Burnin; ++n) {
+            float t = urand();
+            step(K->PVB, K->PVB, t);
+            if (!EXACT && ++since_rebuild == 512) {
+                rebuild_model();
+                since_rebuild = 0;
+            }
+        }
+        is_burnin = 0;
+        for (int k = 0; k < 8; ++k) P[k] = K->PVT[k];
+        for (int n = 0; n < p.N_Trials; ++n) {
+            float t = urand();
+            step(K->PVB, K->PVT, t);
+            if (!EXACT && ++since_rebuild == 512) {
+                rebuild_model();
+                since_rebuild = 0;
+            }
+        }
+    }
+};
+
+template <bool EXACT>
+__global__ void __launch_bounds__(128) rjmcmc_kernel(const __grid_constant__ SamplerConsts Kc,
+                                                     const __grid_constant__ SamplerBatch Bc)
+{
+    extern __shared__ float smem_raw[];
+    const SamplerConsts *Kp = &Kc;
+    const SamplerBatch *Bp = &Bc;
+    const SamplerBatch &Bt = Bc;
+    int warp = threadIdx.x >> 5;
+    int lane = threadIdx.x & 31;
+    int per = warp_smem_floats(Bt.side_max, EXACT);
+    float *sw = smem_raw + (size_t)warp * per;
+
+    ChainWarp<EXACT> w;
+    w.K = Kp;
+    w.B = Bp;
+    w.lane = lane;
+    for (;;) {
+        int slot = 0;
+        if (lane == 0) slot = atomicAdd(Bt.queue, 1);
+        slot = __shfl_sync(BAMF_FULL, slot, 0);
+        if (slot >= Bt.n_rois) break;
+        int roi = Bt.order ? Bt.order[slot] : slot;
+        w.roi = roi;
+        int X = Bt.xsize[roi], Y = Bt.ysize[roi];
+        w.X = X;
+        w.Y = Y;
+        w.npix = X * Y;
+        int npix_max = Bt.side_max * Bt.side_max;
+        int nxs = BAMF_NMAX * Bt.side_max;
+        w.D = sw;
+        w.M = sw + npix_max;
+        w.Mt = sw + 2 * npix_max;
+        w.E = sw + 3 * npix_max;
+        w.scm = sw + 4 * npix_max;
+        w.NX = sw + 5 * npix_max;
+        w.NY = w.NX + nxs;
+        w.cnt = (int *)(w.NY + nxs);
+        w.cl = w.cnt + C_COUNT;
+        /* fast mode only: A's stencil cache and log2 M */
+        w.NXa = (float *)(w.cl + BAMF_NMAX + 2);
+        w.NYa = w.NXa + nxs;
+        w.logM = w.NYa + nxs;
+        bool ok = X >= 1 && Y >= 1 && X <= Bt.side_max && Y <= Bt.side_max;
+        if (!ok) {
+            if (lane == 0 && Bt.status) Bt.status[roi] = BAMF_ERR_TOO_LARGE;
+            continue;
+        }
+        const float *src = Bt.data + Bt.offsets[roi];
+        for (int p = lane; p < w.npix; p += 32) {
+            w.D[p] = src[p];
+            w.scm[p] = Bt.scmos ? Bt.scmos[Bt.offsets[roi] + p] : 0.0f;
+        }
+        if (lane < C_COUNT) {
+            int k = lane;
+            bool isN = (k <= C_N_death) || (k >= C_N_jumpFg && k <= C_N_deathFg) ||
+                       (k >= C_N_jumpBg && k <= C_N_deathBg);
+            w.cnt[k] = isN ? 1 : 0;
+        }
+        float s = Bt.psf_sigma ? Bt.psf_sigma[roi] : Kp->p.PSFsigma;
+        w.sigma = s;
+        w.Cst = 1.0f / (s * sqrtf(2.0f));
+        w.MeanN = Kp->p.Rho * (float)X * (float)Y;
+        /* start state (cRJMCMC.cpp:120-133) */
+        int n0 = Bt.init_n ? Bt.init_n[roi] : 0;
+        if (n0 > BAMF_NMAX) {
+            if (lane == 0 && Bt.status) Bt.status[roi] = BAMF_ERR_TOO_LARGE;
+            continue;
+        }
+        w.an = n0;
+        w.aI = w.aX = w.aY = 0.0f;
+        w.aS = 1;
+        if (n0 > 0 && lane < n0) {
+            const float *ixy = Bt.init_ixy + (size_t)roi * 3 * BAMF_NMAX;
+            w.aI = ixy[lane];
+            w.aX = ixy[BAMF_NMAX + lane];
+            w.aY = ixy[2 * BAMF_NMAX + lane];
+        }
+        w.aBG = Bt.init_bg ? Bt.init_bg[roi] : Kp->bg0;
+        if (w.aBG == 0.0f) w.aBG = 1.0f;
+        w.aABG = 0.0f;
+        w.aBBG = 0.0f;
+        w.seed = Kp->seed;
+        w.chain = Bt.chain_ids ? Bt.chain_ids[roi] : (uint32_t)roi;
+        w.idx = Bt.rng_offset ? Bt.rng_offset[roi] : 0u;
+        w.base = w.idx >> 2;
+        w.refill();
+        w.entries = 0;
+        w.overflow = 0;
+        w.a_dirty = w.t_dirty = 0u;
+        w.removed = -1;
+        w.rec_n[0] = w.rec_n[1] = 0;
+        __syncwarp();
+        w.rebuild_model();
+        w.run_chain();
+        /* outputs */
+        if (Bt.final_n && lane == 0) Bt.final_n[roi] = w.an;
+        if (Bt.final_state) {
+            float *fs = Bt.final_state + (size_t)roi * (4 + 4 * BAMF_NMAX);
+            if (lane == 0) {
+                fs[0] = w.aBG; fs[1] = w.aABG; fs[2] = w.aBBG; fs[3] = (float)w.an;
+            }
+            fs[4 + lane] = lane < w.an ? w.aI : 0.0f;
+            fs[4 + BAMF_NMAX + lane] = lane < w.an ? w.aX : 0.0f;
+            fs[4 + 2 * BAMF_NMAX + lane] = lane < w.an ? w.aY : 0.0f;
+            fs[4 + 3 * BAMF_NMAX + lane] = lane < w.an ? (float)w.aS : 0.0f;
+        }
+        __syncwarp();
+        if (Bt.counters)
+            for (int k = lane; k < C_COUNT; k += 32) Bt.counters[(size_t)roi * C_COUNT + k] = w.cnt[k];
+        if (Bt.chains && lane == 0) {
+            Bt.chains[2 * roi].n_entries = min(w.entries, Bt.chains[2 * roi].capacity_entries);
+            Bt.chains[2 * roi + 1].n_entries = min(w.entries, Bt.chains[2 * roi + 1].capacity_entries);
+            Bt.chains[2 * roi].n_records = w.rec_n[0];
+            Bt.chains[2 * roi + 1].n_records = w.rec_n[1];
+        }
+        if (lane == 0) {
+            if (Bt.n_entries) Bt.n_entries[roi] = w.entries;
+            if (Bt.uniforms_used) Bt.uniforms_used[roi] = w.idx - (Bt.rng_offset ? Bt.rng_offset[roi] : 0u);
+            if (Bt.overflow) Bt.overflow[roi] = w.overflow;
+            if (Bt.status) Bt.status[roi] = BAMF_OK;
+        }
+        __syncwarp();
+    }
+}
+
+
+}  // namespace bamf

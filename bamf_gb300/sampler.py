@@ -1,0 +1,269 @@
+"""Python mirror of the reference sampler interface, over libbamf_gb300.so.
+
+  cRJMCMC(...)       the MEX function's five outputs (source/c/cRJMCMC.cpp:52-308)
+  crjmcmc_raw(...)   one ROI, raw chain vectors (what the MEX marshals)
+  rjmcmc(...)        @RJ/rjmcmc.m: empty start state and MCMC struct from RJStruct
+  Sampler.run(...)   a whole batch of ROIs in one persistent launch
+
+The library must be built (bamf_gb300.build.build()); there is no CPU
+fallback: every call here runs the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from .rjstruct import RJStruct, initial_bg, mcmc_params
+
+ARITH = {"exact": abi.BAMF_ARITH_EXACT, "fast": abi.BAMF_ARITH_FAST}
+FINAL_STRIDE = 4 + 4 * abi.BAMF_NMAX
+
+
+def _declare() -> C.CDLL:
+    L = abi.lib()
+    if getattr(L, "_sampler_declared", False):
+        return L
+    pf = C.POINTER(C.c_float)
+    L.bamf_crjmcmc_host.restype = C.c_int
+    L.bamf_crjmcmc_host.argtypes = [
+        pf, C.c_int, C.c_int, C.POINTER(abi.Emitters), C.POINTER(abi.McmcParams),
+        pf, C.c_int, pf, C.c_int, pf, C.c_int, pf, C.POINTER(abi.Rng), C.c_int,
+        pf, pf, C.POINTER(abi.Chain), C.POINTER(abi.Chain), C.POINTER(abi.Counters)]
+    L.bamf_workspace_create.restype = C.c_int
+    L.bamf_workspace_create.argtypes = [C.POINTER(C.c_void_p)]
+    L.bamf_workspace_destroy.argtypes = [C.c_void_p]
+    L.bamf_rjmcmc_batch_device.restype = C.c_int
+    L.bamf_rjmcmc_batch_device.argtypes = [C.c_void_p, C.POINTER(RoiBatch), C.POINTER(abi.McmcParams),
+                                           C.POINTER(Priors), C.c_uint32, C.c_int,
+                                           C.POINTER(BatchResults), C.c_void_p]
+    L.bamf_rjmcmc_batch_host.restype = C.c_int
+    L.bamf_rjmcmc_batch_host.argtypes = [C.c_void_p, C.POINTER(RoiBatch), C.POINTER(abi.McmcParams),
+                                         C.POINTER(Priors), C.c_uint32, C.c_int,
+                                         C.POINTER(BatchResults)]
+    L.bamf_last_error.restype = C.c_char_p
+    L._sampler_declared = True
+    return L
+
+
+class Priors(C.Structure):
+    _fields_ = [("offset_pdf", C.POINTER(C.c_float)), ("offset_len", C.c_int32),
+                ("signal_pdf", C.POINTER(C.c_float)), ("signal_len", C.c_int32),
+                ("back_pdf", C.POINTER(C.c_float)), ("back_len", C.c_int32)]
+
+
+class RoiBatch(C.Structure):
+    _fields_ = [("n_rois", C.c_int32), ("side_max", C.c_int32), ("data", C.c_void_p),
+                ("offsets", C.c_void_p), ("xsize", C.c_void_p), ("ysize", C.c_void_p),
+                ("psf_sigma", C.c_void_p), ("scmos", C.c_void_p), ("init_n", C.c_void_p),
+                ("init_bg", C.c_void_p), ("init_ixy", C.c_void_p), ("bg0", C.c_float)]
+
+
+class BatchResults(C.Structure):
+    _fields_ = [("map_n", C.c_void_p), ("final_n", C.c_void_p), ("final_state", C.c_void_p),
+                ("counters", C.c_void_p), ("n_entries", C.c_void_p), ("status", C.c_void_p),
+                ("overflow", C.c_void_p)]
+
+
+def _check(L, st: int, where: str) -> None:
+    if st != abi.BAMF_OK:
+        msg = L.bamf_last_error()
+        raise abi.BamfError(st, f"{where} ({msg.decode() if msg else ''})")
+
+
+def crjmcmc_raw(roi: np.ndarray, params: abi.McmcParams, off, sig, back, e0=None,
+                rng=(0, 0, 0), scmos=None, arith: str = "exact", record: bool = True,
+                grids: bool = True) -> dict:
+    """One cRJMCMC call on a (Ysize, Xsize) ROI; raw outputs like oracle.run_chain."""
+    L = _declare()
+    ysize, xsize = roi.shape
+    data = np.ascontiguousarray(np.asarray(roi, np.float32).ravel(order="F"))
+    I, X, Y, BG = e0 if e0 is not None else ([], [], [], 0.0)
+    em, keep = abi.make_emitters(len(I), I, X, Y, BG)
+    off = np.ascontiguousarray(off, np.float32)
+    sig = np.ascontiguousarray(sig, np.float32)
+    back = np.ascontiguousarray(back, np.float32)
+    sc = None if scmos is None else np.ascontiguousarray(np.asarray(scmos, np.float32).ravel(order="F"))
+    r = abi.Rng(*rng)
+    steps = int(params.N_Burnin) + int(params.N_Trials)
+    chains = None
+    if record:
+        chains = [abi.alloc_chain(steps, steps * abi.BAMF_NMAX) for _ in range(2)]
+    Z = int(params.Grid_Zoom)
+    g = xsize * ysize * Z * Z
+    pg = np.zeros(g, np.float32) if grids else None
+    pb = np.zeros(g, np.float32) if grids else None
+    cnt = abi.Counters()
+    st = L.bamf_crjmcmc_host(
+        abi.fptr(data), xsize, ysize, C.byref(em), C.byref(params), abi.fptr(off), off.size,
+        abi.fptr(sig), sig.size, abi.fptr(back), back.size, abi.fptr(sc) if sc is not None else None,
+        C.byref(r), ARITH[arith], abi.fptr(pg) if grids else None, abi.fptr(pb) if grids else None,
+        C.byref(chains[0][0]) if record else None, C.byref(chains[1][0]) if record else None,
+        C.byref(cnt))
+    _check(L, st, "bamf_crjmcmc_host")
+    out = {"counters": cnt.as_dict()}
+    if record:
+        out["chain"] = abi.chain_to_dict(*chains[0])
+        out["chain_test"] = abi.chain_to_dict(*chains[1])
+    if grids:
+        out["pgrid"] = pg.reshape(xsize * Z, ysize * Z).T.copy()
+        out["pback"] = pb.reshape(xsize * Z, ysize * Z).T.copy()
+    return out
+
+
+def _emitters_of(raw: dict, nn: int):
+    """RJMCMCChain::getEmitters (LibRJMCMC.cpp:324-377) on the raw vectors."""
+    N = raw["N"]
+    n = int(N[nn]) if int(N[nn]) != 0 else 1
+    start = int(np.sum(np.maximum(N[:nn], 1)))
+    sl = slice(start, start + n)
+    return (n, raw["Photons"][sl], raw["X"][sl], raw["Y"][sl], raw["Signal"][sl])
+
+
+def mex_chain(raw: dict, accepted: dict | None = None) -> list[dict]:
+    """Marshal a raw chain into the MEX struct array (cRJMCMC.cpp:159-276):
+    one struct per entry except the last; N reported as 0 for the placeholder
+    state; the proposed chain takes LLR/PR/JumpType/Accepted from the
+    accepted chain (:265-272)."""
+    src = accepted if accepted is not None else raw
+    out = []
+    for nn in range(len(raw["N"]) - 1):
+        n, ph, x, y, s = _emitters_of(raw, nn)
+        out.append({
+            "N": 0.0 if ph[0] == 0 else float(n),
+            "X": x.astype(np.float64), "Y": y.astype(np.float64),
+            "Photons": ph.astype(np.float64), "Signal": s.astype(np.float64),
+            "LLR": float(src["LLR"][nn]), "PR": float(src["PR"][nn]),
+            "JumpType": float(src["JumpType"][nn]), "Accepted": float(src["Accepted"][nn]),
+            "BG": float(raw["BG"][nn]), "ABG": float(raw["ABG"][nn]), "BBG": float(raw["BBG"][nn]),
+        })
+    return out
+
+
+STAT_FIELDS = ["NTrials", "Accept_Jump", "Accept_Split", "Accept_Merge", "Accept_Birth",
+               "Accept_Death", "Accept_JumpFg", "Accept_SplitFg", "Accept_MergeFg",
+               "Accept_BirthFg", "Accept_DeathFg", "Accept_JumpBg", "Accept_SplitBg",
+               "Accept_MergeBg", "Accept_BirthBg", "Accept_DeathBg"]
+
+
+def mex_stat(counters: dict, params: abi.McmcParams) -> dict:
+    """The Stat output (cRJMCMC.cpp:282-305): accept/propose ratios."""
+    c = counters
+    vals = [float(params.N_Trials) + float(params.N_Burnin)]
+    for suf in ("", "Fg", "Bg"):
+        for m in ("jump", "split", "merge", "birth", "death"):
+            vals.append(c[f"A_{m}{suf}"] / c[f"N_{m}{suf}"])
+    return dict(zip(STAT_FIELDS, vals))
+
+
+def cRJMCMC(Data, E_active: dict, MCMC: abi.McmcParams, Xsize: int, Ysize: int, OffSetPDF,
+            SignalPDF, BackPDF, sCMOScorr=None, SampledPSF=None, OptModel: int = 0,
+            rng=(0, 0, 0), arith: str = "exact"):
+    """The MEX call of rjmcmc.m:102 / mcmc.m:142 with the same five outputs:
+    PGrid, PBack, accepted chain, proposed chain, Stat."""
+    if OptModel not in (0, None):
+        raise abi.BamfError(abi.BAMF_ERR_UNSUPPORTED, "cRJMCMC(OptModel=1)")
+    data = np.asarray(Data, np.float32)[:Ysize, :Xsize]
+    e0 = (np.asarray(E_active.get("I", []), np.float32), np.asarray(E_active.get("X", []), np.float32),
+          np.asarray(E_active.get("Y", []), np.float32), float(E_active["BG"]))
+    raw = crjmcmc_raw(data, MCMC, OffSetPDF, SignalPDF, BackPDF, e0=e0, rng=rng, scmos=sCMOScorr,
+                      arith=arith)
+    acc = mex_chain(raw["chain"])
+    prop = mex_chain(raw["chain_test"], accepted=raw["chain"])
+    return raw["pgrid"], raw["pback"], acc, prop, mex_stat(raw["counters"], MCMC)
+
+
+def rjmcmc(Data, RJ: RJStruct, Ysize: int, Xsize: int, DriftY: float = 0.0, DriftX: float = 0.0,
+           sCMOSVar=None, rng=(0, 0, 0), arith: str = "exact"):
+    """@RJ/rjmcmc.m:1-105: empty start, MCMC struct from RJStruct; returns
+    (Chain, Stat, PImage, PBackg, ProposedChain)."""
+    E = {"N": 0, "I": [], "X": [], "Y": [], "BG": initial_bg(RJ)}
+    p = mcmc_params(RJ, DriftX, DriftY)
+    pg, pb, acc, prop, stat = cRJMCMC(Data, E, p, Xsize, Ysize, RJ.P_Offset, RJ.P_EmPhotons,
+                                      RJ.P_BgEmPhotons, sCMOSVar, rng=rng, arith=arith)
+    return acc, stat, pg, pb, prop
+
+
+class Sampler:
+    """Batched sampler over device-resident ROIs (torch tensors on cuda)."""
+
+    def __init__(self):
+        L = _declare()
+        h = C.c_void_p()
+        _check(L, L.bamf_workspace_create(C.byref(h)), "bamf_workspace_create")
+        self._ws = h
+        self._L = L
+
+    def close(self):
+        if self._ws:
+            self._L.bamf_workspace_destroy(self._ws)
+            self._ws = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _priors(off, sig, back):
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (off, sig, back)]
+        pr = Priors(abi.fptr(arrs[0]), arrs[0].size, abi.fptr(arrs[1]), arrs[1].size,
+                    abi.fptr(arrs[2]), arrs[2].size)
+        return pr, arrs
+
+    def run_device(self, dev: dict, params: abi.McmcParams, off, sig, back, seed: int,
+                   arith: str = "fast", outs: dict | None = None, stream=None, bg0: float = 0.0):
+        """dev: dict of torch CUDA tensors data/offsets/xsize/ysize[/psf_sigma];
+        outs: dict of torch CUDA tensors to fill (map_n, final_n, final_state,
+        counters, n_entries, status, overflow).  Enqueues on `stream`."""
+        pr, keep = self._priors(off, sig, back)
+        b = RoiBatch()
+        b.n_rois = int(dev["xsize"].numel())
+        b.side_max = int(dev.get("side_max", 0))
+        for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos", "init_n", "init_bg",
+                  "init_ixy"):
+            t = dev.get(k)
+            setattr(b, k, t.data_ptr() if t is not None else None)
+        b.bg0 = float(bg0)
+        res = BatchResults()
+        for k in ("map_n", "final_n", "final_state", "counters", "n_entries", "status", "overflow"):
+            t = (outs or {}).get(k)
+            setattr(res, k, t.data_ptr() if t is not None else None)
+        st = self._L.bamf_rjmcmc_batch_device(self._ws, C.byref(b), C.byref(params), C.byref(pr),
+                                               int(seed), ARITH[arith], C.byref(res),
+                                               C.c_void_p(stream) if stream else None)
+        _check(self._L, st, "bamf_rjmcmc_batch_device")
+
+    def run_host(self, batch, params: abi.McmcParams, off, sig, back, seed: int,
+                 arith: str = "fast", bg0: float = 0.0, init=None) -> dict:
+        """batch: synth.RoiBatch (host numpy); returns numpy results."""
+        pr, keep = self._priors(off, sig, back)
+        n = batch.n
+        b = RoiBatch()
+        b.n_rois = n
+        b.side_max = 0
+        arrays = {"data": np.ascontiguousarray(batch.data, np.float32),
+                  "offsets": np.ascontiguousarray(batch.offsets, np.int64),
+                  "xsize": np.ascontiguousarray(batch.xsize, np.int32),
+                  "ysize": np.ascontiguousarray(batch.ysize, np.int32),
+                  "psf_sigma": np.ascontiguousarray(batch.sigma, np.float32)}
+        if init is not None:
+            arrays["init_n"] = np.ascontiguousarray(init["n"], np.int32)
+            arrays["init_bg"] = np.ascontiguousarray(init["bg"], np.float32)
+            arrays["init_ixy"] = np.ascontiguousarray(init["ixy"], np.float32)
+        for k, a in arrays.items():
+            setattr(b, k, a.ctypes.data)
+        b.bg0 = float(bg0)
+        outs = {"map_n": np.zeros(n, np.int32), "final_n": np.zeros(n, np.int32),
+                "final_state": np.zeros((n, FINAL_STRIDE), np.float32),
+                "counters": np.zeros((n, 30), np.int32), "n_entries": np.zeros(n, np.int32),
+                "status": np.full(n, -1, np.int32), "overflow": np.zeros(n, np.int32)}
+        res = BatchResults()
+        for k, a in outs.items():
+            setattr(res, k, a.ctypes.data)
+        st = self._L.bamf_rjmcmc_batch_host(self._ws, C.byref(b), C.byref(params), C.byref(pr),
+                                             int(seed), ARITH[arith], C.byref(res))
+        _check(self._L, st, "bamf_rjmcmc_batch_host")
+        return outs

@@ -152,6 +152,130 @@ typedef struct bamf_counters {
     int32_t A_jumpBg, A_splitBg, A_mergeBg, A_birthBg, A_deathBg;
 } bamf_counters;
 
+/* ------------------------------------------------------------------ */
+/* Library                                                              */
+/* ------------------------------------------------------------------ */
+
+/* Version string of the library. */
+const char *bamf_version(void);
+
+/* Number of visible CUDA devices (0 when none; never fails). */
+int bamf_device_count(void);
+
+/* Text of the last CUDA error this thread's calls met (empty if none). */
+const char *bamf_last_error(void);
+
+/* ------------------------------------------------------------------ */
+/* Sampler                                                              */
+/* ------------------------------------------------------------------ */
+
+/*
+ * One ROI with the exact semantics of the MEX function cRJMCMC
+ * (source/c/cRJMCMC.cpp:52-308; called from @RJ/rjmcmc.m:102 and
+ * @RJ/mcmc.m:142).  Host buffers in, host buffers out; synchronous.
+ *
+ *   data            Ysize*Xsize floats, y fastest            (prhs[0])
+ *   xsize, ysize                                             (prhs[3], prhs[4])
+ *   e0              starting emitters and offset             (prhs[1])
+ *   p               the MCMC struct                          (prhs[2])
+ *   off/sig/back    OffSetPDF, SignalPDF, BackPDF and lengths (prhs[5..7];
+ *                   length = max(dims) as the gateway takes it, :77-98)
+ *   scmos           Ysize*Xsize sCMOS variance image or NULL (zeros)  (prhs[8])
+ *   rng             the chain's uniform stream (stands in for rand())
+ *   arith           BAMF_ARITH_EXACT or BAMF_ARITH_FAST
+ *   pgrid, pback    (Ysize*Zoom)*(Xsize*Zoom) floats, y fastest; may be
+ *                   NULL together                            (plhs[0], plhs[1])
+ *   chain, chain_test  raw RJMCMCChain vectors (see bamf_chain); may be NULL
+ *                   (plhs[2], plhs[3] before marshalling)
+ *   counters        the 30 counters behind the Stat output  (plhs[4]); may be NULL
+ *
+ * The sampled-PSF model (prhs[9], prhs[10] = OptModel 1) is not supported:
+ * this entry point always uses the Gaussian PSF (OptModel 0).
+ * Errors: BAMF_ERR_INVALID_ARG (null input, size < 1, pdf length < 1),
+ * BAMF_ERR_TOO_LARGE (side > BAMF_MAX_ROI_SIDE or N > BAMF_NMAX),
+ * BAMF_ERR_BAD_PRIOR (NaN/negative pdf, non-increasing grid),
+ * BAMF_ERR_CAPACITY (chain arrays too small), BAMF_ERR_CUDA, BAMF_ERR_NO_DEVICE.
+ */
+bamf_status bamf_crjmcmc_host(const float *data, int xsize, int ysize, const bamf_emitters *e0,
+                              const bamf_mcmc_params *p, const float *off, int off_len,
+                              const float *sig, int sig_len, const float *back, int back_len,
+                              const float *scmos, const bamf_rng *rng, int arith, float *pgrid,
+                              float *pback, bamf_chain *chain, bamf_chain *chain_test,
+                              bamf_counters *counters);
+
+/* Prior PDF tables of a batch (host pointers; the library builds the
+ * reference's CDF tables from them, LibRJMCMC.cpp:176-217). */
+typedef struct bamf_priors {
+    const float *offset_pdf;
+    int32_t offset_len;
+    const float *signal_pdf;
+    int32_t signal_len;
+    const float *back_pdf;
+    int32_t back_len;
+} bamf_priors;
+
+/*
+ * A batch of independent ROIs of possibly different sizes, packed back to
+ * back (the per-ROI calls of analyzeROIs.m:126-159 as one launch).
+ * ROI k occupies data[offsets[k] .. offsets[k] + ysize[k]*xsize[k]), y fastest.
+ * Optional arrays may be NULL: psf_sigma (then p->PSFsigma for all), scmos
+ * (zeros), init_n/init_bg/init_ixy (empty start with BG = bg0, as
+ * rjmcmc.m:43-47 does; init_ixy is [k][3][BAMF_NMAX] = I row, X row, Y row).
+ * Pointers are device pointers for bamf_rjmcmc_batch_device and host
+ * pointers for bamf_rjmcmc_batch_host.
+ */
+typedef struct bamf_roi_batch {
+    int32_t n_rois;
+    int32_t side_max;   /* largest ROI side in the batch; 0 = BAMF_MAX_ROI_SIDE */
+    const float *data;
+    const int64_t *offsets;
+    const int32_t *xsize;
+    const int32_t *ysize;
+    const float *psf_sigma;
+    const float *scmos;
+    const int32_t *init_n;
+    const float *init_bg;
+    const float *init_ixy;
+    float bg0;
+} bamf_roi_batch;
+
+/* Per-ROI results of a batch (any pointer may be NULL).
+ *   map_n        MAP emitter count: mode of the Signal==1 count over the
+ *                second half of the accepted chain (findMap.m:29-45)
+ *   final_n      emitters in the last state
+ *   final_state  [k][4 + 4*BAMF_NMAX]: BG, ABG, BBG, N, I[], X[], Y[], Signal[]
+ *   counters     [k][30] in bamf_counters order
+ *   n_entries    recorded chain entries (cRJMCMC's chain length + 1)
+ *   status       BAMF_OK or the ROI's error
+ *   overflow     proposals rejected because they would exceed BAMF_NMAX */
+typedef struct bamf_batch_results {
+    int32_t *map_n;
+    int32_t *final_n;
+    float *final_state;
+    int32_t *counters;
+    int32_t *n_entries;
+    int32_t *status;
+    int32_t *overflow;
+} bamf_batch_results;
+
+/* Device scratch (prior tables, work queue, per-ROI chain traces) that
+ * grows on demand and is reused across calls on one stream. */
+typedef struct bamf_workspace bamf_workspace;
+bamf_status bamf_workspace_create(bamf_workspace **ws);
+void bamf_workspace_destroy(bamf_workspace *ws);
+
+/* Batched sampler on device-resident data; enqueues on `stream`
+ * (a cudaStream_t, NULL = default stream) and returns. */
+bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_roi_batch *rois,
+                                     const bamf_mcmc_params *p, const bamf_priors *priors,
+                                     uint32_t seed, int arith, const bamf_batch_results *out,
+                                     void *stream);
+
+/* Same with host buffers: copies in, runs, copies out, synchronises. */
+bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi_batch *rois,
+                                   const bamf_mcmc_params *p, const bamf_priors *priors,
+                                   uint32_t seed, int arith, const bamf_batch_results *out);
+
 #ifdef __cplusplus
 }
 #endif

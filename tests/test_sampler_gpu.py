@@ -1,0 +1,94 @@
+"""GPU parity of the sampler against the CPU oracle (the C restatement of
+source/c/LibRJMCMC.cpp, itself pinned to the reference build).
+
+Exact arithmetic must reproduce the oracle chain bit for bit: every chain
+entry (N, LLR, PR, JumpType, Accepted, BG, ABG, BBG), every emitter record,
+the posterior grids and the 30 counters."""
+import numpy as np
+import pytest
+
+from bamf_gb300 import rjstruct, sampler, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _c0(n_rois, steps=None, seed=0):
+    b = synth.roi_batch_c0(n_rois, seed=seed)
+    rj = rjstruct.c0_rjstruct()
+    if steps is not None:
+        rj.N_Burnin = rj.N_Trials = steps
+    return b, rj
+
+
+def _bits(a):
+    a = np.asarray(a)
+    return a.view(np.uint32) if a.dtype == np.float32 else a
+
+
+def assert_same_chain(got, ref):
+    for w in ("chain", "chain_test"):
+        for f, v in ref[w].items():
+            g = got[w][f]
+            assert g.shape == v.shape, (w, f, g.shape, v.shape)
+            bad = np.flatnonzero(_bits(g) != _bits(v))
+            assert bad.size == 0, f"{w}.{f} first mismatch at {bad[0]}: {g[bad[0]]} vs {v[bad[0]]}"
+    np.testing.assert_array_equal(got["pgrid"], ref["pgrid"])
+    np.testing.assert_array_equal(got["pback"], ref["pback"])
+    assert got["counters"] == ref["counters"]
+
+
+@pytest.mark.parametrize("k", [0, 1, 2, 7])
+def test_exact_chain_matches_oracle(cuda_lib, oracle_port, k):
+    b, rj = _c0(8, steps=1500)
+    p = rjstruct.mcmc_params(rj)
+    bg0 = rjstruct.initial_bg(rj)
+    args = (p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons)
+    ref = oracle_port.run_chain("port", b.roi(k), *args, e0=([], [], [], bg0), rng=(11, k, 0))
+    got = sampler.crjmcmc_raw(b.roi(k), *args, e0=([], [], [], bg0), rng=(11, k, 0), arith="exact")
+    assert_same_chain(got, ref)
+
+
+def test_exact_chain_with_start_state(cuda_lib, oracle_port):
+    """A start state with emitters, drift and a nonzero rng offset (the
+    fixed-N refinement call of mcmc.m:142 uses P = [1 0 ... 0])."""
+    b, rj = _c0(4, steps=800, seed=3)
+    p = rjstruct.refine_params(rj, drift_x=0.25, drift_y=-0.5)
+    k = 1
+    X = b.true_x[k].astype(np.float32)
+    Y = b.true_y[k].astype(np.float32)
+    I = b.true_i[k].astype(np.float32)
+    e0 = (I, X, Y, 9.5)
+    args = (p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons)
+    ref = oracle_port.run_chain("port", b.roi(k), *args, e0=e0, rng=(5, 99, 37))
+    got = sampler.crjmcmc_raw(b.roi(k), *args, e0=e0, rng=(5, 99, 37), arith="exact")
+    assert_same_chain(got, ref)
+
+
+def test_exact_batch_matches_oracle(cuda_lib, oracle_port):
+    """Batch path: final emitter count, MAP count and counters of every ROI."""
+    b, rj = _c0(48, steps=1000)
+    p = rjstruct.mcmc_params(rj)
+    bg0 = rjstruct.initial_bg(rj)
+    ref = oracle_port.run_batch(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, bg0, seed=21,
+                                threads=8, kind="port")
+    s = sampler.Sampler()
+    got = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=21, arith="exact", bg0=bg0)
+    assert (got["status"] == 0).all()
+    np.testing.assert_array_equal(got["final_n"], ref["final_n"])
+    np.testing.assert_array_equal(got["map_n"], ref["map_n"])
+    acc = got["counters"][:, 5:10].sum(axis=1)
+    np.testing.assert_array_equal(acc, ref["n_accepted"])
+
+
+def test_fast_batch_runs_and_agrees_in_distribution(cuda_lib):
+    b, rj = _c0(64, steps=1500)
+    p = rjstruct.mcmc_params(rj)
+    bg0 = rjstruct.initial_bg(rj)
+    s = sampler.Sampler()
+    ex = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=3, arith="exact", bg0=bg0)
+    fa = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=3, arith="fast", bg0=bg0)
+    assert (fa["status"] == 0).all() and (fa["overflow"] == 0).all()
+    # same uniforms: most chains follow the exact chain to the end
+    agree = np.mean(fa["map_n"] == ex["map_n"])
+    assert agree > 0.7, agree
+    assert abs(fa["map_n"].mean() - b.true_n.mean()) < 1.0
