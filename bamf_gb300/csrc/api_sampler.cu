@@ -216,19 +216,30 @@ static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, Samp
                                 int arith, cudaStream_t s)
 {
     bamf_status r;
-    if ((r = ws->queue.ensure(sizeof(int32_t)))) return r;
-    B.queue = (int32_t *)ws->queue.p;
-    CU(cudaMemsetAsync(ws->queue.p, 0, sizeof(int32_t), s));
     bool exact = arith == BAMF_ARITH_EXACT;
-    int wpb = 4;
-    int per_sm = exact ? blocks_per_sm_exact(B.side_max, wpb) : blocks_per_sm_fast(B.side_max, wpb);
-    if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
-    int need = (B.n_rois + wpb - 1) / wpb;
-    int blocks = std::min(need, per_sm * sm_count());
-    if (blocks < 1) return BAMF_OK;
-    cudaError_t e = exact ? launch_rjmcmc_exact(K, B, B.side_max, blocks, wpb, s)
-                          : launch_rjmcmc_fast(K, B, B.side_max, blocks, wpb, s);
-    if (e != cudaSuccess) return cuda_fail(e, "rjmcmc kernel launch");
+    const int wpb = 4;
+    int ncls = B.class_range ? BAMF_N_CLASSES : 1;
+    if ((r = ws->queue.ensure(sizeof(int32_t) * BAMF_N_CLASSES))) return r;
+    CU(cudaMemsetAsync(ws->queue.p, 0, sizeof(int32_t) * BAMF_N_CLASSES, s));
+    int sms = sm_count();
+    for (int c = ncls - 1; c >= 0; --c) {
+        SamplerBatch Bc = B;
+        Bc.queue = (int32_t *)ws->queue.p + c;
+        Bc.cls = c;
+        if (B.class_range) {
+            int lo = c == 0 ? 1 : class_side(c - 1) + 1; /* smallest side of class c */
+            if (lo > B.side_max) continue;                /* no ROI of the batch is that large */
+            Bc.side_max = std::min(class_side(c), B.side_max);
+        }
+        int per_sm = exact ? blocks_per_sm_exact(Bc.side_max, wpb) : blocks_per_sm_fast(Bc.side_max, wpb);
+        if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
+        int need = (B.n_rois + wpb - 1) / wpb;
+        int blocks = std::min(need, per_sm * sms);
+        if (blocks < 1) return BAMF_OK;
+        cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, s)
+                              : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, s);
+        if (e != cudaSuccess) return cuda_fail(e, "rjmcmc kernel launch");
+    }
     return BAMF_OK;
 }
 
@@ -263,31 +274,33 @@ __global__ void map_n_kernel(const uint8_t *__restrict__ trace, int trace_cap,
     }
 }
 
-/* Counting sort of ROI ids by side, largest first (one block): the longest
- * chains start first so the persistent warps finish together. */
+/* Counting sort of ROI ids by size class, largest class first (one
+ * block), and the [begin, end) range of every class in the sorted order. */
 __global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__restrict__ ys,
-                            int n, int32_t *__restrict__ order)
+                             int n, int32_t *__restrict__ order, int32_t *__restrict__ class_range)
 {
-    __shared__ int cnt[BAMF_MAX_ROI_SIDE + 2];
-    __shared__ int pos[BAMF_MAX_ROI_SIDE + 2];
-    for (int k = threadIdx.x; k < BAMF_MAX_ROI_SIDE + 2; k += blockDim.x) cnt[k] = 0;
+    __shared__ int cnt[BAMF_N_CLASSES];
+    __shared__ int pos[BAMF_N_CLASSES];
+    if (threadIdx.x < BAMF_N_CLASSES) cnt[threadIdx.x] = 0;
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        int s = min(max(max(xs[i], ys[i]), 0), BAMF_MAX_ROI_SIDE + 1);
-        atomicAdd(&cnt[s], 1);
+        int c = side_class(min(max(max(xs[i], ys[i]), 1), BAMF_MAX_ROI_SIDE));
+        atomicAdd(&cnt[c], 1);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         int acc = 0;
-        for (int s = BAMF_MAX_ROI_SIDE + 1; s >= 0; --s) {
-            pos[s] = acc;
-            acc += cnt[s];
+        for (int c = BAMF_N_CLASSES - 1; c >= 0; --c) {
+            pos[c] = acc;
+            class_range[2 * c] = acc;
+            acc += cnt[c];
+            class_range[2 * c + 1] = acc;
         }
     }
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        int s = min(max(max(xs[i], ys[i]), 0), BAMF_MAX_ROI_SIDE + 1);
-        order[atomicAdd(&pos[s], 1)] = i;
+        int c = side_class(min(max(max(xs[i], ys[i]), 1), BAMF_MAX_ROI_SIDE));
+        order[atomicAdd(&pos[c], 1)] = i;
     }
 }
 
@@ -331,10 +344,13 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     B.counters = out->counters;
     B.status = out->status;
     B.overflow = out->overflow;
-    if ((r = ws->order.ensure((size_t)n * sizeof(int32_t)))) return r;
-    B.order = (int32_t *)ws->order.p;
-    order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)ws->order.p);
+    B.llr_evals = out->llr_evals;
+    if ((r = ws->order.ensure((size_t)n * sizeof(int32_t) + 256))) return r;
+    B.order = (int32_t *)((char *)ws->order.p + 256);
+    int32_t *class_range = (int32_t *)ws->order.p; /* 2 * BAMF_N_CLASSES ints */
+    order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)B.order, class_range);
     CU(cudaGetLastError());
+    B.class_range = class_range;
     if (out->map_n) {
         if ((r = ws->trace.ensure((size_t)n * trace_cap))) return r;
         B.nsig_trace = (uint8_t *)ws->trace.p;
@@ -435,6 +451,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if (out->n_entries && (r = dalloc(o.v, &dout.n_entries, n))) return r;
     if (out->status && (r = dalloc(o.v, &dout.status, n))) return r;
     if (out->overflow && (r = dalloc(o.v, &dout.overflow, n))) return r;
+    if (out->llr_evals && (r = dalloc(o.v, &dout.llr_evals, n))) return r;
     if ((r = bamf_rjmcmc_batch_device(ws, &d, p, priors, seed, arith, &dout, nullptr))) return r;
     CU(cudaDeviceSynchronize());
     if ((r = download(out->map_n, dout.map_n, n))) return r;
@@ -444,6 +461,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if ((r = download(out->n_entries, dout.n_entries, n))) return r;
     if ((r = download(out->status, dout.status, n))) return r;
     if ((r = download(out->overflow, dout.overflow, n))) return r;
+    if ((r = download(out->llr_evals, dout.llr_evals, n))) return r;
     return BAMF_OK;
 }
 

@@ -1,0 +1,441 @@
+/*
+ * findroi.cu - the findROI front end (@RJ/findROI.m driving
+ * source/cuda/cuda_FindROI/cuda_FindROI.cu) for sm_103a.
+ *
+ * Frames arrive as MATLAB hands them over: Ysize x Xsize x Zsize floats,
+ * y fastest.  Like the reference kernels, the passes treat each frame as a
+ * row-major Ysize x Xsize array whose rows are the contiguous runs of Xsize
+ * floats; for square frames this is the MATLAB frame transposed, and the
+ * separable filter and the two 1-D maxima make the result the same.
+ *
+ * Passes (all on the device, no host round trip between them):
+ *   1. rows   - recursive Gaussian (Young & van Vliet, 3rd order) along the
+ *               contiguous rows, forward then backward, for sigma1 and
+ *               sigma2 from one read of the frame (cuda_FindROI.cu:10-46)
+ *   2. cols   - the same along the strided columns, both sigmas, then the
+ *               difference of Gaussians (:48-92); lanes own columns, so
+ *               every access is coalesced
+ *   3. rowmax - window max along rows with floor minval, +max / -max
+ *               (:94-117), window bounds formed in float over the stack's
+ *               linear index exactly as the reference does
+ *   4. colmax - window max of |.| along columns, flag where it equals the
+ *               pixel within 1e-6 (:119-147)
+ *   5. compaction of the flags in memory order (MATLAB find, findROI.m:125),
+ *      box corners (:130-148) and the ROI crop (:157-160)
+ * The recurrence is evaluated with explicit IEEE operations in the order
+ * nvcc gives the reference expression w0*B + (b1*w1 + b2*w2 + b3*w3)/b0:
+ *   q = fma(b3, w3, fma(b1, w1, b2*w2));  out = fma(w0, B, q / b0).
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "bamf.h"
+
+namespace {
+
+struct Coef {
+    float b0, b1, b2, b3, B;
+};
+
+/* findROI.m:169-182 in double; the kernel receives singles. */
+Coef iir_coef(double Sigma)
+{
+    double Q;
+    if (Sigma > 2.5)
+        Q = 0.98711 * Sigma - 0.96330;
+    else
+        Q = 3.97156 - 4.14554 * std::sqrt(1 - 0.26891 * Sigma);
+    double Qq = Q * Q, Qqq = Qq * Q;
+    double B0 = 1.57825 + 2.44413 * Q + 1.4281 * Qq + 0.422205 * Qqq;
+    double B1 = 2.44413 * Q + 2.85619 * Qq + 1.26661 * Qqq;
+    double B2 = -1.4281 * Qq - 1.26661 * Qqq;
+    double B3 = 0.422205 * Qqq;
+    double B = 1 - (B1 + B2 + B3) / B0;
+    return Coef{(float)B0, (float)B1, (float)B2, (float)B3, (float)B};
+}
+
+__device__ __forceinline__ float iir_step(float w0, float w1, float w2, float w3, const Coef &c)
+{
+    float q = __fmaf_rn(c.b3, w3, __fmaf_rn(c.b1, w1, __fmul_rn(c.b2, w2)));
+    return __fmaf_rn(w0, c.B, __fdiv_rn(q, c.b0));
+}
+
+/* Pass 1: one thread per (frame, row); both sigmas from one read of the row.
+ * out_a/out_b may alias nothing; the row is read through L1 as it is
+ * walked, and the backward pass re-reads the forward result it wrote. */
+__global__ void __launch_bounds__(128) rows_kernel(const float *__restrict__ in,
+                                                   float *__restrict__ out_a,
+                                                   float *__restrict__ out_b, int X, int Y, int Z,
+                                                   Coef ca, Coef cb)
+{
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)Y * Z) return;
+    int64_t base = t * X; /* row t of the stack = frame t / Y, row t % Y */
+    const float *src = in + base;
+    float *a = out_a + base, *b = out_b + base;
+    float a1, a2, a3, b1, b2, b3;
+    float v0 = src[0];
+    a1 = a2 = a3 = v0;
+    b1 = b2 = b3 = v0;
+    for (int i = 0; i < X; ++i) {
+        float w0 = src[i];
+        float ta = iir_step(w0, a1, a2, a3, ca);
+        float tb = iir_step(w0, b1, b2, b3, cb);
+        a[i] = ta;
+        b[i] = tb;
+        a3 = a2; a2 = a1; a1 = ta;
+        b3 = b2; b2 = b1; b1 = tb;
+    }
+    a1 = a2 = a3 = a[X - 1];
+    b1 = b2 = b3 = b[X - 1];
+    for (int i = X - 1; i >= 0; --i) {
+        float ta = iir_step(a[i], a1, a2, a3, ca);
+        float tb = iir_step(b[i], b1, b2, b3, cb);
+        a[i] = ta;
+        b[i] = tb;
+        a3 = a2; a2 = a1; a1 = ta;
+        b3 = b2; b2 = b1; b1 = tb;
+    }
+}
+
+/* Pass 2: one thread per (frame, column): column filters of both images in
+ * place, then dog = a - b written over a. */
+__global__ void __launch_bounds__(128) cols_kernel(float *__restrict__ a, float *__restrict__ b,
+                                                   int X, int Y, int Z, Coef ca, Coef cb)
+{
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)X * Z) return;
+    int64_t z = t / X, c = t - z * X;
+    float *pa = a + z * (int64_t)X * Y + c, *pb = b + z * (int64_t)X * Y + c;
+    float a1, a2, a3, b1, b2, b3;
+    a1 = a2 = a3 = pa[0];
+    b1 = b2 = b3 = pb[0];
+    for (int i = 0; i < Y; ++i) {
+        float ta = iir_step(pa[(int64_t)i * X], a1, a2, a3, ca);
+        float tb = iir_step(pb[(int64_t)i * X], b1, b2, b3, cb);
+        pa[(int64_t)i * X] = ta;
+        pb[(int64_t)i * X] = tb;
+        a3 = a2; a2 = a1; a1 = ta;
+        b3 = b2; b2 = b1; b1 = tb;
+    }
+    a1 = a2 = a3 = pa[(int64_t)(Y - 1) * X];
+    b1 = b2 = b3 = pb[(int64_t)(Y - 1) * X];
+    for (int i = Y - 1; i >= 0; --i) {
+        float ta = iir_step(pa[(int64_t)i * X], a1, a2, a3, ca);
+        float tb = iir_step(pb[(int64_t)i * X], b1, b2, b3, cb);
+        pa[(int64_t)i * X] = __fsub_rn(ta, tb); /* kernel_subtract */
+        a3 = a2; a2 = a1; a1 = ta;
+        b3 = b2; b2 = b1; b1 = tb;
+    }
+}
+
+/* Pass 3: kernel_maxX on the DoG stack. Window bounds as the reference forms
+ * them: (int)((fmaxf(0, c-k) + (float)(X*row)) + (float)(X*Y*frame)).  An
+ * index past the stack's end (possible only for the very last row) is left
+ * out of the max (the reference reads beyond its buffer there). */
+__global__ void __launch_bounds__(256) rowmax_kernel(const float *__restrict__ dog,
+                                                     float *__restrict__ out, int X, int Y, int Z,
+                                                     int k, float minval)
+{
+    int64_t n = (int64_t)X * Y * Z;
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    int64_t row = idx / X;              /* global row = frame*Y + r */
+    int c = (int)(idx - row * X);
+    int64_t z = row / Y;
+    int r = (int)(row - z * Y);
+    float lo = fmaxf(0.0f, (float)(c - k));
+    float hi = fminf((float)(X - 1), (float)(c + k));
+    float rb = __uint2float_rn((unsigned)X * (unsigned)r);
+    float zb = __uint2float_rn((unsigned)X * (unsigned)Y * (unsigned)z);
+    int64_t start = (int64_t)__fadd_rn(__fadd_rn(lo, rb), zb);
+    int64_t end = (int64_t)__fadd_rn(__fadd_rn(hi, rb), zb);
+    if (end > n - 1) end = n - 1;
+    float maxval = minval;
+    for (int64_t i = start; i <= end; ++i) maxval = fmaxf(maxval, __ldg(&dog[i]));
+    float inpixel = dog[idx];
+    out[idx] = maxval > inpixel ? -maxval : (maxval == inpixel ? maxval : 0.0f);
+}
+
+/* Pass 4: kernel_maxY; writes 1-byte flags. */
+__global__ void __launch_bounds__(256) colmax_kernel(const float *__restrict__ rm,
+                                                     uint8_t *__restrict__ flags, int X, int Y,
+                                                     int Z, int k, float minval)
+{
+    int64_t n = (int64_t)X * Y * Z;
+    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    int64_t row = idx / X;
+    int c = (int)(idx - row * X);
+    int64_t z = row / Y;
+    int r = (int)(row - z * Y);
+    int start = (int)fmaxf(0.0f, (float)(r - k));
+    int end = (int)fminf((float)(Y - 1), (float)(r + k));
+    const float *col = rm + z * (int64_t)X * Y + c;
+    float maxval = minval;
+    for (int i = start; i <= end; ++i) maxval = fmaxf(maxval, fabsf(__ldg(&col[(int64_t)i * X])));
+    float inpixel = rm[idx];
+    flags[idx] = (double)fabsf(__fsub_rn(maxval, inpixel)) < 1e-6 ? 1 : 0;
+}
+
+/* Compaction, phase 1: flags per 1024-pixel chunk. */
+__global__ void __launch_bounds__(256) count_kernel(const uint8_t *__restrict__ flags, int64_t n,
+                                                    int32_t *__restrict__ counts)
+{
+    __shared__ int s;
+    if (threadIdx.x == 0) s = 0;
+    __syncthreads();
+    int64_t base = (int64_t)blockIdx.x * 1024;
+    int local = 0;
+    for (int i = threadIdx.x; i < 1024; i += 256) {
+        int64_t j = base + i;
+        if (j < n) local += flags[j];
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&s, local);
+    __syncthreads();
+    if (threadIdx.x == 0) counts[blockIdx.x] = s;
+}
+
+/* phase 2: exclusive scan of the chunk counts (one block, serial tiles). */
+__global__ void scan_kernel(int32_t *__restrict__ counts, int64_t nchunks,
+                            int64_t *__restrict__ total)
+{
+    __shared__ int64_t carry;
+    __shared__ int64_t warp_sums[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t b0 = 0; b0 < nchunks; b0 += blockDim.x) {
+        int64_t i = b0 + threadIdx.x;
+        int64_t v = i < nchunks ? counts[i] : 0;
+        int64_t x = v;
+        int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t t = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += t;
+        }
+        if (lane == 31) warp_sums[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int64_t s = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int64_t t = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += t;
+            }
+            warp_sums[lane] = s;
+        }
+        __syncthreads();
+        int64_t incl = x + (w > 0 ? warp_sums[w - 1] : 0) + carry;
+        if (i < nchunks) counts[i] = (int32_t)(incl - v);
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+/* phase 3: write the flagged pixels of each chunk in memory order as MATLAB
+ * 1-based (row, col, frame) = ind2sub([Ysize Xsize Zsize], m+1), plus the
+ * clamped box corners of findROI.m:130-148. */
+__global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ flags, int64_t n,
+                                                   const int32_t *__restrict__ offs, int Ysz,
+                                                   int Xsz, int box, int64_t capacity,
+                                                   int32_t *__restrict__ coords,
+                                                   int32_t *__restrict__ corners)
+{
+    __shared__ int wsum[8];
+    int64_t base = (int64_t)blockIdx.x * 1024;
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    /* each thread owns 4 consecutive pixels: keeps memory order */
+    int64_t j0 = base + threadIdx.x * 4;
+    int f[4], cnt = 0;
+    for (int q = 0; q < 4; ++q) {
+        int64_t j = j0 + q;
+        f[q] = (j < n) ? flags[j] : 0;
+        cnt += f[q];
+    }
+    int x = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += t;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    int before = 0;
+    for (int i = 0; i < w; ++i) before += wsum[i];
+    int64_t pos = (int64_t)offs[blockIdx.x] + before + x - cnt;
+    const int half = (int)floor(box / 2.0 + 0.5);
+    for (int q = 0; q < 4; ++q) {
+        if (!f[q]) continue;
+        if (pos < capacity) {
+            int64_t m = j0 + q;
+            int64_t plane = (int64_t)Ysz * Xsz;
+            int kk = (int)(m / plane);
+            int64_t rem = m - (int64_t)kk * plane;
+            int jj = (int)(rem / Ysz);
+            int ii = (int)(rem - (int64_t)jj * Ysz);
+            int Ii = ii + 1, Jj = jj + 1, Kk = kk + 1;
+            coords[3 * pos + 0] = Ii;
+            coords[3 * pos + 1] = Jj;
+            coords[3 * pos + 2] = Kk;
+            if (corners) {
+                int sr = Ii - half + 1, sc = Jj - half + 1;
+                bool mr = sr < 1, mc = sc < 1;
+                if (mr) sr = 1;
+                if (mc) sc = 1;
+                int er = mr ? box : sr + box - 1;
+                int ec = mc ? box : sc + box - 1;
+                if (er > Ysz) sr = Ysz - box + 1;
+                if (ec > Xsz) sc = Xsz - box + 1;
+                corners[2 * pos + 0] = sr; /* YBoxCorner = StartRow */
+                corners[2 * pos + 1] = sc; /* XBoxCorner = StartCol */
+            }
+        }
+        pos++;
+    }
+}
+
+/* ROI crop (findROI.m:157-160): ROIStack(:,:,b) = Image(rows, cols, Kk). */
+__global__ void crop_kernel(const float *__restrict__ frames, int Ysz, int Xsz,
+                            const int32_t *__restrict__ coords, const int32_t *__restrict__ corners,
+                            const int64_t *__restrict__ count, int box, float *__restrict__ stack,
+                            int64_t capacity)
+{
+    int64_t nroi = *count < capacity ? *count : capacity;
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t per = (int64_t)box * box;
+    if (t >= nroi * per) return;
+    int64_t b = t / per;
+    int p = (int)(t - b * per);
+    int col = p / box, row = p - col * box;
+    int sr = corners[2 * b], sc = corners[2 * b + 1], kk = coords[3 * b + 2];
+    int64_t src = (int64_t)(sr - 1 + row) + (int64_t)(sc - 1 + col) * Ysz + (int64_t)(kk - 1) * Ysz * Xsz;
+    stack[t] = frames[src];
+}
+
+struct Scratch {
+    void *p = nullptr;
+    size_t n = 0;
+    ~Scratch()
+    {
+        if (p) cudaFree(p);
+    }
+    bool ensure(size_t bytes)
+    {
+        if (bytes <= n) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) return false;
+        n = bytes;
+        return true;
+    }
+};
+
+bamf_status launch_err()
+{
+    return cudaGetLastError() == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;
+}
+
+}  // namespace
+
+struct bamf_findroi_ws {
+    Scratch a, b, flags, chunks, total;
+};
+
+extern "C" bamf_status bamf_findroi_workspace_create(bamf_findroi_ws **ws)
+{
+    if (!ws) return BAMF_ERR_INVALID_ARG;
+    *ws = new bamf_findroi_ws();
+    return BAMF_OK;
+}
+
+extern "C" void bamf_findroi_workspace_destroy(bamf_findroi_ws *ws) { delete ws; }
+
+extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *frames, int ysize,
+                                            int xsize, int zsize, double sigma1, double sigma2,
+                                            int boxsize, float minval, int64_t capacity,
+                                            int32_t *coords, int32_t *corners, float *roi_stack,
+                                            int64_t *count, uint8_t *flags_out, void *stream)
+{
+    if (!ws || !frames || !coords || !count || ysize < 1 || xsize < 1 || zsize < 1 || boxsize < 1 ||
+        capacity < 0)
+        return BAMF_ERR_INVALID_ARG;
+    if ((roi_stack != nullptr) && corners == nullptr) return BAMF_ERR_INVALID_ARG;
+    if (xsize > ysize * 64 || ysize > xsize * 64) return BAMF_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t n = (int64_t)xsize * ysize * zsize;
+    /* kernel view (as the reference launches it): each frame is KY = Ysize
+     * runs of KX = Xsize contiguous floats (size(Image,2), findROI.m:186-189) */
+    const int KX = xsize, KY = ysize;
+    Coef ca = iir_coef(sigma1), cb = iir_coef(sigma2);
+    if (!ws->a.ensure(n * sizeof(float)) || !ws->b.ensure(n * sizeof(float))) return BAMF_ERR_CUDA;
+    uint8_t *flags = flags_out;
+    if (!flags) {
+        if (!ws->flags.ensure(n)) return BAMF_ERR_CUDA;
+        flags = (uint8_t *)ws->flags.p;
+    }
+    int64_t nchunks = (n + 1023) / 1024;
+    if (!ws->chunks.ensure(nchunks * sizeof(int32_t)) || !ws->total.ensure(sizeof(int64_t)))
+        return BAMF_ERR_CUDA;
+    float *A = (float *)ws->a.p, *Bb = (float *)ws->b.p;
+    int64_t nrows = (int64_t)KY * zsize, ncols = (int64_t)KX * zsize;
+    rows_kernel<<<(unsigned)((nrows + 127) / 128), 128, 0, s>>>(frames, A, Bb, KX, KY, zsize, ca, cb);
+    cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(A, Bb, KX, KY, zsize, ca, cb);
+    rowmax_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, Bb, KX, KY, zsize, boxsize, minval);
+    colmax_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Bb, flags, KX, KY, zsize, boxsize, minval);
+    count_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
+    scan_kernel<<<1, 1024, 0, s>>>((int32_t *)ws->chunks.p, nchunks, (int64_t *)ws->total.p);
+    emit_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p, ysize, xsize,
+                                                  boxsize, capacity, coords, corners);
+    if (cudaMemcpyAsync(count, ws->total.p, sizeof(int64_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+        return BAMF_ERR_CUDA;
+    if (roi_stack) {
+        int64_t work = capacity * boxsize * boxsize;
+        if (work > 0)
+            crop_kernel<<<(unsigned)((work + 255) / 256), 256, 0, s>>>(frames, ysize, xsize, coords, corners,
+                                                                      (int64_t *)ws->total.p, boxsize,
+                                                                      roi_stack, capacity);
+    }
+    return launch_err();
+}
+
+extern "C" bamf_status bamf_find_roi_host(const float *frames, int ysize, int xsize, int zsize,
+                                          double sigma1, double sigma2, int boxsize, float minval,
+                                          int64_t capacity, int32_t *coords, int32_t *corners,
+                                          float *roi_stack, int64_t *count)
+{
+    if (!frames || !coords || !count || ysize < 1 || xsize < 1 || zsize < 1 || boxsize < 1 || capacity < 0)
+        return BAMF_ERR_INVALID_ARG;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    bamf_findroi_ws ws;
+    const int64_t n = (int64_t)xsize * ysize * zsize;
+    Scratch dframes, dcoords, dcorners, dstack, dcount;
+    int64_t cap = capacity > 0 ? capacity : 1;
+    if (!dframes.ensure(n * sizeof(float)) || !dcoords.ensure(cap * 3 * sizeof(int32_t)) ||
+        !dcorners.ensure(cap * 2 * sizeof(int32_t)) || !dcount.ensure(sizeof(int64_t)))
+        return BAMF_ERR_CUDA;
+    if (roi_stack && !dstack.ensure(cap * boxsize * boxsize * sizeof(float))) return BAMF_ERR_CUDA;
+    if (cudaMemcpy(dframes.p, frames, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+        return BAMF_ERR_CUDA;
+    bamf_status r = bamf_find_roi_device(&ws, (float *)dframes.p, ysize, xsize, zsize, sigma1, sigma2,
+                                         boxsize, minval, capacity, (int32_t *)dcoords.p,
+                                         (int32_t *)dcorners.p, roi_stack ? (float *)dstack.p : nullptr,
+                                         (int64_t *)dcount.p, nullptr, nullptr);
+    if (r) return r;
+    if (cudaDeviceSynchronize() != cudaSuccess) return BAMF_ERR_CUDA;
+    int64_t c = 0;
+    cudaMemcpy(&c, dcount.p, sizeof c, cudaMemcpyDeviceToHost);
+    *count = c;
+    int64_t m = c < capacity ? c : capacity;
+    if (m > 0) {
+        cudaMemcpy(coords, dcoords.p, m * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        if (corners) cudaMemcpy(corners, dcorners.p, m * 2 * sizeof(int32_t), cudaMemcpyDeviceToHost);
+        if (roi_stack)
+            cudaMemcpy(roi_stack, dstack.p, m * boxsize * boxsize * sizeof(float), cudaMemcpyDeviceToHost);
+    }
+    return cudaGetLastError() == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;
+}

@@ -1,0 +1,70 @@
+/*
+ * probe.cu - throughput probes for the sampler's roofline denominators:
+ * FP32 FMA and MUFU log2 issue rates of the current device, measured with
+ * independent chains so the pipes, not latency, set the rate.
+ */
+#include <cuda_runtime.h>
+
+#include "bamf.h"
+
+namespace {
+
+__global__ void fma_probe(float *out, int iters, float a, float b)
+{
+    float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+        x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+    }
+    float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+    if (s == 12345.678f) out[blockIdx.x] = s;
+}
+
+__global__ void mufu_probe(float *out, int iters)
+{
+    float x0 = 1.5f + threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    for (int i = 0; i < iters; ++i) {
+        x0 = __log2f(x0) + 2.0f; x1 = __log2f(x1) + 2.0f;
+        x2 = __log2f(x2) + 2.0f; x3 = __log2f(x3) + 2.0f;
+    }
+    float s = x0 + x1 + x2 + x3;
+    if (s == 12345.678f) out[blockIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" bamf_status bamf_probe_peaks(double *fp32_flops, double *mufu_ops)
+{
+    if (!fp32_flops || !mufu_ops) return BAMF_ERR_INVALID_ARG;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return BAMF_ERR_NO_DEVICE;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    float *out = nullptr;
+    if (cudaMalloc(&out, 65536 * sizeof(float)) != cudaSuccess) return BAMF_ERR_CUDA;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int blocks = sms * 8, threads = 256;
+    const int it_fma = 4096, it_mufu = 2048;
+    float ms = 0.0f;
+    fma_probe<<<blocks, threads>>>(out, 16, 1.0001f, 0.5f); /* warm-up */
+    cudaEventRecord(e0);
+    fma_probe<<<blocks, threads>>>(out, it_fma, 1.0001f, 0.5f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    *fp32_flops = 2.0 * 8.0 * it_fma * (double)blocks * threads / (ms * 1e-3);
+    mufu_probe<<<blocks, threads>>>(out, 16);
+    cudaEventRecord(e0);
+    mufu_probe<<<blocks, threads>>>(out, it_mufu);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    *mufu_ops = 4.0 * it_mufu * (double)blocks * threads / (ms * 1e-3);
+    cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    return err == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;
+}

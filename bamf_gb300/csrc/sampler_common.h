@@ -60,13 +60,26 @@ struct SamplerBatch {
     uint32_t *uniforms_used;      /* [roi]                                 */
     int32_t *status;              /* [roi] 0 ok, else BAMF_ERR_*           */
     int32_t *overflow;            /* [roi] proposals rejected at BAMF_NMAX */
+    int32_t *llr_evals;           /* [roi] likelihood-ratio evaluations     */
     float *pgrid;                 /* [roi][grid_stride] or null            */
     float *pback;
     int64_t grid_stride;
     /* full chain recording (exact cRJMCMC outputs), or null */
     bamf_chain *chains;           /* device array [roi][2] of bamf_chain with device pointers */
     int32_t *queue;               /* work-queue counter (device int)       */
+    /* size-class scheduling: when class_range is set, this launch runs the
+     * ROIs order[class_range[2c] .. class_range[2c+1]) of class c = cls */
+    const int32_t *class_range;
+    int32_t cls;
 };
+
+/* Size classes by ROI side: (0,8] (8,12] (12,16] (16,20] (20,24] (24,28] (28,32]. */
+#define BAMF_N_CLASSES 7
+__host__ __device__ inline int side_class(int side)
+{
+    return side <= 8 ? 0 : (side <= 12 ? 1 : (side <= 16 ? 2 : (side <= 20 ? 3 : (side <= 24 ? 4 : (side <= 28 ? 5 : 6)))));
+}
+__host__ __device__ inline int class_side(int c) { return c == 0 ? 8 : 8 + 4 * c; }
 
 }  // namespace bamf
 

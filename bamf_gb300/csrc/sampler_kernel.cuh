@@ -94,6 +94,7 @@ struct ChainWarp {
     int roi;
     /* geometry */
     int X, Y, npix;
+    int px_dx, px_dy; /* pixel p -> p+32 moves x by px_dx and y by px_dy (then wraps) */
     float sigma, Cst, MeanN;
     /* shared memory */
     float *D, *M, *Mt, *E, *scm, *NX, *NY, *NXa, *NYa, *logM;
@@ -118,6 +119,7 @@ struct ChainWarp {
     float P[8];
     int entries;
     int overflow;
+    int n_llr;
     /* incremental-model bookkeeping (fast mode) */
     uint32_t a_dirty, t_dirty;
     int removed;
@@ -233,23 +235,31 @@ struct ChainWarp {
 
     /* ---------------------------------------------------- prior tables */
     /* Stat::findPDF (:219-246): first grid node strictly above I. */
-    __device__ float findPDF(const DevStat &s, float I) const
+    __device__ __forceinline__ float findPDF(const DevStat &s, float I) const
     {
         const float *x = s.x;
         float xl = __ldg(&x[s.L - 1]);
         if (I >= xl || I <= 0.0f || I != I) return 0.0f;
-        int lo = 0, hi = s.L - 1;
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (__ldg(&x[mid]) > I) hi = mid; else lo = mid;
-        }
-        int j = hi;
+        /* the grid is x[i] = x[i-1] + DX: guess from I / DX, then move to
+         * the first node strictly above I (what the linear scan finds) */
+        float x1 = __ldg(&x[1]);
+        int j = min(max((int)(I / x1) + 1, 1), s.L - 1);
         float xj = __ldg(&x[j]), xj1 = __ldg(&x[j - 1]);
+        while (j > 1 && xj1 > I) {
+            --j;
+            xj = xj1;
+            xj1 = __ldg(&x[j - 1]);
+        }
+        while (j < s.L - 1 && !(xj > I)) {
+            ++j;
+            xj1 = xj;
+            xj = __ldg(&x[j]);
+        }
         return (__ldg(&s.pdf[j]) * (I - xj1) + __ldg(&s.pdf[j - 1]) * (xj - I)) /
-               (__ldg(&x[1]) - __ldg(&x[0]));
+               (x1 - __ldg(&x[0]));
     }
     /* Stat::genRand (:248-282). */
-    __device__ float genRand(const DevStat &s)
+    __device__ __forceinline__ float genRand(const DevStat &s)
     {
         float R = urand();
         if (R <= 0.0f) return 0.0f;
@@ -294,7 +304,7 @@ struct ChainWarp {
         return __ffs(m) - 1;
     }
     /* Emitters::closest (:525-558). */
-    __device__ int closest(int jj, float dmin)
+    __device__ __forceinline__ int closest(int jj, float dmin)
     {
         uint32_t m = near_mask(jj, dmin);
         int num = __popc(m);
@@ -309,7 +319,7 @@ struct ChainWarp {
         return nth_bit(others, mm);
     }
     /* Emitters::closestMulti (:615-650); picks go to cl[] in pick order. */
-    __device__ int closestMulti(int jj, float dmin)
+    __device__ __forceinline__ int closestMulti(int jj, float dmin)
     {
         uint32_t m = near_mask(jj, dmin);
         int num = __popc(m);
@@ -334,7 +344,7 @@ struct ChainWarp {
 
     /* ------------------------------------------------------------ model */
     /* Stencil + Model (:15-59) of a lane-distributed state, into out[]. */
-    __device__ void model_full(int n, float I, float Xv, float Yv, float BG, float ABG, float BBG,
+    __device__ __forceinline__ void model_full(int n, float I, float Xv, float Yv, float BG, float ABG, float BBG,
                                float *out, float *nx, float *ny)
     {
         int totx = n * X, toty = n * Y;
@@ -358,17 +368,23 @@ struct ChainWarp {
                                         MT::erf_(((float)y - Yk) * Cst));
         }
         __syncwarp();
+        int x = lane / Y, y = lane - (lane / Y) * Y;
         for (int p = lane; p < npix; p += 32) {
-            int x = p / Y, y = p - x * Y;
             float m = BG + ABG * (float)x + BBG * (float)y + scm[p];
             for (int k = 0; k < n; ++k) m += nx[k * X + x] * ny[k * Y + y];
             out[p] = m;
+            x += px_dx;
+            y += px_dy;
+            if (y >= Y) {
+                y -= Y;
+                x++;
+            }
         }
         __syncwarp();
     }
 
     /* Stencil rows of the dirty T slots into NX/NY (fast mode). */
-    __device__ void stencils_dirty(uint32_t mask)
+    __device__ __forceinline__ void stencils_dirty(uint32_t mask)
     {
         int nd = __popc(mask);
         int totx = nd * X, toty = nd * Y;
@@ -397,8 +413,9 @@ struct ChainWarp {
     }
 
     /* likelihood_ratio (:1650-1686).  M always holds Model(A). */
-    __device__ float llr()
+    __device__ __forceinline__ float llr()
     {
+        n_llr++;
         if (EXACT) {
             model_full(tn, tI, tX, tY, tBG, tABG, tBBG, Mt, NX, NY);
             for (int p = lane; p < npix; p += 32)
@@ -416,8 +433,8 @@ struct ChainWarp {
             float dBG = tBG - aBG, dABG = tABG - aABG, dBBG = tBBG - aBBG;
             uint32_t am = a_dirty, tm = t_dirty;
             float acc = 0.0f;
+            int x = lane / Y, y = lane - (lane / Y) * Y;
             for (int p = lane; p < npix; p += 32) {
-                int x = p / Y, y = p - x * Y;
                 float d = dBG + dABG * (float)x + dBBG * (float)y;
                 uint32_t m1 = am;
                 while (m1) {
@@ -436,6 +453,12 @@ struct ChainWarp {
                 Mt[p] = mt;
                 E[p] = lmt;
                 acc += D[p] * (lmt - logM[p]) * 0.69314718f - d;
+                x += px_dx;
+                y += px_dy;
+                if (y >= Y) {
+                    y -= Y;
+                    x++;
+                }
             }
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(BAMF_FULL, acc, o);
             return MT::exp_(acc);
@@ -444,7 +467,7 @@ struct ChainWarp {
 
     /* fast mode: fold the accepted proposal into M, log2 M and the
      * stencil cache of A */
-    __device__ void commit_fast()
+    __device__ __forceinline__ void commit_fast()
     {
         for (int p = lane; p < npix; p += 32) {
             M[p] = Mt[p];
@@ -467,7 +490,7 @@ struct ChainWarp {
         __syncwarp();
     }
 
-    __device__ void accept_T()
+    __device__ __forceinline__ void accept_T()
     {
         if (!EXACT) commit_fast();
         an = tn; aI = tI; aX = tX; aY = tY; aS = tS;
@@ -480,7 +503,7 @@ struct ChainWarp {
     }
 
     /* Full rebuild of M (and, in fast mode, log2 M and A's stencil cache). */
-    __device__ void rebuild_model()
+    __device__ __forceinline__ void rebuild_model()
     {
         if (EXACT) {
             model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NX, NY);
@@ -492,7 +515,7 @@ struct ChainWarp {
     }
 
     /* ------------------------------------------------------- recording */
-    __device__ void record_one(int w, int n, float I, float x, float y, int s, float BG, float ABG,
+    __device__ __forceinline__ void record_one(int w, int n, float I, float x, float y, int s, float BG, float ABG,
                                float BBG, float LLR, float PR, int type, int acc)
     {
         bamf_chain *ch = &B->chains[2 * roi + w];
@@ -522,7 +545,7 @@ struct ChainWarp {
     }
 
     /* RJMCMCChain::addEmitters on Chain (A) and Chain_Test (T). */
-    __device__ void record2(float LLR, float PR, int type, int acc)
+    __device__ __forceinline__ void record2(float LLR, float PR, int type, int acc)
     {
         if (B->nsig_trace && entries < B->trace_cap) {
             int ns = __popc(__ballot_sync(BAMF_FULL, lane < an && aS == 1));
@@ -536,7 +559,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::update_grids (:1629-1648). */
-    __device__ void update_grids()
+    __device__ __forceinline__ void update_grids()
     {
         if (is_burnin || !B->pgrid) return;
         int Z = K->p.Grid_Zoom;
@@ -558,7 +581,7 @@ struct ChainWarp {
 
     /* ------------------------------------------------------------ moves */
     /* RJMCMC::jump (:752-970). */
-    __device__ void mv_jump()
+    __device__ __forceinline__ void mv_jump()
     {
         cinc(C_N_jump);
         int type = 1;
@@ -695,7 +718,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::split (:972-1109). */
-    __device__ void mv_split()
+    __device__ __forceinline__ void mv_split()
     {
         const int type = 4;
         cinc(C_N_split);
@@ -749,7 +772,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::merge (:1111-1255). */
-    __device__ void mv_merge()
+    __device__ __forceinline__ void mv_merge()
     {
         const int type = 5;
         cinc(C_N_merge);
@@ -818,7 +841,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::find_Birth (:1688-1736); PixProb is overwritten with 1. */
-    __device__ void find_birth(float *bx, float *by)
+    __device__ __forceinline__ void find_birth(float *bx, float *by)
     {
         float total;
         if (EXACT) {
@@ -866,7 +889,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::birth (:1258-1330). */
-    __device__ void mv_birth()
+    __device__ __forceinline__ void mv_birth()
     {
         const int type = 6;
         cinc(C_N_birth);
@@ -911,7 +934,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::death (:1332-1387). */
-    __device__ void mv_death()
+    __device__ __forceinline__ void mv_death()
     {
         const int type = 7;
         cinc(C_N_death);
@@ -938,7 +961,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::gSplit (:1389-1485). */
-    __device__ void mv_gsplit()
+    __device__ __forceinline__ void mv_gsplit()
     {
         const int type = 8;
         if (an < 2) return;
@@ -1001,7 +1024,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::gMerge (:1487-1584). */
-    __device__ void mv_gmerge()
+    __device__ __forceinline__ void mv_gmerge()
     {
         const int type = 9;
         if (an < 3) return;
@@ -1058,7 +1081,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::backFore (:1586-1627). */
-    __device__ void mv_backfore()
+    __device__ __forceinline__ void mv_backfore()
     {
         if (an == 0) return;
         if (K->p.IsBackg == 0) return;
@@ -1087,7 +1110,7 @@ struct ChainWarp {
         if (lane == nn) aS = ns;
     }
 
-    __device__ void step(const float *V, const float *W, float t)
+    __device__ __forceinline__ void step(const float *V, const float *W, float t)
     {
         /* dispatch of start_Chain (:693-717, :725-748); W = this phase's
          * cumulative vector, V = PV_Burnin for the gSplit/gMerge slots */
@@ -1102,7 +1125,7 @@ struct ChainWarp {
     }
 
     /* RJMCMC::start_Chain (:685-750). */
-    __device__ void run_chain()
+    __device__ __forceinline__ void run_chain()
     {
         const bamf_mcmc_params &p = K->p;
         is_burnin = 1;
@@ -1146,17 +1169,24 @@ __global__ void __launch_bounds__(128) rjmcmc_kernel(const __grid_constant__ Sam
     w.K = Kp;
     w.B = Bp;
     w.lane = lane;
+    int q_begin = 0, q_end = Bt.n_rois;
+    if (Bt.class_range) {
+        q_begin = Bt.class_range[2 * Bt.cls];
+        q_end = Bt.class_range[2 * Bt.cls + 1];
+    }
     for (;;) {
         int slot = 0;
-        if (lane == 0) slot = atomicAdd(Bt.queue, 1);
+        if (lane == 0) slot = q_begin + atomicAdd(Bt.queue, 1);
         slot = __shfl_sync(BAMF_FULL, slot, 0);
-        if (slot >= Bt.n_rois) break;
+        if (slot >= q_end) break;
         int roi = Bt.order ? Bt.order[slot] : slot;
         w.roi = roi;
         int X = Bt.xsize[roi], Y = Bt.ysize[roi];
         w.X = X;
         w.Y = Y;
         w.npix = X * Y;
+        w.px_dx = 32 / Y;
+        w.px_dy = 32 - (32 / Y) * Y;
         int npix_max = Bt.side_max * Bt.side_max;
         int nxs = BAMF_NMAX * Bt.side_max;
         w.D = sw;
@@ -1218,6 +1248,7 @@ __global__ void __launch_bounds__(128) rjmcmc_kernel(const __grid_constant__ Sam
         w.refill();
         w.entries = 0;
         w.overflow = 0;
+        w.n_llr = 0;
         w.a_dirty = w.t_dirty = 0u;
         w.removed = -1;
         w.rec_n[0] = w.rec_n[1] = 0;
@@ -1249,6 +1280,7 @@ __global__ void __launch_bounds__(128) rjmcmc_kernel(const __grid_constant__ Sam
             if (Bt.n_entries) Bt.n_entries[roi] = w.entries;
             if (Bt.uniforms_used) Bt.uniforms_used[roi] = w.idx - (Bt.rng_offset ? Bt.rng_offset[roi] : 0u);
             if (Bt.overflow) Bt.overflow[roi] = w.overflow;
+            if (Bt.llr_evals) Bt.llr_evals[roi] = w.n_llr;
             if (Bt.status) Bt.status[roi] = BAMF_OK;
         }
         __syncwarp();

@@ -108,3 +108,20 @@ def c0_rjstruct(side: int = 16) -> RJStruct:
         PSF_Sigma=1.3, N_Trials=3000, N_Burnin=3000, P_Burnin=P, P_Trials=P,
         P_dP=10.0, Rho=3.0 / (side * side), MinPhoton=0.0, XstdFg=0.1, IstdFg=10.0,
         BGstd=1.0, IsBackg=0)
+
+
+def uneven_rjstruct() -> RJStruct:
+    """Sampler settings of the batched uneven workload (ROI sides
+    {8,12,16,20,24}, N ~ Poisson(U[0,12]), sigma ~ U[1.1,1.5], I ~
+    LogN(ln 1000, 0.4), background ~ U[5,50]): the same move mapping and
+    jump counts as c0_rjstruct; Rho = 6/288 (the mean emitter count over the
+    mean ROI area); signal prior = the generator's log-normal pdf; offset
+    prior = the Gamma with the mean and variance of U[5,50] (shape 4.48,
+    scale 6.14), as findPriors.m:66-67 fits one to measured backgrounds."""
+    grid = np.arange(0, 12001, 10, dtype=np.float64)
+    rj = c0_rjstruct()
+    rj.P_EmPhotons = synth.lognormal_pdf(grid, 1000.0, 0.4).astype(np.float32)
+    mean, var = 27.5, 45.0 ** 2 / 12.0
+    rj.P_Offset = synth.gamma_pdf(grid, mean * mean / var, var / mean).astype(np.float32)
+    rj.Rho = 6.0 / 288.0
+    return rj

@@ -63,7 +63,7 @@ class RoiBatch(C.Structure):
 class BatchResults(C.Structure):
     _fields_ = [("map_n", C.c_void_p), ("final_n", C.c_void_p), ("final_state", C.c_void_p),
                 ("counters", C.c_void_p), ("n_entries", C.c_void_p), ("status", C.c_void_p),
-                ("overflow", C.c_void_p)]
+                ("overflow", C.c_void_p), ("llr_evals", C.c_void_p)]
 
 
 def _check(L, st: int, where: str) -> None:
@@ -228,7 +228,8 @@ class Sampler:
             setattr(b, k, t.data_ptr() if t is not None else None)
         b.bg0 = float(bg0)
         res = BatchResults()
-        for k in ("map_n", "final_n", "final_state", "counters", "n_entries", "status", "overflow"):
+        for k in ("map_n", "final_n", "final_state", "counters", "n_entries", "status", "overflow",
+                  "llr_evals"):
             t = (outs or {}).get(k)
             setattr(res, k, t.data_ptr() if t is not None else None)
         st = self._L.bamf_rjmcmc_batch_device(self._ws, C.byref(b), C.byref(params), C.byref(pr),
@@ -259,7 +260,8 @@ class Sampler:
         outs = {"map_n": np.zeros(n, np.int32), "final_n": np.zeros(n, np.int32),
                 "final_state": np.zeros((n, FINAL_STRIDE), np.float32),
                 "counters": np.zeros((n, 30), np.int32), "n_entries": np.zeros(n, np.int32),
-                "status": np.full(n, -1, np.int32), "overflow": np.zeros(n, np.int32)}
+                "status": np.full(n, -1, np.int32), "overflow": np.zeros(n, np.int32),
+                "llr_evals": np.zeros(n, np.int32)}
         res = BatchResults()
         for k, a in outs.items():
             setattr(res, k, a.ctypes.data)

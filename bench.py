@@ -1,0 +1,289 @@
+"""Headline benchmark: batched RJMCMC sampler throughput (ROIs/s) on GB300.
+
+Workload (one "step"): the batched uneven-size workload - 100,000 ROIs with
+sides uniform over {8,12,16,20,24} px, emitter count ~ Poisson(lambda),
+lambda ~ U[0,12], sigma ~ U[1.1,1.5], intensities LogN(ln 1000, 0.4),
+background U[5,50], Poisson noise (seeded synthetic data from the
+reference forward model) - each ROI run for 3000 burn-in + 3000 trial jumps
+with the reference's moves (fast arithmetic), in one persistent launch,
+followed by the MAP emitter-count reduction.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value     ROIs/s with inputs resident in HBM (device entry point)
+e2e       ROIs/s through bamf_rjmcmc_batch_host with host buffers (H2D/D2H inside)
+roofline  the sampler kernel against the measured MUFU log2 rate: one log2 per
+          ROI pixel per scored proposal (the likelihood-ratio pass)
+cpu_baseline  the CPU restatement of the reference sampler (glibc math, bit-
+          identical to the reference build) on the host cores, on a sample
+
+Under torchrun (N > 1) every rank runs its own 100,000 ROIs (weak scaling,
+no data-path collective); value = all ROIs / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RJMCMC ROIs/s (batched sampler, 3000+3000 jumps per ROI)"
+WORKLOAD = "batched uneven RJMCMC: 100k ROIs, sides {8,12,16,20,24} px, 3000+3000 jumps"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="bamf", choices=["bamf", "reference"])
+    ap.add_argument("--n-rois", type=int, default=100_000)
+    ap.add_argument("--jumps", type=int, default=3000)
+    ap.add_argument("--cpu-sample", type=int, default=0, help="ROIs per CPU-baseline sample (0: auto)")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def workload(n_rois: int, seed: int, jumps: int):
+    from bamf_gb300 import rjstruct, synth
+    b = synth.roi_batch_uneven(n_rois, seed=seed)
+    rj = rjstruct.uneven_rjstruct()
+    rj.N_Burnin = rj.N_Trials = jumps
+    return b, rj, rjstruct.mcmc_params(rj), rjstruct.initial_bg(rj)
+
+
+def cpu_sample_rate(b, rj, p, bg0, n_sample: int, threads: int):
+    """The CPU restatement of the reference sampler (glibc math) on the first
+    n_sample ROIs, all `threads` host threads; returns (ROIs/s, seconds)."""
+    import oracle
+    from bamf_gb300 import synth
+    sub = synth.RoiBatch(
+        data=b.data, offsets=b.offsets[:n_sample], xsize=b.xsize[:n_sample],
+        ysize=b.ysize[:n_sample], sigma=b.sigma[:n_sample], bg=b.bg[:n_sample],
+        true_n=b.true_n[:n_sample], true_x=[], true_y=[], true_i=[])
+    oracle.build(ref=False)
+    t = time.perf_counter()
+    oracle.run_batch(sub, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, bg0, seed=1,
+                     threads=threads, kind="port_native")
+    dt = time.perf_counter() - t
+    return n_sample / dt, dt
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return
+    b, rj, p, bg0 = workload(a.n_rois, 2, a.jumps)
+    threads = os.cpu_count() or 1
+    n = a.cpu_sample or max(threads * 8, 64)
+    for _ in range(a.warmup):
+        cpu_sample_rate(b, rj, p, bg0, min(n, 32), threads)
+    rates, secs = [], []
+    for _ in range(a.steps):
+        r, s = cpu_sample_rate(b, rj, p, bg0, n, threads)
+        rates.append(r)
+        secs.append(s)
+    v = len(rates) * n / sum(secs)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "ROIs/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, reference forward model + Poisson noise)",
+        "config": {"workload": WORKLOAD, "n_rois": a.n_rois, "jumps": [a.jumps, a.jumps],
+                   "parallelism": "host threads", "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": v, "unit": "ROIs/s", "cores": threads, "kind": "port",
+                         "sample": f"first {n} ROIs of the workload per step (same seeds), "
+                                   f"glibc-math C restatement bit-identical to the reference build"},
+        "e2e": {"value": v, "unit": "ROIs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        return run_reference(a, rank, world)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from bamf_gb300 import abi, build, sampler
+    build.build()
+    import ctypes as C
+    L = abi.lib()
+    L.bamf_probe_peaks.restype = C.c_int
+    L.bamf_probe_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+
+    b, rj, p, bg0 = workload(a.n_rois, 2 + rank, a.jumps)
+    dev = {
+        "data": torch.from_numpy(b.data).cuda(), "offsets": torch.from_numpy(b.offsets).cuda(),
+        "xsize": torch.from_numpy(b.xsize).cuda(), "ysize": torch.from_numpy(b.ysize).cuda(),
+        "psf_sigma": torch.from_numpy(b.sigma).cuda(), "side_max": int(max(b.xsize.max(), b.ysize.max())),
+    }
+    n = b.n
+    outs = {"map_n": torch.zeros(n, dtype=torch.int32, device="cuda"),
+            "final_n": torch.zeros(n, dtype=torch.int32, device="cuda"),
+            "status": torch.zeros(n, dtype=torch.int32, device="cuda"),
+            "llr_evals": torch.zeros(n, dtype=torch.int32, device="cuda"),
+            "n_entries": torch.zeros(n, dtype=torch.int32, device="cuda")}
+    s = sampler.Sampler()
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step():
+        s.run_device(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=1234, arith="fast",
+                     outs=outs, stream=stream.cuda_stream, bg0=bg0)
+
+    for _ in range(a.warmup):
+        step()
+    torch.cuda.synchronize()
+    assert int((outs["status"] != 0).sum()) == 0, "sampler reported ROI errors"
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    times = []
+    with Clocks(local) as clk:
+        for _ in range(a.steps):
+            flush.fill_(1.0)  # L2 flush between timed steps (outside the events)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) * 1e-3)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    total = sum(times)
+    if dist:
+        t = torch.tensor([total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    value = world * a.steps * n / total
+    step_s = total / a.steps
+
+    # roofline: one MUFU log2 per ROI pixel per scored proposal
+    llr = outs["llr_evals"].to(torch.int64).cpu().numpy()
+    npix = (b.xsize.astype(np.int64) * b.ysize.astype(np.int64))
+    lg2_per_step = float((llr * npix).sum())
+    achieved = lg2_per_step / step_s
+    fp32 = C.c_double()
+    mufu = C.c_double()
+    abi.check(L.bamf_probe_peaks(C.byref(fp32), C.byref(mufu)), "bamf_probe_peaks")
+
+    e2e = None
+    if not a.no_e2e:
+        host_out = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=1234,
+                              arith="fast", bg0=bg0)  # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_out = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=1234,
+                              arith="fast", bg0=bg0)
+        dt = time.perf_counter() - t0
+        h2d = b.data.nbytes + b.offsets.nbytes + b.xsize.nbytes + b.ysize.nbytes + b.sigma.nbytes
+        d2h = sum(v.nbytes for v in host_out.values())
+        e2e = {"value": world * n / dt, "unit": "ROIs/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+
+    cpu = None
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        ns = a.cpu_sample or max(threads * 6, 48)
+        rate, secs = cpu_sample_rate(b, rj, p, bg0, ns, threads)
+        cpu = {"value": rate, "unit": "ROIs/s", "cores": threads, "kind": "port",
+               "sample": f"first {ns} ROIs of the workload, {secs:.1f} s on {threads} host threads; "
+                         f"glibc-math C restatement bit-identical to the reference sampler build"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "ROIs/s", "n_gpus": world, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded, reference forward model + Poisson noise)",
+            "config": {"workload": WORKLOAD, "n_rois": n, "jumps": [a.jumps, a.jumps],
+                       "arith": "fast", "parallelism": f"replicas x{world}",
+                       "l2": "flushed between timed steps (512 MB write)"},
+            "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": mufu.value / 1e9,
+                         "unit": "Gop/s (MUFU log2)", "frac": achieved / mufu.value,
+                         "traffic": None,
+                         "peak_source": "measured in-process by bamf_probe_peaks (MUFU lg2 probe)",
+                         "fp32_peak_tflops_measured": fp32.value / 1e12},
+            "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": 3 * a.steps,
+            "clocks": clk.summary(),
+            "map_n_mean": float(outs["map_n"].float().mean().item()),
+            "true_n_mean": float(b.true_n.mean()),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -247,7 +247,9 @@ typedef struct bamf_roi_batch {
  *   counters     [k][30] in bamf_counters order
  *   n_entries    recorded chain entries (cRJMCMC's chain length + 1)
  *   status       BAMF_OK or the ROI's error
- *   overflow     proposals rejected because they would exceed BAMF_NMAX */
+ *   overflow     proposals rejected because they would exceed BAMF_NMAX
+ *   llr_evals    likelihood-ratio evaluations (proposals scored against the
+ *                data); each costs one pass over the ROI's pixels */
 typedef struct bamf_batch_results {
     int32_t *map_n;
     int32_t *final_n;
@@ -256,6 +258,7 @@ typedef struct bamf_batch_results {
     int32_t *n_entries;
     int32_t *status;
     int32_t *overflow;
+    int32_t *llr_evals;
 } bamf_batch_results;
 
 /* Device scratch (prior tables, work queue, per-ROI chain traces) that
@@ -275,6 +278,16 @@ bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_roi_batch *r
 bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi_batch *rois,
                                    const bamf_mcmc_params *p, const bamf_priors *priors,
                                    uint32_t seed, int arith, const bamf_batch_results *out);
+
+/* ------------------------------------------------------------------ */
+/* Measurement helpers                                                  */
+/* ------------------------------------------------------------------ */
+
+/* Measured throughput of the two pipes the sampler runs on, on the
+ * current device: dependent-free FP32 FMA (flop/s, 2 per FMA) and MUFU
+ * log2 (op/s).  Runs two short probe kernels (~tens of ms); used as the
+ * roofline denominators of the sampler.  Not used by any sampler path. */
+bamf_status bamf_probe_peaks(double *fp32_flops, double *mufu_ops);
 
 #ifdef __cplusplus
 }
