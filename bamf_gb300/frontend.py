@@ -1,0 +1,98 @@
+"""Python mirror of the reference front end, over libbamf_gb300.so.
+
+  findROI(Image, Sigma1, Sigma2, Boxsize, Minval)  @RJ/findROI.m:1-224
+  gaussMLE(Data, FitType, CameraType, Sigma)        @RJ/gaussMLE.m:64-211 ('Basic', 'CCD')
+
+Images are (Ysize, Xsize[, Zsize]) arrays in MATLAB orientation.  Every call
+runs the CUDA kernels; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import abi
+
+
+def _declare():
+    L = abi.lib()
+    if getattr(L, "_frontend_declared", False):
+        return L
+    pf = C.POINTER(C.c_float)
+    pi = C.POINTER(C.c_int32)
+    L.bamf_find_roi_host.restype = C.c_int
+    L.bamf_find_roi_host.argtypes = [pf, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                     C.c_float, C.c_int64, pi, pi, pf, C.POINTER(C.c_int64)]
+    L.bamf_gauss_mle_host.restype = C.c_int
+    L.bamf_gauss_mle_host.argtypes = [pf, C.c_int, C.c_int, C.c_float, C.c_int, pf, pf, pf]
+    L._frontend_declared = True
+    return L
+
+
+def default_minval(sigma: float = 1.3) -> float:
+    """findROI.m:74: (1/4)*2000*(1/(2*pi*2*1.3^2))."""
+    return (1 / 4) * 2000 * (1 / (2 * math.pi * 2 * 1.3 ** 2))
+
+
+def findROI(Image, Sigma1: float = 1.3, Sigma2: float = 2 * 1.3, Boxsize: int = 7,
+            Minval: float | None = None, capacity: int | None = None):
+    """Returns (SMD, ROIStack, coords): SMD has XBoxCorner, YBoxCorner,
+    FrameNum (1-based, findROI.m:161-163); ROIStack is (Boxsize, Boxsize, N)
+    float32; coords (N, 3) are the 1-based (row, col, frame) of the maxima in
+    MATLAB find order."""
+    L = _declare()
+    img = np.asarray(Image, np.float32)
+    if img.ndim == 2:
+        img = img[:, :, None]
+    ys, xs, zs = img.shape
+    flat = np.ascontiguousarray(img.ravel(order="F"))
+    if Minval is None:
+        Minval = default_minval()
+    cap = capacity if capacity is not None else max(1024, flat.size // 16)
+    while True:
+        coords = np.zeros((cap, 3), np.int32)
+        corners = np.zeros((cap, 2), np.int32)
+        stack = np.zeros((cap, Boxsize, Boxsize), np.float32)
+        count = C.c_int64()
+        st = L.bamf_find_roi_host(abi.fptr(flat), ys, xs, zs, float(Sigma1), float(Sigma2), int(Boxsize),
+                                  float(np.float32(Minval)), cap,
+                                  coords.ctypes.data_as(C.POINTER(C.c_int32)),
+                                  corners.ctypes.data_as(C.POINTER(C.c_int32)), abi.fptr(stack),
+                                  C.byref(count))
+        abi.check(st, "bamf_find_roi_host")
+        n = int(count.value)
+        if n <= cap:
+            break
+        cap = n
+    coords, corners, stack = coords[:n], corners[:n], stack[:n]
+    SMD = {"XBoxCorner": corners[:, 1].copy(), "YBoxCorner": corners[:, 0].copy(),
+           "FrameNum": coords[:, 2].copy()}
+    # stack[k] holds ROI k column-major (y fastest): as MATLAB (B, B, N)
+    roistack = np.ascontiguousarray(np.transpose(stack, (2, 1, 0)))
+    return SMD, roistack, coords
+
+
+def gaussMLE(Data, FitType: str = "Basic", CameraType: str = "CCD", Sigma: float = 1.3,
+             Iterations: int = 20):
+    """Results of gaussMLE.m:183-205 for FitType 'Basic', CameraType 'CCD'.
+    Data: (sz, sz, N).  Iterations defaults to gaussMLE.m:98's 20."""
+    if FitType != "Basic" or CameraType != "CCD":
+        raise abi.BamfError(abi.BAMF_ERR_UNSUPPORTED, f"gaussMLE({FitType}, {CameraType})")
+    L = _declare()
+    d = np.asarray(Data, np.float32)
+    if d.ndim == 2:
+        d = d[:, :, None]
+    sz, _, n = d.shape
+    flat = np.ascontiguousarray(d.ravel(order="F"))
+    P = np.zeros(4 * n, np.float32)
+    CR = np.zeros(4 * n, np.float32)
+    LL = np.zeros(n, np.float32)
+    abi.check(L.bamf_gauss_mle_host(abi.fptr(flat), sz, n, float(np.mean(Sigma)), int(Iterations),
+                                    abi.fptr(P), abi.fptr(CR), abi.fptr(LL)), "bamf_gauss_mle_host")
+    P = P.reshape(4, n).T
+    CR = CR.reshape(4, n).T
+    return {"Y": P[:, 0], "X": P[:, 1], "Photons": P[:, 2], "BG": P[:, 3],
+            "Y_SE": np.sqrt(CR[:, 0]), "X_SE": np.sqrt(CR[:, 1]),
+            "Photons_SE": np.sqrt(CR[:, 2]), "BG_SE": np.sqrt(CR[:, 3]), "LogLikelihood": LL}

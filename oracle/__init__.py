@@ -69,7 +69,7 @@ def load(kind: str = "port") -> C.CDLL:
     if kind.startswith("port"):
         pi = C.POINTER(C.c_int32)
         L.oracle_rjmcmc_batch.argtypes = [
-            pf, C.POINTER(C.c_int64), pi, pi, C.c_int, C.POINTER(abi.McmcParams),
+            pf, C.POINTER(C.c_int64), pi, pi, pf, C.c_int, C.POINTER(abi.McmcParams),
             pf, C.c_int, pf, C.c_int, pf, C.c_int, C.c_float, C.c_uint32, C.c_int, pi, pi, pi]
         L.oracle_findroi_filter.argtypes = [pf, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                             C.c_int, C.c_float, pf, C.c_int]
@@ -147,8 +147,75 @@ def run_batch(batch, params: abi.McmcParams, off, sig, back, bg0: float, seed: i
     pi = C.POINTER(C.c_int32)
     abi.check(L.oracle_rjmcmc_batch(
         abi.fptr(batch.data), batch.offsets.ctypes.data_as(C.POINTER(C.c_int64)),
-        batch.xsize.ctypes.data_as(pi), batch.ysize.ctypes.data_as(pi), n, C.byref(params),
+        batch.xsize.ctypes.data_as(pi), batch.ysize.ctypes.data_as(pi),
+        abi.fptr(np.ascontiguousarray(batch.sigma, np.float32)), n, C.byref(params),
         abi.fptr(off), off.size, abi.fptr(sig), sig.size, abi.fptr(back), back.size,
         float(bg0), int(seed), int(threads), fn.ctypes.data_as(pi), mn.ctypes.data_as(pi),
         na.ctypes.data_as(pi)), "oracle_rjmcmc_batch")
     return {"final_n": fn, "map_n": mn, "n_accepted": na}
+
+
+def findroi(stack: np.ndarray, sigma1: float = 1.3, sigma2: float = 2.6, boxsize: int = 7,
+            minval: float | None = None, threads: int = 8) -> dict:
+    """findROI.m restated: flags from the kernels' restatement, then find /
+    ind2sub (:125-126), the box clamp (:130-148) and the crop (:157-163)."""
+    import math
+    L = load("port")
+    st = np.asarray(stack, np.float32)
+    if st.ndim == 2:
+        st = st[:, :, None]
+    ys, xs, zs = st.shape
+    flat = np.ascontiguousarray(st.ravel(order="F"))
+    flags = np.zeros(flat.size, np.float32)
+    if minval is None:
+        minval = (1 / 4) * 2000 * (1 / (2 * math.pi * 2 * 1.3 ** 2))
+    abi.check(L.oracle_findroi_filter(abi.fptr(flat), ys, xs, zs, float(sigma1), float(sigma2),
+                                      int(boxsize), float(np.float32(minval)), abi.fptr(flags),
+                                      int(threads)), "oracle_findroi_filter")
+    m = np.flatnonzero(flags)
+    Ii = m % ys + 1
+    Jj = (m // ys) % xs + 1
+    Kk = m // (ys * xs) + 1
+    half = int(np.floor(boxsize / 2 + 0.5))
+    sr = Ii - half + 1
+    mr = sr < 1
+    sr[mr] = 1
+    sc = Jj - half + 1
+    mc = sc < 1
+    sc[mc] = 1
+    er = sr + boxsize - 1
+    er[mr] = boxsize
+    lr = er > ys
+    er[lr] = ys
+    sr[lr] = ys - boxsize + 1
+    ec = sc + boxsize - 1
+    ec[mc] = boxsize
+    lc = ec > xs
+    ec[lc] = xs
+    sc[lc] = xs - boxsize + 1
+    rois = np.zeros((boxsize, boxsize, len(m)), np.float32)
+    for b in range(len(m)):
+        rois[:, :, b] = st[sr[b] - 1:er[b], sc[b] - 1:ec[b], Kk[b] - 1]
+    return {"coords": np.stack([Ii, Jj, Kk], 1).astype(np.int32), "YBoxCorner": sr.astype(np.int32),
+            "XBoxCorner": sc.astype(np.int32), "ROIStack": rois, "flags": flags}
+
+
+def gaussmle(rois: np.ndarray, sigma: float, iterations: int, double: bool = False,
+             threads: int = 8) -> dict:
+    """kernel_MLEFit_XYNB_ restated (float, or double as the FP64 oracle);
+    rois (sz, sz, N); outputs param-major like the kernel."""
+    L = load("port")
+    d = np.ascontiguousarray(np.asarray(rois, np.float32).ravel(order="F"))
+    sz, _, n = np.asarray(rois).shape
+    if double:
+        dt, fn = np.float64, L.oracle_gaussmle_xynb_f64
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    else:
+        dt, fn = np.float32, L.oracle_gaussmle_xynb
+        ptr = abi.fptr
+    P = np.zeros(4 * n, dt)
+    CR = np.zeros(4 * n, dt)
+    LLv = np.zeros(n, dt)
+    abi.check(fn(abi.fptr(d), sz, n, sigma, int(iterations), ptr(P), ptr(CR), ptr(LLv), int(threads)),
+              "oracle_gaussmle")
+    return {"P": P.reshape(4, n).T, "CRLB": CR.reshape(4, n).T, "LL": LLv}

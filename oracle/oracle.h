@@ -37,9 +37,10 @@ void oracle_result_free(void *h);
 /* Batch of independent ROIs (same priors and parameters) on `threads` host
  * threads; per ROI it returns only the summary the GPU batch path returns:
  * the final state, the MAP emitter count of the chain's second half and the
- * acceptance counters.  Used as the CPU baseline. */
+ * acceptance counters.  sigma: per-ROI PSF sigma or NULL (p->PSFsigma).
+ * Used as the CPU baseline. */
 int oracle_rjmcmc_batch(const float *data, const int64_t *offsets, const int32_t *xs,
-                        const int32_t *ys, int n_rois, const bamf_mcmc_params *p,
+                        const int32_t *ys, const float *sigma, int n_rois, const bamf_mcmc_params *p,
                         const float *off, int loff, const float *sig, int lsig,
                         const float *back, int lback, float bg0, uint32_t seed, int threads,
                         int32_t *final_n, int32_t *map_n, int32_t *n_accepted);

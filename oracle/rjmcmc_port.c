@@ -1219,6 +1219,7 @@ typedef struct {
     const float *data;
     const int64_t *offsets;
     const int32_t *xs, *ys;
+    const float *sigma;
     int n_rois;
     const bamf_mcmc_params *p;
     const float *off, *sig, *back;
@@ -1241,7 +1242,9 @@ static void *batch_worker(void *arg)
         bamf_emitters e0 = {0, NULL, NULL, NULL, j->bg0};
         bamf_rng rng = {j->seed, (uint32_t)i, 0u};
         orj r;
-        orj_init(&r, j->data + j->offsets[i], j->xs[i], j->ys[i], &e0, j->p, j->off, j->loff, j->sig,
+        bamf_mcmc_params pi = *j->p;
+        if (j->sigma) pi.PSFsigma = j->sigma[i];
+        orj_init(&r, j->data + j->offsets[i], j->xs[i], j->ys[i], &e0, &pi, j->off, j->loff, j->sig,
                  j->lsig, j->back, j->lback, NULL, &rng, 0, 0);
         float *owned = (float *)r.scmos;
         start_chain(&r);
@@ -1256,14 +1259,14 @@ static void *batch_worker(void *arg)
 }
 
 int oracle_rjmcmc_batch(const float *data, const int64_t *offsets, const int32_t *xs,
-                        const int32_t *ys, int n_rois, const bamf_mcmc_params *p,
+                        const int32_t *ys, const float *sigma, int n_rois, const bamf_mcmc_params *p,
                         const float *off, int loff, const float *sig, int lsig,
                         const float *back, int lback, float bg0, uint32_t seed, int threads,
                         int32_t *final_n, int32_t *map_n, int32_t *n_accepted)
 {
     if (!data || !offsets || !xs || !ys || n_rois < 0 || !p || !final_n || !map_n || !n_accepted)
         return BAMF_ERR_INVALID_ARG;
-    batch_job j = {data, offsets, xs, ys, n_rois, p, off, sig, back, loff, lsig, lback, bg0, seed, 0,
+    batch_job j = {data, offsets, xs, ys, sigma, n_rois, p, off, sig, back, loff, lsig, lback, bg0, seed, 0,
                    PTHREAD_MUTEX_INITIALIZER, final_n, map_n, n_accepted};
     if (threads < 1) threads = 1;
     pthread_t *th = (pthread_t *)malloc((size_t)threads * sizeof(pthread_t));

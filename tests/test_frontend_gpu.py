@@ -1,0 +1,83 @@
+"""GPU parity of the front end.
+
+findROI: the maxima coordinates (order included), box corners and ROI
+crops are bit-exact against the CPU restatement of the reference kernels and
+findROI.m glue.  gaussMLE: parameters within 1e-4 relative of the float
+restatement of kernel_MLEFit_XYNB_; the error against the FP64 restatement
+is measured and bounded."""
+import numpy as np
+import pytest
+
+import oracle
+from bamf_gb300 import frontend, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def frames():
+    st, truth = synth.frames(12, seed=1)
+    return st, truth
+
+
+def test_findroi_coords_bit_exact(cuda_lib, frames):
+    st, _ = frames
+    ref = oracle.findroi(st, 1.3, 2.6, 7)
+    SMD, rois, coords = frontend.findROI(st, 1.3, 2.6, 7)
+    np.testing.assert_array_equal(coords, ref["coords"])
+    np.testing.assert_array_equal(SMD["XBoxCorner"], ref["XBoxCorner"])
+    np.testing.assert_array_equal(SMD["YBoxCorner"], ref["YBoxCorner"])
+    np.testing.assert_array_equal(rois, ref["ROIStack"])
+
+
+def test_findroi_boxsize8_findpriors_settings(cuda_lib, frames):
+    """findPriors.m:35-39: Boxsize 8, Minval = MeanPhotons/(4 pi s^2)/4."""
+    st, _ = frames
+    minval = 1500 / (4 * np.pi * 1.3 ** 2) / 4
+    ref = oracle.findroi(st[:, :, :5], 1.3, 2.6, 8, minval)
+    _, rois, coords = frontend.findROI(st[:, :, :5], 1.3, 2.6, 8, minval)
+    np.testing.assert_array_equal(coords, ref["coords"])
+    np.testing.assert_array_equal(rois, ref["ROIStack"])
+
+
+def test_findroi_deep_stack_float_window_bounds(cuda_lib):
+    """300 frames of 256x256: from frame 256 on, the row-max window bounds
+    are rounded in float exactly as the reference kernel forms them."""
+    st, _ = synth.frames(300, seed=5)
+    ref = oracle.findroi(st, 1.3, 2.6, 7, threads=16)
+    _, _, coords = frontend.findROI(st, 1.3, 2.6, 7)
+    np.testing.assert_array_equal(coords, ref["coords"])
+
+
+def test_findroi_small_and_edge_frames(cuda_lib):
+    rng = np.random.default_rng(3)
+    st = rng.poisson(20, size=(32, 32, 3)).astype(np.float32)
+    st[3, 4, 0] += 900
+    st[30, 31, 1] += 900   # near the edge: clamped box
+    st[0, 0, 2] += 900     # corner
+    ref = oracle.findroi(st, 1.3, 2.6, 7)
+    SMD, rois, coords = frontend.findROI(st, 1.3, 2.6, 7)
+    np.testing.assert_array_equal(coords, ref["coords"])
+    np.testing.assert_array_equal(SMD["XBoxCorner"], ref["XBoxCorner"])
+    np.testing.assert_array_equal(SMD["YBoxCorner"], ref["YBoxCorner"])
+    np.testing.assert_array_equal(rois, ref["ROIStack"])
+    assert len(coords) >= 3
+
+
+def test_gaussmle_matches_float_restatement_and_fp64(cuda_lib, frames):
+    st, _ = frames
+    _, rois, _ = frontend.findROI(st, 1.3, 2.6, 7)
+    for it in (10, 20):
+        res = frontend.gaussMLE(rois, "Basic", "CCD", 1.3, Iterations=it)
+        P = np.stack([res["Y"], res["X"], res["Photons"], res["BG"]], 1)
+        ref = oracle.gaussmle(rois, 1.3, it)
+        ref64 = oracle.gaussmle(rois, 1.3, it, double=True)
+        rel = np.abs(P - ref["P"]) / np.maximum(np.abs(ref["P"]), 1e-3)
+        assert np.percentile(rel, 99.9) < 1e-4, np.percentile(rel, 99.9)
+        rel64 = np.abs(P - ref64["P"]) / np.maximum(np.abs(ref64["P"]), 1e-3)
+        assert np.median(rel64) < 1e-5 and np.percentile(rel64, 99) < 1e-3
+        crlb = np.stack([res["Y_SE"], res["X_SE"], res["Photons_SE"], res["BG_SE"]], 1) ** 2
+        good = np.isfinite(ref["CRLB"]).all(1) & (ref["CRLB"] > 0).all(1)
+        relc = np.abs(crlb[good] - ref["CRLB"][good]) / np.abs(ref["CRLB"][good])
+        assert np.percentile(relc, 99) < 1e-3
+        np.testing.assert_allclose(res["LogLikelihood"], ref["LL"], rtol=1e-3, atol=1e-2)
