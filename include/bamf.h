@@ -279,6 +279,39 @@ bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi_batch *roi
                                    const bamf_mcmc_params *p, const bamf_priors *priors,
                                    uint32_t seed, int arith, const bamf_batch_results *out);
 
+/*
+ * Allocation-free variant of bamf_rjmcmc_batch_device.  It has no
+ * counterpart in the reference (which is a single-ROI CPU sampler); it is
+ * for callers that must not allocate device memory: code recorded into a
+ * CUDA graph (no cudaMalloc during stream capture), hosts whose own pool
+ * owns the device memory (MATLAB's gpuArray allocator, a framework's caching
+ * allocator), loops that cannot take the device-wide synchronisation of
+ * cudaMalloc/cudaFree.  Same arguments and results as
+ * bamf_rjmcmc_batch_device minus the workspace; it calls no cudaMalloc,
+ * cudaFree or other allocating routine.
+ *
+ * Its scratch is one fixed array of BAMF_NOALLOC_SCRATCH_BYTES compiled into
+ * the library: every GPU that loads the library holds it until the process
+ * exits, and every call shares it.  A call needs
+ *   512 + sum over the 3 priors of 16*len (each rounded up to 256)
+ *   + 4*n_rois (rounded up to 256)
+ *   + [map_n wanted] n_rois*(N_Burnin+N_Trials) (+ 4*n_rois if n_entries is NULL)
+ * bytes; a call needing more returns BAMF_ERR_TOO_LARGE before any GPU work
+ * (split the batch).  The first call on each device looks up the array's
+ * device address with that device current; make that first call before any
+ * stream capture begins.  Calls that overlap on the GPU (different streams,
+ * or different host threads, not ordered by the caller) race on the shared
+ * scratch and corrupt each other's results; calls on one stream are safe.
+ * The work-queue counters are cleared at the start of every call; nothing
+ * else in the scratch is assumed to start at zero.
+ */
+#define BAMF_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *rois,
+                                             const bamf_mcmc_params *p,
+                                             const bamf_priors *priors, uint32_t seed,
+                                             int arith, const bamf_batch_results *out,
+                                             void *stream);
+
 /* ------------------------------------------------------------------ */
 /* Measurement helpers                                                  */
 /* ------------------------------------------------------------------ */
