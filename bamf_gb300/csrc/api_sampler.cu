@@ -126,6 +126,27 @@ struct DevBuf {
 };
 
 struct bamf_workspace {
+    /* streams the size-class launches fork onto, and their join events */
+    cudaStream_t cls_stream[BAMF_N_CLASSES] = {};
+    cudaEvent_t fork_ev = nullptr;
+    cudaEvent_t join_ev[BAMF_N_CLASSES] = {};
+    ~bamf_workspace()
+    {
+        for (int c = 0; c < BAMF_N_CLASSES; ++c) {
+            if (cls_stream[c]) cudaStreamDestroy(cls_stream[c]);
+            if (join_ev[c]) cudaEventDestroy(join_ev[c]);
+        }
+        if (fork_ev) cudaEventDestroy(fork_ev);
+    }
+    bool streams_ready()
+    {
+        if (fork_ev) return true;
+        for (int c = 0; c < BAMF_N_CLASSES; ++c) {
+            if (cudaStreamCreateWithFlags(&cls_stream[c], cudaStreamNonBlocking) != cudaSuccess) return false;
+            if (cudaEventCreateWithFlags(&join_ev[c], cudaEventDisableTiming) != cudaSuccess) return false;
+        }
+        return cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming) == cudaSuccess;
+    }
     DevBuf tables;   /* the three prior tables                       */
     DevBuf queue;    /* work-queue counter                             */
     DevBuf trace;    /* per-ROI Signal==1 count per chain entry        */
@@ -212,15 +233,38 @@ static int sm_count()
 /* Launch the chains of batch B as a persistent grid: as many CTAs as fit
  * on the GPU at once (or fewer for small batches); warps pull ROI ids from
  * the work queue until it runs dry. */
+/* Warps per CTA for a class: the choice among 4, 2, 1 that keeps the most
+ * warps resident per SM (shared memory per warp grows with the ROI side). */
+static int pick_wpb(bool exact, int side_max, int *per_sm_out)
+{
+    int best_w = 0, best_wpb = 4, best_per = 0;
+    const int cand[3] = {4, 2, 1};
+    for (int i = 0; i < 3; ++i) {
+        int per = exact ? blocks_per_sm_exact(side_max, cand[i]) : blocks_per_sm_fast(side_max, cand[i]);
+        if (per * cand[i] > best_w) {
+            best_w = per * cand[i];
+            best_wpb = cand[i];
+            best_per = per;
+        }
+    }
+    *per_sm_out = best_per;
+    return best_wpb;
+}
+
+/* Launch the chains of batch B as persistent grids.  With size classes, one
+ * launch per non-empty class, each on its own stream forked from s (largest
+ * class first, so the small ones fill the SMs the large ones drain) and
+ * joined back into s. */
 static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, SamplerBatch B,
                                 int arith, cudaStream_t s)
 {
     bamf_status r;
     bool exact = arith == BAMF_ARITH_EXACT;
-    const int wpb = 4;
     int ncls = B.class_range ? BAMF_N_CLASSES : 1;
     if ((r = ws->queue.ensure(sizeof(int32_t) * BAMF_N_CLASSES))) return r;
     CU(cudaMemsetAsync(ws->queue.p, 0, sizeof(int32_t) * BAMF_N_CLASSES, s));
+    bool fork = ncls > 1 && ws->streams_ready();
+    if (fork) CU(cudaEventRecord(ws->fork_ev, s));
     int sms = sm_count();
     for (int c = ncls - 1; c >= 0; --c) {
         SamplerBatch Bc = B;
@@ -231,14 +275,24 @@ static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, Samp
             if (lo > B.side_max) continue;                /* no ROI of the batch is that large */
             Bc.side_max = std::min(class_side(c), B.side_max);
         }
-        int per_sm = exact ? blocks_per_sm_exact(Bc.side_max, wpb) : blocks_per_sm_fast(Bc.side_max, wpb);
+        int per_sm = 0;
+        int wpb = pick_wpb(exact, Bc.side_max, &per_sm);
         if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
         int need = (B.n_rois + wpb - 1) / wpb;
         int blocks = std::min(need, per_sm * sms);
         if (blocks < 1) return BAMF_OK;
-        cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, s)
-                              : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, s);
+        cudaStream_t cs = s;
+        if (fork) {
+            cs = ws->cls_stream[c];
+            CU(cudaStreamWaitEvent(cs, ws->fork_ev, 0));
+        }
+        cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, cs)
+                              : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, cs);
         if (e != cudaSuccess) return cuda_fail(e, "rjmcmc kernel launch");
+        if (fork) {
+            CU(cudaEventRecord(ws->join_ev[c], cs));
+            CU(cudaStreamWaitEvent(s, ws->join_ev[c], 0));
+        }
     }
     return BAMF_OK;
 }

@@ -47,21 +47,28 @@ extern "C" bamf_status bamf_probe_peaks(double *fp32_flops, double *mufu_ops)
     cudaEventCreate(&e1);
     const int blocks = sms * 8, threads = 256;
     const int it_fma = 4096, it_mufu = 2048;
-    float ms = 0.0f;
-    fma_probe<<<blocks, threads>>>(out, 16, 1.0001f, 0.5f); /* warm-up */
-    cudaEventRecord(e0);
-    fma_probe<<<blocks, threads>>>(out, it_fma, 1.0001f, 0.5f);
-    cudaEventRecord(e1);
-    cudaEventSynchronize(e1);
-    cudaEventElapsedTime(&ms, e0, e1);
-    *fp32_flops = 2.0 * 8.0 * it_fma * (double)blocks * threads / (ms * 1e-3);
-    mufu_probe<<<blocks, threads>>>(out, 16);
-    cudaEventRecord(e0);
-    mufu_probe<<<blocks, threads>>>(out, it_mufu);
-    cudaEventRecord(e1);
-    cudaEventSynchronize(e1);
-    cudaEventElapsedTime(&ms, e0, e1);
-    *mufu_ops = 4.0 * it_mufu * (double)blocks * threads / (ms * 1e-3);
+    cudaStream_t st;
+    cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    float ms = 0.0f, best_fma = 1e30f, best_mufu = 1e30f;
+    fma_probe<<<blocks, threads, 0, st>>>(out, 16, 1.0001f, 0.5f); /* warm-up */
+    mufu_probe<<<blocks, threads, 0, st>>>(out, 16);
+    for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(e0, st);
+        fma_probe<<<blocks, threads, 0, st>>>(out, it_fma, 1.0001f, 0.5f);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        best_fma = ms < best_fma ? ms : best_fma;
+        cudaEventRecord(e0, st);
+        mufu_probe<<<blocks, threads, 0, st>>>(out, it_mufu);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        cudaEventElapsedTime(&ms, e0, e1);
+        best_mufu = ms < best_mufu ? ms : best_mufu;
+    }
+    cudaStreamDestroy(st);
+    *fp32_flops = 2.0 * 8.0 * it_fma * (double)blocks * threads / (best_fma * 1e-3);
+    *mufu_ops = 4.0 * it_mufu * (double)blocks * threads / (best_mufu * 1e-3);
     cudaError_t err = cudaGetLastError();
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

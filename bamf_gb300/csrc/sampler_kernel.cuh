@@ -71,14 +71,16 @@ struct SMath<false> {
     static __device__ __forceinline__ float powf_(float x, float y) { return powf(x, y); }
 };
 
-/* Per-warp shared-memory carve-out, in floats: D, M, Mt, E, sCMOS,
- * stencils NX/NY of the proposal, counters, pick list; fast mode adds A's
- * stencil cache NXa/NYa and log2 M. */
+/* Per-warp shared-memory carve-out, in floats.  Exact: data D, model M,
+ * proposal model Mt, per-pixel work E, sCMOS, proposal stencils NX/NY.
+ * Fast: D, M, Mt, log2 M, proposal stencils NX/NY and A's stencil cache
+ * NXa/NYa (sCMOS is read from global memory at model rebuilds only).  Both:
+ * counters and the neighbour pick list. */
 __host__ __device__ inline int warp_smem_floats(int side_max, bool exact)
 {
-    int npix = side_max * side_max;
-    int base = 5 * npix + 2 * BAMF_NMAX * side_max + C_COUNT + BAMF_NMAX + 2;
-    return exact ? base : base + 2 * BAMF_NMAX * side_max + npix;
+    int npix = side_max * side_max, nxs = BAMF_NMAX * side_max;
+    return exact ? 5 * npix + 2 * nxs + C_COUNT + BAMF_NMAX + 2   /* D M Mt E sCMOS NX NY */
+                 : 4 * npix + 4 * nxs + C_COUNT + BAMF_NMAX + 2;  /* D M Mt log2M NX NY NXa NYa */
 }
 
 /* double helpers that nvcc may not contract */
@@ -97,7 +99,8 @@ struct ChainWarp {
     int px_dx, px_dy; /* pixel p -> p+32 moves x by px_dx and y by px_dy (then wraps) */
     float sigma, Cst, MeanN;
     /* shared memory */
-    float *D, *M, *Mt, *E, *scm, *NX, *NY, *NXa, *NYa, *logM;
+    float *D, *M, *Mt, *E, *NX, *NY, *NXa, *NYa, *logM;
+    const float *scm; /* sCMOS: shared memory (exact) or global/null (fast) */
     int *cnt, *cl;
     int rec_n[2];
     /* current state A (lane j = slot j) */
@@ -143,12 +146,36 @@ struct ChainWarp {
         idx++;
         return bamf_u31_to_float(v >> 1);
     }
-    /* Irwin-Hall sum of 12 uniforms (LibRJMCMCreturn.hpp:23-26). */
+    /* Irwin-Hall sum of 12 uniforms (LibRJMCMCreturn.hpp:23-26).  Exact
+     * mode adds them in draw order; fast mode has lanes 0..11 fetch the 12
+     * draws at once and adds them in a butterfly (same distribution, other
+     * rounding). */
     __device__ __forceinline__ float randn()
     {
-        float t = 0;
-        for (int k = 0; k < 12; ++k) t = t + urand();
-        return t - 6.0f;
+        if (EXACT) {
+            float t = 0;
+            for (int k = 0; k < 12; ++k) t = t + urand();
+            return t - 6.0f;
+        }
+        if (((idx + 11u) >> 2) - base >= 32u) {
+            base = idx >> 2;
+            refill();
+        }
+        uint32_t my = idx + (uint32_t)(lane & 15);
+        int src = (int)((my >> 2) - base) & 31;
+        uint32_t v0 = __shfl_sync(BAMF_FULL, r0, src);
+        uint32_t v1 = __shfl_sync(BAMF_FULL, r1, src);
+        uint32_t v2 = __shfl_sync(BAMF_FULL, r2, src);
+        uint32_t v3 = __shfl_sync(BAMF_FULL, r3, src);
+        uint32_t c = my & 3u;
+        uint32_t v = c == 0 ? v0 : (c == 1 ? v1 : (c == 2 ? v2 : v3));
+        float u = (lane & 15) < 12 ? bamf_u31_to_float(v >> 1) : 0.0f;
+        u += __shfl_xor_sync(BAMF_FULL, u, 1);
+        u += __shfl_xor_sync(BAMF_FULL, u, 2);
+        u += __shfl_xor_sync(BAMF_FULL, u, 4);
+        u += __shfl_xor_sync(BAMF_FULL, u, 8);
+        idx += 12u;
+        return u - 6.0f;
     }
 
     /* ------------------------------------------------------ lane access */
@@ -293,7 +320,11 @@ struct ChainWarp {
         bool in = false;
         if (lane < an && lane != jj) {
             float dx = aX - xj, dy = aY - yj;
-            float d = (float)sqrt(dadd(dmul((double)dx, (double)dx), dmul((double)dy, (double)dy)));
+            float d;
+            if (EXACT)
+                d = (float)sqrt(dadd(dmul((double)dx, (double)dx), dmul((double)dy, (double)dy)));
+            else
+                d = sqrtf(dx * dx + dy * dy);
             in = d < dmin;
         }
         return __ballot_sync(BAMF_FULL, in);
@@ -370,7 +401,7 @@ struct ChainWarp {
         __syncwarp();
         int x = lane / Y, y = lane - (lane / Y) * Y;
         for (int p = lane; p < npix; p += 32) {
-            float m = BG + ABG * (float)x + BBG * (float)y + scm[p];
+            float m = BG + ABG * (float)x + BBG * (float)y + (scm ? scm[p] : 0.0f);
             for (int k = 0; k < n; ++k) m += nx[k * X + x] * ny[k * Y + y];
             out[p] = m;
             x += px_dx;
@@ -451,7 +482,6 @@ struct ChainWarp {
                 float mt = M[p] + d;
                 float lmt = __log2f(mt);
                 Mt[p] = mt;
-                E[p] = lmt;
                 acc += D[p] * (lmt - logM[p]) * 0.69314718f - d;
                 x += px_dx;
                 y += px_dy;
@@ -470,8 +500,9 @@ struct ChainWarp {
     __device__ __forceinline__ void commit_fast()
     {
         for (int p = lane; p < npix; p += 32) {
-            M[p] = Mt[p];
-            logM[p] = E[p];
+            float m = Mt[p];
+            M[p] = m;
+            logM[p] = __log2f(m);
         }
         /* stencil cache: drop the removed slot, then take T's dirty rows */
         if (removed >= 0) {
@@ -573,35 +604,42 @@ struct ChainWarp {
         }
     }
 
-    __device__ __forceinline__ void reject_record(int type)
-    {
-        record2(0.0f, 0.0f, type, 0);
-        update_grids();
-    }
 
     /* ------------------------------------------------------------ moves */
-    /* RJMCMC::jump (:752-970). */
-    __device__ __forceinline__ void mv_jump()
+    /* Every move is split in two: propose_*() consumes the move's uniforms,
+     * builds T and returns what happens next; finish_*() turns the
+     * likelihood ratio into the move's posterior ratio (no uniforms).  The
+     * likelihood ratio, the accept draw, the commit and the chain record are
+     * then one shared code path in step(), in the reference's order
+     * (proposal draws, test, likelihood_ratio, priors, accept draw). */
+    enum { ACT_SKIP = 0, ACT_GRIDS = 1, ACT_REJECT = 2, ACT_EVAL = 3 };
+    enum { MV_JUMP, MV_SPLIT, MV_MERGE, MV_BIRTH, MV_DEATH, MV_GSPLIT, MV_GMERGE };
+    /* pending proposal between propose and finish */
+    int pk_move, pk_type, pk_c1, pk_c2, pk_i0, pk_i1, pk_i2;
+    float pk_f0, pk_f1, pk_f2, pk_f3, pk_f4, pk_f5;
+
+    /* RJMCMC::jump (:752-970) up to the likelihood ratio. */
+    __device__ __forceinline__ int propose_jump()
     {
         cinc(C_N_jump);
         int type = 1;
         float PrI = 1.0f, IPDF, IPDFtest;
         copyA2T();
-        if (an < 1) return;
+        if (an < 1) return ACT_SKIP;
         float Ua = urand();
         int nn = min((int)(Ua * (float)tn), tn - 1);
         float Ub = urand();
         const bamf_mcmc_params &p = K->p;
-        if ((double)Ub < 0.25) {
+        if (Ub < 0.25f) {
             type = 2;
             tBG = tBG + p.BG_std * randn();
             tABG = tABG + p.ABBG_std * randn();
             tBBG = tBBG + p.ABBG_std * randn();
-        } else if ((double)Ub < 0.50 && (double)Ub >= 0.25) {
-            if (an < 2) return;
+        } else if (Ub < 0.50f && Ub >= 0.25f) {
+            if (an < 2) return ACT_SKIP;
             type = 10;
             int Np = closestMulti(nn, 2 * sigma);
-            if (Np == 0) return;
+            if (Np == 0) return ACT_SKIP;
             float I0 = A_I(nn);
             for (int i = 0; i < Np; ++i) I0 = I0 + A_I(cl[i]);
             float II0 = 0, XI0 = 0, YI0 = 0, XII0 = 0, YII0 = 0;
@@ -642,7 +680,7 @@ struct ChainWarp {
             IPDFtest = sob(aSn, tIn);
             IPDF = sob(aSn, aIn);
             PrI = PrI * IPDFtest / IPDF;
-        } else if ((double)Ub >= 0.5 && (double)Ub < 0.75) {
+        } else if (Ub >= 0.5f && Ub < 0.75f) {
             type = 3;
             int NN = closestMulti(nn, 2 * sigma);
             if (lane == 0) cl[NN] = nn;
@@ -697,33 +735,28 @@ struct ChainWarp {
             setT(nn, nI, nX, nY);
             if (!EXACT) a_dirty |= 1u << nn;
         }
-        if (!testT()) {
-            reject_record(type);
-            return;
-        }
-        float LLR = llr();
+        pk_move = MV_JUMP;
+        pk_type = type;
+        pk_f0 = PrI;
+        pk_c1 = C_A_jump;
+        pk_c2 = A_S(nn) == 1 ? C_A_jumpFg : C_A_jumpBg;
+        return testT() ? ACT_EVAL : ACT_REJECT;
+    }
+    __device__ __forceinline__ float finish_jump(float LLR)
+    {
         float BgPDF = findPDF(K->off, aBG);
         float BgPDFtest = findPDF(K->off, tBG);
         float PrBg = (BgPDFtest / BgPDF) * MT::exp_(-(tBBG * tBBG - aBBG * aBBG) / 2.0f) *
                      MT::exp_(-(tABG * tABG - aABG * aABG) / 2.0f);
-        float PR = LLR * PrI * PrBg;
-        int accept = (urand() < PR);
-        if (accept) {
-            cinc(C_A_jump);
-            cinc(A_S(nn) == 1 ? C_A_jumpFg : C_A_jumpBg);
-            accept_T();
-        }
-        record2(LLR, PR, type, accept);
-        update_grids();
+        return LLR * pk_f0 * PrBg;
     }
 
     /* RJMCMC::split (:972-1109). */
-    __device__ __forceinline__ void mv_split()
+    __device__ __forceinline__ int propose_split()
     {
-        const int type = 4;
         cinc(C_N_split);
         copyA2T();
-        if (an < 1) return;
+        if (an < 1) return ACT_SKIP;
         const bamf_mcmc_params &p = K->p;
         float Ua = urand();
         int jj = min((int)floorf((float)an * Ua), an - 1);
@@ -736,16 +769,26 @@ struct ChainWarp {
         setT(jj, u1 * Ijp, mux + u2, muy + u3);
         if (!EXACT) a_dirty |= 1u << jj;
         addT((1.0f - u1) * Ijp, mux - u1 * u2 / (1.0f - u1), muy - u1 * u3 / (1.0f - u1), BF);
+        pk_move = MV_SPLIT;
+        pk_type = 4;
+        pk_i0 = jj;
+        pk_f0 = u1;
+        pk_f1 = u2;
+        pk_f2 = u3;
+        pk_f3 = Ijp;
+        pk_c1 = C_A_split;
+        pk_c2 = BF == 1 ? C_A_splitFg : C_A_splitBg;
         if (t_overflow) {
             overflow++;
-            reject_record(type);
-            return;
+            return ACT_REJECT;
         }
-        if (!testT()) {
-            reject_record(type);
-            return;
-        }
-        float LLR = llr();
+        return testT() ? ACT_EVAL : ACT_REJECT;
+    }
+    __device__ __forceinline__ float finish_split(float LLR)
+    {
+        const bamf_mcmc_params &p = K->p;
+        int jj = pk_i0;
+        float u1 = pk_f0, u2 = pk_f1, u3 = pk_f2, Ijp = pk_f3;
         float tmp1 = 1.0f, tmp2 = 1.0f;
         tmp1 = tmp1 * sob(A_S(jj), A_I(jj));
         tmp2 = tmp2 * sob(T_S(jj), T_I(jj));
@@ -759,29 +802,16 @@ struct ChainWarp {
         float PrX = 1.0f / Area;
         float Us = 1.0f / (Norm1 * Norm2);
         float om = 1.0f - u1;
-        float Jacob = (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om)));
-        float PR = LLR * PrI * PrX * Us * Jacob * (P[1] / P[2]) * PrM;
-        int accept = (urand() < PR);
-        if (accept) {
-            cinc(C_A_split);
-            cinc(BF == 1 ? C_A_splitFg : C_A_splitBg);
-            accept_T();
-        }
-        record2(LLR, PR, type, accept);
-        update_grids();
+        float Jacob = EXACT ? (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om))) : Ijp / (om * om);
+        return LLR * PrI * PrX * Us * Jacob * (P[1] / P[2]) * PrM;
     }
 
     /* RJMCMC::merge (:1111-1255). */
-    __device__ __forceinline__ void mv_merge()
+    __device__ __forceinline__ int propose_merge()
     {
-        const int type = 5;
         cinc(C_N_merge);
         copyA2T();
-        if (an < 2) {
-            update_grids();
-            return;
-        }
-        const bamf_mcmc_params &p = K->p;
+        if (an < 2) return ACT_GRIDS;
         float Ua = urand();
         int jj = min((int)floorf((float)an * Ua), an - 1);
         int ii = closest(jj, 3 * sigma);
@@ -791,11 +821,9 @@ struct ChainWarp {
         float aIi = A_I(ii), aXi = A_X(ii), aYi = A_Y(ii);
         {
             float dx = aXj - aXi, dy = aYj - aYi;
-            float d2 = (float)dadd(dmul((double)dx, (double)dx), dmul((double)dy, (double)dy));
-            if (sqrtf(d2) > 3 * sigma) {
-                update_grids();
-                return;
-            }
+            float d2 = EXACT ? (float)dadd(dmul((double)dx, (double)dx), dmul((double)dy, (double)dy))
+                             : dx * dx + dy * dy;
+            if (sqrtf(d2) > 3 * sigma) return ACT_GRIDS;
         }
         float Ijp = aIj + aIi;
         float muxjp = (aIj * aXj + aIi * aXi) / Ijp;
@@ -809,11 +837,26 @@ struct ChainWarp {
         if (lane == jj) tS = (PDFbg > PDFfg) ? 0 : 1;
         if (!EXACT) a_dirty |= (1u << jj) | (1u << ii);
         removeT(ii);
-        if (!testT()) {
-            reject_record(type);
-            return;
-        }
-        float LLR = llr();
+        pk_move = MV_MERGE;
+        pk_type = 5;
+        pk_i0 = jj;
+        pk_i1 = ii;
+        pk_i2 = aSj;
+        pk_f0 = u1;
+        pk_f1 = u2;
+        pk_f2 = u3;
+        pk_f3 = Ijp;
+        pk_f4 = aIj;
+        pk_f5 = aIi;
+        pk_c1 = aSj == 1 ? C_A_mergeFg : C_A_mergeBg;
+        pk_c2 = C_A_merge;
+        return testT() ? ACT_EVAL : ACT_REJECT;
+    }
+    __device__ __forceinline__ float finish_merge(float LLR)
+    {
+        const bamf_mcmc_params &p = K->p;
+        int jj = pk_i0, ii = pk_i1, aSj = pk_i2;
+        float u1 = pk_f0, u2 = pk_f1, u3 = pk_f2, Ijp = pk_f3, aIj = pk_f4, aIi = pk_f5;
         float tmp1 = 1.0f, tmp2 = 1.0f;
         tmp1 = tmp1 * sob(aSj, aIj);
         tmp1 = tmp1 * sob(A_S(ii), aIi);
@@ -827,23 +870,16 @@ struct ChainWarp {
         float PrX = 1.0f / Area;
         float Us = 1.0f / (Norm1 * Norm2);
         float om = 1.0f - u1;
-        float Jacob = (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om)));
+        float Jacob = EXACT ? (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om))) : Ijp / (om * om);
         float PrM = MeanN / NEm;
-        float PR = LLR / (PrI * PrX * Jacob * Us * PrM * P[1] / P[2]);
-        int accept = (urand() < PR);
-        if (accept) {
-            cinc(aSj == 1 ? C_A_mergeFg : C_A_mergeBg);
-            cinc(C_A_merge);
-            accept_T();
-        }
-        record2(LLR, PR, type, accept);
-        update_grids();
+        return LLR / (PrI * PrX * Jacob * Us * PrM * P[1] / P[2]);
     }
 
     /* RJMCMC::find_Birth (:1688-1736); PixProb is overwritten with 1. */
     __device__ __forceinline__ void find_birth(float *bx, float *by)
     {
         float total;
+        float *Pf = EXACT ? E : Mt; /* prefix buffer; Mt is free before the proposal is scored */
         if (EXACT) {
             for (int p = lane; p < npix; p += 32) {
                 float v = D[p] - M[p];
@@ -862,7 +898,7 @@ struct ChainWarp {
             for (int p = p0; p < p1; ++p) {
                 float v = D[p] - M[p];
                 s += v > 0.0f ? v : 0.0f;
-                E[p] = s;
+                Pf[p] = s;
             }
             float incl = s;
             for (int o = 1; o < 32; o <<= 1) {
@@ -870,14 +906,14 @@ struct ChainWarp {
                 if (lane >= o) incl += t;
             }
             float excl = incl - s;
-            for (int p = p0; p < p1; ++p) E[p] += excl;
+            for (int p = p0; p < p1; ++p) Pf[p] += excl;
             __syncwarp();
             total = __shfl_sync(BAMF_FULL, incl, 31);
         }
         float rr = total * urand();
         int first = npix;
         for (int p = lane; p < npix; p += 32)
-            if (rr <= E[p]) {
+            if (rr <= Pf[p]) {
                 first = p;
                 break;
             }
@@ -889,16 +925,15 @@ struct ChainWarp {
     }
 
     /* RJMCMC::birth (:1258-1330). */
-    __device__ __forceinline__ void mv_birth()
+    __device__ __forceinline__ int propose_birth()
     {
-        const int type = 6;
         cinc(C_N_birth);
         copyA2T();
         const bamf_mcmc_params &p = K->p;
         float bx, by;
         find_birth(&bx, &by);
         int BF;
-        if (p.IsBackg == 1) BF = (int)floor(dadd((double)urand(), 0.5));
+        if (p.IsBackg == 1) BF = EXACT ? (int)floor(dadd((double)urand(), 0.5)) : (int)floorf(urand() + 0.5f);
         else BF = 1;
         float I_new;
         if (BF == 1) {
@@ -909,62 +944,55 @@ struct ChainWarp {
             I_new = genRand(K->back);
         }
         addT(I_new, bx, by, BF);
+        pk_move = MV_BIRTH;
+        pk_type = 6;
+        pk_c1 = BF == 1 ? C_A_birthFg : C_A_birthBg;
+        pk_c2 = C_A_birth;
         if (t_overflow) {
             overflow++;
-            reject_record(type);
-            return;
+            return ACT_REJECT;
         }
-        if (!testT()) {
-            reject_record(type);
-            return;
-        }
-        float LLR = llr();
+        return testT() ? ACT_EVAL : ACT_REJECT;
+    }
+    __device__ __forceinline__ float finish_birth(float LLR)
+    {
+        const bamf_mcmc_params &p = K->p;
         float NEm = nsignalA();
         float PrM = MeanN / (NEm + 1.0f);
         const float PixProb = 1.0f;
-        float PR = LLR * P[3] / (P[4] * ((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out) * PixProb) * PrM;
-        int accept = (urand() < PR);
-        if (accept) {
-            cinc(BF == 1 ? C_A_birthFg : C_A_birthBg);
-            cinc(C_A_birth);
-            accept_T();
-        }
-        record2(LLR, PR, type, accept);
-        update_grids();
+        return LLR * P[3] / (P[4] * ((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out) * PixProb) * PrM;
     }
 
     /* RJMCMC::death (:1332-1387). */
-    __device__ __forceinline__ void mv_death()
+    __device__ __forceinline__ int propose_death()
     {
-        const int type = 7;
         cinc(C_N_death);
         copyA2T();
-        if (an < 1) return;
+        if (an < 1) return ACT_SKIP;
         float Ua = urand();
         int jj = min((int)floorf((float)an * Ua), an - 1);
         int aSj = A_S(jj);
         cinc(aSj == 1 ? C_N_deathFg : C_N_deathBg);
         if (!EXACT) a_dirty |= 1u << jj;
         removeT(jj);
-        float LLR = llr();
+        pk_move = MV_DEATH;
+        pk_type = 7;
+        pk_c1 = C_A_death;
+        pk_c2 = aSj == 1 ? C_A_deathFg : C_A_deathBg;
+        return ACT_EVAL;
+    }
+    __device__ __forceinline__ float finish_death(float LLR)
+    {
         float NEm = nsignalA();
         float PrM = NEm / MeanN;
-        float PR = LLR * (P[4] / P[3]) * PrM;
-        int accept = (urand() < PR);
-        if (accept) {
-            cinc(C_A_death);
-            cinc(aSj == 1 ? C_A_deathFg : C_A_deathBg);
-            accept_T();
-        }
-        record2(LLR, PR, type, accept);
-        update_grids();
+        return LLR * (P[4] / P[3]) * PrM;
     }
 
-    /* RJMCMC::gSplit (:1389-1485). */
-    __device__ __forceinline__ void mv_gsplit()
+    /* RJMCMC::gSplit (:1389-1485).  The reference does not test the
+     * proposal's bounds here. */
+    __device__ __forceinline__ int propose_gsplit()
     {
-        const int type = 8;
-        if (an < 2) return;
+        if (an < 2) return ACT_SKIP;
         copyA2T();
         float Ua = urand();
         int jj = min((int)floorf((float)an * Ua), an - 1);
@@ -972,7 +1000,7 @@ struct ChainWarp {
         if (lane == 0) cl[Np] = jj;
         __syncwarp();
         Np++;
-        if (Np == 1) return;
+        if (Np == 1) return ACT_SKIP;
         float I0 = 0.0f, X0 = 0.0f, Y0 = 0.0f;
         for (int n = 0; n < Np; ++n) {
             int c = cl[n];
@@ -991,12 +1019,24 @@ struct ChainWarp {
             if (!EXACT) a_dirty |= 1u << c;
         }
         addT(u3 * I0, X0 / (float)Np + u1, Y0 / (float)Np + u2, 1);
+        pk_move = MV_GSPLIT;
+        pk_type = 8;
+        pk_i0 = Np;
+        pk_f0 = u1;
+        pk_f1 = u2;
+        pk_f2 = u3;
+        pk_f3 = I0;
+        pk_c1 = pk_c2 = -1;
         if (t_overflow) {
             overflow++;
-            reject_record(type);
-            return;
+            return ACT_REJECT;
         }
-        float LLR = llr();
+        return ACT_EVAL;
+    }
+    __device__ __forceinline__ float finish_gsplit(float LLR)
+    {
+        int Np = pk_i0;
+        float u1 = pk_f0, u2 = pk_f1, u3 = pk_f2, I0 = pk_f3;
         float PrI = 1.0f, tmpCurrent, tmpProposed;
         for (int n = 0; n < Np; ++n) {
             int c = cl[n];
@@ -1016,23 +1056,18 @@ struct ChainWarp {
         float Area = (float)(((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out));
         float PrX = 1.0f / Area;
         float Jacob = I0 / MT::powf_(1.0f - u3, (float)(Np + 1));
-        float PR = LLR * PrI * PrX * Us * Jacob * PrM * (P[5] / P[6]);
-        int accept = (urand() < PR);
-        if (accept) accept_T();
-        record2(LLR, PR, type, accept);
-        update_grids();
+        return LLR * PrI * PrX * Us * Jacob * PrM * (P[5] / P[6]);
     }
 
     /* RJMCMC::gMerge (:1487-1584). */
-    __device__ __forceinline__ void mv_gmerge()
+    __device__ __forceinline__ int propose_gmerge()
     {
-        const int type = 9;
-        if (an < 3) return;
+        if (an < 3) return ACT_SKIP;
         copyA2T();
         float Ua = urand();
         int jj = min((int)floorf((float)an * Ua), an - 1);
         int Np = closestMulti(jj, 3 * sigma);
-        if (Np == 0) return;
+        if (Np == 0) return ACT_SKIP;
         float aIj = A_I(jj), aXj = A_X(jj), aYj = A_Y(jj);
         float I0 = aIj;
         for (int n = 0; n < Np; ++n) I0 = I0 + A_I(cl[n]);
@@ -1061,7 +1096,21 @@ struct ChainWarp {
         PrI = PrI * tmpCurrent;
         if (!EXACT) a_dirty |= 1u << jj;
         removeT(jj);
-        float LLR = llr();
+        pk_move = MV_GMERGE;
+        pk_type = 9;
+        pk_i0 = Np;
+        pk_f0 = U1;
+        pk_f1 = U2;
+        pk_f2 = U3;
+        pk_f3 = I0;
+        pk_f4 = PrI;
+        pk_c1 = pk_c2 = -1;
+        return ACT_EVAL;
+    }
+    __device__ __forceinline__ float finish_gmerge(float LLR)
+    {
+        int Np = pk_i0;
+        float U1 = pk_f0, U2 = pk_f1, U3 = pk_f2, I0 = pk_f3, PrI = pk_f4;
         float PDFu1 = normpdf(U1, 0.0f, 0.4f);
         float PDFu2 = normpdf(U2, 0.0f, 0.4f);
         float PDFu3 = (float)Np;
@@ -1074,13 +1123,10 @@ struct ChainWarp {
         float Jacob = I0 / MT::powf_(1.0f - U3, (float)(Np + 1));
         float PR = LLR / (PrI * PrX * Us * Jacob * PrM * (P[5] / P[6]));
         if (PDFu1 == 0.0f || PDFu2 == 0.0f) PR = -1.0f;
-        int accept = (urand() < PR);
-        if (accept) accept_T();
-        record2(LLR, PR, type, accept);
-        update_grids();
+        return PR;
     }
 
-    /* RJMCMC::backFore (:1586-1627). */
+    /* RJMCMC::backFore (:1586-1627): relabels in place, records nothing. */
     __device__ __forceinline__ void mv_backfore()
     {
         if (an == 0) return;
@@ -1110,18 +1156,48 @@ struct ChainWarp {
         if (lane == nn) aS = ns;
     }
 
+    /* One jump of start_Chain (:693-717, :725-748): W = this phase's
+     * cumulative probabilities, V = PV_Burnin for the gSplit/gMerge slots. */
     __device__ __forceinline__ void step(const float *V, const float *W, float t)
     {
-        /* dispatch of start_Chain (:693-717, :725-748); W = this phase's
-         * cumulative vector, V = PV_Burnin for the gSplit/gMerge slots */
-        if (t < W[0]) mv_jump();
-        else if (t >= W[0] && t < W[1]) mv_split();
-        else if (t >= W[1] && t < W[2]) mv_merge();
-        else if (t >= W[2] && t < W[3]) mv_birth();
-        else if (t >= W[3] && t < W[4]) mv_death();
-        else if (t >= V[4] && t < V[5]) mv_gsplit();
-        else if (t >= V[5] && t < V[6]) mv_gmerge();
-        else mv_backfore();
+        int act;
+        if (t < W[0]) act = propose_jump();
+        else if (t >= W[0] && t < W[1]) act = propose_split();
+        else if (t >= W[1] && t < W[2]) act = propose_merge();
+        else if (t >= W[2] && t < W[3]) act = propose_birth();
+        else if (t >= W[3] && t < W[4]) act = propose_death();
+        else if (t >= V[4] && t < V[5]) act = propose_gsplit();
+        else if (t >= V[5] && t < V[6]) act = propose_gmerge();
+        else {
+            mv_backfore();
+            act = ACT_SKIP;
+        }
+        if (act == ACT_EVAL) {
+            float LLR = llr();
+            float PR;
+            switch (pk_move) {
+            case MV_JUMP: PR = finish_jump(LLR); break;
+            case MV_SPLIT: PR = finish_split(LLR); break;
+            case MV_MERGE: PR = finish_merge(LLR); break;
+            case MV_BIRTH: PR = finish_birth(LLR); break;
+            case MV_DEATH: PR = finish_death(LLR); break;
+            case MV_GSPLIT: PR = finish_gsplit(LLR); break;
+            default: PR = finish_gmerge(LLR); break;
+            }
+            int accept = (urand() < PR);
+            if (accept) {
+                if (pk_c1 >= 0) cinc(pk_c1);
+                if (pk_c2 >= 0) cinc(pk_c2);
+                accept_T();
+            }
+            record2(LLR, PR, pk_type, accept);
+            update_grids();
+        } else if (act == ACT_REJECT) {
+            record2(0.0f, 0.0f, pk_type, 0);
+            update_grids();
+        } else if (act == ACT_GRIDS) {
+            update_grids();
+        }
     }
 
     /* RJMCMC::start_Chain (:685-750). */
@@ -1153,7 +1229,7 @@ struct ChainWarp {
 };
 
 template <bool EXACT>
-__global__ void __launch_bounds__(128) rjmcmc_kernel(const __grid_constant__ SamplerConsts Kc,
+__global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ SamplerConsts Kc,
                                                      const __grid_constant__ SamplerBatch Bc)
 {
     extern __shared__ float smem_raw[];
@@ -1192,26 +1268,37 @@ __global__ void __launch_bounds__(128) rjmcmc_kernel(const __grid_constant__ Sam
         w.D = sw;
         w.M = sw + npix_max;
         w.Mt = sw + 2 * npix_max;
-        w.E = sw + 3 * npix_max;
-        w.scm = sw + 4 * npix_max;
-        w.NX = sw + 5 * npix_max;
-        w.NY = w.NX + nxs;
-        w.cnt = (int *)(w.NY + nxs);
+        float *scm_smem = nullptr;
+        if (EXACT) {
+            w.E = sw + 3 * npix_max;
+            scm_smem = sw + 4 * npix_max;
+            w.logM = nullptr;
+            w.NX = sw + 5 * npix_max;
+            w.NY = w.NX + nxs;
+            w.NXa = w.NYa = nullptr;
+            w.cnt = (int *)(w.NY + nxs);
+        } else {
+            w.E = nullptr;
+            w.logM = sw + 3 * npix_max;
+            w.NX = sw + 4 * npix_max;
+            w.NY = w.NX + nxs;
+            w.NXa = w.NY + nxs;
+            w.NYa = w.NXa + nxs;
+            w.cnt = (int *)(w.NYa + nxs);
+        }
         w.cl = w.cnt + C_COUNT;
-        /* fast mode only: A's stencil cache and log2 M */
-        w.NXa = (float *)(w.cl + BAMF_NMAX + 2);
-        w.NYa = w.NXa + nxs;
-        w.logM = w.NYa + nxs;
         bool ok = X >= 1 && Y >= 1 && X <= Bt.side_max && Y <= Bt.side_max;
         if (!ok) {
             if (lane == 0 && Bt.status) Bt.status[roi] = BAMF_ERR_TOO_LARGE;
             continue;
         }
         const float *src = Bt.data + Bt.offsets[roi];
+        const float *scm_src = Bt.scmos ? Bt.scmos + Bt.offsets[roi] : nullptr;
         for (int p = lane; p < w.npix; p += 32) {
             w.D[p] = src[p];
-            w.scm[p] = Bt.scmos ? Bt.scmos[Bt.offsets[roi] + p] : 0.0f;
+            if (EXACT) scm_smem[p] = scm_src ? scm_src[p] : 0.0f;
         }
+        w.scm = EXACT ? scm_smem : scm_src;
         if (lane < C_COUNT) {
             int k = lane;
             bool isN = (k <= C_N_death) || (k >= C_N_jumpFg && k <= C_N_deathFg) ||

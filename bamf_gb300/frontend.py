@@ -25,6 +25,16 @@ def _declare():
     L.bamf_find_roi_host.restype = C.c_int
     L.bamf_find_roi_host.argtypes = [pf, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
                                      C.c_float, C.c_int64, pi, pi, pf, C.POINTER(C.c_int64)]
+    L.bamf_findroi_workspace_create.restype = C.c_int
+    L.bamf_findroi_workspace_create.argtypes = [C.POINTER(C.c_void_p)]
+    L.bamf_findroi_workspace_destroy.argtypes = [C.c_void_p]
+    L.bamf_find_roi_device.restype = C.c_int
+    L.bamf_find_roi_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                       C.c_double, C.c_int, C.c_float, C.c_int64, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.bamf_gauss_mle_device.restype = C.c_int
+    L.bamf_gauss_mle_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_int, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p]
     L.bamf_gauss_mle_host.restype = C.c_int
     L.bamf_gauss_mle_host.argtypes = [pf, C.c_int, C.c_int, C.c_float, C.c_int, pf, pf, pf]
     L._frontend_declared = True
@@ -96,3 +106,63 @@ def gaussMLE(Data, FitType: str = "Basic", CameraType: str = "CCD", Sigma: float
     return {"Y": P[:, 0], "X": P[:, 1], "Photons": P[:, 2], "BG": P[:, 3],
             "Y_SE": np.sqrt(CR[:, 0]), "X_SE": np.sqrt(CR[:, 1]),
             "Photons_SE": np.sqrt(CR[:, 2]), "BG_SE": np.sqrt(CR[:, 3]), "LogLikelihood": LL}
+
+
+class FindRoiDevice:
+    """findROI on device-resident stacks (torch CUDA tensors)."""
+
+    def __init__(self):
+        L = _declare()
+        h = C.c_void_p()
+        abi.check(L.bamf_findroi_workspace_create(C.byref(h)), "bamf_findroi_workspace_create")
+        self._ws, self._L = h, L
+
+    def close(self):
+        if self._ws:
+            self._L.bamf_findroi_workspace_destroy(self._ws)
+            self._ws = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, frames, ysize, xsize, zsize, sigma1=1.3, sigma2=2.6, boxsize=7, minval=None,
+            capacity=None, stream=None, want_flags=False, want_stack=True):
+        """Returns dict of CUDA tensors: coords (cap, 3), corners (cap, 2),
+        stack (cap, box*box), count (1,), flags (n,) uint8 when asked.
+        Enqueued on `stream`; read count after synchronising."""
+        import torch
+        if minval is None:
+            minval = default_minval()
+        n = ysize * xsize * zsize
+        cap = capacity if capacity is not None else max(1024, n // 64)
+        out = {"coords": torch.empty((cap, 3), dtype=torch.int32, device="cuda"),
+               "corners": torch.empty((cap, 2), dtype=torch.int32, device="cuda"),
+               "count": torch.zeros(1, dtype=torch.int64, device="cuda")}
+        if want_stack:
+            out["stack"] = torch.empty((cap, boxsize * boxsize), dtype=torch.float32, device="cuda")
+        if want_flags:
+            out["flags"] = torch.empty(n, dtype=torch.uint8, device="cuda")
+        st = self._L.bamf_find_roi_device(
+            self._ws, frames.data_ptr(), ysize, xsize, zsize, float(sigma1), float(sigma2), int(boxsize),
+            float(np.float32(minval)), cap, out["coords"].data_ptr(), out["corners"].data_ptr(),
+            out["stack"].data_ptr() if want_stack else None, out["count"].data_ptr(),
+            out["flags"].data_ptr() if want_flags else None, C.c_void_p(stream) if stream else None)
+        abi.check(st, "bamf_find_roi_device")
+        return out
+
+
+def gauss_mle_device(rois, sz: int, nfits: int, sigma: float, iterations: int, stream=None):
+    """kernel on device-resident ROIs (CUDA tensor, nfits*sz*sz); returns
+    (P, CRLB, LL) CUDA tensors, param-major."""
+    import torch
+    L = _declare()
+    P = torch.empty(4 * nfits, dtype=torch.float32, device="cuda")
+    CR = torch.empty(4 * nfits, dtype=torch.float32, device="cuda")
+    LL = torch.empty(nfits, dtype=torch.float32, device="cuda")
+    abi.check(L.bamf_gauss_mle_device(rois.data_ptr(), sz, nfits, float(sigma), int(iterations),
+                                      P.data_ptr(), CR.data_ptr(), LL.data_ptr(),
+                                      C.c_void_p(stream) if stream else None), "bamf_gauss_mle_device")
+    return P, CR, LL

@@ -313,6 +313,67 @@ bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *rois,
                                              void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Front end: findROI                                                   */
+/* ------------------------------------------------------------------ */
+
+/* Device scratch of the ROI finder (two float images and one byte of flags
+ * per pixel of the stack, chunk counts); grows on demand. */
+typedef struct bamf_findroi_ws bamf_findroi_ws;
+bamf_status bamf_findroi_workspace_create(bamf_findroi_ws **ws);
+void bamf_findroi_workspace_destroy(bamf_findroi_ws *ws);
+
+/*
+ * findROI (@RJ/findROI.m:1-224 with the kernels of
+ * source/cuda/cuda_FindROI/cuda_FindROI.cu): difference-of-Gaussians local
+ * maxima of a frame stack.
+ *   frames       ysize*xsize*zsize floats, y fastest (MATLAB Y x X x Z)
+ *   sigma1/2     the two recursive-Gaussian widths (findROI.m Sigma1/Sigma2)
+ *   boxsize      maximum-window half width and ROI side (Boxsize)
+ *   minval       floor of the maxima (Minval), as the single the kernel gets
+ *   capacity     rows available in coords/corners/roi_stack
+ *   coords       [capacity][3] 1-based (row, col, frame) of each maximum in
+ *                MATLAB find() order (findROI.m:125-126)
+ *   corners      [capacity][2] (YBoxCorner, XBoxCorner) after the clamp of
+ *                findROI.m:130-148, or NULL
+ *   roi_stack    [capacity][boxsize*boxsize] crops, y fastest (findROI.m:157-160),
+ *                or NULL (needs corners)
+ *   count        number of maxima found (may exceed capacity: then only the
+ *                first `capacity` are written)
+ *   flags_out    optional ysize*xsize*zsize bytes, 1 at each maximum (Res)
+ * _device: device pointers, count is a device int64, enqueued on stream.
+ * _host: host pointers, synchronous.
+ */
+bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *frames, int ysize, int xsize,
+                                 int zsize, double sigma1, double sigma2, int boxsize,
+                                 float minval, int64_t capacity, int32_t *coords,
+                                 int32_t *corners, float *roi_stack, int64_t *count,
+                                 uint8_t *flags_out, void *stream);
+bamf_status bamf_find_roi_host(const float *frames, int ysize, int xsize, int zsize,
+                               double sigma1, double sigma2, int boxsize, float minval,
+                               int64_t capacity, int32_t *coords, int32_t *corners,
+                               float *roi_stack, int64_t *count);
+
+/* ------------------------------------------------------------------ */
+/* Front end: gaussMLE                                                  */
+/* ------------------------------------------------------------------ */
+
+/*
+ * gaussMLE 'Basic' / 'CCD' (@RJ/gaussMLE.m:64-211, kernel_MLEFit_XYNB_ of
+ * cuda_gaussMLEv2.cu:16-141): Newton-Raphson fit of (x, y, N, bg) per ROI.
+ *   rois        nfits * sz * sz floats, each ROI y fastest (sz <= 21)
+ *   iterations  Newton iterations (gaussMLE.m uses 20)
+ *   params      [4][nfits] param-major: contiguous-axis position (MATLAB Y),
+ *               other position (X), photons, background
+ *   crlb        [4][nfits] Cramer-Rao lower bounds (variances)
+ *   loglik      [nfits] log-likelihood ratio
+ */
+bamf_status bamf_gauss_mle_device(const float *rois, int sz, int nfits, float psf_sigma,
+                                  int iterations, float *params, float *crlb, float *loglik,
+                                  void *stream);
+bamf_status bamf_gauss_mle_host(const float *rois, int sz, int nfits, float psf_sigma,
+                                int iterations, float *params, float *crlb, float *loglik);
+
+/* ------------------------------------------------------------------ */
 /* Measurement helpers                                                  */
 /* ------------------------------------------------------------------ */
 
