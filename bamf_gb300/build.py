@@ -2,7 +2,8 @@
 
 Each translation unit is compiled in parallel; the sampler's exact
 instantiation is compiled with -fmad=false so that nvcc fuses no float
-multiply-add (its chain must round like the reference's).  Rebuilds only
+multiply-add (its chain must round like the reference's), the fast one with
+-use_fast_math.  Rebuilds only
 when a source or header is newer than the library.
 """
 from __future__ import annotations
@@ -24,7 +25,10 @@ OBJDIR = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                  "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
-PER_FILE = {"sampler_exact.cu": ["-fmad=false"]}
+# The exact sampler must round every float operation as the reference does;
+# the fast sampler promises no bitwise parity, and approximate division and
+# square root shrink its code (the chain loop is instruction-cache bound).
+PER_FILE = {"sampler_exact.cu": ["-fmad=false"], "sampler_fast.cu": ["-use_fast_math"]}
 
 
 def nvcc() -> str:

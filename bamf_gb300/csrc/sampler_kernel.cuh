@@ -73,19 +73,109 @@ struct SMath<false> {
 
 /* Per-warp shared-memory carve-out, in floats.  Exact: data D, model M,
  * proposal model Mt, per-pixel work E, sCMOS, proposal stencils NX/NY.
- * Fast: D, M, Mt, log2 M, proposal stencils NX/NY and A's stencil cache
- * NXa/NYa (sCMOS is read from global memory at model rebuilds only).  Both:
- * counters and the neighbour pick list. */
+ * Fast: D, M, Mt, log2 M and the compact stencil rows SXo/SYo (old, of A)
+ * and SXn/SYn (new, of T); sCMOS is read from global memory at model
+ * rebuilds only.  Both: counters and the neighbour pick list. */
+/* Fast mode keeps stencil rows only for the emitters a proposal changes:
+ * up to FAST_ROWS old rows (A) and FAST_ROWS new rows (T); larger proposals
+ * and periodic rebuilds stream the model one emitter at a time. */
+#define FAST_ROWS 8
 __host__ __device__ inline int warp_smem_floats(int side_max, bool exact)
 {
     int npix = side_max * side_max, nxs = BAMF_NMAX * side_max;
-    return exact ? 5 * npix + 2 * nxs + C_COUNT + BAMF_NMAX + 2   /* D M Mt E sCMOS NX NY */
-                 : 4 * npix + 4 * nxs + C_COUNT + BAMF_NMAX + 2;  /* D M Mt log2M NX NY NXa NYa */
+    return exact ? 5 * npix + 2 * nxs + C_COUNT + BAMF_NMAX + 2                 /* D M Mt E sCMOS NX NY */
+                 : 4 * npix + 4 * FAST_ROWS * side_max + C_COUNT + BAMF_NMAX + 2; /* D M Mt log2M SXo SYo SXn SYn */
 }
 
 /* double helpers that nvcc may not contract */
 __device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+
+/* Out-of-line helpers.  They are called from many places of the chain loop
+ * but run rarely per jump; keeping one copy of each keeps the loop's code
+ * small enough for the instruction cache (a fully inlined loop spent most
+ * of its cycles waiting on instruction fetch). */
+
+/* One Philox4x32-10 block of a chain's stream (include/bamf_philox.h). */
+static __device__ __noinline__ uint4 philox_block(uint32_t ctr, uint32_t seed, uint32_t chain)
+{
+    bamf_philox_block b = bamf_philox4x32_10(ctr, 0u, 0u, 0u, seed, chain);
+    return make_uint4(b.v[0], b.v[1], b.v[2], b.v[3]);
+}
+
+/* Stat::findPDF (source/c/LibRJMCMC.cpp:219-246): linear interpolation of
+ * the pdf at I, 0 outside (0, x[L-1]).  The grid is x[i] = x[i-1] + DX, so
+ * the first node strictly above I (what the reference's linear scan finds)
+ * is reached from the guess I / DX in a step or two. */
+static __device__ __noinline__ float stat_pdf(const float *__restrict__ x, const float *__restrict__ pdf, int L,
+                                       float I)
+{
+    float xl = __ldg(&x[L - 1]);
+    if (I >= xl || I <= 0.0f || I != I) return 0.0f;
+    float x1 = __ldg(&x[1]);
+    int j = min(max((int)(I / x1) + 1, 1), L - 1);
+    float xj = __ldg(&x[j]), xj1 = __ldg(&x[j - 1]);
+    while (j > 1 && xj1 > I) {
+        --j;
+        xj = xj1;
+        xj1 = __ldg(&x[j - 1]);
+    }
+    while (j < L - 1 && !(xj > I)) {
+        ++j;
+        xj1 = xj;
+        xj = __ldg(&x[j]);
+    }
+    return (__ldg(&pdf[j]) * (I - xj1) + __ldg(&pdf[j - 1]) * (xj - I)) / (x1 - __ldg(&x[0]));
+}
+
+/* Stat::genRand (:248-282) given its uniform R: first unique-CDF node above R
+ * by binary search (the CDF is strictly increasing), then interpolation. */
+static __device__ __noinline__ float stat_rand(const float *__restrict__ ux, const float *__restrict__ uc, int nu,
+                                        float R)
+{
+    if (R <= 0.0f) return 0.0f;
+    if (R >= 1.0f) return __ldg(&ux[nu - 1]);
+    if (nu < 2) return 0.0f;
+    int lo = 0, hi = nu - 1;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (__ldg(&uc[mid]) > R) hi = mid; else lo = mid;
+    }
+    float uc1 = __ldg(&uc[hi]), uc0 = __ldg(&uc[hi - 1]);
+    return (__ldg(&ux[hi - 1]) * (uc1 - R) + __ldg(&ux[hi]) * (R - uc0)) / (uc1 - uc0);
+}
+
+/* Fast-mode Irwin-Hall draw: lanes 0..11 fetch uniforms idx..idx+11 of the
+ * warp's buffered Philox blocks (lane l holds block base+l in r0..r3) and
+ * add them in a butterfly.  Call with the whole warp and the 12 draws inside
+ * the buffer. */
+static __device__ __noinline__ float irwin_hall12(uint32_t idx, uint32_t base, uint32_t r0, uint32_t r1,
+                                           uint32_t r2, uint32_t r3, int lane)
+{
+    uint32_t my = idx + (uint32_t)(lane & 15);
+    int src = (int)((my >> 2) - base) & 31;
+    uint32_t v0 = __shfl_sync(0xffffffffu, r0, src);
+    uint32_t v1 = __shfl_sync(0xffffffffu, r1, src);
+    uint32_t v2 = __shfl_sync(0xffffffffu, r2, src);
+    uint32_t v3 = __shfl_sync(0xffffffffu, r3, src);
+    uint32_t c = my & 3u;
+    uint32_t v = c == 0 ? v0 : (c == 1 ? v1 : (c == 2 ? v2 : v3));
+    float u = (lane & 15) < 12 ? bamf_u31_to_float(v >> 1) : 0.0f;
+    u += __shfl_xor_sync(0xffffffffu, u, 1);
+    u += __shfl_xor_sync(0xffffffffu, u, 2);
+    u += __shfl_xor_sync(0xffffffffu, u, 4);
+    u += __shfl_xor_sync(0xffffffffu, u, 8);
+    return u - 6.0f;
+}
+
+/* normpdf (LibRJMCMCreturn.hpp:19-21) with (float)sqrt(2.0f*pi), pi = 3.141592. */
+template <bool EXACT>
+static __device__ __noinline__ float normpdf_f(float x, float u, float s)
+{
+    const float sq2pi = (float)sqrt(2.0 * 3.141592);
+    float d = x - u;
+    return 1.0f / (sq2pi * s) * SMath<EXACT>::exp_(-d * d / (2.0f * s * s));
+}
 
 template <bool EXACT>
 struct ChainWarp {
@@ -99,7 +189,8 @@ struct ChainWarp {
     int px_dx, px_dy; /* pixel p -> p+32 moves x by px_dx and y by px_dy (then wraps) */
     float sigma, Cst, MeanN;
     /* shared memory */
-    float *D, *M, *Mt, *E, *NX, *NY, *NXa, *NYa, *logM;
+    float *D, *M, *Mt, *E, *NX, *NY, *logM;
+    float *SXo, *SYo, *SXn, *SYn; /* fast mode: compact stencil rows */
     const float *scm; /* sCMOS: shared memory (exact) or global/null (fast) */
     int *cnt, *cl;
     int rec_n[2];
@@ -125,13 +216,12 @@ struct ChainWarp {
     int n_llr;
     /* incremental-model bookkeeping (fast mode) */
     uint32_t a_dirty, t_dirty;
-    int removed;
 
     /* ---------------------------------------------------------- RNG */
     __device__ __forceinline__ void refill()
     {
-        bamf_philox_block b = bamf_philox4x32_10(base + (uint32_t)lane, 0u, 0u, 0u, seed, chain);
-        r0 = b.v[0]; r1 = b.v[1]; r2 = b.v[2]; r3 = b.v[3];
+        uint4 b = philox_block(base + (uint32_t)lane, seed, chain);
+        r0 = b.x; r1 = b.y; r2 = b.z; r3 = b.w;
     }
     __device__ __forceinline__ float urand()
     {
@@ -161,21 +251,9 @@ struct ChainWarp {
             base = idx >> 2;
             refill();
         }
-        uint32_t my = idx + (uint32_t)(lane & 15);
-        int src = (int)((my >> 2) - base) & 31;
-        uint32_t v0 = __shfl_sync(BAMF_FULL, r0, src);
-        uint32_t v1 = __shfl_sync(BAMF_FULL, r1, src);
-        uint32_t v2 = __shfl_sync(BAMF_FULL, r2, src);
-        uint32_t v3 = __shfl_sync(BAMF_FULL, r3, src);
-        uint32_t c = my & 3u;
-        uint32_t v = c == 0 ? v0 : (c == 1 ? v1 : (c == 2 ? v2 : v3));
-        float u = (lane & 15) < 12 ? bamf_u31_to_float(v >> 1) : 0.0f;
-        u += __shfl_xor_sync(BAMF_FULL, u, 1);
-        u += __shfl_xor_sync(BAMF_FULL, u, 2);
-        u += __shfl_xor_sync(BAMF_FULL, u, 4);
-        u += __shfl_xor_sync(BAMF_FULL, u, 8);
+        float u = irwin_hall12(idx, base, r0, r1, r2, r3, lane);
         idx += 12u;
-        return u - 6.0f;
+        return u;
     }
 
     /* ------------------------------------------------------ lane access */
@@ -224,7 +302,6 @@ struct ChainWarp {
             uint32_t lo = t_dirty & ((1u << id) - 1u);
             uint32_t hi = id < 31 ? (t_dirty >> (id + 1)) << id : 0u;
             t_dirty = lo | hi;
-            removed = id;
         }
         tn--;
     }
@@ -236,7 +313,6 @@ struct ChainWarp {
         if (!EXACT) {
             a_dirty = 0u;
             t_dirty = 0u;
-            removed = -1;
         }
     }
     __device__ __forceinline__ void cinc(int k)
@@ -261,56 +337,23 @@ struct ChainWarp {
     }
 
     /* ---------------------------------------------------- prior tables */
-    /* Stat::findPDF (:219-246): first grid node strictly above I. */
     __device__ __forceinline__ float findPDF(const DevStat &s, float I) const
     {
-        const float *x = s.x;
-        float xl = __ldg(&x[s.L - 1]);
-        if (I >= xl || I <= 0.0f || I != I) return 0.0f;
-        /* the grid is x[i] = x[i-1] + DX: guess from I / DX, then move to
-         * the first node strictly above I (what the linear scan finds) */
-        float x1 = __ldg(&x[1]);
-        int j = min(max((int)(I / x1) + 1, 1), s.L - 1);
-        float xj = __ldg(&x[j]), xj1 = __ldg(&x[j - 1]);
-        while (j > 1 && xj1 > I) {
-            --j;
-            xj = xj1;
-            xj1 = __ldg(&x[j - 1]);
-        }
-        while (j < s.L - 1 && !(xj > I)) {
-            ++j;
-            xj1 = xj;
-            xj = __ldg(&x[j]);
-        }
-        return (__ldg(&s.pdf[j]) * (I - xj1) + __ldg(&s.pdf[j - 1]) * (xj - I)) /
-               (x1 - __ldg(&x[0]));
+        return stat_pdf(s.x, s.pdf, s.L, I);
     }
-    /* Stat::genRand (:248-282). */
     __device__ __forceinline__ float genRand(const DevStat &s)
     {
         float R = urand();
-        if (R <= 0.0f) return 0.0f;
-        if (R >= 1.0f) return __ldg(&s.ux[s.nu - 1]);
-        if (s.nu < 2) return 0.0f;
-        int lo = 0, hi = s.nu - 1;
-        while (hi - lo > 1) {
-            int mid = (lo + hi) >> 1;
-            if (__ldg(&s.uc[mid]) > R) hi = mid; else lo = mid;
-        }
-        int si = hi;
-        float uc1 = __ldg(&s.uc[si]), uc0 = __ldg(&s.uc[si - 1]);
-        return (__ldg(&s.ux[si - 1]) * (uc1 - R) + __ldg(&s.ux[si]) * (R - uc0)) / (uc1 - uc0);
+        return stat_rand(s.ux, s.uc, s.nu, R);
     }
     __device__ __forceinline__ float sob(int signal, float I) const
     {
-        return signal == 1 ? findPDF(K->sig, I) : findPDF(K->back, I);
+        const DevStat &s = signal == 1 ? K->sig : K->back;
+        return stat_pdf(s.x, s.pdf, s.L, I);
     }
-    /* normpdf (LibRJMCMCreturn.hpp:19-21); sq2pi = (float)sqrt(2.0f*pi). */
     __device__ __forceinline__ float normpdf(float x, float u, float s) const
     {
-        const float sq2pi = (float)sqrt(2.0 * 3.141592);
-        float d = x - u;
-        return 1.0f / (sq2pi * s) * MT::exp_(-d * d / (2.0f * s * s));
+        return normpdf_f<EXACT>(x, u, s);
     }
 
     /* ------------------------------------------------ neighbour search */
@@ -379,6 +422,7 @@ struct ChainWarp {
                                float *out, float *nx, float *ny)
     {
         int totx = n * X, toty = n * Y;
+#pragma unroll 1
         for (int b0 = 0; b0 < totx; b0 += 32) {
             int item = b0 + lane;
             int k = min(item / X, n - 1);
@@ -389,6 +433,7 @@ struct ChainWarp {
                 nx[k * X + x] = Ik * 0.5f * (MT::erf_(((float)x - Xk + 1.0f) * Cst) -
                                              MT::erf_(((float)x - Xk) * Cst));
         }
+#pragma unroll 1
         for (int b0 = 0; b0 < toty; b0 += 32) {
             int item = b0 + lane;
             int k = min(item / Y, n - 1);
@@ -400,6 +445,7 @@ struct ChainWarp {
         }
         __syncwarp();
         int x = lane / Y, y = lane - (lane / Y) * Y;
+#pragma unroll 1
         for (int p = lane; p < npix; p += 32) {
             float m = BG + ABG * (float)x + BBG * (float)y + (scm ? scm[p] : 0.0f);
             for (int k = 0; k < n; ++k) m += nx[k * X + x] * ny[k * Y + y];
@@ -414,31 +460,81 @@ struct ChainWarp {
         __syncwarp();
     }
 
-    /* Stencil rows of the dirty T slots into NX/NY (fast mode). */
-    __device__ __forceinline__ void stencils_dirty(uint32_t mask)
+    /* Fast mode: stencil rows of the emitters a proposal changes, compact:
+     * row q of SXo/SYo is the old stencil of the q-th slot of a_dirty (from
+     * A), row q of SXn/SYn the new stencil of the q-th slot of t_dirty (from
+     * T).  One pass over both sets keeps one copy of the code. */
+    __device__ __forceinline__ void stencil_rows(int na, int nt)
     {
-        int nd = __popc(mask);
-        int totx = nd * X, toty = nd * Y;
-        for (int b0 = 0; b0 < totx; b0 += 32) {
-            int item = b0 + lane;
-            int q = min(item / X, nd - 1);
-            int x = item - q * X;
-            int k = nth_bit(mask, q);
-            float Ik = __shfl_sync(BAMF_FULL, tI, k);
-            float Xk = __shfl_sync(BAMF_FULL, tX, k);
-            if (item < totx)
-                NX[k * X + x] = Ik * 0.5f * (MT::erf_(((float)x - Xk + 1.0f) * Cst) -
-                                             MT::erf_(((float)x - Xk) * Cst));
+        const int XY = X + Y;
+        const int tot = (na + nt) * XY;
+#pragma unroll 1
+        for (int b0 = 0; b0 < tot; b0 += 32) {
+            int item = min(b0 + lane, tot - 1);
+            int row = item / XY;
+            int col = item - row * XY;
+            bool isnew = row >= na;
+            int q = isnew ? row - na : row;
+            int k = nth_bit(isnew ? t_dirty : a_dirty, q);
+            float Ia = __shfl_sync(BAMF_FULL, aI, k), Xa = __shfl_sync(BAMF_FULL, aX, k);
+            float Ya = __shfl_sync(BAMF_FULL, aY, k);
+            float It = __shfl_sync(BAMF_FULL, tI, k), Xt = __shfl_sync(BAMF_FULL, tX, k);
+            float Yt = __shfl_sync(BAMF_FULL, tY, k);
+            bool isx = col < X;
+            int c = isx ? col : col - X;
+            float mu = isx ? (isnew ? Xt : Xa) : (isnew ? Yt : Ya);
+            float v = 0.5f * (MT::erf_(((float)c - mu + 1.0f) * Cst) - MT::erf_(((float)c - mu) * Cst));
+            if (b0 + lane < tot) {
+                if (isx) (isnew ? SXn : SXo)[q * X + c] = (isnew ? It : Ia) * v;
+                else (isnew ? SYn : SYo)[q * Y + c] = v;
+            }
         }
-        for (int b0 = 0; b0 < toty; b0 += 32) {
-            int item = b0 + lane;
-            int q = min(item / Y, nd - 1);
-            int y = item - q * Y;
-            int k = nth_bit(mask, q);
-            float Yk = __shfl_sync(BAMF_FULL, tY, k);
-            if (item < toty)
-                NY[k * Y + y] = 0.5f * (MT::erf_(((float)y - Yk + 1.0f) * Cst) -
-                                        MT::erf_(((float)y - Yk) * Cst));
+        __syncwarp();
+    }
+
+    /* Fast mode: out = background plane + sCMOS + sum of the state's emitter
+     * stencils, one emitter at a time (its rows go through SXn/SYn row 0). */
+    __device__ __forceinline__ void model_stream(int n, float I, float Xv, float Yv, float BG, float ABG,
+                                                 float BBG, float *out)
+    {
+        int x = lane / Y, y = lane - (lane / Y) * Y;
+#pragma unroll 1
+        for (int p = lane; p < npix; p += 32) {
+            out[p] = BG + ABG * (float)x + BBG * (float)y + (scm ? scm[p] : 0.0f);
+            x += px_dx;
+            y += px_dy;
+            if (y >= Y) {
+                y -= Y;
+                x++;
+            }
+        }
+#pragma unroll 1
+        for (int k = 0; k < n; ++k) {
+            float Ik = __shfl_sync(BAMF_FULL, I, k), Xk = __shfl_sync(BAMF_FULL, Xv, k);
+            float Yk = __shfl_sync(BAMF_FULL, Yv, k);
+            __syncwarp();
+#pragma unroll 1
+            for (int c = lane; c < X + Y; c += 32) {
+                bool isx = c < X;
+                int cc = isx ? c : c - X;
+                float mu = isx ? Xk : Yk;
+                float v = 0.5f * (MT::erf_(((float)cc - mu + 1.0f) * Cst) - MT::erf_(((float)cc - mu) * Cst));
+                if (isx) SXn[cc] = Ik * v;
+                else SYn[cc] = v;
+            }
+            __syncwarp();
+            x = lane / Y;
+            y = lane - (lane / Y) * Y;
+#pragma unroll 1
+            for (int p = lane; p < npix; p += 32) {
+                out[p] += SXn[x] * SYn[y];
+                x += px_dx;
+                y += px_dy;
+                if (y >= Y) {
+                    y -= Y;
+                    x++;
+                }
+            }
         }
         __syncwarp();
     }
@@ -458,36 +554,37 @@ struct ChainWarp {
             tmp = __shfl_sync(BAMF_FULL, tmp, 0);
             return MT::exp_(tmp);
         } else {
-            /* Mt = M - sum(old stencils of A's dirty/removed slots)
-             *        + sum(new stencils of T's dirty slots) + background delta */
-            stencils_dirty(t_dirty);
-            float dBG = tBG - aBG, dABG = tABG - aABG, dBBG = tBBG - aBBG;
-            uint32_t am = a_dirty, tm = t_dirty;
+            /* Mt = M + background delta - old stencils of A's changed slots
+             *        + new stencils of T's changed slots;
+             * sum over pixels of (M - Mt) + D (ln Mt - ln M) */
+            const float LN2 = 0.69314718f;
+            int na = __popc(a_dirty), nt = __popc(t_dirty);
             float acc = 0.0f;
             int x = lane / Y, y = lane - (lane / Y) * Y;
-            for (int p = lane; p < npix; p += 32) {
-                float d = dBG + dABG * (float)x + dBBG * (float)y;
-                uint32_t m1 = am;
-                while (m1) {
-                    int k = __ffs(m1) - 1;
-                    m1 &= m1 - 1u;
-                    d -= NXa[k * X + x] * NYa[k * Y + y];
+            if (na <= FAST_ROWS && nt <= FAST_ROWS) {
+                stencil_rows(na, nt);
+                float dBG = tBG - aBG, dABG = tABG - aABG, dBBG = tBBG - aBBG;
+#pragma unroll 2
+                for (int p = lane; p < npix; p += 32) {
+                    float d = dBG + dABG * (float)x + dBBG * (float)y;
+                    for (int q = 0; q < na; ++q) d -= SXo[q * X + x] * SYo[q * Y + y];
+                    for (int q = 0; q < nt; ++q) d += SXn[q * X + x] * SYn[q * Y + y];
+                    float mt = M[p] + d;
+                    Mt[p] = mt;
+                    acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - d;
+                    x += px_dx;
+                    y += px_dy;
+                    if (y >= Y) {
+                        y -= Y;
+                        x++;
+                    }
                 }
-                uint32_t m2 = tm;
-                while (m2) {
-                    int k = __ffs(m2) - 1;
-                    m2 &= m2 - 1u;
-                    d += NX[k * X + x] * NY[k * Y + y];
-                }
-                float mt = M[p] + d;
-                float lmt = __log2f(mt);
-                Mt[p] = mt;
-                acc += D[p] * (lmt - logM[p]) * 0.69314718f - d;
-                x += px_dx;
-                y += px_dy;
-                if (y >= Y) {
-                    y -= Y;
-                    x++;
+            } else {
+                model_stream(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
+#pragma unroll 1
+                for (int p = lane; p < npix; p += 32) {
+                    float mt = Mt[p];
+                    acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - (mt - M[p]);
                 }
             }
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(BAMF_FULL, acc, o);
@@ -495,28 +592,14 @@ struct ChainWarp {
         }
     }
 
-    /* fast mode: fold the accepted proposal into M, log2 M and the
-     * stencil cache of A */
+    /* fast mode: fold the accepted proposal into M and log2 M */
     __device__ __forceinline__ void commit_fast()
     {
+#pragma unroll 1
         for (int p = lane; p < npix; p += 32) {
             float m = Mt[p];
             M[p] = m;
             logM[p] = __log2f(m);
-        }
-        /* stencil cache: drop the removed slot, then take T's dirty rows */
-        if (removed >= 0) {
-            for (int k = removed; k < an - 1; ++k) {
-                for (int x = lane; x < X; x += 32) NXa[k * X + x] = NXa[(k + 1) * X + x];
-                for (int y = lane; y < Y; y += 32) NYa[k * Y + y] = NYa[(k + 1) * Y + y];
-            }
-        }
-        uint32_t m = t_dirty;
-        while (m) {
-            int k = __ffs(m) - 1;
-            m &= m - 1u;
-            for (int x = lane; x < X; x += 32) NXa[k * X + x] = NX[k * X + x];
-            for (int y = lane; y < Y; y += 32) NYa[k * Y + y] = NY[k * Y + y];
         }
         __syncwarp();
     }
@@ -533,13 +616,14 @@ struct ChainWarp {
         }
     }
 
-    /* Full rebuild of M (and, in fast mode, log2 M and A's stencil cache). */
+    /* Full rebuild of M (and, in fast mode, log2 M). */
     __device__ __forceinline__ void rebuild_model()
     {
         if (EXACT) {
             model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NX, NY);
         } else {
-            model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NXa, NYa);
+            model_stream(an, aI, aX, aY, aBG, aABG, aBBG, M);
+#pragma unroll 1
             for (int p = lane; p < npix; p += 32) logM[p] = __log2f(M[p]);
             __syncwarp();
         }
@@ -895,6 +979,7 @@ struct ChainWarp {
             int per = (npix + 31) >> 5;
             int p0 = min(lane * per, npix), p1 = min(p0 + per, npix);
             float s = 0.0f;
+#pragma unroll 1
             for (int p = p0; p < p1; ++p) {
                 float v = D[p] - M[p];
                 s += v > 0.0f ? v : 0.0f;
@@ -906,12 +991,14 @@ struct ChainWarp {
                 if (lane >= o) incl += t;
             }
             float excl = incl - s;
+#pragma unroll 1
             for (int p = p0; p < p1; ++p) Pf[p] += excl;
             __syncwarp();
             total = __shfl_sync(BAMF_FULL, incl, 31);
         }
         float rr = total * urand();
         int first = npix;
+#pragma unroll 1
         for (int p = lane; p < npix; p += 32)
             if (rr <= Pf[p]) {
                 first = p;
@@ -1172,9 +1259,10 @@ struct ChainWarp {
             mv_backfore();
             act = ACT_SKIP;
         }
+        float LLR = 0.0f, PR = 0.0f;
+        int accept = 0;
         if (act == ACT_EVAL) {
-            float LLR = llr();
-            float PR;
+            LLR = llr();
             switch (pk_move) {
             case MV_JUMP: PR = finish_jump(LLR); break;
             case MV_SPLIT: PR = finish_split(LLR); break;
@@ -1184,20 +1272,15 @@ struct ChainWarp {
             case MV_GSPLIT: PR = finish_gsplit(LLR); break;
             default: PR = finish_gmerge(LLR); break;
             }
-            int accept = (urand() < PR);
+            accept = (urand() < PR);
             if (accept) {
                 if (pk_c1 >= 0) cinc(pk_c1);
                 if (pk_c2 >= 0) cinc(pk_c2);
                 accept_T();
             }
-            record2(LLR, PR, pk_type, accept);
-            update_grids();
-        } else if (act == ACT_REJECT) {
-            record2(0.0f, 0.0f, pk_type, 0);
-            update_grids();
-        } else if (act == ACT_GRIDS) {
-            update_grids();
         }
+        if (act >= ACT_REJECT) record2(LLR, PR, pk_type, accept);
+        if (act >= ACT_GRIDS) update_grids();
     }
 
     /* RJMCMC::start_Chain (:685-750). */
@@ -1275,16 +1358,18 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ 
             w.logM = nullptr;
             w.NX = sw + 5 * npix_max;
             w.NY = w.NX + nxs;
-            w.NXa = w.NYa = nullptr;
+            w.SXo = w.SYo = w.SXn = w.SYn = nullptr;
             w.cnt = (int *)(w.NY + nxs);
         } else {
+            const int rs = FAST_ROWS * Bt.side_max;
             w.E = nullptr;
             w.logM = sw + 3 * npix_max;
-            w.NX = sw + 4 * npix_max;
-            w.NY = w.NX + nxs;
-            w.NXa = w.NY + nxs;
-            w.NYa = w.NXa + nxs;
-            w.cnt = (int *)(w.NYa + nxs);
+            w.NX = w.NY = nullptr;
+            w.SXo = sw + 4 * npix_max;
+            w.SYo = w.SXo + rs;
+            w.SXn = w.SYo + rs;
+            w.SYn = w.SXn + rs;
+            w.cnt = (int *)(w.SYn + rs);
         }
         w.cl = w.cnt + C_COUNT;
         bool ok = X >= 1 && Y >= 1 && X <= Bt.side_max && Y <= Bt.side_max;
@@ -1337,7 +1422,6 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ 
         w.overflow = 0;
         w.n_llr = 0;
         w.a_dirty = w.t_dirty = 0u;
-        w.removed = -1;
         w.rec_n[0] = w.rec_n[1] = 0;
         __syncwarp();
         w.rebuild_model();
