@@ -223,6 +223,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     }
     K.seed = seed;
     K.bg0 = rois->bg0;
+    K.sync_moves = arith == BAMF_ARITH_FAST ? 1 : 0;
 
     SamplerBatch B;
     std::memset(&B, 0, sizeof B);

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -260,6 +261,9 @@ static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, Samp
 {
     bamf_status r;
     bool exact = arith == BAMF_ARITH_EXACT;
+    SamplerConsts Kl = K;
+    /* fast arithmetic runs move-synchronous CTAs (rjmcmc_kernel_sync) */
+    Kl.sync_moves = exact ? 0 : 1;
     int ncls = B.class_range ? BAMF_N_CLASSES : 1;
     if ((r = ws->queue.ensure(sizeof(int32_t) * BAMF_N_CLASSES))) return r;
     CU(cudaMemsetAsync(ws->queue.p, 0, sizeof(int32_t) * BAMF_N_CLASSES, s));
@@ -286,8 +290,8 @@ static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, Samp
             cs = ws->cls_stream[c];
             CU(cudaStreamWaitEvent(cs, ws->fork_ev, 0));
         }
-        cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, cs)
-                              : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, cs);
+        cudaError_t e = exact ? launch_rjmcmc_exact(Kl, Bc, Bc.side_max, blocks, wpb, cs)
+                              : launch_rjmcmc_fast(Kl, Bc, Bc.side_max, blocks, wpb, cs);
         if (e != cudaSuccess) return cuda_fail(e, "rjmcmc kernel launch");
         if (fork) {
             CU(cudaEventRecord(ws->join_ev[c], cs));
@@ -328,13 +332,17 @@ __global__ void map_n_kernel(const uint8_t *__restrict__ trace, int trace_cap,
     }
 }
 
-/* Counting sort of ROI ids by size class, largest class first (one
- * block), and the [begin, end) range of every class in the sorted order. */
+/* Stable counting sort of ROI ids by size class, largest class first (one
+ * block of up to 1024 threads), and the [begin, end) range of every class in
+ * the sorted order.  Within a class the ROIs keep their input order, so the
+ * order (and with it which chains share a CTA) is the same on every call. */
 __global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__restrict__ ys,
                              int n, int32_t *__restrict__ order, int32_t *__restrict__ class_range)
 {
     __shared__ int cnt[BAMF_N_CLASSES];
     __shared__ int pos[BAMF_N_CLASSES];
+    __shared__ int wbase[32][BAMF_N_CLASSES];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if (threadIdx.x < BAMF_N_CLASSES) cnt[threadIdx.x] = 0;
     __syncthreads();
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -352,9 +360,30 @@ __global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__re
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        int c = side_class(min(max(max(xs[i], ys[i]), 1), BAMF_MAX_ROI_SIDE));
-        order[atomicAdd(&pos[c], 1)] = i;
+    /* chunks of blockDim.x ids: rank within the warp by ballot, warp offsets
+     * by a per-class scan over the warps, in id order */
+    for (int base = 0; base < n; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        int c = i < n ? side_class(min(max(max(xs[i], ys[i]), 1), BAMF_MAX_ROI_SIDE)) : -1;
+        int rank = 0;
+        for (int k = 0; k < BAMF_N_CLASSES; ++k) {
+            unsigned m = __ballot_sync(0xffffffffu, c == k);
+            if (c == k) rank = __popc(m & ((1u << lane) - 1u));
+            if (lane == 0) wbase[wid][k] = __popc(m);
+        }
+        __syncthreads();
+        if (threadIdx.x < BAMF_N_CLASSES) {
+            int k = threadIdx.x, acc = pos[k];
+            for (int w = 0; w < nw; ++w) {
+                int t = wbase[w][k];
+                wbase[w][k] = acc;
+                acc += t;
+            }
+            pos[k] = acc;
+        }
+        __syncthreads();
+        if (c >= 0) order[wbase[wid][c] + rank] = i;
+        __syncthreads();
     }
 }
 

@@ -168,6 +168,22 @@ static __device__ __noinline__ float irwin_hall12(uint32_t idx, uint32_t base, u
     return u - 6.0f;
 }
 
+/* Uniform in [0, 1) shared by the warps of a CTA in move-synchronous mode:
+ * a 32-bit integer hash (the "lowbias32" xorshift-multiply finaliser,
+ * applied twice) of (seed, group, step, which). */
+__device__ __forceinline__ float shared_uniform(uint32_t seed, uint32_t grp, uint32_t step, uint32_t which)
+{
+    uint32_t x = seed * 0x9E3779B1u ^ grp * 0x85EBCA77u ^ (step * 2u + which) * 0xC2B2AE3Du;
+    for (int r = 0; r < 2; ++r) {
+        x ^= x >> 16;
+        x *= 0x7feb352du;
+        x ^= x >> 15;
+        x *= 0x846ca68bu;
+        x ^= x >> 16;
+    }
+    return (float)(x >> 8) * 5.9604644775390625e-08f;
+}
+
 /* normpdf (LibRJMCMCreturn.hpp:19-21) with (float)sqrt(2.0f*pi), pi = 3.141592. */
 template <bool EXACT>
 static __device__ __noinline__ float normpdf_f(float x, float u, float s)
@@ -216,6 +232,9 @@ struct ChainWarp {
     int n_llr;
     /* incremental-model bookkeeping (fast mode) */
     uint32_t a_dirty, t_dirty;
+    /* move-synchronous mode: the jump sub-branch uniform comes from the CTA */
+    bool use_shared_ub;
+    float shared_ub;
 
     /* ---------------------------------------------------------- RNG */
     __device__ __forceinline__ void refill()
@@ -712,7 +731,7 @@ struct ChainWarp {
         if (an < 1) return ACT_SKIP;
         float Ua = urand();
         int nn = min((int)(Ua * (float)tn), tn - 1);
-        float Ub = urand();
+        float Ub = use_shared_ub ? shared_ub : urand();
         const bamf_mcmc_params &p = K->p;
         if (Ub < 0.25f) {
             type = 2;
@@ -1284,6 +1303,36 @@ struct ChainWarp {
     }
 
     /* RJMCMC::start_Chain (:685-750). */
+    /* Move-synchronous chain (fast mode): every warp of the CTA takes the
+     * same move type and jump sub-branch at each jump, drawn from a stream
+     * shared by the CTA, and the warps meet at a barrier before each jump,
+     * so the warps of an SM run the same code.  For each chain the move
+     * choice is still i.i.d. with the configured probabilities and
+     * independent of its state, so its transition kernel is unchanged.
+     * Warps without a ROI (the tail of the queue) only take the barriers. */
+    __device__ __forceinline__ void run_chain_sync(bool active, uint32_t grp)
+    {
+        const bamf_mcmc_params &p = K->p;
+        use_shared_ub = true;
+        int since_rebuild = 0;
+        const int total = p.N_Burnin + p.N_Trials;
+        for (int n = 0; n < total; ++n) {
+            __syncthreads();
+            if (n == 0 || n == p.N_Burnin) {
+                is_burnin = n < p.N_Burnin;
+                for (int k = 0; k < 8; ++k) P[k] = is_burnin ? p.P_Burnin[k] : K->PVT[k];
+            }
+            if (!active) continue;
+            float t = shared_uniform(K->seed, grp, (uint32_t)n, 0u);
+            shared_ub = shared_uniform(K->seed, grp, (uint32_t)n, 1u);
+            step(K->PVB, is_burnin ? K->PVB : K->PVT, t);
+            if (++since_rebuild == 512) {
+                rebuild_model();
+                since_rebuild = 0;
+            }
+        }
+    }
+
     __device__ __forceinline__ void run_chain()
     {
         const bamf_mcmc_params &p = K->p;
@@ -1311,22 +1360,150 @@ struct ChainWarp {
     }
 };
 
+/* Loads ROI `roi` into a warp's carve-out and sets up its chain (the
+ * set-up of cRJMCMC.cpp:103-148).  Returns false, with the ROI's status set,
+ * when the ROI does not fit the launch. */
+template <bool EXACT>
+__device__ __forceinline__ bool begin_roi(ChainWarp<EXACT> &w, const SamplerConsts *Kp, const SamplerBatch &Bt,
+                                          float *sw, int roi)
+{
+    const int lane = w.lane;
+    w.roi = roi;
+    int X = Bt.xsize[roi], Y = Bt.ysize[roi];
+    w.X = X;
+    w.Y = Y;
+    w.npix = X * Y;
+    w.px_dx = 32 / Y;
+    w.px_dy = 32 - (32 / Y) * Y;
+    int npix_max = Bt.side_max * Bt.side_max;
+    int nxs = BAMF_NMAX * Bt.side_max;
+    w.D = sw;
+    w.M = sw + npix_max;
+    w.Mt = sw + 2 * npix_max;
+    float *scm_smem = nullptr;
+    if (EXACT) {
+        w.E = sw + 3 * npix_max;
+        scm_smem = sw + 4 * npix_max;
+        w.logM = nullptr;
+        w.NX = sw + 5 * npix_max;
+        w.NY = w.NX + nxs;
+        w.SXo = w.SYo = w.SXn = w.SYn = nullptr;
+        w.cnt = (int *)(w.NY + nxs);
+    } else {
+        const int rs = FAST_ROWS * Bt.side_max;
+        w.E = nullptr;
+        w.logM = sw + 3 * npix_max;
+        w.NX = w.NY = nullptr;
+        w.SXo = sw + 4 * npix_max;
+        w.SYo = w.SXo + rs;
+        w.SXn = w.SYo + rs;
+        w.SYn = w.SXn + rs;
+        w.cnt = (int *)(w.SYn + rs);
+    }
+    w.cl = w.cnt + C_COUNT;
+    int n0 = Bt.init_n ? Bt.init_n[roi] : 0;
+    bool ok = X >= 1 && Y >= 1 && X <= Bt.side_max && Y <= Bt.side_max && n0 <= BAMF_NMAX;
+    if (!ok) {
+        if (lane == 0 && Bt.status) Bt.status[roi] = BAMF_ERR_TOO_LARGE;
+        return false;
+    }
+    const float *src = Bt.data + Bt.offsets[roi];
+    const float *scm_src = Bt.scmos ? Bt.scmos + Bt.offsets[roi] : nullptr;
+    for (int p = lane; p < w.npix; p += 32) {
+        w.D[p] = src[p];
+        if (EXACT) scm_smem[p] = scm_src ? scm_src[p] : 0.0f;
+    }
+    w.scm = EXACT ? scm_smem : scm_src;
+    if (lane < C_COUNT) {
+        int k = lane;
+        bool isN = (k <= C_N_death) || (k >= C_N_jumpFg && k <= C_N_deathFg) ||
+                   (k >= C_N_jumpBg && k <= C_N_deathBg);
+        w.cnt[k] = isN ? 1 : 0;
+    }
+    float s = Bt.psf_sigma ? Bt.psf_sigma[roi] : Kp->p.PSFsigma;
+    w.sigma = s;
+    w.Cst = 1.0f / (s * sqrtf(2.0f));
+    w.MeanN = Kp->p.Rho * (float)X * (float)Y;
+    /* start state (cRJMCMC.cpp:120-133) */
+    w.an = n0;
+    w.aI = w.aX = w.aY = 0.0f;
+    w.aS = 1;
+    if (n0 > 0 && lane < n0) {
+        const float *ixy = Bt.init_ixy + (size_t)roi * 3 * BAMF_NMAX;
+        w.aI = ixy[lane];
+        w.aX = ixy[BAMF_NMAX + lane];
+        w.aY = ixy[2 * BAMF_NMAX + lane];
+    }
+    w.aBG = Bt.init_bg ? Bt.init_bg[roi] : Kp->bg0;
+    if (w.aBG == 0.0f) w.aBG = 1.0f;
+    w.aABG = 0.0f;
+    w.aBBG = 0.0f;
+    w.seed = Kp->seed;
+    w.chain = Bt.chain_ids ? Bt.chain_ids[roi] : (uint32_t)roi;
+    w.idx = Bt.rng_offset ? Bt.rng_offset[roi] : 0u;
+    w.base = w.idx >> 2;
+    w.refill();
+    w.entries = 0;
+    w.overflow = 0;
+    w.n_llr = 0;
+    w.a_dirty = w.t_dirty = 0u;
+    w.use_shared_ub = false;
+    w.shared_ub = 0.0f;
+    w.rec_n[0] = w.rec_n[1] = 0;
+    __syncwarp();
+    w.rebuild_model();
+    return true;
+}
+
+/* Writes the chain's per-ROI results. */
+template <bool EXACT>
+__device__ __forceinline__ void end_roi(ChainWarp<EXACT> &w, const SamplerBatch &Bt)
+{
+    const int lane = w.lane, roi = w.roi;
+    if (Bt.final_n && lane == 0) Bt.final_n[roi] = w.an;
+    if (Bt.final_state) {
+        float *fs = Bt.final_state + (size_t)roi * (4 + 4 * BAMF_NMAX);
+        if (lane == 0) {
+            fs[0] = w.aBG; fs[1] = w.aABG; fs[2] = w.aBBG; fs[3] = (float)w.an;
+        }
+        fs[4 + lane] = lane < w.an ? w.aI : 0.0f;
+        fs[4 + BAMF_NMAX + lane] = lane < w.an ? w.aX : 0.0f;
+        fs[4 + 2 * BAMF_NMAX + lane] = lane < w.an ? w.aY : 0.0f;
+        fs[4 + 3 * BAMF_NMAX + lane] = lane < w.an ? (float)w.aS : 0.0f;
+    }
+    __syncwarp();
+    if (Bt.counters)
+        for (int k = lane; k < C_COUNT; k += 32) Bt.counters[(size_t)roi * C_COUNT + k] = w.cnt[k];
+    if (Bt.chains && lane == 0) {
+        Bt.chains[2 * roi].n_entries = min(w.entries, Bt.chains[2 * roi].capacity_entries);
+        Bt.chains[2 * roi + 1].n_entries = min(w.entries, Bt.chains[2 * roi + 1].capacity_entries);
+        Bt.chains[2 * roi].n_records = w.rec_n[0];
+        Bt.chains[2 * roi + 1].n_records = w.rec_n[1];
+    }
+    if (lane == 0) {
+        if (Bt.n_entries) Bt.n_entries[roi] = w.entries;
+        if (Bt.uniforms_used) Bt.uniforms_used[roi] = w.idx - (Bt.rng_offset ? Bt.rng_offset[roi] : 0u);
+        if (Bt.overflow) Bt.overflow[roi] = w.overflow;
+        if (Bt.llr_evals) Bt.llr_evals[roi] = w.n_llr;
+        if (Bt.status) Bt.status[roi] = BAMF_OK;
+    }
+    __syncwarp();
+}
+
+/* Persistent sampler: each warp pulls ROI ids from the work queue and runs
+ * their chains one after another. */
 template <bool EXACT>
 __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ SamplerConsts Kc,
                                                      const __grid_constant__ SamplerBatch Bc)
 {
     extern __shared__ float smem_raw[];
-    const SamplerConsts *Kp = &Kc;
-    const SamplerBatch *Bp = &Bc;
     const SamplerBatch &Bt = Bc;
     int warp = threadIdx.x >> 5;
     int lane = threadIdx.x & 31;
-    int per = warp_smem_floats(Bt.side_max, EXACT);
-    float *sw = smem_raw + (size_t)warp * per;
-
+    float *sw = smem_raw + (size_t)warp * warp_smem_floats(Bt.side_max, EXACT);
     ChainWarp<EXACT> w;
-    w.K = Kp;
-    w.B = Bp;
+    w.K = &Kc;
+    w.B = &Bc;
     w.lane = lane;
     int q_begin = 0, q_end = Bt.n_rois;
     if (Bt.class_range) {
@@ -1339,124 +1516,54 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ 
         slot = __shfl_sync(BAMF_FULL, slot, 0);
         if (slot >= q_end) break;
         int roi = Bt.order ? Bt.order[slot] : slot;
-        w.roi = roi;
-        int X = Bt.xsize[roi], Y = Bt.ysize[roi];
-        w.X = X;
-        w.Y = Y;
-        w.npix = X * Y;
-        w.px_dx = 32 / Y;
-        w.px_dy = 32 - (32 / Y) * Y;
-        int npix_max = Bt.side_max * Bt.side_max;
-        int nxs = BAMF_NMAX * Bt.side_max;
-        w.D = sw;
-        w.M = sw + npix_max;
-        w.Mt = sw + 2 * npix_max;
-        float *scm_smem = nullptr;
-        if (EXACT) {
-            w.E = sw + 3 * npix_max;
-            scm_smem = sw + 4 * npix_max;
-            w.logM = nullptr;
-            w.NX = sw + 5 * npix_max;
-            w.NY = w.NX + nxs;
-            w.SXo = w.SYo = w.SXn = w.SYn = nullptr;
-            w.cnt = (int *)(w.NY + nxs);
-        } else {
-            const int rs = FAST_ROWS * Bt.side_max;
-            w.E = nullptr;
-            w.logM = sw + 3 * npix_max;
-            w.NX = w.NY = nullptr;
-            w.SXo = sw + 4 * npix_max;
-            w.SYo = w.SXo + rs;
-            w.SXn = w.SYo + rs;
-            w.SYn = w.SXn + rs;
-            w.cnt = (int *)(w.SYn + rs);
-        }
-        w.cl = w.cnt + C_COUNT;
-        bool ok = X >= 1 && Y >= 1 && X <= Bt.side_max && Y <= Bt.side_max;
-        if (!ok) {
-            if (lane == 0 && Bt.status) Bt.status[roi] = BAMF_ERR_TOO_LARGE;
-            continue;
-        }
-        const float *src = Bt.data + Bt.offsets[roi];
-        const float *scm_src = Bt.scmos ? Bt.scmos + Bt.offsets[roi] : nullptr;
-        for (int p = lane; p < w.npix; p += 32) {
-            w.D[p] = src[p];
-            if (EXACT) scm_smem[p] = scm_src ? scm_src[p] : 0.0f;
-        }
-        w.scm = EXACT ? scm_smem : scm_src;
-        if (lane < C_COUNT) {
-            int k = lane;
-            bool isN = (k <= C_N_death) || (k >= C_N_jumpFg && k <= C_N_deathFg) ||
-                       (k >= C_N_jumpBg && k <= C_N_deathBg);
-            w.cnt[k] = isN ? 1 : 0;
-        }
-        float s = Bt.psf_sigma ? Bt.psf_sigma[roi] : Kp->p.PSFsigma;
-        w.sigma = s;
-        w.Cst = 1.0f / (s * sqrtf(2.0f));
-        w.MeanN = Kp->p.Rho * (float)X * (float)Y;
-        /* start state (cRJMCMC.cpp:120-133) */
-        int n0 = Bt.init_n ? Bt.init_n[roi] : 0;
-        if (n0 > BAMF_NMAX) {
-            if (lane == 0 && Bt.status) Bt.status[roi] = BAMF_ERR_TOO_LARGE;
-            continue;
-        }
-        w.an = n0;
-        w.aI = w.aX = w.aY = 0.0f;
-        w.aS = 1;
-        if (n0 > 0 && lane < n0) {
-            const float *ixy = Bt.init_ixy + (size_t)roi * 3 * BAMF_NMAX;
-            w.aI = ixy[lane];
-            w.aX = ixy[BAMF_NMAX + lane];
-            w.aY = ixy[2 * BAMF_NMAX + lane];
-        }
-        w.aBG = Bt.init_bg ? Bt.init_bg[roi] : Kp->bg0;
-        if (w.aBG == 0.0f) w.aBG = 1.0f;
-        w.aABG = 0.0f;
-        w.aBBG = 0.0f;
-        w.seed = Kp->seed;
-        w.chain = Bt.chain_ids ? Bt.chain_ids[roi] : (uint32_t)roi;
-        w.idx = Bt.rng_offset ? Bt.rng_offset[roi] : 0u;
-        w.base = w.idx >> 2;
-        w.refill();
-        w.entries = 0;
-        w.overflow = 0;
-        w.n_llr = 0;
-        w.a_dirty = w.t_dirty = 0u;
-        w.rec_n[0] = w.rec_n[1] = 0;
-        __syncwarp();
-        w.rebuild_model();
+        if (!begin_roi(w, &Kc, Bt, sw, roi)) continue;
         w.run_chain();
-        /* outputs */
-        if (Bt.final_n && lane == 0) Bt.final_n[roi] = w.an;
-        if (Bt.final_state) {
-            float *fs = Bt.final_state + (size_t)roi * (4 + 4 * BAMF_NMAX);
-            if (lane == 0) {
-                fs[0] = w.aBG; fs[1] = w.aABG; fs[2] = w.aBBG; fs[3] = (float)w.an;
-            }
-            fs[4 + lane] = lane < w.an ? w.aI : 0.0f;
-            fs[4 + BAMF_NMAX + lane] = lane < w.an ? w.aX : 0.0f;
-            fs[4 + 2 * BAMF_NMAX + lane] = lane < w.an ? w.aY : 0.0f;
-            fs[4 + 3 * BAMF_NMAX + lane] = lane < w.an ? (float)w.aS : 0.0f;
-        }
-        __syncwarp();
-        if (Bt.counters)
-            for (int k = lane; k < C_COUNT; k += 32) Bt.counters[(size_t)roi * C_COUNT + k] = w.cnt[k];
-        if (Bt.chains && lane == 0) {
-            Bt.chains[2 * roi].n_entries = min(w.entries, Bt.chains[2 * roi].capacity_entries);
-            Bt.chains[2 * roi + 1].n_entries = min(w.entries, Bt.chains[2 * roi + 1].capacity_entries);
-            Bt.chains[2 * roi].n_records = w.rec_n[0];
-            Bt.chains[2 * roi + 1].n_records = w.rec_n[1];
-        }
-        if (lane == 0) {
-            if (Bt.n_entries) Bt.n_entries[roi] = w.entries;
-            if (Bt.uniforms_used) Bt.uniforms_used[roi] = w.idx - (Bt.rng_offset ? Bt.rng_offset[roi] : 0u);
-            if (Bt.overflow) Bt.overflow[roi] = w.overflow;
-            if (Bt.llr_evals) Bt.llr_evals[roi] = w.n_llr;
-            if (Bt.status) Bt.status[roi] = BAMF_OK;
-        }
-        __syncwarp();
+        end_roi(w, Bt);
     }
 }
 
+/* Move-synchronous persistent sampler (fast arithmetic): the CTA pulls one
+ * ROI per warp at a time and its warps run their chains in lockstep, one
+ * barrier per jump, with the move type and jump sub-branch shared across the
+ * CTA (run_chain_sync). */
+template <int UNUSED>
+__global__ void __launch_bounds__(128, 4) rjmcmc_kernel_sync(const __grid_constant__ SamplerConsts Kc,
+                                                          const __grid_constant__ SamplerBatch Bc)
+{
+    extern __shared__ float smem_raw[];
+    __shared__ int grp_base;
+    const SamplerBatch &Bt = Bc;
+    const int nwarps = blockDim.x >> 5;
+    int warp = threadIdx.x >> 5;
+    int lane = threadIdx.x & 31;
+    float *sw = smem_raw + (size_t)warp * warp_smem_floats(Bt.side_max, false);
+    ChainWarp<false> w;
+    w.K = &Kc;
+    w.B = &Bc;
+    w.lane = lane;
+    int q_begin = 0, q_end = Bt.n_rois;
+    if (Bt.class_range) {
+        q_begin = Bt.class_range[2 * Bt.cls];
+        q_end = Bt.class_range[2 * Bt.cls + 1];
+    }
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) grp_base = q_begin + atomicAdd(Bt.queue, nwarps);
+        __syncthreads();
+        int base = grp_base;
+        if (base >= q_end) break;
+        int slot = base + warp;
+        bool active = slot < q_end;
+        if (active) {
+            int roi = Bt.order ? Bt.order[slot] : slot;
+            active = begin_roi(w, &Kc, Bt, sw, roi);
+        }
+        /* the shared move stream is keyed by the slot group of BAMF_SYNC_GROUP
+         * ROIs, not by the CTA, so a chain's moves (and its result) do not
+         * depend on the launch's warps per block (1, 2 or 4) */
+        w.run_chain_sync(active, (uint32_t)(q_begin + ((base - q_begin) & ~(BAMF_SYNC_GROUP - 1))));
+        if (active) end_roi(w, Bt);
+    }
+}
 
 }  // namespace bamf

@@ -81,14 +81,39 @@ def test_exact_batch_matches_oracle(cuda_lib, oracle_port):
 
 
 def test_fast_batch_runs_and_agrees_in_distribution(cuda_lib):
-    b, rj = _c0(64, steps=1500)
+    """Fast arithmetic draws each jump's move type from a stream shared by the
+    chains of a CTA, so its chains do not follow the exact chains path by
+    path; each chain's law is the same, so MAP counts, proposal mix and
+    acceptance rates agree in distribution."""
+    b, rj = _c0(256, steps=1500)
     p = rjstruct.mcmc_params(rj)
     bg0 = rjstruct.initial_bg(rj)
     s = sampler.Sampler()
     ex = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=3, arith="exact", bg0=bg0)
     fa = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=3, arith="fast", bg0=bg0)
     assert (fa["status"] == 0).all() and (fa["overflow"] == 0).all()
-    # same uniforms: most chains follow the exact chain to the end
+    # the MAP count is set by the data: both arithmetics find the same one on most ROIs
     agree = np.mean(fa["map_n"] == ex["map_n"])
-    assert agree > 0.7, agree
+    assert agree > 0.6, agree
+    assert abs(fa["map_n"].mean() - ex["map_n"].mean()) < 0.3
     assert abs(fa["map_n"].mean() - b.true_n.mean()) < 1.0
+    # proposal mix: the move-type frequencies follow P_Burnin / P_Trials in both
+    nf = fa["counters"][:, 0:5].sum(axis=0).astype(float)
+    ne = ex["counters"][:, 0:5].sum(axis=0).astype(float)
+    np.testing.assert_allclose(nf / nf.sum(), ne / ne.sum(), atol=0.01)
+    # acceptance rate per move type within a few points
+    af = fa["counters"][:, 5:10].sum(axis=0) / nf
+    ae = ex["counters"][:, 5:10].sum(axis=0) / ne
+    np.testing.assert_allclose(af, ae, atol=0.04)
+
+def test_fast_batch_is_deterministic(cuda_lib):
+    """The same seed gives the same chains on every call: the size-class order
+    of the ROIs (and so which chains share a move stream) is a stable sort."""
+    b, rj = _c0(200, steps=400)
+    p = rjstruct.mcmc_params(rj)
+    bg0 = rjstruct.initial_bg(rj)
+    s = sampler.Sampler()
+    r1 = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=5, arith="fast", bg0=bg0)
+    r2 = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=5, arith="fast", bg0=bg0)
+    for k in ("map_n", "final_n", "final_state", "counters"):
+        np.testing.assert_array_equal(r1[k], r2[k], err_msg=k)
