@@ -43,6 +43,8 @@ int blocks_per_sm_fast(int side_max, int warps_per_block);
 }  // namespace bamf
 
 /* defined in api_sampler.cu */
+bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcmc_params *p, int arith,
+                                      const bamf_batch_results *out);
 __global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__restrict__ ys, int n,
                              int32_t *__restrict__ order, int32_t *__restrict__ class_range);
 __global__ void map_n_kernel(const uint8_t *__restrict__ trace, int trace_cap,
@@ -165,10 +167,13 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         bamf_status r = count_unique(pdf[k], L[k], p->DX, &nu[k]);
         if (r) return r;
     }
+    bamf_status r0 = check_proposal_and_traces(rois, p, arith, out);
+    if (r0) return r0;
     /* scratch plan; reject what does not fit */
     const int n = rois->n_rois;
     const int64_t steps = (int64_t)p->N_Burnin + p->N_Trials;
     const bool want_map = out->map_n != nullptr;
+    const bool user_trace = out->n_trace != nullptr;
     size_t off_tables = 512, tab_off[3], used = off_tables;
     for (int k = 0; k < 3; ++k) {
         tab_off[k] = used;
@@ -180,7 +185,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     bool own_entries = want_map && out->n_entries == nullptr;
     if (own_entries) used = align256(used + (size_t)n * sizeof(int32_t));
     size_t off_trace = used;
-    if (want_map) {
+    if (want_map && !user_trace) {
         if (steps > INT32_MAX) return BAMF_ERR_TOO_LARGE;
         used += (size_t)n * (size_t)steps;
     }
@@ -224,6 +229,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     K.seed = seed;
     K.bg0 = rois->bg0;
     K.sync_moves = arith == BAMF_ARITH_FAST ? 1 : 0;
+    K.proposal = rois->proposal;
 
     SamplerBatch B;
     std::memset(&B, 0, sizeof B);
@@ -250,10 +256,19 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     int32_t *entries = out->n_entries;
     if (own_entries) entries = (int32_t *)(S + off_entries);
     B.n_entries = entries;
-    if (want_map) {
+    if (user_trace) {
+        B.nsig_trace = out->n_trace;
+        B.trace_cap = out->trace_len;
+    } else if (want_map) {
         B.nsig_trace = S + off_trace;
         B.trace_cap = (int32_t)steps;
     }
+    if (out->x_trace) {
+        B.x_trace = out->x_trace;
+        B.x_cap = out->trace_len;
+    }
+    B.birth_cdf = rois->birth_cdf;
+    B.birth_sub = rois->birth_sub;
     if (cudaGetLastError() != cudaSuccess) return BAMF_ERR_CUDA;
 
     const bool exact = arith == BAMF_ARITH_EXACT;
@@ -273,7 +288,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         if (e != cudaSuccess) return BAMF_ERR_CUDA;
     }
     if (want_map) {
-        map_n_kernel<<<(n + 7) / 8, 256, 0, s>>>(B.nsig_trace, (int)steps, entries, n, out->map_n);
+        map_n_kernel<<<(n + 7) / 8, 256, 0, s>>>(B.nsig_trace, B.trace_cap, entries, n, out->map_n);
         if (cudaGetLastError() != cudaSuccess) return BAMF_ERR_CUDA;
     }
     return BAMF_OK;

@@ -387,6 +387,22 @@ __global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__re
     }
 }
 
+/* Checks of the proposal fields of a batch and of the trace outputs, shared
+ * with the allocation-free entry point. */
+bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcmc_params *p, int arith,
+                                      const bamf_batch_results *out)
+{
+    if (rois->proposal < BAMF_PROPOSAL_REFERENCE || rois->proposal > BAMF_PROPOSAL_LEARNED)
+        return BAMF_ERR_INVALID_ARG;
+    if (rois->proposal != BAMF_PROPOSAL_REFERENCE && arith != BAMF_ARITH_FAST) return BAMF_ERR_INVALID_ARG;
+    if (rois->proposal == BAMF_PROPOSAL_LEARNED && (!rois->birth_cdf || !rois->birth_sub))
+        return BAMF_ERR_INVALID_ARG;
+    if ((out->n_trace || out->x_trace) && out->trace_len < 1) return BAMF_ERR_INVALID_ARG;
+    if (out->n_trace && out->map_n && (int64_t)out->trace_len < (int64_t)p->N_Burnin + p->N_Trials)
+        return BAMF_ERR_INVALID_ARG;
+    return BAMF_OK;
+}
+
 extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_roi_batch *rois,
                                                 const bamf_mcmc_params *p,
                                                 const bamf_priors *priors, uint32_t seed,
@@ -401,11 +417,14 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     if ((rois->init_n != nullptr) != (rois->init_ixy != nullptr)) return BAMF_ERR_INVALID_ARG;
     int side_max = rois->side_max > 0 ? rois->side_max : BAMF_MAX_ROI_SIDE;
     if (side_max > BAMF_MAX_ROI_SIDE) return BAMF_ERR_TOO_LARGE;
+    bamf_status r0 = check_proposal_and_traces(rois, p, arith, out);
+    if (r0) return r0;
     if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
     cudaStream_t s = (cudaStream_t)stream;
     SamplerConsts K;
     bamf_status r = make_consts(ws, p, priors, seed, rois->bg0, K, s);
     if (r) return r;
+    K.proposal = rois->proposal;
     int n = rois->n_rois;
     int64_t steps = (int64_t)p->N_Burnin + p->N_Trials;
     int trace_cap = (int)std::min<int64_t>(steps, INT32_MAX);
@@ -428,13 +447,22 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     B.status = out->status;
     B.overflow = out->overflow;
     B.llr_evals = out->llr_evals;
+    B.birth_cdf = rois->birth_cdf;
+    B.birth_sub = rois->birth_sub;
+    if (out->x_trace) {
+        B.x_trace = out->x_trace;
+        B.x_cap = out->trace_len;
+    }
     if ((r = ws->order.ensure((size_t)n * sizeof(int32_t) + 256))) return r;
     B.order = (int32_t *)((char *)ws->order.p + 256);
     int32_t *class_range = (int32_t *)ws->order.p; /* 2 * BAMF_N_CLASSES ints */
     order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)B.order, class_range);
     CU(cudaGetLastError());
     B.class_range = class_range;
-    if (out->map_n) {
+    if (out->n_trace) {
+        B.nsig_trace = out->n_trace;
+        B.trace_cap = out->trace_len;
+    } else if (out->map_n) {
         if ((r = ws->trace.ensure((size_t)n * trace_cap))) return r;
         B.nsig_trace = (uint8_t *)ws->trace.p;
         B.trace_cap = trace_cap;
@@ -447,7 +475,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     B.n_entries = entries;
     if ((r = launch_batch(ws, K, B, arith, s))) return r;
     if (out->map_n) {
-        map_n_kernel<<<(n + 7) / 8, 256, 0, s>>>(B.nsig_trace, trace_cap, entries, n, out->map_n);
+        map_n_kernel<<<(n + 7) / 8, 256, 0, s>>>(B.nsig_trace, B.trace_cap, entries, n, out->map_n);
         CU(cudaGetLastError());
     }
     return BAMF_OK;
@@ -502,6 +530,8 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if (n < 0) return BAMF_ERR_INVALID_ARG;
     if (n == 0) return BAMF_OK;
     if (!rois->data || !rois->offsets || !rois->xsize || !rois->ysize) return BAMF_ERR_INVALID_ARG;
+    bamf_status r0 = check_proposal_and_traces(rois, p, arith, out);
+    if (r0) return r0;
     if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
     int64_t npix = 0;
     int side_max = 0;
@@ -524,6 +554,10 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if ((r = upload(o, (int32_t **)&d.init_n, rois->init_n, (size_t)n))) return r;
     if ((r = upload(o, (float **)&d.init_bg, rois->init_bg, (size_t)n))) return r;
     if ((r = upload(o, (float **)&d.init_ixy, rois->init_ixy, (size_t)n * 3 * BAMF_NMAX))) return r;
+    if (rois->proposal == BAMF_PROPOSAL_LEARNED) {
+        if ((r = upload(o, (float **)&d.birth_cdf, rois->birth_cdf, (size_t)npix))) return r;
+        if ((r = upload(o, (float **)&d.birth_sub, rois->birth_sub, (size_t)npix * 16))) return r;
+    }
     bamf_batch_results dout;
     std::memset(&dout, 0, sizeof dout);
     const size_t fs = 4 + 4 * BAMF_NMAX;
@@ -535,6 +569,10 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if (out->status && (r = dalloc(o.v, &dout.status, n))) return r;
     if (out->overflow && (r = dalloc(o.v, &dout.overflow, n))) return r;
     if (out->llr_evals && (r = dalloc(o.v, &dout.llr_evals, n))) return r;
+    const size_t tl = out->trace_len > 0 ? (size_t)out->trace_len : 0;
+    dout.trace_len = out->trace_len;
+    if (out->n_trace && tl && (r = dalloc(o.v, &dout.n_trace, (size_t)n * tl))) return r;
+    if (out->x_trace && tl && (r = dalloc(o.v, &dout.x_trace, (size_t)n * tl))) return r;
     if ((r = bamf_rjmcmc_batch_device(ws, &d, p, priors, seed, arith, &dout, nullptr))) return r;
     CU(cudaDeviceSynchronize());
     if ((r = download(out->map_n, dout.map_n, n))) return r;
@@ -545,6 +583,8 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if ((r = download(out->status, dout.status, n))) return r;
     if ((r = download(out->overflow, dout.overflow, n))) return r;
     if ((r = download(out->llr_evals, dout.llr_evals, n))) return r;
+    if ((r = download(out->n_trace, dout.n_trace, (size_t)n * tl))) return r;
+    if ((r = download(out->x_trace, dout.x_trace, (size_t)n * tl))) return r;
     return BAMF_OK;
 }
 

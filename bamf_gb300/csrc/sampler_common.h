@@ -32,6 +32,7 @@ struct SamplerConsts {
     uint32_t seed;
     float bg0;      /* starting BG when no per-ROI start state is given */
     int32_t sync_moves; /* fast mode: CTA-synchronous move choice (rjmcmc_kernel_sync) */
+    int32_t proposal;   /* BAMF_PROPOSAL_* (fast mode only) */
 };
 
 /* Per-ROI inputs and outputs of a batch.  Arrays indexed by ROI id. */
@@ -57,6 +58,10 @@ struct SamplerBatch {
     int32_t *counters;            /* [roi][30] bamf_counters order          */
     uint8_t *nsig_trace;          /* [roi][trace_cap] Signal==1 count per entry */
     int32_t trace_cap;
+    float *x_trace;               /* [roi][x_cap] mean X of the Signal==1 emitters */
+    int32_t x_cap;
+    const float *birth_cdf;       /* learned birth density (bamf_roi_batch)  */
+    const float *birth_sub;
     int32_t *n_entries;           /* [roi] recorded chain entries          */
     uint32_t *uniforms_used;      /* [roi]                                 */
     int32_t *status;              /* [roi] 0 ok, else BAMF_ERR_*           */

@@ -184,6 +184,27 @@ __device__ __forceinline__ float shared_uniform(uint32_t seed, uint32_t grp, uin
     return (float)(x >> 8) * 5.9604644775390625e-08f;
 }
 
+/* (1 / A) / q(x, y) for the LEARNED birth proposal q = (learned + uniform)/2
+ * on a box of area A; the learned part is the ROI's pixel running sum cdf
+ * times the pixel's 16 sub-cell probabilities sub (16 cells per px^2). */
+static __device__ __noinline__ float learned_q_ratio(float x, float y, int X, int Y, int npix, float A,
+                                                     const float *__restrict__ cdf,
+                                                     const float *__restrict__ sub)
+{
+    float qa = 0.0f; /* learned density times box area */
+    if (x >= 0.0f && y >= 0.0f && x < (float)X && y < (float)Y) {
+        int px = min((int)x, X - 1), py = min((int)y, Y - 1);
+        int pix = py + px * Y;
+        int sc = min((int)((y - (float)py) * 4.0f), 3) + 4 * min((int)((x - (float)px) * 4.0f), 3);
+        float pp = __ldg(&cdf[pix]) - (pix > 0 ? __ldg(&cdf[pix - 1]) : 0.0f);
+        const float *sp = sub + 16 * pix;
+        float ps = 0.0f;
+        for (int k = 0; k < 16; ++k) ps += __ldg(&sp[k]);
+        qa = (pp / __ldg(&cdf[npix - 1])) * (__ldg(&sp[sc]) / ps) * 16.0f * A;
+    }
+    return 1.0f / (0.5f * qa + 0.5f);
+}
+
 /* normpdf (LibRJMCMCreturn.hpp:19-21) with (float)sqrt(2.0f*pi), pi = 3.141592. */
 template <bool EXACT>
 static __device__ __noinline__ float normpdf_f(float x, float u, float s)
@@ -678,6 +699,17 @@ struct ChainWarp {
         rec_n[w] = rc + nrec;
     }
 
+    /* mean X of the Signal==1 emitters of A (NaN when none) into x_trace */
+    __device__ __forceinline__ void record_x()
+    {
+        bool on = lane < an && aS == 1;
+        float sx = on ? aX : 0.0f;
+        for (int o = 16; o > 0; o >>= 1) sx += __shfl_xor_sync(BAMF_FULL, sx, o);
+        int ns = __popc(__ballot_sync(BAMF_FULL, on));
+        if (lane == 0)
+            B->x_trace[(int64_t)roi * B->x_cap + entries] = ns > 0 ? sx / (float)ns : __int_as_float(0x7fc00000);
+    }
+
     /* RJMCMCChain::addEmitters on Chain (A) and Chain_Test (T). */
     __device__ __forceinline__ void record2(float LLR, float PR, int type, int acc)
     {
@@ -685,6 +717,7 @@ struct ChainWarp {
             int ns = __popc(__ballot_sync(BAMF_FULL, lane < an && aS == 1));
             if (lane == 0) B->nsig_trace[(int64_t)roi * B->trace_cap + entries] = (uint8_t)(an < 1 ? 0 : ns);
         }
+        if (B->x_trace && entries < B->x_cap) record_x();
         if (B->chains) {
             record_one(0, an, aI, aX, aY, aS, aBG, aABG, aBBG, LLR, PR, type, acc);
             record_one(1, tn, tI, tX, tY, tS, tBG, tABG, tBBG, LLR, PR, type, acc);
@@ -906,6 +939,8 @@ struct ChainWarp {
         float Us = 1.0f / (Norm1 * Norm2);
         float om = 1.0f - u1;
         float Jacob = EXACT ? (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om))) : Ijp / (om * om);
+        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE)
+            return LLR * PrI * (1.0f / box_area()) * Us * Jacob * (P[2] / P[1]) * PrM;
         return LLR * PrI * PrX * Us * Jacob * (P[1] / P[2]) * PrM;
     }
 
@@ -975,7 +1010,67 @@ struct ChainWarp {
         float om = 1.0f - u1;
         float Jacob = EXACT ? (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om))) : Ijp / (om * om);
         float PrM = MeanN / NEm;
+        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE)
+            return LLR / (PrI * (1.0f / box_area()) * Jacob * Us * PrM * P[2] / P[1]);
         return LLR / (PrI * PrX * Jacob * Us * PrM * P[1] / P[2]);
+    }
+
+    /* Area of the extended box [-Bnd, X+Bnd] x [-Bnd, Y+Bnd] that test()
+     * admits (Bnd = (int)Bnd_out): the support of the position prior. */
+    __device__ __forceinline__ float box_area() const
+    {
+        int bnd = (int)K->p.Bnd_out;
+        return (float)(X + 2 * bnd) * (float)(Y + 2 * bnd);
+    }
+
+    /* Birth position of the UNIFORM and LEARNED proposals: uniform on the
+     * extended box, or (LEARNED, with probability 1/2) a pixel drawn from
+     * the ROI's running sum birth_cdf, a sub-cell drawn from birth_sub and a
+     * uniform point inside that sub-cell. */
+    __device__ __forceinline__ void birth_position(float *bx, float *by)
+    {
+        const int bnd = (int)K->p.Bnd_out;
+        bool learned = K->proposal == BAMF_PROPOSAL_LEARNED && urand() < 0.5f;
+        if (!learned) {
+            *bx = (float)(-bnd) + (float)(X + 2 * bnd) * urand();
+            *by = (float)(-bnd) + (float)(Y + 2 * bnd) * urand();
+            return;
+        }
+        const int64_t off = B->offsets[roi];
+        const float *cdf = B->birth_cdf + off;
+        float rr = urand() * __ldg(&cdf[npix - 1]);
+        int pix = npix - 1;
+#pragma unroll 1
+        for (int b0 = 0; b0 < npix; b0 += 32) {
+            int q = b0 + lane;
+            uint32_t m = __ballot_sync(BAMF_FULL, q < npix && rr <= __ldg(&cdf[min(q, npix - 1)]));
+            if (m) {
+                pix = b0 + __ffs(m) - 1;
+                break;
+            }
+        }
+        const float *sub = B->birth_sub + 16 * (off + pix);
+        float v = lane < 16 ? __ldg(&sub[lane]) : 0.0f;
+        for (int o = 1; o < 16; o <<= 1) {
+            float t = __shfl_up_sync(BAMF_FULL, v, o);
+            if (lane >= o) v += t;
+        }
+        float tot = __shfl_sync(BAMF_FULL, v, 15);
+        float r2 = urand() * tot;
+        uint32_t m = __ballot_sync(BAMF_FULL, lane < 16 && r2 <= v);
+        int sc = m ? __ffs(m) - 1 : 15;
+        int px = pix / Y, py = pix - px * Y;
+        *bx = (float)px + ((float)(sc >> 2) + urand()) * 0.25f;
+        *by = (float)py + ((float)(sc & 3) + urand()) * 0.25f;
+    }
+
+    /* (1 / box area) / q(x, y): the position prior over the birth proposal
+     * density at (x, y); 1 for UNIFORM. */
+    __device__ __forceinline__ float birth_q_ratio(float x, float y) const
+    {
+        if (K->proposal != BAMF_PROPOSAL_LEARNED) return 1.0f;
+        const int64_t off = B->offsets[roi];
+        return learned_q_ratio(x, y, X, Y, npix, box_area(), B->birth_cdf + off, B->birth_sub + 16 * off);
     }
 
     /* RJMCMC::find_Birth (:1688-1736); PixProb is overwritten with 1. */
@@ -1037,7 +1132,10 @@ struct ChainWarp {
         copyA2T();
         const bamf_mcmc_params &p = K->p;
         float bx, by;
-        find_birth(&bx, &by);
+        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE) birth_position(&bx, &by);
+        else find_birth(&bx, &by);
+        pk_f0 = bx;
+        pk_f1 = by;
         int BF;
         if (p.IsBackg == 1) BF = EXACT ? (int)floor(dadd((double)urand(), 0.5)) : (int)floorf(urand() + 0.5f);
         else BF = 1;
@@ -1065,6 +1163,8 @@ struct ChainWarp {
         const bamf_mcmc_params &p = K->p;
         float NEm = nsignalA();
         float PrM = MeanN / (NEm + 1.0f);
+        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE)
+            return LLR * PrM * (P[4] / P[3]) * birth_q_ratio(pk_f0, pk_f1);
         const float PixProb = 1.0f;
         return LLR * P[3] / (P[4] * ((float)X + p.Bnd_out) * ((float)Y + p.Bnd_out) * PixProb) * PrM;
     }
@@ -1083,6 +1183,7 @@ struct ChainWarp {
         removeT(jj);
         pk_move = MV_DEATH;
         pk_type = 7;
+        pk_i0 = jj;
         pk_c1 = C_A_death;
         pk_c2 = aSj == 1 ? C_A_deathFg : C_A_deathBg;
         return ACT_EVAL;
@@ -1091,6 +1192,8 @@ struct ChainWarp {
     {
         float NEm = nsignalA();
         float PrM = NEm / MeanN;
+        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE)
+            return LLR * PrM * (P[3] / P[4]) / birth_q_ratio(A_X(pk_i0), A_Y(pk_i0));
         return LLR * (P[4] / P[3]) * PrM;
     }
 
@@ -1320,7 +1423,10 @@ struct ChainWarp {
             __syncthreads();
             if (n == 0 || n == p.N_Burnin) {
                 is_burnin = n < p.N_Burnin;
-                for (int k = 0; k < 8; ++k) P[k] = is_burnin ? p.P_Burnin[k] : K->PVT[k];
+                /* the reference's ratios see the cumulative trial vector
+                 * (LibRJMCMC.cpp:721-722); the other proposals use the raw one */
+                const float *Pt = K->proposal == BAMF_PROPOSAL_REFERENCE ? K->PVT : p.P_Trials;
+                for (int k = 0; k < 8; ++k) P[k] = is_burnin ? p.P_Burnin[k] : Pt[k];
             }
             if (!active) continue;
             float t = shared_uniform(K->seed, grp, (uint32_t)n, 0u);

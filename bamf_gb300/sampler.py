@@ -57,13 +57,19 @@ class RoiBatch(C.Structure):
     _fields_ = [("n_rois", C.c_int32), ("side_max", C.c_int32), ("data", C.c_void_p),
                 ("offsets", C.c_void_p), ("xsize", C.c_void_p), ("ysize", C.c_void_p),
                 ("psf_sigma", C.c_void_p), ("scmos", C.c_void_p), ("init_n", C.c_void_p),
-                ("init_bg", C.c_void_p), ("init_ixy", C.c_void_p), ("bg0", C.c_float)]
+                ("init_bg", C.c_void_p), ("init_ixy", C.c_void_p), ("bg0", C.c_float),
+                ("proposal", C.c_int32), ("birth_cdf", C.c_void_p), ("birth_sub", C.c_void_p)]
 
 
 class BatchResults(C.Structure):
     _fields_ = [("map_n", C.c_void_p), ("final_n", C.c_void_p), ("final_state", C.c_void_p),
                 ("counters", C.c_void_p), ("n_entries", C.c_void_p), ("status", C.c_void_p),
-                ("overflow", C.c_void_p), ("llr_evals", C.c_void_p)]
+                ("overflow", C.c_void_p), ("llr_evals", C.c_void_p), ("trace_len", C.c_int32),
+                ("n_trace", C.c_void_p), ("x_trace", C.c_void_p)]
+
+
+# birth proposals of the batched sampler (bamf_roi_batch.proposal)
+PROPOSAL = {"reference": 0, "uniform": 1, "learned": 2}
 
 
 def _check(L, st: int, where: str) -> None:
@@ -214,32 +220,45 @@ class Sampler:
         return pr, arrs
 
     def run_device(self, dev: dict, params: abi.McmcParams, off, sig, back, seed: int,
-                   arith: str = "fast", outs: dict | None = None, stream=None, bg0: float = 0.0):
-        """dev: dict of torch CUDA tensors data/offsets/xsize/ysize[/psf_sigma];
+                   arith: str = "fast", outs: dict | None = None, stream=None, bg0: float = 0.0,
+                   proposal: str = "reference"):
+        """dev: dict of torch CUDA tensors data/offsets/xsize/ysize[/psf_sigma,
+        scmos, init_n, init_bg, init_ixy, birth_cdf, birth_sub];
         outs: dict of torch CUDA tensors to fill (map_n, final_n, final_state,
-        counters, n_entries, status, overflow).  Enqueues on `stream`."""
+        counters, n_entries, status, overflow, llr_evals, and the [n][T]
+        traces n_trace (uint8) / x_trace (float32)).  Enqueues on `stream`."""
         pr, keep = self._priors(off, sig, back)
         b = RoiBatch()
         b.n_rois = int(dev["xsize"].numel())
         b.side_max = int(dev.get("side_max", 0))
         for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos", "init_n", "init_bg",
-                  "init_ixy"):
+                  "init_ixy", "birth_cdf", "birth_sub"):
             t = dev.get(k)
             setattr(b, k, t.data_ptr() if t is not None else None)
         b.bg0 = float(bg0)
+        b.proposal = PROPOSAL[proposal]
         res = BatchResults()
+        outs = outs or {}
         for k in ("map_n", "final_n", "final_state", "counters", "n_entries", "status", "overflow",
-                  "llr_evals"):
-            t = (outs or {}).get(k)
+                  "llr_evals", "n_trace", "x_trace"):
+            t = outs.get(k)
             setattr(res, k, t.data_ptr() if t is not None else None)
+        tr = [outs[k] for k in ("n_trace", "x_trace") if outs.get(k) is not None]
+        if tr:
+            if any(t.dim() != 2 or t.shape[1] != tr[0].shape[1] for t in tr):
+                raise ValueError("n_trace and x_trace must be [n_rois][trace_len] of one length")
+            res.trace_len = int(tr[0].shape[1])
         st = self._L.bamf_rjmcmc_batch_device(self._ws, C.byref(b), C.byref(params), C.byref(pr),
                                                int(seed), ARITH[arith], C.byref(res),
                                                C.c_void_p(stream) if stream else None)
         _check(self._L, st, "bamf_rjmcmc_batch_device")
 
     def run_host(self, batch, params: abi.McmcParams, off, sig, back, seed: int,
-                 arith: str = "fast", bg0: float = 0.0, init=None) -> dict:
-        """batch: synth.RoiBatch (host numpy); returns numpy results."""
+                 arith: str = "fast", bg0: float = 0.0, init=None, proposal: str = "reference",
+                 birth=None, trace_len: int = 0) -> dict:
+        """batch: synth.RoiBatch (host numpy); returns numpy results.
+        birth: (cdf, sub) host arrays of the LEARNED proposal; trace_len > 0
+        adds the n_trace / x_trace outputs."""
         pr, keep = self._priors(off, sig, back)
         n = batch.n
         b = RoiBatch()
@@ -254,17 +273,25 @@ class Sampler:
             arrays["init_n"] = np.ascontiguousarray(init["n"], np.int32)
             arrays["init_bg"] = np.ascontiguousarray(init["bg"], np.float32)
             arrays["init_ixy"] = np.ascontiguousarray(init["ixy"], np.float32)
+        if birth is not None:
+            arrays["birth_cdf"] = np.ascontiguousarray(birth[0], np.float32)
+            arrays["birth_sub"] = np.ascontiguousarray(birth[1], np.float32)
         for k, a in arrays.items():
             setattr(b, k, a.ctypes.data)
         b.bg0 = float(bg0)
+        b.proposal = PROPOSAL[proposal]
         outs = {"map_n": np.zeros(n, np.int32), "final_n": np.zeros(n, np.int32),
                 "final_state": np.zeros((n, FINAL_STRIDE), np.float32),
                 "counters": np.zeros((n, 30), np.int32), "n_entries": np.zeros(n, np.int32),
                 "status": np.full(n, -1, np.int32), "overflow": np.zeros(n, np.int32),
                 "llr_evals": np.zeros(n, np.int32)}
+        if trace_len > 0:
+            outs["n_trace"] = np.zeros((n, trace_len), np.uint8)
+            outs["x_trace"] = np.zeros((n, trace_len), np.float32)
         res = BatchResults()
         for k, a in outs.items():
             setattr(res, k, a.ctypes.data)
+        res.trace_len = int(trace_len)
         st = self._L.bamf_rjmcmc_batch_host(self._ws, C.byref(b), C.byref(params), C.byref(pr),
                                              int(seed), ARITH[arith], C.byref(res))
         _check(self._L, st, "bamf_rjmcmc_batch_host")

@@ -237,7 +237,36 @@ typedef struct bamf_roi_batch {
     const float *init_bg;
     const float *init_ixy;
     float bg0;
+    /* Birth proposal (fields past here may be left zero):
+     *   BAMF_PROPOSAL_REFERENCE  the reference's: residual-weighted pixel,
+     *                            position pixel + U - 0.5, its Hastings terms
+     *                            (LibRJMCMC.cpp:1258-1387, 1688-1736)
+     *   BAMF_PROPOSAL_UNIFORM    position uniform on the extended box
+     *                            [-Bnd, X+Bnd] x [-Bnd, Y+Bnd] (Bnd = (int)Bnd_out),
+     *                            intensity from SignalPDF; birth ratio
+     *                            LLR * MeanN/(NEm+1) * P_death/P_birth and death
+     *                            its inverse; raw phase probabilities in every
+     *                            ratio; split/merge position prior 1/area of
+     *                            the extended box
+     *   BAMF_PROPOSAL_LEARNED    UNIFORM, with the birth position drawn half of
+     *                            the time from a per-ROI density over 4x4
+     *                            sub-cells of each pixel; its exact density
+     *                            enters the birth and death ratios
+     * Anything but REFERENCE needs BAMF_ARITH_FAST.  LEARNED reads
+     *   birth_cdf   [pixel] running sum of the pixel probabilities, laid out
+     *               like data (ROI k at offsets[k], y fastest)
+     *   birth_sub   [pixel][16] probabilities of the sub-cells of each pixel
+     *               (sub-cell s = sy + 4*sx covers [x + sx/4, x + (sx+1)/4) x
+     *               [y + sy/4, y + (sy+1)/4)), summing to 1 per pixel; ROI k
+     *               at 16*offsets[k] */
+    int32_t proposal;
+    const float *birth_cdf;
+    const float *birth_sub;
 } bamf_roi_batch;
+
+#define BAMF_PROPOSAL_REFERENCE 0
+#define BAMF_PROPOSAL_UNIFORM 1
+#define BAMF_PROPOSAL_LEARNED 2
 
 /* Per-ROI results of a batch (any pointer may be NULL).
  *   map_n        MAP emitter count: mode of the Signal==1 count over the
@@ -249,7 +278,12 @@ typedef struct bamf_roi_batch {
  *   status       BAMF_OK or the ROI's error
  *   overflow     proposals rejected because they would exceed BAMF_NMAX
  *   llr_evals    likelihood-ratio evaluations (proposals scored against the
- *                data); each costs one pass over the ROI's pixels */
+ *                data); each costs one pass over the ROI's pixels
+ *   n_trace      [k][trace_len] Signal==1 emitter count of the accepted
+ *                state at each chain entry (the first trace_len entries);
+ *                with map_n it must hold N_Burnin + N_Trials entries
+ *   x_trace      [k][trace_len] mean X of those emitters (NaN when none): a
+ *                permutation-invariant position functional for ESS */
 typedef struct bamf_batch_results {
     int32_t *map_n;
     int32_t *final_n;
@@ -259,6 +293,9 @@ typedef struct bamf_batch_results {
     int32_t *status;
     int32_t *overflow;
     int32_t *llr_evals;
+    int32_t trace_len;
+    uint8_t *n_trace;
+    float *x_trace;
 } bamf_batch_results;
 
 /* Device scratch (prior tables, work queue, per-ROI chain traces) that

@@ -48,3 +48,51 @@ def test_host_entry_points_reject_bad_arguments_without_touching_the_gpu():
     st = L.bamf_crjmcmc_host(None, 16, 16, None, None, None, 0, None, 0, None, 0, None, None, 0,
                              None, None, None, None, None)
     assert st == abi.BAMF_ERR_INVALID_ARG
+
+
+def test_batch_proposal_and_trace_arguments_are_checked_before_the_gpu():
+    """Non-reference proposals need fast arithmetic, LEARNED needs its
+    tables, traces need a length (and one long enough for map_n)."""
+    import ctypes as C
+
+    import numpy as np
+
+    from bamf_gb300 import abi, build, rjstruct, sampler
+    build.build()
+    L = sampler._declare()
+    rj = rjstruct.c0_rjstruct()
+    p = rjstruct.mcmc_params(rj)
+    pr, keep = sampler.Sampler._priors(rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons)
+    data = np.zeros(256, np.float32)
+    off = np.zeros(1, np.int64)
+    side = np.full(1, 16, np.int32)
+    out_i = np.zeros(1, np.int32)
+    tr = np.zeros(8, np.uint8)
+
+    def call(proposal=0, cdf=None, sub=None, arith=1, trace_len=0, n_trace=None, map_n=None):
+        b = sampler.RoiBatch()
+        b.n_rois = 1
+        b.data, b.offsets, b.xsize, b.ysize = data.ctypes.data, off.ctypes.data, side.ctypes.data, side.ctypes.data
+        b.proposal = proposal
+        b.birth_cdf = cdf
+        b.birth_sub = sub
+        r = sampler.BatchResults()
+        r.final_n = out_i.ctypes.data
+        r.map_n = map_n
+        r.trace_len = trace_len
+        r.n_trace = n_trace
+        ws = C.c_void_p()
+        assert L.bamf_workspace_create(C.byref(ws)) == abi.BAMF_OK
+        try:
+            return L.bamf_rjmcmc_batch_host(ws, C.byref(b), C.byref(p), C.byref(pr), 1, arith, C.byref(r))
+        finally:
+            L.bamf_workspace_destroy(ws)
+
+    assert call(proposal=1, arith=0) == abi.BAMF_ERR_INVALID_ARG        # uniform needs fast
+    assert call(proposal=3) == abi.BAMF_ERR_INVALID_ARG                 # unknown proposal
+    assert call(proposal=2) == abi.BAMF_ERR_INVALID_ARG                 # learned without tables
+    assert call(n_trace=tr.ctypes.data) == abi.BAMF_ERR_INVALID_ARG     # trace without a length
+    assert call(trace_len=8, n_trace=tr.ctypes.data, map_n=out_i.ctypes.data) == abi.BAMF_ERR_INVALID_ARG
+    # well-formed calls get past the checks (and stop at the missing GPU here)
+    ok = call(proposal=1, trace_len=8, n_trace=tr.ctypes.data)
+    assert ok in (abi.BAMF_OK, abi.BAMF_ERR_NO_DEVICE)
