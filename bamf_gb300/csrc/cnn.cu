@@ -1,0 +1,946 @@
+/*
+ * cnn.cu - the learned birth proposal (include/bamf_cnn.h): synthetic ROI
+ * generator, the network's forward and backward kernels, Adam, a CUDA-graph
+ * training step, and inference into the sampler's LEARNED birth tables.
+ *
+ * Layouts.  Activations are channels-last BF16, [roi][p][32] with pixel
+ * p = y + 16 x.  The three 32 -> 32 convolutions are implicit GEMMs on the
+ * tensor cores (mma.sync m16n8k16, BF16 in, FP32 accumulate): a CTA stages
+ * one ROI's activations in shared memory as an 18 x 18 zero-bordered tile
+ * with a 40-channel pixel stride (80 bytes: the eight rows an ldmatrix phase
+ * reads fall in eight different 16-byte bank groups), an M tile is one image
+ * row x (16 pixels along y), N = 32 output channels (4 tiles of 8), and
+ * K = 9 taps x 32 input channels (18 steps of 16).  The input gradient of a
+ * convolution is the same kernel run with the taps flipped and the channel
+ * roles swapped (packed once per step); the weight gradient is a GEMM with
+ * M = (tap, input channel) = 288 and K = the pixels of every ROI of the
+ * CTA, with both operands read transposed by ldmatrix.trans.
+ */
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "bamf.h"
+#include "bamf_cnn.h"
+#include "bamf_philox.h"
+
+namespace {
+
+constexpr int S = BAMF_CNN_SIDE;  /* 16 */
+constexpr int NPX = S * S;        /* 256 */
+constexpr int CH = BAMF_CNN_CH;   /* 32 */
+constexpr int CP = 40;            /* smem channel stride (bf16) */
+constexpr int PS = S + 2;         /* padded side */
+constexpr int NC = BAMF_CNN_COUNTS;
+constexpr int NSUB = 16;
+constexpr int MAX_BATCH = 4096;
+
+/* parameter offsets */
+constexpr int O_W1 = 0, O_B1 = 288, O_W2 = 320, O_B2 = 9536, O_W3 = 9568, O_B3 = 18784, O_W4 = 18816,
+              O_B4 = 28032, O_WL = 28064, O_BL = 28576, O_WC = 28592, O_BC = 28944, NPARAM = 28955;
+static_assert(NPARAM == BAMF_CNN_NPARAM, "parameter count");
+static_assert(O_B1 == O_W1 + 288 && O_BC + NC == NPARAM, "conv1 block and head layout");
+constexpr int O_W[3] = {O_W2, O_W3, O_W4};
+constexpr int O_B[3] = {O_B2, O_B3, O_B4};
+constexpr int PK = 9 * CH * CP; /* packed bf16 weights of one layer */
+
+typedef __nv_bfloat16 bf16;
+
+/* ------------------------------------------------------------ PTX helpers */
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void *p)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_addr(p)));
+}
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+                 "{%8,%9}, {%0,%1,%2,%3};\n"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ float u01(uint32_t w)
+{
+    return ((float)(w >> 8) + 0.5f) * (1.0f / 16777216.0f); /* (0, 1) */
+}
+
+/* ------------------------------------------------------------- generator */
+/* Poisson(lam): multiplication method below 10, else the PTRS transformed
+ * rejection of W. Hoermann, "The transformed rejection method for generating
+ * Poisson random variables", Insurance: Mathematics and Economics 12 (1993).
+ * Uniforms come from the Philox blocks (c0, c1, c2, j) of key (k0, k1). */
+__device__ int poisson_draw(float lam, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t k0, uint32_t k1)
+{
+    if (!(lam > 0.0f)) return 0;
+    if (lam < 10.0f) {
+        float L = expf(-lam), prod = 1.0f;
+        int n = 0;
+        for (uint32_t j = 0; j < 16; ++j) {
+            bamf_philox_block b = bamf_philox4x32_10(c0, c1, c2, j, k0, k1);
+            for (int w = 0; w < 4; ++w) {
+                prod *= u01(b.v[w]);
+                if (prod <= L) return n;
+                ++n;
+            }
+        }
+        return n;
+    }
+    const float slam = sqrtf(lam), loglam = logf(lam);
+    const float b = 0.931f + 2.53f * slam;
+    const float a = -0.059f + 0.02483f * b;
+    const float invalpha = 1.1239f + 1.1328f / (b - 3.4f);
+    const float vr = 0.9277f - 3.6224f / (b - 2.0f);
+    for (uint32_t j = 0; j < 32; ++j) {
+        bamf_philox_block blk = bamf_philox4x32_10(c0, c1, c2, j, k0, k1);
+        for (int h = 0; h < 2; ++h) {
+            float U = u01(blk.v[2 * h]) - 0.5f;
+            float V = u01(blk.v[2 * h + 1]);
+            float us = 0.5f - fabsf(U);
+            float k = floorf((2.0f * a / us + b) * U + lam + 0.43f);
+            if (us >= 0.07f && V <= vr) return (int)k;
+            if (k < 0.0f || (us < 0.013f && V > us)) continue;
+            if (logf(V) + logf(invalpha) - logf(a / (us * us) + b) <= -lam + k * loglam - lgammaf(k + 1.0f))
+                return (int)k;
+        }
+    }
+    return (int)floorf(lam + 0.5f); /* not reached in practice (acceptance > 0.9 per round) */
+}
+
+__global__ void synth_kernel(bamf_synth_params sp, uint32_t seed, uint64_t first, const int *step_dev,
+                             int batch, int n, float *__restrict__ data, int32_t *__restrict__ n_em,
+                             float *__restrict__ xyi)
+{
+    __shared__ float ex[BAMF_SYNTH_NMAX], ey[BAMF_SYNTH_NMAX], ei[BAMF_SYNTH_NMAX];
+    __shared__ int ne;
+    int r = blockIdx.x;
+    if (r >= n) return;
+    uint64_t k = (step_dev ? (uint64_t)(*step_dev) * (uint64_t)batch : first) + (uint64_t)r;
+    uint32_t klo = (uint32_t)k, khi = (uint32_t)(k >> 32);
+    const uint32_t K1 = 0x6a09e667u ^ khi;
+    int t = threadIdx.x;
+    if (t == 0) {
+        float L = expf(-sp.mean_n), prod = 1.0f;
+        int cnt = 0;
+        bool done = false;
+        for (uint32_t j = 0; j < 16 && !done; ++j) {
+            bamf_philox_block b = bamf_philox4x32_10(klo, 0u, j, 0u, seed, K1);
+            for (int w = 0; w < 4; ++w) {
+                prod *= u01(b.v[w]);
+                if (prod <= L) {
+                    done = true;
+                    break;
+                }
+                ++cnt;
+            }
+        }
+        ne = min(cnt, BAMF_SYNTH_NMAX);
+    }
+    if (t < BAMF_SYNTH_NMAX) {
+        bamf_philox_block b = bamf_philox4x32_10(klo, 1u, (uint32_t)t, 0u, seed, K1);
+        ex[t] = (float)S * u01(b.v[0]);
+        ey[t] = (float)S * u01(b.v[1]);
+        float z = sqrtf(-2.0f * logf(u01(b.v[2]))) * cospif(2.0f * u01(b.v[3]));
+        ei[t] = expf(logf(sp.i_median) + sp.i_logsd * z);
+    }
+    __syncthreads();
+    const int nn = ne;
+    if (t < BAMF_SYNTH_NMAX) {
+        float *o = xyi + ((size_t)r * BAMF_SYNTH_NMAX + t) * 3;
+        bool on = t < nn;
+        o[0] = on ? ex[t] : 0.0f;
+        o[1] = on ? ey[t] : 0.0f;
+        o[2] = on ? ei[t] : 0.0f;
+    }
+    if (t == 0) n_em[r] = nn;
+    int x = t / S, y = t - (t / S) * S;
+    const float c = 1.0f / (sqrtf(2.0f) * sp.sigma);
+    float lam = sp.bg;
+    for (int e = 0; e < nn; ++e) {
+        float sx = 0.5f * (erff(((float)x - ex[e] + 1.0f) * c) - erff(((float)x - ex[e]) * c));
+        float sy = 0.5f * (erff(((float)y - ey[e] + 1.0f) * c) - erff(((float)y - ey[e]) * c));
+        lam += ei[e] * sx * sy;
+    }
+    data[(size_t)r * NPX + t] = (float)poisson_draw(lam, klo, 2u, (uint32_t)t, seed, K1);
+}
+
+/* -------------------------------------------------------- weight packing */
+/* Wf[l][tap][co][ci] (forward) and Wb[l][tap][ci][co] = W_l[co][ci][8 - tap]
+ * (input gradient), BF16, channel stride CP. */
+__global__ void pack_kernel(const float *__restrict__ P, bf16 *__restrict__ Wf, bf16 *__restrict__ Wb)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * 9 * CH * CH) return;
+    int l = i / (9 * CH * CH), rem = i - l * 9 * CH * CH;
+    int tap = rem / (CH * CH), nk = rem - tap * CH * CH;
+    int nn = nk / CH, kk = nk - nn * CH;
+    const float *W = P + (l == 0 ? O_W2 : (l == 1 ? O_W3 : O_W4));
+    Wf[l * PK + (tap * CH + nn) * CP + kk] = __float2bfloat16_rn(W[(nn * CH + kk) * 9 + tap]);
+    Wb[l * PK + (tap * CH + nn) * CP + kk] = __float2bfloat16_rn(W[(kk * CH + nn) * 9 + (8 - tap)]);
+}
+
+/* --------------------------------------------------------------- conv1 */
+/* x0 normalisation and the 1 -> 32 convolution (FP32), one CTA per ROI. */
+__global__ void conv1_fwd_kernel(const float *__restrict__ data, int n, const float *__restrict__ P,
+                                 float *__restrict__ x0, bf16 *__restrict__ a1)
+{
+    __shared__ float xp[PS * PS];
+    __shared__ float w[288 + 32];
+    __shared__ float red[8];
+    int r = blockIdx.x, t = threadIdx.x;
+    if (r >= n) return;
+    for (int i = t; i < 320; i += blockDim.x) w[i] = P[O_W1 + i];
+    for (int i = t; i < PS * PS; i += blockDim.x) xp[i] = 0.0f;
+    float v = sqrtf(fmaxf(data[(size_t)r * NPX + t], 0.0f) + 0.375f);
+    float s = v;
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((t & 31) == 0) red[t >> 5] = s;
+    __syncthreads();
+    float mean = 0.0f;
+    for (int k = 0; k < 8; ++k) mean += red[k];
+    mean *= (1.0f / NPX);
+    float xv = (v - mean) * 0.25f;
+    int x = t / S, y = t - (t / S) * S;
+    xp[(x + 1) * PS + (y + 1)] = xv;
+    if (x0) x0[(size_t)r * NPX + t] = xv;
+    __syncthreads();
+    float in[9];
+    for (int kx = 0; kx < 3; ++kx)
+        for (int ky = 0; ky < 3; ++ky) in[kx * 3 + ky] = xp[(x + kx) * PS + (y + ky)];
+    __align__(16) bf16 o[CH];
+    for (int co = 0; co < CH; ++co) {
+        float z = w[288 + co];
+        for (int tp = 0; tp < 9; ++tp) z += w[co * 9 + tp] * in[tp];
+        o[co] = __float2bfloat16_rn(fmaxf(z, 0.0f));
+    }
+    uint4 *dst = (uint4 *)(a1 + ((size_t)r * NPX + t) * CH);
+    const uint4 *src = (const uint4 *)o;
+    for (int q = 0; q < 4; ++q) dst[q] = src[q];
+}
+
+/* dW1, db1 from dz1 (= dL/d pre-activation of conv1) and x0. */
+__global__ void conv1_bwd_kernel(const float *__restrict__ x0, const bf16 *__restrict__ dz1, int n,
+                                 float *__restrict__ G)
+{
+    __shared__ float xp[PS * PS];
+    __shared__ float dz[NPX * (CH + 1)];
+    int t = threadIdx.x;
+    float acc0 = 0.0f, acc1 = 0.0f;
+    const int o0 = t, o1 = t + 256; /* outputs: co*9+tap (288), then 288+co */
+    for (int i = t; i < PS * PS; i += blockDim.x) xp[i] = 0.0f;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        __syncthreads();
+        int x = t / S, y = t - (t / S) * S;
+        xp[(x + 1) * PS + (y + 1)] = x0[(size_t)r * NPX + t];
+        for (int c = 0; c < CH; ++c) dz[t * (CH + 1) + c] = __bfloat162float(dz1[((size_t)r * NPX + t) * CH + c]);
+        __syncthreads();
+        for (int h = 0; h < 2; ++h) {
+            int o = h ? o1 : o0;
+            if (o >= 320) continue;
+            float acc = 0.0f;
+            if (o < 288) {
+                int co = o / 9, tp = o - co * 9, kx = tp / 3, ky = tp - kx * 3;
+                for (int p = 0; p < NPX; ++p) {
+                    int px = p / S, py = p - px * S;
+                    acc += dz[p * (CH + 1) + co] * xp[(px + kx) * PS + (py + ky)];
+                }
+            } else {
+                int co = o - 288;
+                for (int p = 0; p < NPX; ++p) acc += dz[p * (CH + 1) + co];
+            }
+            if (h) acc1 += acc;
+            else acc0 += acc;
+        }
+    }
+    if (o0 < 320) atomicAdd(&G[O_W1 + o0], acc0);
+    if (o1 < 320) atomicAdd(&G[O_W1 + o1], acc1);
+}
+
+/* -------------------------------------------------- 32 -> 32 convolution */
+/* MODE 0: out = relu(conv(in, Wpk) + bias).  MODE 1 (input gradient):
+ * out = conv(in, Wpk) * (mask > 0).  One ROI per CTA iteration, 8 warps,
+ * warp w computes image rows x = 2w, 2w+1. */
+template <int MODE>
+__global__ void __launch_bounds__(256) conv_mma_kernel(const bf16 *__restrict__ in, const bf16 *__restrict__ Wpk,
+                                                       const float *__restrict__ bias,
+                                                       const bf16 *__restrict__ mask, bf16 *__restrict__ out,
+                                                       int n)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16 *Ws = (bf16 *)smem_raw;      /* [9][32][CP] */
+    bf16 *T = Ws + PK;                /* [PS][PS][CP] */
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    {
+        const uint4 *src = (const uint4 *)Wpk;
+        uint4 *dst = (uint4 *)Ws;
+        for (int i = t; i < PK * 2 / 16; i += blockDim.x) dst[i] = src[i];
+        /* zero the whole tile once; the interior is overwritten per ROI */
+        uint4 z = make_uint4(0, 0, 0, 0);
+        uint4 *tt = (uint4 *)T;
+        for (int i = t; i < PS * PS * CP * 2 / 16; i += blockDim.x) tt[i] = z;
+    }
+    const int g = lane >> 2, q = lane & 3;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        __syncthreads();
+        /* interior: 256 pixels x 64 bytes */
+        const uint4 *src = (const uint4 *)(in + (size_t)r * NPX * CH);
+        for (int i = t; i < NPX * 4; i += blockDim.x) {
+            int p = i >> 2, c = i & 3;
+            int x = p / S, y = p - (p / S) * S;
+            *(uint4 *)(T + ((x + 1) * PS + (y + 1)) * CP + c * 8) = src[i];
+        }
+        __syncthreads();
+        for (int mt = 0; mt < 2; ++mt) {
+            const int x = 2 * warp + mt;
+            float acc[4][4];
+            for (int a = 0; a < 4; ++a)
+                for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
+#pragma unroll
+            for (int tap = 0; tap < 9; ++tap) {
+                const int kx = tap / 3, ky = tap - (tap / 3) * 3;
+#pragma unroll
+                for (int cb = 0; cb < 2; ++cb) {
+                    uint32_t A[4];
+                    {
+                        int j = lane >> 3, rr = lane & 7;
+                        int y = rr + 8 * (j & 1), ch = cb * 16 + 8 * (j >> 1);
+                        ldsm_x4(A, T + ((x + kx) * PS + (y + ky)) * CP + ch);
+                    }
+#pragma unroll
+                    for (int np = 0; np < 2; ++np) {
+                        uint32_t Bf[4];
+                        int j = lane >> 3, rr = lane & 7;
+                        int co = np * 16 + 8 * (j >> 1) + rr, ci = cb * 16 + 8 * (j & 1);
+                        ldsm_x4(Bf, Ws + (tap * CH + co) * CP + ci);
+                        mma16816(acc[2 * np], A, Bf[0], Bf[1]);
+                        mma16816(acc[2 * np + 1], A, Bf[2], Bf[3]);
+                    }
+                }
+            }
+            /* epilogue */
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                int co = nt * 8 + 2 * q;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    int y = g + 8 * h;
+                    size_t off = ((size_t)r * NPX + x * S + y) * CH + co;
+                    float v0 = acc[nt][2 * h], v1 = acc[nt][2 * h + 1];
+                    if (MODE == 0) {
+                        v0 = fmaxf(v0 + bias[co], 0.0f);
+                        v1 = fmaxf(v1 + bias[co + 1], 0.0f);
+                    } else {
+                        __nv_bfloat162 m = *(const __nv_bfloat162 *)(mask + off);
+                        v0 = __bfloat162float(m.x) > 0.0f ? v0 : 0.0f;
+                        v1 = __bfloat162float(m.y) > 0.0f ? v1 : 0.0f;
+                    }
+                    *(__nv_bfloat162 *)(out + off) = __floats2bfloat162_rn(v0, v1);
+                }
+            }
+        }
+    }
+}
+
+/* Weight and bias gradient of a 32 -> 32 convolution: dW[co][ci][tap] +=
+ * sum over ROIs and pixels of act[p + tap][ci] * dz[p][co].  9 warps; warp
+ * w owns M tiles 2w, 2w+1 of M = (tap, ci block) = 18 tiles of 16. */
+__global__ void __launch_bounds__(288) conv_dw_kernel(const bf16 *__restrict__ act, const bf16 *__restrict__ dz,
+                                                      int n, float *__restrict__ dW, float *__restrict__ db)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    bf16 *A = (bf16 *)smem_raw;       /* [PS][PS][CP] */
+    bf16 *D = A + PS * PS * CP;       /* [S][S][CP]   */
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    {
+        uint4 z = make_uint4(0, 0, 0, 0);
+        uint4 *aa = (uint4 *)A;
+        for (int i = t; i < PS * PS * CP * 2 / 16; i += blockDim.x) aa[i] = z;
+    }
+    float acc[2][4][4];
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 4; ++b)
+            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.0f;
+    float accb = 0.0f;
+    for (int r = blockIdx.x; r < n; r += gridDim.x) {
+        __syncthreads();
+        const uint4 *sa = (const uint4 *)(act + (size_t)r * NPX * CH);
+        const uint4 *sd = (const uint4 *)(dz + (size_t)r * NPX * CH);
+        for (int i = t; i < NPX * 4; i += blockDim.x) {
+            int p = i >> 2, c = i & 3;
+            int x = p / S, y = p - (p / S) * S;
+            *(uint4 *)(A + ((x + 1) * PS + (y + 1)) * CP + c * 8) = sa[i];
+            *(uint4 *)(D + p * CP + c * 8) = sd[i];
+        }
+        __syncthreads();
+        if (t < CH)
+            for (int p = 0; p < NPX; ++p) accb += __bfloat162float(D[p * CP + t]);
+        for (int x = 0; x < S; ++x) {
+            uint32_t Bf[2][4];
+#pragma unroll
+            for (int np = 0; np < 2; ++np) {
+                int j = lane >> 3, rr = lane & 7;
+                int y = rr + 8 * (j & 1), co = (2 * np + (j >> 1)) * 8;
+                ldsm_x4_t(Bf[np], D + (x * S + y) * CP + co);
+            }
+#pragma unroll
+            for (int mi = 0; mi < 2; ++mi) {
+                int mt = 2 * warp + mi;
+                int tap = mt >> 1, cib = (mt & 1) * 16;
+                int kx = tap / 3, ky = tap - (tap / 3) * 3;
+                uint32_t Af[4];
+                int j = lane >> 3, rr = lane & 7;
+                int y = rr + 8 * (j >> 1), ci = cib + 8 * (j & 1);
+                ldsm_x4_t(Af, A + ((x + kx) * PS + (y + ky)) * CP + ci);
+#pragma unroll
+                for (int np = 0; np < 2; ++np) {
+                    mma16816(acc[mi][2 * np], Af, Bf[np][0], Bf[np][1]);
+                    mma16816(acc[mi][2 * np + 1], Af, Bf[np][2], Bf[np][3]);
+                }
+            }
+        }
+    }
+    const int g = lane >> 2, q = lane & 3;
+#pragma unroll
+    for (int mi = 0; mi < 2; ++mi) {
+        int mt = 2 * warp + mi;
+        int tap = mt >> 1, cib = (mt & 1) * 16;
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                int ci = cib + g + 8 * (e >> 1), co = nt * 8 + 2 * q + (e & 1);
+                atomicAdd(&dW[(co * CH + ci) * 9 + tap], acc[mi][nt][e]);
+            }
+    }
+    if (t < CH) atomicAdd(&db[t], accb);
+}
+
+/* ----------------------------------------------------------------- heads */
+/* One CTA (256 threads, thread = pixel) per ROI.  TRAIN: loss, head
+ * gradients (atomics into G), dz4 = dL/d(pre-activation of conv4).  INFER:
+ * the sampler's birth tables and the count logits. */
+template <bool TRAIN>
+__global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, int n, const float *__restrict__ P,
+                                                   const int32_t *__restrict__ n_em, const float *__restrict__ xyi,
+                                                   float inv_batch, float *__restrict__ G, bf16 *__restrict__ dz4,
+                                                   float *__restrict__ loss_buf, const int *__restrict__ step_dev,
+                                                   float *__restrict__ cdf, float *__restrict__ sub,
+                                                   float *__restrict__ cnt_out)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *H = (float *)smem_raw;             /* [256][33] */
+    float *DZ = H + NPX * (CH + 1);           /* [256][17] */
+    __shared__ float Wl[NSUB * CH], bl[NSUB], Wc[NC * CH], bc[NC];
+    __shared__ float red[8], gmean[CH], part[8][CH], zc[NC], dzc[NC], dg[CH];
+    __shared__ float ex[BAMF_SYNTH_NMAX], ey[BAMF_SYNTH_NMAX];
+    __shared__ float sm_max, sm_sum, loss_loc_sh;
+    const int r = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (r >= n) return;
+    for (int i = t; i < NSUB * CH; i += 256) Wl[i] = P[O_WL + i];
+    for (int i = t; i < NC * CH; i += 256) Wc[i] = P[O_WC + i];
+    if (t < NSUB) bl[t] = P[O_BL + t];
+    if (t < NC) bc[t] = P[O_BC + t];
+    float h[CH];
+    {
+        const uint4 *src = (const uint4 *)(a4 + ((size_t)r * NPX + t) * CH);
+        for (int qd = 0; qd < 4; ++qd) {
+            uint4 u = src[qd];
+            const bf16 *b = (const bf16 *)&u;
+            for (int e = 0; e < 8; ++e) h[qd * 8 + e] = __bfloat162float(b[e]);
+        }
+    }
+    for (int c = 0; c < CH; ++c) H[t * (CH + 1) + c] = h[c];
+    __syncthreads();
+    float z[NSUB];
+    float mx = -INFINITY;
+    for (int s = 0; s < NSUB; ++s) {
+        float v = bl[s];
+        for (int c = 0; c < CH; ++c) v += Wl[s * CH + c] * h[c];
+        z[s] = v;
+        mx = fmaxf(mx, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) red[warp] = mx;
+    /* count head: mean of a4 over pixels */
+    {
+        int c = t & 31, grp = t >> 5;
+        float sacc = 0.0f;
+        for (int p = grp; p < NPX; p += 8) sacc += H[p * (CH + 1) + c];
+        part[grp][c] = sacc;
+    }
+    __syncthreads();
+    if (t == 0) {
+        float m = red[0];
+        for (int k = 1; k < 8; ++k) m = fmaxf(m, red[k]);
+        sm_max = m;
+    }
+    if (t < CH) {
+        float sacc = 0.0f;
+        for (int k = 0; k < 8; ++k) sacc += part[k][t];
+        gmean[t] = sacc * (1.0f / NPX);
+    }
+    __syncthreads();
+    float e[NSUB], se = 0.0f;
+    for (int s = 0; s < NSUB; ++s) {
+        e[s] = expf(z[s] - sm_max);
+        se += e[s];
+    }
+    float tot = se;
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if (lane == 0) red[warp] = tot;
+    if (t < NC) {
+        float v = bc[t];
+        for (int c = 0; c < CH; ++c) v += Wc[t * CH + c] * gmean[c];
+        zc[t] = v;
+    }
+    __syncthreads();
+    if (t == 0) {
+        float sacc = 0.0f;
+        for (int k = 0; k < 8; ++k) sacc += red[k];
+        sm_sum = sacc;
+    }
+    __syncthreads();
+    const float inv_sum = 1.0f / sm_sum;
+    if (!TRAIN) {
+        /* pixel probability, inclusive scan over pixels (thread order = p) */
+        float pp = se * inv_sum;
+        float incl = pp;
+        for (int o = 1; o < 32; o <<= 1) {
+            float v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        __syncthreads();
+        if (lane == 31) red[warp] = incl;
+        __syncthreads();
+        float base = 0.0f;
+        for (int k = 0; k < warp; ++k) base += red[k];
+        cdf[(size_t)r * NPX + t] = base + incl;
+        float inv_se = 1.0f / se;
+        for (int s = 0; s < NSUB; ++s) sub[((size_t)r * NPX + t) * NSUB + s] = e[s] * inv_se;
+        if (cnt_out && t < NC) cnt_out[(size_t)r * NC + t] = zc[t];
+        return;
+    }
+    /* ---- training: targets, loss, gradients */
+    const int ntrue = n_em[r];
+    if (t < BAMF_SYNTH_NMAX) {
+        ex[t] = xyi[((size_t)r * BAMF_SYNTH_NMAX + t) * 3 + 0];
+        ey[t] = xyi[((size_t)r * BAMF_SYNTH_NMAX + t) * 3 + 1];
+    }
+    if (t == 0) loss_loc_sh = 0.0f;
+    __syncthreads();
+    const int px = t / S, py = t - (t / S) * S;
+    float tgt[NSUB];
+    for (int s = 0; s < NSUB; ++s) tgt[s] = 0.0f;
+    int nin = 0;
+    for (int k = 0; k < ntrue; ++k) {
+        float X = ex[k], Y = ey[k];
+        if (!(X >= 0.0f && X < (float)S && Y >= 0.0f && Y < (float)S)) continue;
+        nin++;
+        int cx = min((int)X, S - 1), cy = min((int)Y, S - 1);
+        if (cx == px && cy == py) {
+            int s = min((int)((Y - (float)cy) * 4.0f), 3) + 4 * min((int)((X - (float)cx) * 4.0f), 3);
+            tgt[s] += 1.0f;
+        }
+    }
+    const float wloc = nin > 0 ? 1.0f / (float)nin : 0.0f;
+    float lloc = 0.0f;
+    const float logS = logf(sm_sum) + sm_max;
+    for (int s = 0; s < NSUB; ++s) {
+        if (tgt[s] > 0.0f) lloc -= tgt[s] * wloc * (z[s] - logS);
+        float d = (e[s] * inv_sum - tgt[s] * wloc) * (nin > 0 ? inv_batch : 0.0f);
+        DZ[t * (NSUB + 1) + s] = d;
+    }
+    for (int o = 16; o > 0; o >>= 1) lloc += __shfl_xor_sync(0xffffffffu, lloc, o);
+    if (lane == 0) atomicAdd(&loss_loc_sh, lloc);
+    if (t == 0) {
+        float m = zc[0];
+        for (int c = 1; c < NC; ++c) m = fmaxf(m, zc[c]);
+        float sacc = 0.0f;
+        for (int c = 0; c < NC; ++c) sacc += expf(zc[c] - m);
+        int cls = min(ntrue, NC - 1);
+        float lcnt = -(zc[cls] - m - logf(sacc));
+        for (int c = 0; c < NC; ++c) dzc[c] = (expf(zc[c] - m) / sacc - (c == cls ? 1.0f : 0.0f)) * inv_batch;
+        red[0] = lcnt;
+    }
+    __syncthreads();
+    if (t == 0) {
+        float l = (loss_loc_sh + red[0]) * inv_batch;
+        atomicAdd(&loss_buf[step_dev ? *step_dev : 0], l);
+    }
+    if (t < CH) {
+        float v = 0.0f;
+        for (int c = 0; c < NC; ++c) v += Wc[c * CH + t] * dzc[c];
+        dg[t] = v * (1.0f / NPX);
+    }
+    __syncthreads();
+    /* dz4 of this pixel */
+    {
+        __align__(16) bf16 o[CH];
+        for (int c = 0; c < CH; ++c) {
+            float v = dg[c];
+            for (int s = 0; s < NSUB; ++s) v += DZ[t * (NSUB + 1) + s] * Wl[s * CH + c];
+            o[c] = __float2bfloat16_rn(h[c] > 0.0f ? v : 0.0f);
+        }
+        uint4 *dst = (uint4 *)(dz4 + ((size_t)r * NPX + t) * CH);
+        const uint4 *src = (const uint4 *)o;
+        for (int qd = 0; qd < 4; ++qd) dst[qd] = src[qd];
+    }
+    /* head parameter gradients */
+    for (int o = t; o < NSUB * CH; o += 256) {
+        int s = o / CH, c = o - (o / CH) * CH;
+        float v = 0.0f;
+        for (int p = 0; p < NPX; ++p) v += DZ[p * (NSUB + 1) + s] * H[p * (CH + 1) + c];
+        atomicAdd(&G[O_WL + o], v);
+    }
+    if (t < NSUB) {
+        float v = 0.0f;
+        for (int p = 0; p < NPX; ++p) v += DZ[p * (NSUB + 1) + t];
+        atomicAdd(&G[O_BL + t], v);
+    }
+    for (int o = t; o < NC * CH; o += 256) atomicAdd(&G[O_WC + o], dzc[o / CH] * gmean[o - (o / CH) * CH]);
+    if (t < NC) atomicAdd(&G[O_BC + t], dzc[t]);
+}
+
+/* ------------------------------------------------------------------ Adam */
+__global__ void adam_kernel(float *__restrict__ P, float *__restrict__ G, float *__restrict__ m,
+                            float *__restrict__ v, const int *__restrict__ step_dev, int steps_total, float lr0)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= NPARAM) return;
+    int step = *step_dev;
+    float frac = steps_total > 1 ? (float)step / (float)(steps_total - 1) : 0.0f;
+    float lr = lr0 * (1.0f - 0.9f * fminf(frac, 1.0f));
+    const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    float g = G[i];
+    float mi = b1 * m[i] + (1.0f - b1) * g;
+    float vi = b2 * v[i] + (1.0f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    float t = (float)(step + 1);
+    float mh = mi / (1.0f - powf(b1, t));
+    float vh = vi / (1.0f - powf(b2, t));
+    P[i] -= lr * mh / (sqrtf(vh) + eps);
+    G[i] = 0.0f;
+}
+
+__global__ void step_inc_kernel(int *step_dev) { *step_dev += 1; }
+
+}  // namespace
+
+/* ================================================================ host */
+struct bamf_cnn {
+    float *P = nullptr, *G = nullptr, *M = nullptr, *V = nullptr;
+    bf16 *Wf = nullptr, *Wb = nullptr;
+    /* batch buffers (MAX_BATCH) */
+    float *x0 = nullptr;
+    bf16 *a[4] = {nullptr, nullptr, nullptr, nullptr};
+    bf16 *dzA = nullptr, *dzB = nullptr;
+    float *gdata = nullptr, *gxyi = nullptr;
+    int32_t *gn = nullptr;
+    int *step = nullptr;
+    float *loss = nullptr;
+    int loss_cap = 0;
+    int sms = 1;
+    bool packed = false;
+};
+
+namespace {
+
+std::mutex g_attr_mutex;
+bool g_attr_done = false;
+
+const size_t SMEM_CONV = (size_t)(PK + PS * PS * CP) * sizeof(bf16);
+const size_t SMEM_DW = (size_t)(PS * PS * CP + NPX * CP) * sizeof(bf16);
+const size_t SMEM_HEAD = (size_t)(NPX * (CH + 1) + NPX * (NSUB + 1)) * sizeof(float);
+
+cudaError_t set_attrs()
+{
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    if (g_attr_done) return cudaSuccess;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(conv_mma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CONV)))
+        return e;
+    if ((e = cudaFuncSetAttribute(conv_mma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CONV)))
+        return e;
+    if ((e = cudaFuncSetAttribute(conv_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_DW)))
+        return e;
+    if ((e = cudaFuncSetAttribute(head_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_HEAD)))
+        return e;
+    if ((e = cudaFuncSetAttribute(head_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_HEAD)))
+        return e;
+    g_attr_done = true;
+    return cudaSuccess;
+}
+
+#define CK(x)                                                                                                    \
+    do {                                                                                                         \
+        cudaError_t e_ = (x);                                                                                    \
+        if (e_ != cudaSuccess) {                                                                                 \
+            cudaGetLastError();                                                                                  \
+            return BAMF_ERR_CUDA;                                                                                \
+        }                                                                                                        \
+    } while (0)
+
+int grid_for(int n, int per_sm, int sms) { return std::max(1, std::min(n, per_sm * sms)); }
+
+/* forward of a batch of n <= capacity ROIs from data, activations kept */
+bamf_status forward(bamf_cnn *net, const float *data, int n, cudaStream_t s)
+{
+    conv1_fwd_kernel<<<n, 256, 0, s>>>(data, n, net->P, net->x0, net->a[0]);
+    for (int l = 0; l < 3; ++l)
+        conv_mma_kernel<0><<<grid_for(n, 4, net->sms), 256, SMEM_CONV, s>>>(net->a[l], net->Wf + l * PK,
+                                                                           net->P + O_B[l], nullptr, net->a[l + 1], n);
+    CK(cudaGetLastError());
+    return BAMF_OK;
+}
+
+/* loss and gradients (accumulated into G) of the batch whose forward ran */
+bamf_status backward(bamf_cnn *net, const int32_t *n_em, const float *xyi, int n, float inv_batch, cudaStream_t s)
+{
+    head_kernel<true><<<n, 256, SMEM_HEAD, s>>>(net->a[3], n, net->P, n_em, xyi, inv_batch, net->G, net->dzA,
+                                                net->loss, net->step, nullptr, nullptr, nullptr);
+    bf16 *dz = net->dzA, *dzn = net->dzB;
+    for (int l = 2; l >= 0; --l) {
+        /* layer l+2: input a[l], output a[l+1]; dz = dL/dz_{l+2} */
+        conv_dw_kernel<<<grid_for(n, 3, net->sms), 288, SMEM_DW, s>>>(net->a[l], dz, n, net->G + O_W[l],
+                                                                     net->G + O_B[l]);
+        conv_mma_kernel<1><<<grid_for(n, 4, net->sms), 256, SMEM_CONV, s>>>(dz, net->Wb + l * PK, nullptr,
+                                                                           net->a[l], dzn, n);
+        bf16 *tmp = dz;
+        dz = dzn;
+        dzn = tmp;
+    }
+    conv1_bwd_kernel<<<grid_for(n, 4, net->sms), 256, 0, s>>>(net->x0, dz, n, net->G);
+    CK(cudaGetLastError());
+    return BAMF_OK;
+}
+
+bamf_status pack(bamf_cnn *net, cudaStream_t s)
+{
+    pack_kernel<<<(3 * 9 * CH * CH + 255) / 256, 256, 0, s>>>(net->P, net->Wf, net->Wb);
+    CK(cudaGetLastError());
+    return BAMF_OK;
+}
+
+}  // namespace
+
+extern "C" bamf_status bamf_synth_generate(const bamf_synth_params *sp, uint32_t seed, uint64_t first, int n,
+                                           float *data, int32_t *n_em, float *xyi, void *stream)
+{
+    if (!sp || n < 0 || (n > 0 && (!data || !n_em || !xyi))) return BAMF_ERR_INVALID_ARG;
+    if (!(sp->sigma > 0.0f) || !(sp->mean_n >= 0.0f) || !(sp->i_median > 0.0f) || !(sp->bg >= 0.0f))
+        return BAMF_ERR_INVALID_ARG;
+    if (n == 0) return BAMF_OK;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    synth_kernel<<<n, 256, 0, (cudaStream_t)stream>>>(*sp, seed, first, nullptr, 0, n, data, n_em, xyi);
+    CK(cudaGetLastError());
+    return BAMF_OK;
+}
+
+extern "C" void bamf_cnn_destroy(bamf_cnn *net)
+{
+    if (!net) return;
+    void *ps[] = {net->P, net->G, net->M, net->V, net->Wf, net->Wb, net->x0, net->a[0], net->a[1], net->a[2],
+                  net->a[3], net->dzA, net->dzB, net->gdata, net->gxyi, net->gn, net->step, net->loss};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    delete net;
+}
+
+extern "C" bamf_status bamf_cnn_create(bamf_cnn **out, uint32_t seed)
+{
+    if (!out) return BAMF_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    if (set_attrs() != cudaSuccess) return BAMF_ERR_CUDA;
+    bamf_cnn *net = new bamf_cnn();
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&net->sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t B = MAX_BATCH;
+    bool ok = cudaMalloc(&net->P, NPARAM * 4) == cudaSuccess && cudaMalloc(&net->G, NPARAM * 4) == cudaSuccess &&
+              cudaMalloc(&net->M, NPARAM * 4) == cudaSuccess && cudaMalloc(&net->V, NPARAM * 4) == cudaSuccess &&
+              cudaMalloc(&net->Wf, 3 * PK * 2) == cudaSuccess && cudaMalloc(&net->Wb, 3 * PK * 2) == cudaSuccess &&
+              cudaMalloc(&net->x0, B * NPX * 4) == cudaSuccess && cudaMalloc(&net->dzA, B * NPX * CH * 2) == cudaSuccess &&
+              cudaMalloc(&net->dzB, B * NPX * CH * 2) == cudaSuccess &&
+              cudaMalloc(&net->gdata, B * NPX * 4) == cudaSuccess &&
+              cudaMalloc(&net->gxyi, B * BAMF_SYNTH_NMAX * 3 * 4) == cudaSuccess &&
+              cudaMalloc(&net->gn, B * 4) == cudaSuccess && cudaMalloc(&net->step, sizeof(int)) == cudaSuccess;
+    for (int l = 0; l < 4 && ok; ++l) ok = cudaMalloc(&net->a[l], B * NPX * CH * 2) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        bamf_cnn_destroy(net);
+        return BAMF_ERR_CUDA;
+    }
+    /* He initialisation from a Philox stream (Box-Muller), zero biases */
+    std::vector<float> h(NPARAM, 0.0f);
+    uint32_t ctr = 0;
+    auto normal = [&]() {
+        bamf_philox_block b = bamf_philox4x32_10(ctr++, 0u, 0u, 0u, seed, 0x2545F491u);
+        double u1 = ((double)(b.v[0] >> 8) + 0.5) / 16777216.0, u2 = ((double)(b.v[1] >> 8) + 0.5) / 16777216.0;
+        return (float)(std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2));
+    };
+    auto fill = [&](int off, int count, int fan_in) {
+        float sd = std::sqrt(2.0f / (float)fan_in);
+        for (int i = 0; i < count; ++i) h[off + i] = sd * normal();
+    };
+    fill(O_W1, 288, 9);
+    fill(O_W2, 9216, 288);
+    fill(O_W3, 9216, 288);
+    fill(O_W4, 9216, 288);
+    fill(O_WL, 512, 32);
+    fill(O_WC, 352, 32);
+    bool ok2 = cudaMemcpy(net->P, h.data(), NPARAM * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+               cudaMemset(net->G, 0, NPARAM * 4) == cudaSuccess && cudaMemset(net->M, 0, NPARAM * 4) == cudaSuccess &&
+               cudaMemset(net->V, 0, NPARAM * 4) == cudaSuccess && cudaMemset(net->step, 0, sizeof(int)) == cudaSuccess;
+    if (!ok2 || pack(net, nullptr) != BAMF_OK || cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        bamf_cnn_destroy(net);
+        return BAMF_ERR_CUDA;
+    }
+    *out = net;
+    return BAMF_OK;
+}
+
+extern "C" bamf_status bamf_cnn_get_params(bamf_cnn *net, float *params)
+{
+    if (!net || !params) return BAMF_ERR_INVALID_ARG;
+    CK(cudaMemcpy(params, net->P, NPARAM * 4, cudaMemcpyDeviceToHost));
+    return BAMF_OK;
+}
+
+extern "C" bamf_status bamf_cnn_set_params(bamf_cnn *net, const float *params)
+{
+    if (!net || !params) return BAMF_ERR_INVALID_ARG;
+    CK(cudaMemcpy(net->P, params, NPARAM * 4, cudaMemcpyHostToDevice));
+    bamf_status r = pack(net, nullptr);
+    if (r) return r;
+    CK(cudaDeviceSynchronize());
+    return BAMF_OK;
+}
+
+static bamf_status ensure_loss(bamf_cnn *net, int cap)
+{
+    if (net->loss_cap >= cap) return BAMF_OK;
+    if (net->loss) cudaFree(net->loss);
+    net->loss = nullptr;
+    net->loss_cap = 0;
+    CK(cudaMalloc(&net->loss, (size_t)cap * sizeof(float)));
+    net->loss_cap = cap;
+    return BAMF_OK;
+}
+
+extern "C" bamf_status bamf_cnn_loss_grad(bamf_cnn *net, const float *data, const int32_t *n_em, const float *xyi,
+                                          int n, float *loss, float *grad)
+{
+    if (!net || !data || !n_em || !xyi || n < 1 || n > MAX_BATCH) return BAMF_ERR_INVALID_ARG;
+    bamf_status r;
+    if ((r = ensure_loss(net, 1))) return r;
+    int saved = 0;
+    CK(cudaMemcpy(&saved, net->step, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemset(net->step, 0, sizeof(int)));
+    CK(cudaMemset(net->loss, 0, sizeof(float)));
+    CK(cudaMemset(net->G, 0, NPARAM * 4));
+    if ((r = forward(net, data, n, nullptr))) return r;
+    if ((r = backward(net, n_em, xyi, n, 1.0f / (float)n, nullptr))) return r;
+    CK(cudaDeviceSynchronize());
+    if (loss) CK(cudaMemcpy(loss, net->loss, sizeof(float), cudaMemcpyDeviceToHost));
+    if (grad) CK(cudaMemcpy(grad, net->G, NPARAM * 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemset(net->G, 0, NPARAM * 4));
+    CK(cudaMemcpy(net->step, &saved, sizeof(int), cudaMemcpyHostToDevice));
+    return BAMF_OK;
+}
+
+extern "C" bamf_status bamf_cnn_train(bamf_cnn *net, const bamf_synth_params *sp, int steps, int batch, float lr,
+                                      uint32_t data_seed, float *loss_trace)
+{
+    if (!net || !sp || steps < 0 || batch < 1 || batch > MAX_BATCH || !(lr > 0.0f)) return BAMF_ERR_INVALID_ARG;
+    if (steps == 0) return BAMF_OK;
+    bamf_status r;
+    if ((r = ensure_loss(net, steps))) return r;
+    cudaStream_t s;
+    CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bamf_status res = BAMF_OK;
+    do {
+        if (cudaMemsetAsync(net->step, 0, sizeof(int), s) != cudaSuccess ||
+            cudaMemsetAsync(net->loss, 0, (size_t)steps * sizeof(float), s) != cudaSuccess ||
+            cudaMemsetAsync(net->G, 0, NPARAM * 4, s) != cudaSuccess ||
+            cudaMemsetAsync(net->M, 0, NPARAM * 4, s) != cudaSuccess ||
+            cudaMemsetAsync(net->V, 0, NPARAM * 4, s) != cudaSuccess) {
+            res = BAMF_ERR_CUDA;
+            break;
+        }
+        if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            res = BAMF_ERR_CUDA;
+            break;
+        }
+        synth_kernel<<<batch, 256, 0, s>>>(*sp, data_seed, 0, net->step, batch, batch, net->gdata, net->gn, net->gxyi);
+        bamf_status r1 = forward(net, net->gdata, batch, s);
+        bamf_status r2 = r1 ? r1 : backward(net, net->gn, net->gxyi, batch, 1.0f / (float)batch, s);
+        adam_kernel<<<(NPARAM + 255) / 256, 256, 0, s>>>(net->P, net->G, net->M, net->V, net->step, steps, lr);
+        pack_kernel<<<(3 * 9 * CH * CH + 255) / 256, 256, 0, s>>>(net->P, net->Wf, net->Wb);
+        step_inc_kernel<<<1, 1, 0, s>>>(net->step);
+        cudaError_t ec = cudaStreamEndCapture(s, &graph);
+        if (r2 || ec != cudaSuccess) {
+            res = r2 ? r2 : BAMF_ERR_CUDA;
+            break;
+        }
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+            res = BAMF_ERR_CUDA;
+            break;
+        }
+        for (int i = 0; i < steps; ++i)
+            if (cudaGraphLaunch(exec, s) != cudaSuccess) {
+                res = BAMF_ERR_CUDA;
+                break;
+            }
+        if (res) break;
+        if (cudaStreamSynchronize(s) != cudaSuccess) {
+            res = BAMF_ERR_CUDA;
+            break;
+        }
+        if (loss_trace &&
+            cudaMemcpy(loss_trace, net->loss, (size_t)steps * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+            res = BAMF_ERR_CUDA;
+    } while (0);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(s);
+    if (res) cudaGetLastError();
+    return res;
+}
+
+extern "C" bamf_status bamf_cnn_infer(bamf_cnn *net, const float *data, int n, float *cdf, float *sub,
+                                      float *count_logits, void *stream)
+{
+    if (!net || n < 0 || (n > 0 && (!data || !cdf || !sub))) return BAMF_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int b0 = 0; b0 < n; b0 += MAX_BATCH) {
+        int m = std::min(MAX_BATCH, n - b0);
+        bamf_status r = forward(net, data + (size_t)b0 * NPX, m, s);
+        if (r) return r;
+        head_kernel<false><<<m, 256, SMEM_HEAD, s>>>(net->a[3], m, net->P, nullptr, nullptr, 0.0f, nullptr, nullptr,
+                                                     nullptr, nullptr, cdf + (size_t)b0 * NPX,
+                                                     sub + (size_t)b0 * NPX * NSUB,
+                                                     count_logits ? count_logits + (size_t)b0 * NC : nullptr);
+        CK(cudaGetLastError());
+    }
+    return BAMF_OK;
+}

@@ -1,0 +1,102 @@
+"""The learned birth proposal on the GPU: synthetic generator, network
+forward (birth tables, count logits) and gradients against the torch CPU
+oracle (oracle/cnn_torch.py), and training."""
+import numpy as np
+import pytest
+
+from bamf_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _host(b):
+    return {k: v.cpu().numpy() for k, v in b.items()}
+
+
+def test_generator_follows_the_forward_model_with_poisson_noise(cuda_lib):
+    from bamf_gb300 import learned
+    b = _host(learned.generate(3000, seed=7))
+    n = b["n_em"]
+    assert abs(n.mean() - 5.0) < 0.15 and n.max() <= learned.SYNTH_NMAX
+    z = []
+    for r in range(3000):
+        k = int(n[r])
+        X, Y, I = b["xyi"][r, :k, 0], b["xyi"][r, :k, 1], b["xyi"][r, :k, 2]
+        assert ((X >= 0) & (X < 16) & (Y >= 0) & (Y < 16)).all()
+        lam = synth.model_image(16, 16, X, Y, I, 10.0, 1.3).ravel(order="F")
+        z.append((b["data"][r] - lam) / np.sqrt(lam))
+        assert (b["xyi"][r, k:] == 0).all()
+    z = np.concatenate(z)
+    assert abs(z.mean()) < 0.01 and abs(z.var() - 1.0) < 0.02, (z.mean(), z.var())
+    allI = np.concatenate([b["xyi"][r, :int(n[r]), 2] for r in range(3000)])
+    assert abs(np.median(allI) / 1000.0 - 1) < 0.03
+    assert abs(np.log(allI).std() - 0.3) < 0.01
+    # the same (seed, index) gives the same ROI
+    b2 = _host(learned.generate(10, seed=7, first=5))
+    np.testing.assert_array_equal(b2["data"], b["data"][5:15])
+
+
+def test_forward_matches_the_torch_oracle(cuda_lib):
+    import torch
+
+    from bamf_gb300 import learned
+    from oracle import cnn_torch
+    net = learned.ProposalNet(seed=3)
+    b = learned.generate(48, seed=9)
+    out = net.infer(b["data"])
+    theta = torch.tensor(net.get_params())
+    data = b["data"].cpu()
+    _, cnt_ref, _ = cnn_torch.forward(theta, data, bf16=True)
+    cdf_ref, sub_ref = cnn_torch.birth_tables(theta, data, bf16=True)
+    cnt = out["count_logits"].cpu()
+    assert torch.allclose(cnt, cnt_ref, rtol=2e-2, atol=2e-2), (cnt - cnt_ref).abs().max()
+    cdf = out["cdf"].cpu()
+    assert (cdf - cdf_ref).abs().max() < 5e-3
+    cdf2 = cdf.reshape(48, 256)
+    assert torch.allclose(cdf2[:, -1], torch.ones(48), atol=1e-4)
+    assert (cdf2[:, 1:] >= cdf2[:, :-1] - 1e-7).all()
+    sub = out["sub"].cpu()
+    assert (sub - sub_ref).abs().mean() < 1e-3
+    assert torch.allclose(sub.reshape(-1, 16).sum(1), torch.ones(48 * 256), atol=1e-4)
+
+
+def test_gradients_match_torch_autograd(cuda_lib):
+    import torch
+
+    from bamf_gb300 import learned
+    from oracle import cnn_torch
+    net = learned.ProposalNet(seed=4)
+    b = learned.generate(32, seed=11)
+    loss, grad = net.loss_grad(b)
+    h = _host(b)
+    theta = torch.tensor(net.get_params()).requires_grad_(True)
+    L = cnn_torch.loss(theta, torch.tensor(h["data"]), h["n_em"], h["xyi"], bf16=True)
+    (g,) = torch.autograd.grad(L, theta)
+    assert loss == pytest.approx(L.item(), rel=2e-3)
+    g = g.numpy()
+    for name, (o, shp) in cnn_torch.OFF.items():
+        k = int(np.prod(shp))
+        a, r = grad[o:o + k].astype(np.float64), g[o:o + k].astype(np.float64)
+        rel = np.linalg.norm(a - r) / max(np.linalg.norm(r), 1e-12)
+        cos = float(a @ r / max(np.linalg.norm(a) * np.linalg.norm(r), 1e-30))
+        assert rel < 5e-2 and cos > 0.998, (name, rel, cos)
+
+
+def test_training_lowers_the_loss_and_finds_the_emitters(cuda_lib):
+    from bamf_gb300 import learned, proposal
+    net = learned.ProposalNet(seed=5)
+    tr = net.train(400, batch=256, lr=2e-3, data_seed=21)
+    assert np.isfinite(tr).all()
+    assert tr[-20:].mean() < 0.8 * tr[:20].mean(), (tr[:20].mean(), tr[-20:].mean())
+    ev = learned.generate(200, seed=99)
+    out = net.infer(ev["data"])
+    cdf = out["cdf"].cpu().numpy().reshape(200, 256)
+    sub = out["sub"].cpu().numpy().reshape(200, 256 * 16)
+    h = _host(ev)
+    gain = []
+    for r in range(200):
+        for e in range(int(h["n_em"][r])):
+            x, y = h["xyi"][r, e, 0], h["xyi"][r, e, 1]
+            gain.append(proposal.density(cdf[r], sub[r], 16, 16, x, y) * 256.0)
+    print("mean learned density at the true emitters, relative to uniform:", np.mean(gain))
+    assert np.mean(gain) > 5.0
