@@ -616,6 +616,86 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
     if (t < NC) atomicAdd(&G[O_BC + t], dzc[t]);
 }
 
+/* --------------------------------------------------------- start states */
+/* A chain start per ROI from the network: n0 = argmax of the count logits
+ * (at most max_n), positions = the n0 most probable sub-cells, greedily,
+ * each suppressing the cells within 1 px of it; intensity `intensity`.
+ * One CTA (256 threads, thread = pixel) per ROI. */
+__global__ void __launch_bounds__(256) init_kernel(const float *__restrict__ cdf, const float *__restrict__ sub,
+                                                   const float *__restrict__ cnt, int n, float intensity,
+                                                   int max_n, int32_t *__restrict__ init_n,
+                                                   float *__restrict__ init_ixy)
+{
+    __shared__ float bv[8];
+    __shared__ int bi[8];
+    __shared__ int win;
+    const int r = blockIdx.x, t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    if (r >= n) return;
+    int n0 = 0;
+    {
+        const float *c = cnt + (size_t)r * NC;
+        float m = c[0];
+        for (int k = 1; k < NC; ++k)
+            if (c[k] > m) {
+                m = c[k];
+                n0 = k;
+            }
+        n0 = min(n0, max_n);
+    }
+    const float pp = cdf[(size_t)r * NPX + t] - (t > 0 ? cdf[(size_t)r * NPX + t - 1] : 0.0f);
+    float pr[NSUB];
+    for (int s = 0; s < NSUB; ++s) pr[s] = pp * sub[((size_t)r * NPX + t) * NSUB + s];
+    const int px = t / S, py = t - (t / S) * S;
+    float *ixy = init_ixy + (size_t)r * 3 * BAMF_NMAX;
+    for (int k = 0; k < n0; ++k) {
+        float v = -1.0f;
+        int idx = 0;
+        for (int s = 0; s < NSUB; ++s)
+            if (pr[s] > v) {
+                v = pr[s];
+                idx = t * NSUB + s;
+            }
+        for (int o = 16; o > 0; o >>= 1) {
+            float ov = __shfl_xor_sync(0xffffffffu, v, o);
+            int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+            if (ov > v || (ov == v && oi < idx)) {
+                v = ov;
+                idx = oi;
+            }
+        }
+        if (lane == 0) {
+            bv[warp] = v;
+            bi[warp] = idx;
+        }
+        __syncthreads();
+        if (t == 0) {
+            float m = bv[0];
+            int w = bi[0];
+            for (int q = 1; q < 8; ++q)
+                if (bv[q] > m || (bv[q] == m && bi[q] < w)) {
+                    m = bv[q];
+                    w = bi[q];
+                }
+            win = w;
+        }
+        __syncthreads();
+        const int wp = win / NSUB, ws = win - (win / NSUB) * NSUB;
+        const float wx = (float)(wp / S) + ((float)(ws >> 2) + 0.5f) * 0.25f;
+        const float wy = (float)(wp - (wp / S) * S) + ((float)(ws & 3) + 0.5f) * 0.25f;
+        if (t == 0) {
+            ixy[k] = intensity;
+            ixy[BAMF_NMAX + k] = wx;
+            ixy[2 * BAMF_NMAX + k] = wy;
+        }
+        for (int s = 0; s < NSUB; ++s) {
+            float cx = (float)px + ((float)(s >> 2) + 0.5f) * 0.25f, cy = (float)py + ((float)(s & 3) + 0.5f) * 0.25f;
+            if ((cx - wx) * (cx - wx) + (cy - wy) * (cy - wy) < 1.0f) pr[s] = 0.0f;
+        }
+        __syncthreads();
+    }
+    if (t == 0) init_n[r] = n0;
+}
+
 /* ------------------------------------------------------------------ Adam */
 __global__ void adam_kernel(float *__restrict__ P, float *__restrict__ G, float *__restrict__ m,
                             float *__restrict__ v, const int *__restrict__ step_dev, int steps_total, float lr0)
@@ -925,6 +1005,18 @@ extern "C" bamf_status bamf_cnn_train(bamf_cnn *net, const bamf_synth_params *sp
     cudaStreamDestroy(s);
     if (res) cudaGetLastError();
     return res;
+}
+
+extern "C" bamf_status bamf_cnn_init_states(const float *cdf, const float *sub, const float *count_logits, int n,
+                                            float intensity, int max_n, int32_t *init_n, float *init_ixy,
+                                            void *stream)
+{
+    if (n < 0 || max_n < 0 || max_n > BAMF_NMAX) return BAMF_ERR_INVALID_ARG;
+    if (n > 0 && (!cdf || !sub || !count_logits || !init_n || !init_ixy)) return BAMF_ERR_INVALID_ARG;
+    if (n == 0) return BAMF_OK;
+    init_kernel<<<n, 256, 0, (cudaStream_t)stream>>>(cdf, sub, count_logits, n, intensity, max_n, init_n, init_ixy);
+    CK(cudaGetLastError());
+    return BAMF_OK;
 }
 
 extern "C" bamf_status bamf_cnn_infer(bamf_cnn *net, const float *data, int n, float *cdf, float *sub,

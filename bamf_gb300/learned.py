@@ -44,8 +44,9 @@ def _lib() -> C.CDLL:
     L.bamf_cnn_loss_grad.argtypes = [vp, vp, vp, vp, i32, f32p, f32p]
     L.bamf_cnn_train.argtypes = [vp, C.POINTER(SynthParams), i32, i32, C.c_float, C.c_uint32, f32p]
     L.bamf_cnn_infer.argtypes = [vp, vp, i32, vp, vp, vp, vp]
+    L.bamf_cnn_init_states.argtypes = [vp, vp, vp, i32, C.c_float, i32, vp, vp, vp]
     for f in ("bamf_synth_generate", "bamf_cnn_create", "bamf_cnn_get_params", "bamf_cnn_set_params",
-              "bamf_cnn_loss_grad", "bamf_cnn_train", "bamf_cnn_infer"):
+              "bamf_cnn_loss_grad", "bamf_cnn_train", "bamf_cnn_infer", "bamf_cnn_init_states"):
         getattr(L, f).restype = C.c_int
     L._cnn_declared = True
     return L
@@ -140,3 +141,19 @@ class ProposalNet:
                                     C.c_void_p(stream) if stream else None)
         _check(self._L, st, "bamf_cnn_infer")
         return out
+
+
+def init_states(tables: dict, intensity: float = 1000.0, max_n: int = 10, stream=None) -> dict:
+    """Sampler start states (init_n [n], init_ixy [n][3][32]) from `infer`'s
+    output: argmax count, greedy most probable sub-cells."""
+    import torch
+    L = _lib()
+    n = int(tables["count_logits"].shape[0])
+    out = {"init_n": torch.zeros(n, dtype=torch.int32, device="cuda"),
+           "init_ixy": torch.zeros((n, 3, 32), dtype=torch.float32, device="cuda")}
+    st = L.bamf_cnn_init_states(tables["cdf"].data_ptr(), tables["sub"].data_ptr(),
+                                tables["count_logits"].data_ptr(), n, float(intensity), int(max_n),
+                                out["init_n"].data_ptr(), out["init_ixy"].data_ptr(),
+                                C.c_void_p(stream) if stream else None)
+    _check(L, st, "bamf_cnn_init_states")
+    return out

@@ -16,6 +16,11 @@ roofline  the sampler kernel against the measured MUFU log2 rate: one log2 per
           ROI pixel per scored proposal (the likelihood-ratio pass)
 cpu_baseline  the CPU restatement of the reference sampler (glibc math, bit-
           identical to the reference build) on the host cores, on a sample
+learned_proposal  (rank 0, outside the timed region) the learned-vs-uniform
+          birth-proposal evaluation on 16x16 ROIs (bamf_gb300.learned_eval):
+          network training rate, per-arm ROIs/s, ESS/s of the emitter count
+          and of the mean-X functional, MAP count accuracy, RMSE, and the
+          throughput at equal MAP accuracy
 
 Under torchrun (N > 1) every rank runs its own 100,000 ROIs (weak scaling,
 no data-path collective); value = all ROIs / max rank time.
@@ -37,7 +42,6 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "RJMCMC ROIs/s (batched sampler, 3000+3000 jumps per ROI)"
-WORKLOAD = "batched uneven RJMCMC: 100k ROIs, sides {8,12,16,20,24} px, 3000+3000 jumps"
 
 
 def parse():
@@ -50,7 +54,16 @@ def parse():
     ap.add_argument("--jumps", type=int, default=3000)
     ap.add_argument("--cpu-sample", type=int, default=0, help="ROIs per CPU-baseline sample (0: auto)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the learned-vs-uniform proposal evaluation (16x16 ROIs)")
+    ap.add_argument("--learned-train-rois", type=int, default=2_000_000)
+    ap.add_argument("--learned-eval-rois", type=int, default=50_000)
     return ap.parse_args()
+
+
+def workload_label(n_rois: int, jumps: int) -> str:
+    return (f"batched uneven RJMCMC: {n_rois // 1000}k ROIs, sides {{8,12,16,20,24}} px, "
+            f"{jumps}+{jumps} jumps")
 
 
 class Clocks:
@@ -147,8 +160,8 @@ def run_reference(a, rank, world):
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded, reference forward model + Poisson noise)",
-        "config": {"workload": WORKLOAD, "n_rois": a.n_rois, "jumps": [a.jumps, a.jumps],
-                   "parallelism": "host threads", "l2": "n/a (CPU)"},
+        "config": {"workload": workload_label(a.n_rois, a.jumps), "n_rois": a.n_rois,
+                   "jumps": [a.jumps, a.jumps], "parallelism": "host threads", "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": v, "unit": "ROIs/s", "cores": threads, "kind": "port",
                          "sample": f"first {n} ROIs of the workload per step (same seeds), "
                                    f"glibc-math C restatement bit-identical to the reference build"},
@@ -251,6 +264,26 @@ def main():
         e2e = {"value": world * n / dt, "unit": "ROIs/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
 
+    # per step: order_kernel, one sampler launch per non-empty size class, map_n_kernel
+    sides = np.maximum(b.xsize, b.ysize)
+    bounds = [8, 12, 16, 20, 24, 28, 32]
+    classes = {next(i for i, hi in enumerate(bounds) if sd <= hi) for sd in np.unique(sides)}
+    launches_per_step = 2 + len(classes)
+
+    learned_block = None
+    if rank == 0 and not a.no_learned:
+        from bamf_gb300 import learned_eval
+        r = learned_eval.evaluate(train_rois=a.learned_train_rois, n_eval=a.learned_eval_rois)
+        arms = r["arms"]
+        learned_block = {
+            "workload": r["workload"],
+            "train_rois_per_s": r["train_rois_per_s"], "infer_seconds": r["infer_seconds"],
+            **{f"{k}_{f}": arms[k][f] for k in arms for f in
+               ("rois_per_s", "ess_n_per_s", "ess_x_per_s", "map_count_accuracy", "rmse_px")},
+            "ess_n_per_s_ratio": r["ess_n_per_s_ratio"], "ess_x_per_s_ratio": r["ess_x_per_s_ratio"],
+            "equal_accuracy": r["equal_accuracy_vs_uniform_at_full_length"],
+        }
+
     cpu = None
     if rank == 0:
         threads = os.cpu_count() or 1
@@ -266,7 +299,7 @@ def main():
             "warmup": a.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded, reference forward model + Poisson noise)",
-            "config": {"workload": WORKLOAD, "n_rois": n, "jumps": [a.jumps, a.jumps],
+            "config": {"workload": workload_label(n, a.jumps), "n_rois": n, "jumps": [a.jumps, a.jumps],
                        "arith": "fast", "parallelism": f"replicas x{world}",
                        "l2": "flushed between timed steps (512 MB write)"},
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": mufu.value / 1e9,
@@ -275,8 +308,9 @@ def main():
                          "peak_source": "measured in-process by bamf_probe_peaks (MUFU lg2 probe)",
                          "fp32_peak_tflops_measured": fp32.value / 1e12},
             "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": 3 * a.steps,
+            "gpu_launches": launches_per_step * a.steps,
             "clocks": clk.summary(),
+            "learned_proposal": learned_block,
             "map_n_mean": float(outs["map_n"].float().mean().item()),
             "true_n_mean": float(b.true_n.mean()),
         }

@@ -94,6 +94,15 @@ bamf_status bamf_cnn_train(bamf_cnn *net, const bamf_synth_params *sp, int steps
 bamf_status bamf_cnn_infer(bamf_cnn *net, const float *data, int n, float *cdf, float *sub,
                            float *count_logits, void *stream);
 
+/* Chain start states from the network's output (the count logits may only
+ * initialise a chain; the target is unchanged): n0 = argmax of the count
+ * logits (at most max_n <= BAMF_NMAX) emitters at the n0 most probable
+ * sub-cell centres, taken greedily with cells within 1 px of a chosen one
+ * suppressed, each with intensity `intensity`.  Writes the sampler's
+ * bamf_roi_batch.init_n [n] and init_ixy [n][3][BAMF_NMAX] (device). */
+bamf_status bamf_cnn_init_states(const float *cdf, const float *sub, const float *count_logits, int n,
+                                 float intensity, int max_n, int32_t *init_n, float *init_ixy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

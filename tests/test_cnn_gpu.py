@@ -100,3 +100,36 @@ def test_training_lowers_the_loss_and_finds_the_emitters(cuda_lib):
             gain.append(proposal.density(cdf[r], sub[r], 16, 16, x, y) * 256.0)
     print("mean learned density at the true emitters, relative to uniform:", np.mean(gain))
     assert np.mean(gain) > 5.0
+
+
+def test_start_states_follow_the_count_logits_and_density(cuda_lib):
+    """The network start state: n0 = argmax of the count logits, positions
+    at distinct high-density sub-cells; a trained network puts them near the
+    true emitters."""
+    from bamf_gb300 import learned
+    net = learned.ProposalNet(seed=6)
+    net.train(300, batch=256, lr=2e-3, data_seed=31)
+    ev = learned.generate(300, seed=77)
+    tab = net.infer(ev["data"])
+    st = learned.init_states(tab, intensity=900.0, max_n=10)
+    n0 = st["init_n"].cpu().numpy()
+    ixy = st["init_ixy"].cpu().numpy()
+    cl = tab["count_logits"].cpu().numpy()
+    np.testing.assert_array_equal(n0, np.minimum(cl.argmax(1), 10))
+    h = {k: v.cpu().numpy() for k, v in ev.items()}
+    near = []
+    for r in range(300):
+        k = int(n0[r])
+        assert (ixy[r, 0, :k] == 900.0).all() and (ixy[r, :, k:] == 0).all()
+        X, Y = ixy[r, 1, :k], ixy[r, 2, :k]
+        assert ((X > 0) & (X < 16) & (Y > 0) & (Y < 16)).all()
+        for a in range(k):
+            for b in range(a):
+                assert (X[a] - X[b]) ** 2 + (Y[a] - Y[b]) ** 2 >= 1.0 - 1e-5
+            m = int(h["n_em"][r])
+            if m:
+                d = np.min((h["xyi"][r, :m, 0] - X[a]) ** 2 + (h["xyi"][r, :m, 1] - Y[a]) ** 2)
+                near.append(d < 0.5 ** 2)
+    print("start emitters within 0.5 px of a true one:", np.mean(near))
+    assert np.mean(near) > 0.6
+    print("count accuracy of the start state:", np.mean(n0 == np.minimum(h["n_em"], 10)))
