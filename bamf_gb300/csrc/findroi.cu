@@ -28,6 +28,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -63,41 +64,94 @@ __device__ __forceinline__ float iir_step(float w0, float w1, float w2, float w3
     return __fmaf_rn(w0, c.B, __fdiv_rn(q, c.b0));
 }
 
-/* Pass 1: one thread per (frame, row); both sigmas from one read of the row.
- * out_a/out_b may alias nothing; the row is read through L1 as it is
- * walked, and the backward pass re-reads the forward result it wrote. */
-__global__ void __launch_bounds__(128) rows_kernel(const float *__restrict__ in,
-                                                   float *__restrict__ out_a,
-                                                   float *__restrict__ out_b, int X, int Y, int Z,
-                                                   Coef ca, Coef cb)
+/* Pass 1: one thread per (frame, row) runs the row's recurrence for both
+ * sigmas, in the reference's sequential order.  Rows are contiguous, so the
+ * warp moves its 32 rows through shared memory in chunks of 32 columns: a
+ * [32][33] tile is loaded with 128-byte row segments (coalesced), each
+ * thread walks its own tile row (stride 33: conflict-free), and the
+ * results leave the same way.  The forward results go to out_a/out_b and
+ * come back chunk by chunk, last chunk first, for the backward pass; the
+ * grid is persistent with ROWS_CTAS_PER_SM CTAs per SM so that the rows in
+ * flight (and their forward results) stay within L2. */
+constexpr int ROWS_WARPS = 3;
+constexpr int ROWS_CTAS_PER_SM = 3;
+
+__global__ void __launch_bounds__(32 * ROWS_WARPS) rows_kernel(const float *__restrict__ in,
+                                                               float *__restrict__ out_a,
+                                                               float *__restrict__ out_b, int X, int Y,
+                                                               int Z, Coef ca, Coef cb)
 {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (int64_t)Y * Z) return;
-    int64_t base = t * X; /* row t of the stack = frame t / Y, row t % Y */
-    const float *src = in + base;
-    float *a = out_a + base, *b = out_b + base;
-    float a1, a2, a3, b1, b2, b3;
-    float v0 = src[0];
-    a1 = a2 = a3 = v0;
-    b1 = b2 = b3 = v0;
-    for (int i = 0; i < X; ++i) {
-        float w0 = src[i];
-        float ta = iir_step(w0, a1, a2, a3, ca);
-        float tb = iir_step(w0, b1, b2, b3, cb);
-        a[i] = ta;
-        b[i] = tb;
-        a3 = a2; a2 = a1; a1 = ta;
-        b3 = b2; b2 = b1; b1 = tb;
-    }
-    a1 = a2 = a3 = a[X - 1];
-    b1 = b2 = b3 = b[X - 1];
-    for (int i = X - 1; i >= 0; --i) {
-        float ta = iir_step(a[i], a1, a2, a3, ca);
-        float tb = iir_step(b[i], b1, b2, b3, cb);
-        a[i] = ta;
-        b[i] = tb;
-        a3 = a2; a2 = a1; a1 = ta;
-        b3 = b2; b2 = b1; b1 = tb;
+    __shared__ float tile[ROWS_WARPS][3][32][33];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float(*ti)[33] = tile[warp][0];
+    float(*ta_)[33] = tile[warp][1];
+    float(*tb_)[33] = tile[warp][2];
+    const int64_t nrows = (int64_t)Y * Z;
+    const int64_t ngroups = (nrows + 31) / 32;
+    const int nch = (X + 31) / 32;
+    for (int64_t g = (int64_t)blockIdx.x * ROWS_WARPS + warp; g < ngroups; g += (int64_t)gridDim.x * ROWS_WARPS) {
+        const int64_t row0 = g * 32;
+        const int rows_here = (int)min((int64_t)32, nrows - row0);
+        const bool mine = lane < rows_here;
+        float a1 = 0.0f, a2 = 0.0f, a3 = 0.0f, b1 = 0.0f, b2 = 0.0f, b3 = 0.0f;
+        for (int c = 0; c < nch; ++c) {
+            const int c0 = c * 32, w = min(32, X - c0);
+            for (int r = 0; r < rows_here; ++r)
+                if (lane < w) ti[r][lane] = in[(row0 + r) * X + c0 + lane];
+            __syncwarp();
+            if (mine) {
+                if (c == 0) {
+                    a1 = a2 = a3 = ti[lane][0];
+                    b1 = b2 = b3 = ti[lane][0];
+                }
+                for (int j = 0; j < w; ++j) {
+                    float w0 = ti[lane][j];
+                    float ta = iir_step(w0, a1, a2, a3, ca);
+                    float tb = iir_step(w0, b1, b2, b3, cb);
+                    ta_[lane][j] = ta;
+                    tb_[lane][j] = tb;
+                    a3 = a2; a2 = a1; a1 = ta;
+                    b3 = b2; b2 = b1; b1 = tb;
+                }
+            }
+            __syncwarp();
+            for (int r = 0; r < rows_here; ++r)
+                if (lane < w) {
+                    out_a[(row0 + r) * X + c0 + lane] = ta_[r][lane];
+                    out_b[(row0 + r) * X + c0 + lane] = tb_[r][lane];
+                }
+            __syncwarp();
+        }
+        for (int c = nch - 1; c >= 0; --c) {
+            const int c0 = c * 32, w = min(32, X - c0);
+            for (int r = 0; r < rows_here; ++r)
+                if (lane < w) {
+                    ta_[r][lane] = out_a[(row0 + r) * X + c0 + lane];
+                    tb_[r][lane] = out_b[(row0 + r) * X + c0 + lane];
+                }
+            __syncwarp();
+            if (mine) {
+                if (c == nch - 1) {
+                    a1 = a2 = a3 = ta_[lane][w - 1];
+                    b1 = b2 = b3 = tb_[lane][w - 1];
+                }
+                for (int j = w - 1; j >= 0; --j) {
+                    float ta = iir_step(ta_[lane][j], a1, a2, a3, ca);
+                    float tb = iir_step(tb_[lane][j], b1, b2, b3, cb);
+                    ta_[lane][j] = ta;
+                    tb_[lane][j] = tb;
+                    a3 = a2; a2 = a1; a1 = ta;
+                    b3 = b2; b2 = b1; b1 = tb;
+                }
+            }
+            __syncwarp();
+            for (int r = 0; r < rows_here; ++r)
+                if (lane < w) {
+                    out_a[(row0 + r) * X + c0 + lane] = ta_[r][lane];
+                    out_b[(row0 + r) * X + c0 + lane] = tb_[r][lane];
+                }
+            __syncwarp();
+        }
     }
 }
 
@@ -383,7 +437,15 @@ extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *fr
         return BAMF_ERR_CUDA;
     float *A = (float *)ws->a.p, *Bb = (float *)ws->b.p;
     int64_t nrows = (int64_t)KY * zsize, ncols = (int64_t)KX * zsize;
-    rows_kernel<<<(unsigned)((nrows + 127) / 128), 128, 0, s>>>(frames, A, Bb, KX, KY, zsize, ca, cb);
+    {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int64_t groups = (nrows + 31) / 32;
+        unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((groups + ROWS_WARPS - 1) / ROWS_WARPS,
+                                                                         (int64_t)sms * ROWS_CTAS_PER_SM));
+        rows_kernel<<<grid, 32 * ROWS_WARPS, 0, s>>>(frames, A, Bb, KX, KY, zsize, ca, cb);
+    }
     cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(A, Bb, KX, KY, zsize, ca, cb);
     rowmax_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, Bb, KX, KY, zsize, boxsize, minval);
     colmax_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Bb, flags, KX, KY, zsize, boxsize, minval);

@@ -16,6 +16,10 @@ roofline  the sampler kernel against the measured MUFU log2 rate: one log2 per
           ROI pixel per scored proposal (the likelihood-ratio pass)
 cpu_baseline  the CPU restatement of the reference sampler (glibc math, bit-
           identical to the reference build) on the host cores, on a sample
+frontend  (rank 0, outside the timed region) FindROI + gaussMLE on the
+          2000-frame 256x256 front-end workload: frames/s, FindROI against the
+          measured HBM bandwidth (one 4-byte read per pixel), fits/s, and an
+          end-to-end frames/s with the stack copied from pinned host memory
 learned_proposal  (rank 0, outside the timed region) the learned-vs-uniform
           birth-proposal evaluation on 16x16 ROIs (bamf_gb300.learned_eval):
           network training rate, per-arm ROIs/s, ESS/s of the emitter count
@@ -58,7 +62,84 @@ def parse():
                     help="skip the learned-vs-uniform proposal evaluation (16x16 ROIs)")
     ap.add_argument("--learned-train-rois", type=int, default=2_000_000)
     ap.add_argument("--learned-eval-rois", type=int, default=50_000)
+    ap.add_argument("--no-frontend", action="store_true", help="skip the FindROI + gaussMLE measurement")
+    ap.add_argument("--frontend-frames", type=int, default=2000)
     return ap.parse_args()
+
+
+def measured_hbm_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s (of fallback)"
+
+
+def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3) -> dict:
+    """FindROI + gaussMLE on n_frames 256x256 frames (Poisson(50) emitters
+    per frame, sigma 1.3, I ~ LogN(ln 1500, 0.3), bg 20; Boxsize 7, Minval
+    from findROI.m:74, 10 Newton iterations).  The stack (524 MB at 2000
+    frames) is larger than L2, so no flush between calls."""
+    import torch
+
+    from bamf_gb300 import frontend, synth
+    stack, _ = synth.frames(n_frames, seed=3)
+    host = torch.from_numpy(np.asfortranarray(stack).ravel(order="F")).pin_memory()
+    dev = host.cuda()
+    n = dev.numel()
+    mv = frontend.default_minval()
+    fr = frontend.FindRoiDevice()
+    ev = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))  # noqa: E731
+    for _ in range(warmup):
+        out = fr.run(dev, 256, 256, n_frames, boxsize=7, minval=mv)
+    torch.cuda.synchronize()
+    t_find = []
+    for _ in range(steps):
+        e0, e1 = ev()
+        e0.record()
+        out = fr.run(dev, 256, 256, n_frames, boxsize=7, minval=mv)
+        e1.record()
+        torch.cuda.synchronize()
+        t_find.append(e0.elapsed_time(e1) * 1e-3)
+    count = int(out["count"].item())
+    rois = out["stack"][:count].contiguous()
+    for _ in range(warmup):
+        frontend.gauss_mle_device(rois, 7, count, 1.3, 10)
+    torch.cuda.synchronize()
+    t_mle = []
+    for _ in range(steps):
+        e0, e1 = ev()
+        e0.record()
+        frontend.gauss_mle_device(rois, 7, count, 1.3, 10)
+        e1.record()
+        torch.cuda.synchronize()
+        t_mle.append(e0.elapsed_time(e1) * 1e-3)
+    # end to end through the device API: pinned host frames in, fits out
+    e2e = []
+    for _ in range(steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d = host.to("cuda", non_blocking=True)
+        o = fr.run(d, 256, 256, n_frames, boxsize=7, minval=mv)
+        c = int(o["count"].item())
+        P, CR, LL = frontend.gauss_mle_device(o["stack"][:c].contiguous(), 7, c, 1.3, 10)
+        res = (o["coords"][:c].cpu(), P.cpu(), CR.cpu(), LL.cpu())
+        e2e.append(time.perf_counter() - t0)
+    d2h = sum(r.numel() * r.element_size() for r in res)
+    tf, tm = statistics.median(t_find), statistics.median(t_mle)
+    peak, src = measured_hbm_gbs()
+    alg = 4.0 * n + count * (3 + 2 + 49) * 4.0
+    return {
+        "workload": f"FindROI + gaussMLE: {n_frames} frames 256x256, Boxsize 7, 10 iterations",
+        "findroi_ms": tf * 1e3, "findroi_frames_per_s": n_frames / tf,
+        "findroi_roofline": {"bound": "hbm", "achieved": alg / tf / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": alg / tf / 1e9 / peak, "traffic": None, "peak_source": src,
+                             "algorithmic_bytes": alg},
+        "maxima": count, "gaussmle_ms": tm * 1e3, "gaussmle_fits_per_s": count / tm,
+        "gaussmle_achieved_gbs": count * (49 + 9) * 4.0 / tm / 1e9,
+        "e2e": {"value": n_frames / statistics.median(e2e[1:]), "unit": "frames/s",
+                "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(d2h)},
+    }
 
 
 def workload_label(n_rois: int, jumps: int) -> str:
@@ -284,6 +365,10 @@ def main():
             "equal_accuracy": r["equal_accuracy_vs_uniform_at_full_length"],
         }
 
+    frontend_block = None
+    if rank == 0 and not a.no_frontend:
+        frontend_block = frontend_bench(a.frontend_frames)
+
     cpu = None
     if rank == 0:
         threads = os.cpu_count() or 1
@@ -311,6 +396,7 @@ def main():
             "gpu_launches": launches_per_step * a.steps,
             "clocks": clk.summary(),
             "learned_proposal": learned_block,
+            "frontend": frontend_block,
             "map_n_mean": float(outs["map_n"].float().mean().item()),
             "true_n_mean": float(b.true_n.mean()),
         }
