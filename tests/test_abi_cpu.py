@@ -10,7 +10,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_functions():
     names = set()
-    for h in ("bamf.h", "bamf_cnn.h"):
+    for h in ("bamf.h", "bamf_cnn.h", "bamf_tiles.h"):
         txt = open(os.path.join(ROOT, "include", h)).read()
         txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
         for m in re.finditer(r"^\s*(?:const\s+)?[\w\s\*]*?\b(bamf_\w+)\s*\(", txt, flags=re.M):
