@@ -269,6 +269,11 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     }
     B.birth_cdf = rois->birth_cdf;
     B.birth_sub = rois->birth_sub;
+    B.pgrid = out->pgrid;
+    B.pback = out->pback;
+    B.grid_stride = out->grid_stride;
+    B.grid_ld = out->grid_ld;
+    B.grid_slot = out->grid_slot;
     if (cudaGetLastError() != cudaSuccess) return BAMF_ERR_CUDA;
 
     const bool exact = arith == BAMF_ARITH_EXACT;

@@ -398,6 +398,8 @@ bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcm
     if (rois->proposal == BAMF_PROPOSAL_LEARNED && (!rois->birth_cdf || !rois->birth_sub))
         return BAMF_ERR_INVALID_ARG;
     if ((out->n_trace || out->x_trace) && out->trace_len < 1) return BAMF_ERR_INVALID_ARG;
+    if ((out->pgrid || out->pback) && (out->grid_stride < 1 || out->grid_ld < 0 || p->Grid_Zoom < 1))
+        return BAMF_ERR_INVALID_ARG;
     if (out->n_trace && out->map_n && (int64_t)out->trace_len < (int64_t)p->N_Burnin + p->N_Trials)
         return BAMF_ERR_INVALID_ARG;
     return BAMF_OK;
@@ -449,6 +451,11 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     B.llr_evals = out->llr_evals;
     B.birth_cdf = rois->birth_cdf;
     B.birth_sub = rois->birth_sub;
+    B.pgrid = out->pgrid;
+    B.pback = out->pback;
+    B.grid_stride = out->grid_stride;
+    B.grid_ld = out->grid_ld;
+    B.grid_slot = out->grid_slot;
     if (out->x_trace) {
         B.x_trace = out->x_trace;
         B.x_cap = out->trace_len;

@@ -67,9 +67,11 @@ struct SamplerBatch {
     int32_t *status;              /* [roi] 0 ok, else BAMF_ERR_*           */
     int32_t *overflow;            /* [roi] proposals rejected at BAMF_NMAX */
     int32_t *llr_evals;           /* [roi] likelihood-ratio evaluations     */
-    float *pgrid;                 /* [roi][grid_stride] or null            */
+    float *pgrid;                 /* [slot][grid_stride] or null           */
     float *pback;
     int64_t grid_stride;
+    int32_t grid_ld;              /* column stride of a grid; 0: the ROI's zoomed height */
+    const int32_t *grid_slot;     /* grid of each ROI, or null: the ROI's own */
     /* full chain recording (exact cRJMCMC outputs), or null */
     bamf_chain *chains;           /* device array [roi][2] of bamf_chain with device pointers */
     int32_t *queue;               /* work-queue counter (device int)       */

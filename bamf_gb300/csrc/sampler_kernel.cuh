@@ -733,9 +733,12 @@ struct ChainWarp {
         if (lane < an) {
             int x = (int)floor(dadd((double)((float)Z * (aX + K->p.DriftX)), 0.5));
             int y = (int)floor(dadd((double)((float)Z * (aY + K->p.DriftY)), 0.5));
-            if (x >= 0 && x < X * Z && y >= 0 && y < Y * Z && aI > K->p.Icutoff) {
-                float *g = (aS == 1 ? B->pgrid : B->pback) + (int64_t)roi * B->grid_stride;
-                atomicAdd(&g[x * Y * Z + y], 1.0f);
+            float *gb = aS == 1 ? B->pgrid : B->pback;
+            if (gb && x >= 0 && x < X * Z && y >= 0 && y < Y * Z && aI > K->p.Icutoff) {
+                /* grid slot (ROIs sharing one accumulate) and column stride */
+                int64_t slot = B->grid_slot ? (int64_t)B->grid_slot[roi] : (int64_t)roi;
+                int64_t ld = B->grid_ld > 0 ? (int64_t)B->grid_ld : (int64_t)Y * Z;
+                atomicAdd(&gb[slot * B->grid_stride + (int64_t)x * ld + y], 1.0f);
             }
         }
     }

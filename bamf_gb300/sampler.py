@@ -65,7 +65,8 @@ class BatchResults(C.Structure):
     _fields_ = [("map_n", C.c_void_p), ("final_n", C.c_void_p), ("final_state", C.c_void_p),
                 ("counters", C.c_void_p), ("n_entries", C.c_void_p), ("status", C.c_void_p),
                 ("overflow", C.c_void_p), ("llr_evals", C.c_void_p), ("trace_len", C.c_int32),
-                ("n_trace", C.c_void_p), ("x_trace", C.c_void_p)]
+                ("n_trace", C.c_void_p), ("x_trace", C.c_void_p), ("pgrid", C.c_void_p), ("pback", C.c_void_p),
+                ("grid_stride", C.c_int64), ("grid_ld", C.c_int32), ("grid_slot", C.c_void_p)]
 
 
 # birth proposals of the batched sampler (bamf_roi_batch.proposal)
@@ -243,6 +244,11 @@ class Sampler:
                   "llr_evals", "n_trace", "x_trace"):
             t = outs.get(k)
             setattr(res, k, t.data_ptr() if t is not None else None)
+        for k in ("pgrid", "pback", "grid_slot"):
+            t = outs.get(k)
+            setattr(res, k, t.data_ptr() if t is not None else None)
+        res.grid_stride = int(outs.get("grid_stride", 0))
+        res.grid_ld = int(outs.get("grid_ld", 0))
         tr = [outs[k] for k in ("n_trace", "x_trace") if outs.get(k) is not None]
         if tr:
             if any(t.dim() != 2 or t.shape[1] != tr[0].shape[1] for t in tr):

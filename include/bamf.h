@@ -283,7 +283,16 @@ typedef struct bamf_roi_batch {
  *                state at each chain entry (the first trace_len entries);
  *                with map_n it must hold N_Burnin + N_Trials entries
  *   x_trace      [k][trace_len] mean X of those emitters (NaN when none): a
- *                permutation-invariant position functional for ESS */
+ *                permutation-invariant position functional for ESS
+ *   pgrid, pback posterior grids (update_grids, LibRJMCMC.cpp:1629-1648):
+ *                each trial-phase step adds 1 at (round(Zoom (Y+DriftY)),
+ *                round(Zoom (X+DriftX))) for every emitter with I > Icutoff,
+ *                Signal==1 into pgrid, Signal==0 into pback (either may be
+ *                NULL); grid g starts at g * grid_stride floats, column
+ *                stride grid_ld (0: the ROI's Zoom*Ysize); ROI k writes grid
+ *                grid_slot[k] (grid_slot NULL: grid k), so ROIs sharing a
+ *                slot accumulate into one grid (the per-sub-region sum over
+ *                frames of analyzeROIs.m:153).  The caller zeroes them. */
 typedef struct bamf_batch_results {
     int32_t *map_n;
     int32_t *final_n;
@@ -296,6 +305,11 @@ typedef struct bamf_batch_results {
     int32_t trace_len;
     uint8_t *n_trace;
     float *x_trace;
+    float *pgrid;
+    float *pback;
+    int64_t grid_stride;
+    int32_t grid_ld;
+    const int32_t *grid_slot;
 } bamf_batch_results;
 
 /* Device scratch (prior tables, work queue, per-ROI chain traces) that

@@ -117,3 +117,41 @@ def test_fast_batch_is_deterministic(cuda_lib):
     r2 = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=5, arith="fast", bg0=bg0)
     for k in ("map_n", "final_n", "final_state", "counters"):
         np.testing.assert_array_equal(r1[k], r2[k], err_msg=k)
+
+
+def test_batch_posterior_grids_match_single_roi_and_accumulate_by_slot(cuda_lib):
+    """Batched grids (exact arithmetic): ROI k's grid equals cRJMCMC's PGrid
+    for the same chain; with grid_slot, ROIs sharing a slot add up."""
+    import torch
+    b, rj = _c0(6, steps=300)
+    p = rjstruct.mcmc_params(rj)
+    bg0 = rjstruct.initial_bg(rj)
+    Z = int(p.Grid_Zoom)
+    gs = 16 * Z * 16 * Z
+    dev = {k: torch.from_numpy(v).cuda() for k, v in
+           (("data", b.data), ("offsets", b.offsets), ("xsize", b.xsize), ("ysize", b.ysize))}
+    dev["side_max"] = 16
+    s = sampler.Sampler()
+
+    def run(slots):
+        ng = 6 if slots is None else int(max(slots)) + 1
+        outs = {"status": torch.zeros(6, dtype=torch.int32, device="cuda"),
+                "pgrid": torch.zeros(ng * gs, dtype=torch.float32, device="cuda"),
+                "pback": torch.zeros(ng * gs, dtype=torch.float32, device="cuda"), "grid_stride": gs}
+        if slots is not None:
+            outs["grid_slot"] = torch.tensor(slots, dtype=torch.int32, device="cuda")
+        s.run_device(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=13, arith="exact", outs=outs,
+                     bg0=bg0)
+        torch.cuda.synchronize()
+        assert (outs["status"] == 0).all()
+        return outs["pgrid"].cpu().numpy().reshape(ng, 16 * Z, 16 * Z)  # [g][x][y]
+
+    own = run(None)
+    for k in (0, 3):
+        one = sampler.crjmcmc_raw(b.roi(k), p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons,
+                                  e0=([], [], [], bg0), rng=(13, k, 0), record=False)
+        np.testing.assert_array_equal(own[k].T, one["pgrid"])
+    assert own.sum() > 0
+    shared = run([0, 0, 1, 1, 2, 2])
+    for g in range(3):
+        np.testing.assert_array_equal(shared[g], own[2 * g] + own[2 * g + 1])
