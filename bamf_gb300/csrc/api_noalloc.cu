@@ -274,6 +274,9 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     B.grid_stride = out->grid_stride;
     B.grid_ld = out->grid_ld;
     B.grid_slot = out->grid_slot;
+    B.pos_trace = out->pos_trace;
+    B.pos_len = out->pos_len;
+    B.pos_thin = out->pos_thin;
     if (cudaGetLastError() != cudaSuccess) return BAMF_ERR_CUDA;
 
     const bool exact = arith == BAMF_ARITH_EXACT;

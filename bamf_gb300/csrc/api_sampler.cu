@@ -400,6 +400,7 @@ bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcm
     if ((out->n_trace || out->x_trace) && out->trace_len < 1) return BAMF_ERR_INVALID_ARG;
     if ((out->pgrid || out->pback) && (out->grid_stride < 1 || out->grid_ld < 0 || p->Grid_Zoom < 1))
         return BAMF_ERR_INVALID_ARG;
+    if (out->pos_trace && (out->pos_len < 1 || out->pos_thin < 1)) return BAMF_ERR_INVALID_ARG;
     if (out->n_trace && out->map_n && (int64_t)out->trace_len < (int64_t)p->N_Burnin + p->N_Trials)
         return BAMF_ERR_INVALID_ARG;
     return BAMF_OK;
@@ -456,6 +457,9 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     B.grid_stride = out->grid_stride;
     B.grid_ld = out->grid_ld;
     B.grid_slot = out->grid_slot;
+    B.pos_trace = out->pos_trace;
+    B.pos_len = out->pos_len;
+    B.pos_thin = out->pos_thin;
     if (out->x_trace) {
         B.x_trace = out->x_trace;
         B.x_cap = out->trace_len;

@@ -72,6 +72,9 @@ struct SamplerBatch {
     int64_t grid_stride;
     int32_t grid_ld;              /* column stride of a grid; 0: the ROI's zoomed height */
     const int32_t *grid_slot;     /* grid of each ROI, or null: the ROI's own */
+    float *pos_trace;             /* [roi][pos_len][BAMF_POS_RECORD] thinned states */
+    int32_t pos_len;
+    int32_t pos_thin;
     /* full chain recording (exact cRJMCMC outputs), or null */
     bamf_chain *chains;           /* device array [roi][2] of bamf_chain with device pointers */
     int32_t *queue;               /* work-queue counter (device int)       */

@@ -710,6 +710,36 @@ struct ChainWarp {
             B->x_trace[(int64_t)roi * B->x_cap + entries] = ns > 0 ? sx / (float)ns : __int_as_float(0x7fc00000);
     }
 
+    /* thinned state record: entry, Signal==1 count, BG, ABG, BBG, then X, Y,
+     * I of the Signal==1 emitters in slot order (NaN past the count) */
+    __device__ __forceinline__ void record_pos()
+    {
+        float *rec = B->pos_trace + ((int64_t)roi * B->pos_len + entries / B->pos_thin) * BAMF_POS_RECORD;
+        bool on = lane < an && aS == 1;
+        uint32_t m = __ballot_sync(BAMF_FULL, on);
+        int rank = __popc(m & ((1u << lane) - 1u));
+        int ns = __popc(m);
+        if (lane == 0) {
+            rec[0] = (float)entries;
+            rec[1] = (float)ns;
+            rec[2] = aBG;
+            rec[3] = aABG;
+            rec[4] = aBBG;
+        }
+        if (lane < BAMF_POS_SLOTS) {
+            const float nan = __int_as_float(0x7fc00000);
+            rec[5 + lane] = nan;
+            rec[5 + BAMF_POS_SLOTS + lane] = nan;
+            rec[5 + 2 * BAMF_POS_SLOTS + lane] = nan;
+        }
+        __syncwarp();
+        if (on && rank < BAMF_POS_SLOTS) {
+            rec[5 + rank] = aX;
+            rec[5 + BAMF_POS_SLOTS + rank] = aY;
+            rec[5 + 2 * BAMF_POS_SLOTS + rank] = aI;
+        }
+    }
+
     /* RJMCMCChain::addEmitters on Chain (A) and Chain_Test (T). */
     __device__ __forceinline__ void record2(float LLR, float PR, int type, int acc)
     {
@@ -718,6 +748,7 @@ struct ChainWarp {
             if (lane == 0) B->nsig_trace[(int64_t)roi * B->trace_cap + entries] = (uint8_t)(an < 1 ? 0 : ns);
         }
         if (B->x_trace && entries < B->x_cap) record_x();
+        if (B->pos_trace && entries % B->pos_thin == 0 && entries / B->pos_thin < B->pos_len) record_pos();
         if (B->chains) {
             record_one(0, an, aI, aX, aY, aS, aBG, aABG, aBBG, LLR, PR, type, acc);
             record_one(1, tn, tI, tX, tY, tS, tBG, tABG, tBBG, LLR, PR, type, acc);

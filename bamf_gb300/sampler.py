@@ -66,7 +66,11 @@ class BatchResults(C.Structure):
                 ("counters", C.c_void_p), ("n_entries", C.c_void_p), ("status", C.c_void_p),
                 ("overflow", C.c_void_p), ("llr_evals", C.c_void_p), ("trace_len", C.c_int32),
                 ("n_trace", C.c_void_p), ("x_trace", C.c_void_p), ("pgrid", C.c_void_p), ("pback", C.c_void_p),
-                ("grid_stride", C.c_int64), ("grid_ld", C.c_int32), ("grid_slot", C.c_void_p)]
+                ("grid_stride", C.c_int64), ("grid_ld", C.c_int32), ("grid_slot", C.c_void_p),
+                ("pos_trace", C.c_void_p), ("pos_len", C.c_int32), ("pos_thin", C.c_int32)]
+
+POS_SLOTS = 16
+POS_RECORD = 5 + 3 * POS_SLOTS
 
 
 # birth proposals of the batched sampler (bamf_roi_batch.proposal)
@@ -244,11 +248,14 @@ class Sampler:
                   "llr_evals", "n_trace", "x_trace"):
             t = outs.get(k)
             setattr(res, k, t.data_ptr() if t is not None else None)
-        for k in ("pgrid", "pback", "grid_slot"):
+        for k in ("pgrid", "pback", "grid_slot", "pos_trace"):
             t = outs.get(k)
             setattr(res, k, t.data_ptr() if t is not None else None)
         res.grid_stride = int(outs.get("grid_stride", 0))
         res.grid_ld = int(outs.get("grid_ld", 0))
+        if outs.get("pos_trace") is not None:
+            res.pos_len = int(outs["pos_trace"].shape[1])
+            res.pos_thin = int(outs.get("pos_thin", 1))
         tr = [outs[k] for k in ("n_trace", "x_trace") if outs.get(k) is not None]
         if tr:
             if any(t.dim() != 2 or t.shape[1] != tr[0].shape[1] for t in tr):

@@ -292,7 +292,13 @@ typedef struct bamf_roi_batch {
  *                stride grid_ld (0: the ROI's Zoom*Ysize); ROI k writes grid
  *                grid_slot[k] (grid_slot NULL: grid k), so ROIs sharing a
  *                slot accumulate into one grid (the per-sub-region sum over
- *                frames of analyzeROIs.m:153).  The caller zeroes them. */
+ *                frames of analyzeROIs.m:153).  The caller zeroes them.
+ *   pos_trace    [k][pos_len][BAMF_POS_RECORD] thinned chain states: chain
+ *                entry e = r * pos_thin is record r (r < pos_len): entry
+ *                index, Signal==1 count, BG, ABG, BBG, then X, Y, I of up
+ *                to BAMF_POS_SLOTS Signal==1 emitters in slot order (NaN
+ *                past the count); the input of bamf_map_kmeans_device and
+ *                bamf_refine_stats_device (findMap.m, mcmc.m) */
 typedef struct bamf_batch_results {
     int32_t *map_n;
     int32_t *final_n;
@@ -310,7 +316,32 @@ typedef struct bamf_batch_results {
     int64_t grid_stride;
     int32_t grid_ld;
     const int32_t *grid_slot;
+    float *pos_trace;
+    int32_t pos_len;
+    int32_t pos_thin;
 } bamf_batch_results;
+
+#define BAMF_POS_SLOTS 16
+#define BAMF_POS_RECORD (5 + 3 * BAMF_POS_SLOTS)
+
+/* Chain summaries from pos_trace (device pointers; pos_trace as the batch
+ * wrote it with pos_len <= 256 records of every pos_thin-th entry).  Output
+ * per ROI: BAMF_MAP_RECORD floats = count, records used, Bg mean, Bg std,
+ * ABg mean, BBg mean, then X[16], Y[16], I[16], X_SE[16], Y_SE[16],
+ * I_SE[16] (NaN past the count).
+ *   bamf_map_kmeans_device   findMap.m:29-111 (FB = 1): MAP count map_n
+ *                            (from the full count trace, e.g. the batch's
+ *                            map_n), then k-means of the positions of the
+ *                            recorded second-half states with that count
+ *                            and per-cluster mean / std (n-1) of X, Y, I
+ *   bamf_refine_stats_device mcmc.m:142-169: per-emitter mean / std over
+ *                            the recorded second half of a jumps-only chain
+ */
+#define BAMF_MAP_RECORD (6 + 6 * BAMF_POS_SLOTS)
+bamf_status bamf_map_kmeans_device(const float *pos_trace, int pos_len, int pos_thin, const int32_t *n_entries,
+                                   const int32_t *map_n, int n, int max_iter, float *out, void *stream);
+bamf_status bamf_refine_stats_device(const float *pos_trace, int pos_len, int pos_thin, const int32_t *n_entries,
+                                     int n, float *out, void *stream);
 
 /* Device scratch (prior tables, work queue, per-ROI chain traces) that
  * grows on demand and is reused across calls on one stream. */
