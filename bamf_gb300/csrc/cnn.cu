@@ -170,7 +170,12 @@ __global__ void synth_kernel(bamf_synth_params sp, uint32_t seed, uint64_t first
     if (t == 0) n_em[r] = nn;
     int x = t / S, y = t - (t / S) * S;
     const float c = 1.0f / (sqrtf(2.0f) * sp.sigma);
-    float lam = sp.bg;
+    float bgv = sp.bg;
+    if (sp.bg_max > sp.bg) {
+        bamf_philox_block bb = bamf_philox4x32_10(klo, 3u, 0u, 0u, seed, K1);
+        bgv = sp.bg + (sp.bg_max - sp.bg) * u01(bb.v[0]);
+    }
+    float lam = bgv;
     for (int e = 0; e < nn; ++e) {
         float sx = 0.5f * (erff(((float)x - ex[e] + 1.0f) * c) - erff(((float)x - ex[e]) * c));
         float sy = 0.5f * (erff(((float)y - ey[e] + 1.0f) * c) - erff(((float)y - ey[e]) * c));

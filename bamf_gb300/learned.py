@@ -22,12 +22,12 @@ SYNTH_NMAX = 16
 
 class SynthParams(C.Structure):
     _fields_ = [("mean_n", C.c_float), ("sigma", C.c_float), ("i_median", C.c_float),
-                ("i_logsd", C.c_float), ("bg", C.c_float)]
+                ("i_logsd", C.c_float), ("bg", C.c_float), ("bg_max", C.c_float)]
 
 
 # the plain-RJMCMC generator (16x16, sigma 1.3, I ~ LogN(ln 1000, 0.3), bg 10)
 # with Poisson(5) emitter counts: the training distribution of the network
-C3_SYNTH = dict(mean_n=5.0, sigma=1.3, i_median=1000.0, i_logsd=0.3, bg=10.0)
+C3_SYNTH = dict(mean_n=5.0, sigma=1.3, i_median=1000.0, i_logsd=0.3, bg=10.0, bg_max=0.0)
 
 
 def _lib() -> C.CDLL:

@@ -140,6 +140,33 @@ def frames(n_frames: int = 2000, size: int = 256, seed: int = 1, density: float 
     return stack, truth
 
 
+def frames_dense(n_frames: int = 10_000, size: int = 256, seed: int = 5, px_nm: float = 100.0,
+                 density=(1.0, 10.0), sigma: float = 1.3, median_i: float = 800.0, log_sd: float = 0.5,
+                 bg=(50.0, 200.0)):
+    """The dense end-to-end stress frames: per frame an emitter density
+    uniform on `density` per um^2 (pixel size px_nm), Poisson count over the
+    frame, positions uniform, LogN(ln median_i, log_sd) intensities, a
+    uniform background drawn per frame from `bg`, Poisson noise.  Returns
+    (stack (size, size, n) float32 MATLAB orientation, truth per frame as
+    (X, Y, I) arrays, backgrounds)."""
+    rng = np.random.default_rng(seed)
+    area_um2 = (size * px_nm / 1000.0) ** 2
+    stack = np.empty((size, size, n_frames), dtype=np.float32, order="F")
+    truth, bgs = [], []
+    for k in range(n_frames):
+        rho = rng.uniform(*density)
+        n = rng.poisson(rho * area_um2)
+        X = rng.uniform(0, size, n)
+        Y = rng.uniform(0, size, n)
+        I = rng.lognormal(np.log(median_i), log_sd, n)
+        b = rng.uniform(*bg)
+        lam = model_image(size, size, X, Y, I, b, sigma)
+        stack[:, :, k] = rng.poisson(lam)
+        truth.append((X, Y, I))
+        bgs.append(b)
+    return stack, truth, np.array(bgs)
+
+
 def lognormal_pdf(x: np.ndarray, median: float, log_sd: float) -> np.ndarray:
     x = np.asarray(x, dtype=np.float64)
     out = np.zeros_like(x)

@@ -49,13 +49,15 @@ extern "C" {
  * model (source/c/LibRJMCMC.cpp:15-59: background plus per-emitter
  * erf-integrated Gaussian) with Poisson noise.  n ~ Poisson(mean_n) clipped
  * to BAMF_SYNTH_NMAX, positions uniform on [0, 16)^2, intensity
- * log-normal(ln i_median, i_logsd), background bg, PSF sigma. */
+ * log-normal(ln i_median, i_logsd), background bg (uniform on [bg, bg_max]
+ * when bg_max > bg), PSF sigma. */
 typedef struct bamf_synth_params {
     float mean_n;
     float sigma;
     float i_median;
     float i_logsd;
     float bg;
+    float bg_max;
 } bamf_synth_params;
 
 /* n ROIs numbered first .. first+n-1 of the stream `seed` (ROI k depends
