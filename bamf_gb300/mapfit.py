@@ -17,7 +17,7 @@ import numpy as np
 
 from . import abi, rjstruct, sampler
 
-POS_SLOTS = 16
+POS_SLOTS = 32
 POS_RECORD = 5 + 3 * POS_SLOTS
 MAP_RECORD = 6 + 6 * POS_SLOTS
 MAX_POS_LEN = 256
@@ -64,7 +64,7 @@ def refine_stats(pos_trace, pos_thin: int, n_entries, stream=None):
 
 
 def unpack(rec: np.ndarray) -> dict:
-    """Rows of BAMF_MAP_RECORD floats -> named arrays ([n] and [n][16])."""
+    """Rows of BAMF_MAP_RECORD floats -> named arrays ([n] and [n][POS_SLOTS])."""
     S = POS_SLOTS
     d = {"N": np.nan_to_num(rec[:, 0]).astype(np.int64), "records": np.nan_to_num(rec[:, 1]).astype(np.int64),
          "Bg": rec[:, 2],

@@ -69,7 +69,7 @@ class BatchResults(C.Structure):
                 ("grid_stride", C.c_int64), ("grid_ld", C.c_int32), ("grid_slot", C.c_void_p),
                 ("pos_trace", C.c_void_p), ("pos_len", C.c_int32), ("pos_thin", C.c_int32)]
 
-POS_SLOTS = 16
+POS_SLOTS = 32
 POS_RECORD = 5 + 3 * POS_SLOTS
 
 

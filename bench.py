@@ -20,6 +20,9 @@ frontend  (rank 0, outside the timed region) FindROI + gaussMLE on the
           2000-frame 256x256 front-end workload: frames/s, FindROI against the
           measured HBM bandwidth (one 4-byte read per pixel), fits/s, and an
           end-to-end frames/s with the stack copied from pinned host memory
+dense_e2e (rank 0, outside the timed region) the dense end-to-end frame
+          analysis (bamf_gb300.pipeline) on 20 of its frames: frames/s,
+          stage times, localisation RMSE / recall / precision
 learned_proposal  (rank 0, outside the timed region) the learned-vs-uniform
           birth-proposal evaluation on 16x16 ROIs (bamf_gb300.learned_eval):
           network training rate, per-arm ROIs/s, ESS/s of the emitter count
@@ -64,7 +67,46 @@ def parse():
     ap.add_argument("--learned-eval-rois", type=int, default=50_000)
     ap.add_argument("--no-frontend", action="store_true", help="skip the FindROI + gaussMLE measurement")
     ap.add_argument("--frontend-frames", type=int, default=2000)
+    ap.add_argument("--no-dense", action="store_true", help="skip the dense end-to-end frame analysis")
+    ap.add_argument("--dense-frames", type=int, default=20)
     return ap.parse_args()
+
+
+def dense_bench(n_frames: int) -> dict:
+    """The dense end-to-end stress workload on n_frames of its 10,000
+    frames (256x256, 100 nm pixels, U[1,10] emitters/um^2, sigma 1.3,
+    LogN(ln 800, 0.5), background U[50,200]): priors from the front end,
+    16x16 sub-regions (BoxSize 10, Overlap 3), batched sampler with learned
+    births (network trained on the generator with this workload's
+    statistics), MAP + refinement, stitched posterior image; frames/s of a
+    warmed second run, localisation against the truth."""
+    from bamf_gb300 import learned, pipeline, priors, rjstruct, synth
+    frames, truth, _ = synth.frames_dense(n_frames, seed=5)
+    rj = rjstruct.c0_rjstruct()
+    rj.N_Burnin = rj.N_Trials = 3000
+    rj.N_BurninMCMC = rj.N_TrialsMCMC = 1000
+    rj.SRZoom = 20
+    sma = {"MeanPhotons": 800.0, "MinPValue": 0.01, "MinPhotons": 100.0}
+    t0 = time.perf_counter()
+    priors.findPriors(frames, rj, sma, "No")
+    t_priors = time.perf_counter() - t0
+    rho = 5.5 * 0.01  # mean emitters per pixel: U[1,10] per um^2, 0.01 um^2 pixels
+    rj.Rho = rho
+    net = learned.ProposalNet(seed=0)
+    t0 = time.perf_counter()
+    net.train(1000, batch=1024, lr=2e-3, data_seed=9, mean_n=rho * 256, i_median=800.0, i_logsd=0.5,
+              bg=50.0, bg_max=200.0)
+    t_train = time.perf_counter() - t0
+    pipeline.analyze_frames(frames[:, :, :2], rj, proposal="learned", net=net, seed=2)  # warm-up
+    out = pipeline.analyze_frames(frames, rj, proposal="learned", net=net, seed=2)
+    st = pipeline.localisation_stats(out["ClustInfo"], truth)
+    t = out["timing"]
+    return {"workload": f"dense end to end: {n_frames} frames 256x256, U[1,10] emitters/um^2, 16x16 sub-regions "
+                        f"(BoxSize 10, Overlap 3), learned births, 3000+3000 jumps + 1000+1000 refinement",
+            "frames_per_s": n_frames / t["total"], "subregions": out["n_subregions"],
+            "subregions_per_s": out["n_subregions"] / t["total"],
+            "stage_seconds": {k: round(v, 4) for k, v in t.items()},
+            "priors_seconds": t_priors, "network_train_seconds": t_train, **st}
 
 
 def measured_hbm_gbs():
@@ -368,6 +410,9 @@ def main():
     frontend_block = None
     if rank == 0 and not a.no_frontend:
         frontend_block = frontend_bench(a.frontend_frames)
+    dense_block = None
+    if rank == 0 and not a.no_dense:
+        dense_block = dense_bench(a.dense_frames)
 
     cpu = None
     if rank == 0:
@@ -397,6 +442,7 @@ def main():
             "clocks": clk.summary(),
             "learned_proposal": learned_block,
             "frontend": frontend_block,
+            "dense_e2e": dense_block,
             "map_n_mean": float(outs["map_n"].float().mean().item()),
             "true_n_mean": float(b.true_n.mean()),
         }

@@ -321,14 +321,14 @@ typedef struct bamf_batch_results {
     int32_t pos_thin;
 } bamf_batch_results;
 
-#define BAMF_POS_SLOTS 16
+#define BAMF_POS_SLOTS 32
 #define BAMF_POS_RECORD (5 + 3 * BAMF_POS_SLOTS)
 
 /* Chain summaries from pos_trace (device pointers; pos_trace as the batch
  * wrote it with pos_len <= 256 records of every pos_thin-th entry).  Output
  * per ROI: BAMF_MAP_RECORD floats = count, records used, Bg mean, Bg std,
- * ABg mean, BBg mean, then X[16], Y[16], I[16], X_SE[16], Y_SE[16],
- * I_SE[16] (NaN past the count).
+ * ABg mean, BBg mean, then X, Y, I, X_SE, Y_SE, I_SE of BAMF_POS_SLOTS each
+ * (NaN past the count).
  *   bamf_map_kmeans_device   findMap.m:29-111 (FB = 1): MAP count map_n
  *                            (from the full count trace, e.g. the batch's
  *                            map_n), then k-means of the positions of the

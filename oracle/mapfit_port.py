@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import numpy as np
 
-S = 16
+S = 32
 
 
 def _half(n_entries):
