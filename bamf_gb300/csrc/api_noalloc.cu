@@ -225,6 +225,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         ds[k]->uc = t + 3 * L[k];
         ds[k]->L = L[k];
         ds[k]->nu = nu[k];
+        ds[k]->inv_dx = 1.0f / p->DX;
     }
     K.seed = seed;
     K.bg0 = rois->bg0;

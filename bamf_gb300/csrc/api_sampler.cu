@@ -194,6 +194,7 @@ static bamf_status upload_tables(bamf_workspace *ws, const HostStat st[3], DevSt
         out[k].uc = base + off[k][3];
         out[k].L = (int)st[k].x.size();
         out[k].nu = (int)st[k].ux.size();
+        out[k].inv_dx = st[k].x.size() > 1 ? 1.0f / (st[k].x[1] - st[k].x[0]) : 0.0f; /* x[1] - x[0] = DX */
     }
     return BAMF_OK;
 }

@@ -21,6 +21,7 @@ struct DevStat {
     const float *uc;
     int L;
     int nu;
+    float inv_dx; /* 1 / grid step (fast-arithmetic lookups) */
 };
 
 /* Everything uniform over a batch of chains. */

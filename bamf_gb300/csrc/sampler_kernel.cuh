@@ -128,6 +128,49 @@ static __device__ __noinline__ float stat_pdf(const float *__restrict__ x, const
     return (__ldg(&pdf[j]) * (I - xj1) + __ldg(&pdf[j - 1]) * (xj - I)) / (x1 - __ldg(&x[0]));
 }
 
+/* Fast-arithmetic findPDF: the grid is uniform (x[i] = i DX up to float
+ * rounding), so the interval of I is found by one multiply and its two
+ * nodes are loaded together with the grid's end - one memory round trip
+ * instead of a dependent walk.  Same linear interpolation, 0 outside
+ * (0, x[L-1]). */
+static __device__ __noinline__ float stat_pdf_fast(const float *__restrict__ x, const float *__restrict__ pdf, int L,
+                                                   float inv_dx, float I)
+{
+    if (L < 2) return 0.0f;
+    float u = fminf(fmaxf(I * inv_dx, 0.0f), (float)(L - 1)); /* NaN -> 0 */
+    int j = min((int)u + 1, L - 1);
+    float xl = __ldg(&x[L - 1]);
+    float p1 = __ldg(&pdf[j]), p0 = __ldg(&pdf[j - 1]);
+    float w = u - (float)(j - 1);
+    float v = p1 * w + p0 * (1.0f - w);
+    return (I >= xl || I <= 0.0f || I != I) ? 0.0f : v;
+}
+
+/* Fast-arithmetic genRand: the same first unique-CDF node above R, found by
+ * a 32-way search (each lane tests one candidate, a ballot keeps the
+ * bracket: two or three rounds of loads instead of a dependent binary
+ * search), then the same interpolation.  Call with the whole warp. */
+static __device__ __noinline__ float stat_rand_warp(const float *__restrict__ ux, const float *__restrict__ uc,
+                                                    int nu, float R, int lane)
+{
+    if (R <= 0.0f) return 0.0f;
+    if (R >= 1.0f) return __ldg(&ux[nu - 1]);
+    if (nu < 2) return 0.0f;
+    int lo = 0, hi = nu - 1; /* uc[lo] <= R < uc[hi] */
+    while (hi - lo > 1) {
+        int step = (hi - lo + 31) >> 5;
+        int k = lo + (lane + 1) * step;
+        bool above = k >= hi || __ldg(&uc[k]) > R;
+        uint32_t m = __ballot_sync(0xffffffffu, above);
+        int f = __ffs(m) - 1;
+        int nlo = f == 0 ? lo : lo + f * step;
+        hi = min(lo + (f + 1) * step, hi);
+        lo = nlo;
+    }
+    float uc1 = __ldg(&uc[hi]), uc0 = __ldg(&uc[hi - 1]);
+    return (__ldg(&ux[hi - 1]) * (uc1 - R) + __ldg(&ux[hi]) * (R - uc0)) / (uc1 - uc0);
+}
+
 /* Stat::genRand (:248-282) given its uniform R: first unique-CDF node above R
  * by binary search (the CDF is strictly increasing), then interpolation. */
 static __device__ __noinline__ float stat_rand(const float *__restrict__ ux, const float *__restrict__ uc, int nu,
@@ -379,17 +422,19 @@ struct ChainWarp {
     /* ---------------------------------------------------- prior tables */
     __device__ __forceinline__ float findPDF(const DevStat &s, float I) const
     {
-        return stat_pdf(s.x, s.pdf, s.L, I);
+        if (EXACT) return stat_pdf(s.x, s.pdf, s.L, I);
+        return stat_pdf_fast(s.x, s.pdf, s.L, s.inv_dx, I);
     }
     __device__ __forceinline__ float genRand(const DevStat &s)
     {
         float R = urand();
-        return stat_rand(s.ux, s.uc, s.nu, R);
+        if (EXACT) return stat_rand(s.ux, s.uc, s.nu, R);
+        return stat_rand_warp(s.ux, s.uc, s.nu, R, lane);
     }
     __device__ __forceinline__ float sob(int signal, float I) const
     {
         const DevStat &s = signal == 1 ? K->sig : K->back;
-        return stat_pdf(s.x, s.pdf, s.L, I);
+        return findPDF(s, I);
     }
     __device__ __forceinline__ float normpdf(float x, float u, float s) const
     {
