@@ -648,20 +648,38 @@ struct ChainWarp {
             int x = lane / Y, y = lane - (lane / Y) * Y;
             if (na <= FAST_ROWS && nt <= FAST_ROWS) {
                 stencil_rows(na, nt);
-                float dBG = tBG - aBG, dABG = tABG - aABG, dBBG = tBBG - aBBG;
-#pragma unroll 2
-                for (int p = lane; p < npix; p += 32) {
-                    float d = dBG + dABG * (float)x + dBBG * (float)y;
-                    for (int q = 0; q < na; ++q) d -= SXo[q * X + x] * SYo[q * Y + y];
-                    for (int q = 0; q < nt; ++q) d += SXn[q * X + x] * SYn[q * Y + y];
-                    float mt = M[p] + d;
-                    Mt[p] = mt;
-                    acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - d;
-                    x += px_dx;
-                    y += px_dy;
-                    if (y >= Y) {
-                        y -= Y;
-                        x++;
+                /* lane -> row y = lane mod Y of column x0 + lane / Y; a pass
+                 * covers 32 / Y columns.  The model change of a pixel is
+                 * bg delta + sum_q w_q(y) SX_q[x] over the changed rows q
+                 * (old rows with weight -SYo, new with +SYn); each lane
+                 * holds its first four weights in registers. */
+                const int yl = lane % Y, xo = lane / Y, R = 32 / Y;
+                const int nr = na + nt;
+                float w[4];
+                const float *sx[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    bool old = q < na;
+                    int qq = old ? q : q - na;
+                    w[q] = q < nr ? (old ? -SYo[qq * Y + yl] : SYn[qq * Y + yl]) : 0.0f;
+                    sx[q] = old ? SXo + qq * X : SXn + qq * X;
+                }
+                const float base = (tBG - aBG) + (tBBG - aBBG) * (float)yl, dABG = tABG - aABG;
+                if (xo < R) {
+#pragma unroll 1
+                    for (int xx = xo; xx < X; xx += R) {
+                        float d = base + dABG * (float)xx;
+                        if (nr > 0) d += w[0] * sx[0][xx];
+                        if (nr > 1) d += w[1] * sx[1][xx];
+                        if (nr > 2) d += w[2] * sx[2][xx];
+                        if (nr > 3) d += w[3] * sx[3][xx];
+                        for (int q = 4; q < nr; ++q)
+                            d += q < na ? -SXo[q * X + xx] * SYo[q * Y + yl]
+                                        : SXn[(q - na) * X + xx] * SYn[(q - na) * Y + yl];
+                        int p = yl + Y * xx;
+                        float mt = M[p] + d;
+                        Mt[p] = mt;
+                        acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - d;
                     }
                 }
             } else {
