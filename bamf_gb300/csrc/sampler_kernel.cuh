@@ -548,30 +548,38 @@ struct ChainWarp {
     /* Fast mode: stencil rows of the emitters a proposal changes, compact:
      * row q of SXo/SYo is the old stencil of the q-th slot of a_dirty (from
      * A), row q of SXn/SYn the new stencil of the q-th slot of t_dirty (from
-     * T).  One pass over both sets keeps one copy of the code. */
+     * T). */
     __device__ __forceinline__ void stencil_rows(int na, int nt)
     {
-        const int XY = X + Y;
-        const int tot = (na + nt) * XY;
+        const int XY = X + Y, nr = na + nt;
+        /* G rows per 32-lane pass when a row (X + Y entries) fits in 32
+         * lanes, else one row at a time over ceil(XY / 32) passes; each
+         * lane fetches its row's emitter with three shuffles */
+        const int G = XY <= 32 ? 32 / XY : 1;
+        const int rg = XY <= 32 ? lane / XY : 0;
+        const int c0 = XY <= 32 ? lane - rg * XY : lane;
 #pragma unroll 1
-        for (int b0 = 0; b0 < tot; b0 += 32) {
-            int item = min(b0 + lane, tot - 1);
-            int row = item / XY;
-            int col = item - row * XY;
-            bool isnew = row >= na;
-            int q = isnew ? row - na : row;
+        for (int r0 = 0; r0 < nr; r0 += G) {
+            int r = min(r0 + rg, nr - 1);
+            bool isnew = r >= na;
+            int q = isnew ? r - na : r;
             int k = nth_bit(isnew ? t_dirty : a_dirty, q);
-            float Ia = __shfl_sync(BAMF_FULL, aI, k), Xa = __shfl_sync(BAMF_FULL, aX, k);
-            float Ya = __shfl_sync(BAMF_FULL, aY, k);
-            float It = __shfl_sync(BAMF_FULL, tI, k), Xt = __shfl_sync(BAMF_FULL, tX, k);
-            float Yt = __shfl_sync(BAMF_FULL, tY, k);
-            bool isx = col < X;
-            int c = isx ? col : col - X;
-            float mu = isx ? (isnew ? Xt : Xa) : (isnew ? Yt : Ya);
-            float v = 0.5f * (MT::erf_(((float)c - mu + 1.0f) * Cst) - MT::erf_(((float)c - mu) * Cst));
-            if (b0 + lane < tot) {
-                if (isx) (isnew ? SXn : SXo)[q * X + c] = (isnew ? It : Ia) * v;
-                else (isnew ? SYn : SYo)[q * Y + c] = v;
+            float Ik = __shfl_sync(BAMF_FULL, isnew ? tI : aI, k);
+            float Xk = __shfl_sync(BAMF_FULL, isnew ? tX : aX, k);
+            float Yk = __shfl_sync(BAMF_FULL, isnew ? tY : aY, k);
+            bool on = rg < G && r0 + rg < nr;
+            float *sxr = (isnew ? SXn : SXo) + q * X, *syr = (isnew ? SYn : SYo) + q * Y;
+#pragma unroll 1
+            for (int c = c0; c < XY; c += 32) {
+                bool isx = c < X;
+                int cc = isx ? c : c - X;
+                float mu = isx ? Xk : Yk;
+                float v = 0.5f * (MT::erf_(((float)cc - mu + 1.0f) * Cst) - MT::erf_(((float)cc - mu) * Cst));
+                if (on) {
+                    if (isx) sxr[cc] = Ik * v;
+                    else syr[cc] = v;
+                }
+                if (XY <= 32) break;
             }
         }
         __syncwarp();
