@@ -239,8 +239,11 @@ static int sm_count()
  * warps resident per SM (shared memory per warp grows with the ROI side). */
 static int pick_wpb(bool exact, int side_max, int *per_sm_out)
 {
-    int best_w = 0, best_wpb = 4, best_per = 0;
-    const int cand[3] = {4, 2, 1};
+    /* fast arithmetic: CTAs of up to one move-stream group (8 chains);
+     * exact: the per-warp kernel's 4 */
+    int best_w = 0, best_wpb = exact ? 4 : 8, best_per = 0;
+    const int cand_f[3] = {8, 4, 2}, cand_e[3] = {4, 2, 1};
+    const int *cand = exact ? cand_e : cand_f;
     for (int i = 0; i < 3; ++i) {
         int per = exact ? blocks_per_sm_exact(side_max, cand[i]) : blocks_per_sm_fast(side_max, cand[i]);
         if (per * cand[i] > best_w) {

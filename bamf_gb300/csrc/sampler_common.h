@@ -88,7 +88,7 @@ struct SamplerBatch {
 /* Size classes by ROI side: (0,8] (8,12] (12,16] (16,20] (20,24] (24,28] (28,32]. */
 /* ROIs (consecutive slots of a size class) that share one move-type stream in
  * the move-synchronous fast kernel; a CTA holds at most this many chains. */
-#define BAMF_SYNC_GROUP 4
+#define BAMF_SYNC_GROUP 8
 #define BAMF_N_CLASSES 7
 __host__ __device__ inline int side_class(int side)
 {

@@ -553,8 +553,7 @@ struct ChainWarp {
     {
         const int XY = X + Y, nr = na + nt;
         /* G rows per 32-lane pass when a row (X + Y entries) fits in 32
-         * lanes, else one row at a time over ceil(XY / 32) passes; each
-         * lane fetches its row's emitter with three shuffles */
+         * lanes, else one row at a time over ceil(XY / 32) passes */
         const int G = XY <= 32 ? 32 / XY : 1;
         const int rg = XY <= 32 ? lane / XY : 0;
         const int c0 = XY <= 32 ? lane - rg * XY : lane;
@@ -564,9 +563,13 @@ struct ChainWarp {
             bool isnew = r >= na;
             int q = isnew ? r - na : r;
             int k = nth_bit(isnew ? t_dirty : a_dirty, q);
-            float Ik = __shfl_sync(BAMF_FULL, isnew ? tI : aI, k);
-            float Xk = __shfl_sync(BAMF_FULL, isnew ? tX : aX, k);
-            float Yk = __shfl_sync(BAMF_FULL, isnew ? tY : aY, k);
+            /* a shuffle returns the source lane's value, so fetch both
+             * states and select here (lanes of one pass may read rows of
+             * different states) */
+            float Ia = __shfl_sync(BAMF_FULL, aI, k), It = __shfl_sync(BAMF_FULL, tI, k);
+            float Xa = __shfl_sync(BAMF_FULL, aX, k), Xt = __shfl_sync(BAMF_FULL, tX, k);
+            float Ya = __shfl_sync(BAMF_FULL, aY, k), Yt = __shfl_sync(BAMF_FULL, tY, k);
+            float Ik = isnew ? It : Ia, Xk = isnew ? Xt : Xa, Yk = isnew ? Yt : Ya;
             bool on = rg < G && r0 + rg < nr;
             float *sxr = (isnew ? SXn : SXo) + q * X, *syr = (isnew ? SYn : SYo) + q * Y;
 #pragma unroll 1
@@ -1738,7 +1741,7 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ 
  * barrier per jump, with the move type and jump sub-branch shared across the
  * CTA (run_chain_sync). */
 template <int UNUSED>
-__global__ void __launch_bounds__(128, 4) rjmcmc_kernel_sync(const __grid_constant__ SamplerConsts Kc,
+__global__ void __launch_bounds__(32 * BAMF_SYNC_GROUP, 2) rjmcmc_kernel_sync(const __grid_constant__ SamplerConsts Kc,
                                                           const __grid_constant__ SamplerBatch Bc)
 {
     extern __shared__ float smem_raw[];
@@ -1771,7 +1774,7 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel_sync(const __grid_consta
         }
         /* the shared move stream is keyed by the slot group of BAMF_SYNC_GROUP
          * ROIs, not by the CTA, so a chain's moves (and its result) do not
-         * depend on the launch's warps per block (1, 2 or 4) */
+         * depend on the launch's warps per block (any divisor of the group) */
         w.run_chain_sync(active, (uint32_t)(q_begin + ((base - q_begin) & ~(BAMF_SYNC_GROUP - 1))));
         if (active) end_roi(w, Bt);
     }
