@@ -656,7 +656,6 @@ struct ChainWarp {
             const float LN2 = 0.69314718f;
             int na = __popc(a_dirty), nt = __popc(t_dirty);
             float acc = 0.0f;
-            int x = lane / Y, y = lane - (lane / Y) * Y;
             if (na <= FAST_ROWS && nt <= FAST_ROWS) {
                 stencil_rows(na, nt);
                 /* lane -> row y = lane mod Y of column x0 + lane / Y; a pass

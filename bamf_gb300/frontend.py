@@ -1,7 +1,7 @@
 """Python mirror of the reference front end, over libbamf_gb300.so.
 
   findROI(Image, Sigma1, Sigma2, Boxsize, Minval)  @RJ/findROI.m:1-224
-  gaussMLE(Data, FitType, CameraType, Sigma)        @RJ/gaussMLE.m:64-211 ('Basic', 'CCD')
+  gaussMLE(Data, FitType, CameraType, Sigma, ...)   @RJ/gaussMLE.m:64-211 (all fit and camera types)
 
 Images are (Ysize, Xsize[, Zsize]) arrays in MATLAB orientation.  Every call
 runs the CUDA kernels; there is no CPU fallback.
@@ -37,6 +37,11 @@ def _declare():
                                         C.c_void_p, C.c_void_p, C.c_void_p]
     L.bamf_gauss_mle_host.restype = C.c_int
     L.bamf_gauss_mle_host.argtypes = [pf, C.c_int, C.c_int, C.c_float, C.c_int, pf, pf, pf]
+    L.bamf_gauss_mle_nparams.restype = C.c_int
+    L.bamf_gauss_mle_nparams.argtypes = [C.c_int]
+    L.bamf_gauss_mle_fit_host.restype = C.c_int
+    L.bamf_gauss_mle_fit_host.argtypes = [pf, C.c_int, C.c_int, C.c_int, C.c_float, C.c_void_p, pf, pf, C.c_int,
+                                          C.c_int, pf, pf, pf]
     L._frontend_declared = True
     return L
 
@@ -84,11 +89,23 @@ def findROI(Image, Sigma1: float = 1.3, Sigma2: float = 2 * 1.3, Boxsize: int = 
     return SMD, roistack, coords
 
 
-def gaussMLE(Data, FitType: str = "Basic", CameraType: str = "CCD", Sigma: float = 1.3,
-             Iterations: int = 20):
-    """Results of gaussMLE.m:183-205 for FitType 'Basic', CameraType 'CCD'.
-    Data: (sz, sz, N).  Iterations defaults to gaussMLE.m:98's 20."""
-    if FitType != "Basic" or CameraType != "CCD":
+FIT_TYPES = {"Basic": 0, "Sigma": 1, "Z": 2, "SigmaYX": 3}
+FIT_EXTRA = {"Basic": [], "Sigma": ["Sigma"], "Z": ["Z"], "SigmaYX": ["SigmaY", "SigmaX"]}
+
+
+class ZFit(C.Structure):
+    _fields_ = [(k, C.c_float) for k in ("sigma_x", "sigma_y", "Ax", "Ay", "Bx", "By", "gamma", "d")]
+
+
+def gaussMLE(Data, FitType: str = "Basic", CameraType: str = "CCD", Sigma=1.3, *args, Iterations: int = 20):
+    """Results of gaussMLE.m:64-205: gaussMLE(Data, FitType, CameraType,
+    Sigma[, ZStruct]) for 'CCD' and gaussMLE(Data, FitType, 'SCMOS', Sigma,
+    VarianceImage, BoxCorners[, ZStruct]).  Data: (sz, sz, N); Sigma a
+    scalar, or [sigma_x0, sigma_y0] for 'Z'; ZStruct a dict with Ax, Ay, Bx,
+    By, Gamma, D; BoxCorners (N, 2) per fit (the pair the kernel reads at
+    2 k, 2 k + 1); VarianceImage square.  Iterations defaults to
+    gaussMLE.m:98's 20."""
+    if FitType not in FIT_TYPES or CameraType not in ("CCD", "SCMOS"):
         raise abi.BamfError(abi.BAMF_ERR_UNSUPPORTED, f"gaussMLE({FitType}, {CameraType})")
     L = _declare()
     d = np.asarray(Data, np.float32)
@@ -96,16 +113,43 @@ def gaussMLE(Data, FitType: str = "Basic", CameraType: str = "CCD", Sigma: float
         d = d[:, :, None]
     sz, _, n = d.shape
     flat = np.ascontiguousarray(d.ravel(order="F"))
-    P = np.zeros(4 * n, np.float32)
-    CR = np.zeros(4 * n, np.float32)
+    sig = np.atleast_1d(np.asarray(Sigma, np.float64))
+    zf = None
+    var = corners = None
+    rest = list(args)
+    if CameraType == "SCMOS":
+        if len(rest) < 2:
+            raise abi.BamfError(abi.BAMF_ERR_INVALID_ARG, "SCMOS needs VarianceImage and BoxCorners")
+        var = np.ascontiguousarray(np.asarray(rest[0], np.float32))
+        if var.ndim != 2 or var.shape[0] != var.shape[1]:
+            raise abi.BamfError(abi.BAMF_ERR_INVALID_ARG, "gaussMLE: SCMOS fitting needs a square variance image")
+        var = np.ascontiguousarray(var.ravel(order="F"))
+        corners = np.ascontiguousarray(np.asarray(rest[1], np.float32).reshape(n, 2))
+        rest = rest[2:]
+    if FitType == "Z":
+        z = rest[0]
+        zf = ZFit(float(sig[0]), float(sig[1] if len(sig) > 1 else sig[0]), z["Ax"], z["Ay"], z["Bx"], z["By"],
+                  z["Gamma"], z["D"])
+    npar = L.bamf_gauss_mle_nparams(FIT_TYPES[FitType])
+    P = np.zeros(npar * n, np.float32)
+    CR = np.zeros(npar * n, np.float32)
     LL = np.zeros(n, np.float32)
-    abi.check(L.bamf_gauss_mle_host(abi.fptr(flat), sz, n, float(np.mean(Sigma)), int(Iterations),
-                                    abi.fptr(P), abi.fptr(CR), abi.fptr(LL)), "bamf_gauss_mle_host")
-    P = P.reshape(4, n).T
-    CR = CR.reshape(4, n).T
-    return {"Y": P[:, 0], "X": P[:, 1], "Photons": P[:, 2], "BG": P[:, 3],
-            "Y_SE": np.sqrt(CR[:, 0]), "X_SE": np.sqrt(CR[:, 1]),
-            "Photons_SE": np.sqrt(CR[:, 2]), "BG_SE": np.sqrt(CR[:, 3]), "LogLikelihood": LL}
+    msz = int(np.sqrt(var.size)) if var is not None else 0
+    abi.check(L.bamf_gauss_mle_fit_host(abi.fptr(flat), sz, n, FIT_TYPES[FitType], float(np.mean(sig)),
+                                        C.byref(zf) if zf is not None else None,
+                                        abi.fptr(corners) if corners is not None else None,
+                                        abi.fptr(var) if var is not None else None, msz, int(Iterations),
+                                        abi.fptr(P), abi.fptr(CR), abi.fptr(LL)), "bamf_gauss_mle_fit_host")
+    P = P.reshape(npar, n).T
+    CR = CR.reshape(npar, n).T
+    out = {"Y": P[:, 0], "X": P[:, 1], "Photons": P[:, 2], "BG": P[:, 3],
+           "Y_SE": np.sqrt(CR[:, 0]), "X_SE": np.sqrt(CR[:, 1]),
+           "Photons_SE": np.sqrt(CR[:, 2]), "BG_SE": np.sqrt(CR[:, 3])}
+    for k, name in enumerate(FIT_EXTRA[FitType]):
+        out[name] = P[:, 4 + k]
+        out[name + "_SE"] = np.sqrt(CR[:, 4 + k])
+    out["LogLikelihood"] = LL
+    return out
 
 
 class FindRoiDevice:

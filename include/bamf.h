@@ -455,6 +455,35 @@ bamf_status bamf_gauss_mle_device(const float *rois, int sz, int nfits, float ps
 bamf_status bamf_gauss_mle_host(const float *rois, int sz, int nfits, float psf_sigma,
                                 int iterations, float *params, float *crlb, float *loglik);
 
+/* The other fit types of gaussMLE.m (FitType; cuda_gaussMLEv2.cu:144-1125):
+ *   BAMF_FIT_BASIC    x, y, N, bg                    (NP 4, '_XYNB_')
+ *   BAMF_FIT_SIGMA    + sigma                        (NP 5, '_XYNBS_')
+ *   BAMF_FIT_Z        + z, astigmatic PSF (zfit)     (NP 5, '_XYNBZ_')
+ *   BAMF_FIT_SIGMAYX  + sigma along each axis        (NP 6, '_XYNBSXSY_')
+ * CameraType 'SCMOS' when var_gain_map is given: a map_size x map_size
+ * variance / gain^2 image indexed at each ROI's box corner (box_corners
+ * [n][2] floats: (axis-1 start, axis-0 start) as BoxCorners), '_SCMOS*_'.
+ * Outputs param-major: params [NP][n], crlb [NP][n], loglik [n]; parameter
+ * order (Y, X, Photons, BG, then Sigma | Z | SigmaY, SigmaX) as gaussMLE.m
+ * unpacks them.  zfit: Sigma(1), Sigma(2) and ZStruct.Ax, Ay, Bx, By,
+ * Gamma, D of gaussMLE.m:155-158. */
+#define BAMF_FIT_BASIC 0
+#define BAMF_FIT_SIGMA 1
+#define BAMF_FIT_Z 2
+#define BAMF_FIT_SIGMAYX 3
+typedef struct bamf_zfit {
+    float sigma_x, sigma_y;
+    float Ax, Ay, Bx, By, gamma, d;
+} bamf_zfit;
+int bamf_gauss_mle_nparams(int fit_type);
+bamf_status bamf_gauss_mle_fit_device(const float *rois, int sz, int nfits, int fit_type, float psf_sigma,
+                                      const bamf_zfit *zfit, const float *box_corners, const float *var_gain_map,
+                                      int map_size, int iterations, float *params, float *crlb, float *loglik,
+                                      void *stream);
+bamf_status bamf_gauss_mle_fit_host(const float *rois, int sz, int nfits, int fit_type, float psf_sigma,
+                                    const bamf_zfit *zfit, const float *box_corners, const float *var_gain_map,
+                                    int map_size, int iterations, float *params, float *crlb, float *loglik);
+
 /* ------------------------------------------------------------------ */
 /* Measurement helpers                                                  */
 /* ------------------------------------------------------------------ */

@@ -38,7 +38,18 @@ NAMES = {
     "maxX": "_Z11kernel_maxXPfS_if",
     "maxY": "_Z11kernel_maxYPfS_if",
     "mle_xynb": "_Z19kernel_MLEFit_XYNB_PKffiiPfS1_S1_i",
+    # the other fit types (cuda_gaussMLEv2.cu:144-1125), names from their
+    # source signatures
+    "mle_xynbs": "_Z20kernel_MLEFit_XYNBS_PKffiiPfS1_S1_i",
+    "mle_xynbsxsy": "_Z23kernel_MLEFit_XYNBSXSY_PKffiiPfS1_S1_i",
+    "mle_xynbz": "_Z20kernel_MLEFit_XYNBZ_PKfffffffffiiPfS1_S1_i",
+    "mle_scmos_xynb": "_Z24kernel_MLEFit_SCMOSXYNB_PKfS0_S0_fiiiPfS1_S1_i",
+    "mle_scmos_xynbs": "_Z25kernel_MLEFit_SCMOSXYNBS_PKfS0_S0_fiiiPfS1_S1_i",
+    "mle_scmos_xynbsxsy": "_Z28kernel_MLEFit_SCMOSXYNBSXSY_PKfS0_S0_fiiiPfS1_S1_i",
+    "mle_scmos_xynbz": "_Z25kernel_MLEFit_SCMOSXYNBZ_PKfS0_S0_S0_ffffffffiiiPfS1_S1_i",
 }
+NPARAM = {"Basic": 4, "Sigma": 5, "Z": 5, "SigmaYX": 6}
+KNAME = {"Basic": "xynb", "Sigma": "xynbs", "Z": "xynbz", "SigmaYX": "xynbsxsy"}
 
 
 def available(which: str) -> bool:
@@ -158,5 +169,38 @@ def gaussmle_xynb(rois_dev, sz: int, nfits: int, sigma: float, iterations: int):
     d.launch("gaussmle", "mle_xynb", ((nfits + 127) // 128,), (128,),
              [ptr(rois_dev), C.c_float(sigma), C.c_int(sz), C.c_int(iterations), ptr(P), ptr(CR), ptr(LL),
               C.c_int(nfits)])
+    torch.cuda.synchronize()
+    return P, CR, LL
+
+
+def gaussmle_fit(rois_dev, sz: int, nfits: int, fit_type: str, sigma, iterations: int, zstruct=None,
+                 var_map_dev=None, corners_dev=None, map_size: int = 0):
+    """(P, CRLB, LL) CUDA tensors from the reference kernel of `fit_type`
+    ('Basic', 'Sigma', 'Z', 'SigmaYX'; sCMOS when var_map_dev is given),
+    with the arguments gaussMLE.m:150-168 passes."""
+    import torch
+    d = driver()
+    np_ = NPARAM[fit_type]
+    P = torch.zeros(np_ * nfits, dtype=torch.float32, device="cuda")
+    CR = torch.zeros(np_ * nfits, dtype=torch.float32, device="cuda")
+    LL = torch.zeros(nfits, dtype=torch.float32, device="cuda")
+    ptr = lambda t: C.c_uint64(t.data_ptr())  # noqa: E731
+    scmos = var_map_dev is not None
+    name = ("mle_scmos_" if scmos else "mle_") + KNAME[fit_type]
+    tail = [C.c_int(sz)] + ([C.c_int(map_size)] if scmos else []) + [C.c_int(iterations), ptr(P), ptr(CR), ptr(LL),
+                                                                    C.c_int(nfits)]
+    if fit_type == "Z":
+        z = zstruct
+        zargs = [C.c_float(sigma[0]), C.c_float(z["Ax"]), C.c_float(z["Ay"]), C.c_float(z["Bx"]),
+                 C.c_float(z["By"]), C.c_float(z["Gamma"]), C.c_float(z["D"]), C.c_float(sigma[1])]
+        if scmos:
+            z0 = torch.zeros(nfits, dtype=torch.float32, device="cuda")
+            args = [ptr(rois_dev), ptr(corners_dev), ptr(var_map_dev), ptr(z0)] + zargs + tail
+        else:
+            args = [ptr(rois_dev)] + zargs + tail
+    else:
+        s_ = C.c_float(float(np.mean(sigma)))
+        args = ([ptr(rois_dev), ptr(corners_dev), ptr(var_map_dev), s_] if scmos else [ptr(rois_dev), s_]) + tail
+    d.launch("gaussmle", name, ((nfits + 127) // 128,), (128,), args)
     torch.cuda.synchronize()
     return P, CR, LL
