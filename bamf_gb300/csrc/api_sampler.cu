@@ -148,6 +148,10 @@ struct bamf_workspace {
         }
         return cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming) == cudaSuccess;
     }
+    /* CTA shape (chains per CTA) per arithmetic and size class chosen by
+     * bamf_autotune; 0 = not tuned (occupancy rule) */
+    int tuned_wpb[2][BAMF_N_CLASSES] = {};
+    DevBuf tune_range; /* class ranges clipped to the tuning sample    */
     DevBuf tables;   /* the three prior tables                       */
     DevBuf queue;    /* work-queue counter                             */
     DevBuf trace;    /* per-ROI Signal==1 count per chain entry        */
@@ -286,6 +290,14 @@ static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, Samp
         int per_sm = 0;
         int wpb = pick_wpb(exact, Bc.side_max, &per_sm);
         if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
+        const int tw = ws->tuned_wpb[exact ? 0 : 1][c];
+        if (tw > 0) {
+            int pt = exact ? blocks_per_sm_exact(Bc.side_max, tw) : blocks_per_sm_fast(Bc.side_max, tw);
+            if (pt > 0) {
+                wpb = tw;
+                per_sm = pt;
+            }
+        }
         int need = (B.n_rois + wpb - 1) / wpb;
         int blocks = std::min(need, per_sm * sms);
         if (blocks < 1) return BAMF_OK;
@@ -493,6 +505,117 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
         map_n_kernel<<<(n + 7) / 8, 256, 0, s>>>(B.nsig_trace, B.trace_cap, entries, n, out->map_n);
         CU(cudaGetLastError());
     }
+    return BAMF_OK;
+}
+
+/* ---------------------------------------------------------------- autotuner */
+/* Times every CTA shape (chains per CTA) on a sample of each size class of
+ * the batch, with chains of `jumps` burn-in jumps, and keeps the fastest
+ * per class in the workspace for later batches of that arithmetic.  In
+ * fast arithmetic the chains' results do not depend on the shape (move
+ * streams are keyed by slot groups), in exact arithmetic every chain is one
+ * warp's, so tuning changes speed only. */
+extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *rois, const bamf_mcmc_params *p,
+                                     const bamf_priors *priors, int arith, int jumps, int sample, void *stream)
+{
+    if (!ws || !rois || !p || !priors || jumps < 1 || sample < 1) return BAMF_ERR_INVALID_ARG;
+    if (arith != BAMF_ARITH_EXACT && arith != BAMF_ARITH_FAST) return BAMF_ERR_INVALID_ARG;
+    if (rois->n_rois < 1 || !rois->data || !rois->offsets || !rois->xsize || !rois->ysize) return BAMF_ERR_INVALID_ARG;
+    int side_max = rois->side_max > 0 ? rois->side_max : BAMF_MAX_ROI_SIDE;
+    if (side_max > BAMF_MAX_ROI_SIDE) return BAMF_ERR_TOO_LARGE;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    cudaStream_t s = (cudaStream_t)stream;
+    bamf_mcmc_params pt = *p;
+    pt.N_Burnin = jumps;
+    pt.N_Trials = 0;
+    SamplerConsts K;
+    bamf_status r = make_consts(ws, &pt, priors, 1u, rois->bg0, K, s);
+    if (r) return r;
+    K.sync_moves = arith == BAMF_ARITH_FAST ? 1 : 0;
+    const bool exact = arith == BAMF_ARITH_EXACT;
+    const int n = rois->n_rois;
+    SamplerBatch B;
+    std::memset(&B, 0, sizeof B);
+    B.n_rois = n;
+    B.data = rois->data;
+    B.offsets = rois->offsets;
+    B.xsize = rois->xsize;
+    B.ysize = rois->ysize;
+    B.psf_sigma = rois->psf_sigma;
+    B.scmos = rois->scmos;
+    if ((r = ws->order.ensure((size_t)n * sizeof(int32_t) + 256))) return r;
+    if ((r = ws->tune_range.ensure(sizeof(int32_t) * 2 * BAMF_N_CLASSES))) return r;
+    if ((r = ws->queue.ensure(sizeof(int32_t) * BAMF_N_CLASSES))) return r;
+    B.order = (int32_t *)((char *)ws->order.p + 256);
+    int32_t *class_range = (int32_t *)ws->order.p;
+    order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)B.order, class_range);
+    CU(cudaGetLastError());
+    int32_t cr[2 * BAMF_N_CLASSES];
+    CU(cudaMemcpyAsync(cr, class_range, sizeof cr, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    const int sms = sm_count();
+    const int cand_f[4] = {8, 4, 2, 1}, cand_e[3] = {4, 2, 1};
+    const int *cand = exact ? cand_e : cand_f;
+    const int ncand = exact ? 3 : 4;
+    bamf_status res = BAMF_OK;
+    for (int c = 0; c < BAMF_N_CLASSES && !res; ++c) {
+        int lo = cr[2 * c], hi = cr[2 * c + 1];
+        if (hi <= lo) continue;
+        int32_t clip[2 * BAMF_N_CLASSES] = {};
+        clip[2 * c] = lo;
+        clip[2 * c + 1] = std::min(hi, lo + sample);
+        int m = clip[2 * c + 1] - lo;
+        if (cudaMemcpyAsync(ws->tune_range.p, clip, sizeof clip, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            res = BAMF_ERR_CUDA;
+            break;
+        }
+        SamplerBatch Bc = B;
+        Bc.class_range = (const int32_t *)ws->tune_range.p;
+        Bc.cls = c;
+        Bc.queue = (int32_t *)ws->queue.p + c;
+        Bc.side_max = std::min(class_side(c), side_max);
+        float best_ms = 0.0f;
+        int best = 0;
+        for (int k = 0; k < ncand && !res; ++k) {
+            int wpb = cand[k];
+            int per = exact ? blocks_per_sm_exact(Bc.side_max, wpb) : blocks_per_sm_fast(Bc.side_max, wpb);
+            if (per < 1) continue;
+            int blocks = std::min((m + wpb - 1) / wpb, per * sms);
+            for (int rep = 0; rep < 2 && !res; ++rep) { /* the first launch warms up */
+                if (cudaMemsetAsync(Bc.queue, 0, sizeof(int32_t), s) != cudaSuccess ||
+                    cudaEventRecord(e0, s) != cudaSuccess) {
+                    res = BAMF_ERR_CUDA;
+                    break;
+                }
+                cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, s)
+                                      : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, s);
+                float ms = 0.0f;
+                if (e != cudaSuccess || cudaEventRecord(e1, s) != cudaSuccess ||
+                    cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+                    res = cuda_fail(e != cudaSuccess ? e : cudaGetLastError(), "autotune launch");
+                    break;
+                }
+                if (rep == 1 && (best == 0 || ms < best_ms)) {
+                    best_ms = ms;
+                    best = wpb;
+                }
+            }
+        }
+        ws->tuned_wpb[exact ? 0 : 1][c] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return res;
+}
+
+extern "C" bamf_status bamf_autotune_result(const bamf_workspace *ws, int arith, int32_t *chains_per_cta)
+{
+    if (!ws || !chains_per_cta || (arith != BAMF_ARITH_EXACT && arith != BAMF_ARITH_FAST))
+        return BAMF_ERR_INVALID_ARG;
+    for (int c = 0; c < BAMF_N_CLASSES; ++c) chains_per_cta[c] = ws->tuned_wpb[arith == BAMF_ARITH_EXACT ? 0 : 1][c];
     return BAMF_OK;
 }
 

@@ -42,6 +42,11 @@ def _declare() -> C.CDLL:
     L.bamf_rjmcmc_batch_host.argtypes = [C.c_void_p, C.POINTER(RoiBatch), C.POINTER(abi.McmcParams),
                                          C.POINTER(Priors), C.c_uint32, C.c_int,
                                          C.POINTER(BatchResults)]
+    L.bamf_autotune.restype = C.c_int
+    L.bamf_autotune.argtypes = [C.c_void_p, C.POINTER(RoiBatch), C.POINTER(abi.McmcParams), C.POINTER(Priors),
+                                C.c_int, C.c_int, C.c_int, C.c_void_p]
+    L.bamf_autotune_result.restype = C.c_int
+    L.bamf_autotune_result.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int32)]
     L.bamf_last_error.restype = C.c_char_p
     L._sampler_declared = True
     return L
@@ -265,6 +270,25 @@ class Sampler:
                                                int(seed), ARITH[arith], C.byref(res),
                                                C.c_void_p(stream) if stream else None)
         _check(self._L, st, "bamf_rjmcmc_batch_device")
+
+    def autotune(self, dev: dict, params: abi.McmcParams, off, sig, back, arith: str = "fast", jumps: int = 200,
+                 sample: int = 4864, stream=None, bg0: float = 0.0) -> list:
+        """bamf_autotune on a device batch (run_device layout); returns the
+        chosen chains per CTA of the 7 size classes (0: class absent)."""
+        pr, keep = self._priors(off, sig, back)
+        b = RoiBatch()
+        b.n_rois = int(dev["xsize"].numel())
+        b.side_max = int(dev.get("side_max", 0))
+        for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos"):
+            t = dev.get(k)
+            setattr(b, k, t.data_ptr() if t is not None else None)
+        b.bg0 = float(bg0)
+        L = self._L
+        _check(L, L.bamf_autotune(self._ws, C.byref(b), C.byref(params), C.byref(pr), ARITH[arith], int(jumps),
+                                  int(sample), C.c_void_p(stream) if stream else None), "bamf_autotune")
+        out = (C.c_int32 * 7)()
+        _check(L, L.bamf_autotune_result(self._ws, ARITH[arith], out), "bamf_autotune_result")
+        return list(out)
 
     def run_host(self, batch, params: abi.McmcParams, off, sig, back, seed: int,
                  arith: str = "fast", bg0: float = 0.0, init=None, proposal: str = "reference",

@@ -334,6 +334,9 @@ def main():
         s.run_device(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=1234, arith="fast",
                      outs=outs, stream=stream.cuda_stream, bg0=bg0)
 
+    # CTA shape per size class by the project's autotuner (short chains on a sample of each class)
+    tuned = s.autotune(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, arith="fast", jumps=200,
+                       sample=4864, stream=stream.cuda_stream, bg0=bg0)
     for _ in range(a.warmup):
         step()
     torch.cuda.synchronize()
@@ -431,7 +434,8 @@ def main():
             "data": "synthetic (seeded, reference forward model + Poisson noise)",
             "config": {"workload": workload_label(n, a.jumps), "n_rois": n, "jumps": [a.jumps, a.jumps],
                        "arith": "fast", "parallelism": f"replicas x{world}",
-                       "l2": "flushed between timed steps (512 MB write)"},
+                       "l2": "flushed between timed steps (512 MB write)",
+                       "chains_per_cta_by_size_class": tuned},
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": mufu.value / 1e9,
                          "unit": "Gop/s (MUFU log2)", "frac": achieved / mufu.value,
                          "traffic": None,

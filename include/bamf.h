@@ -344,7 +344,8 @@ bamf_status bamf_refine_stats_device(const float *pos_trace, int pos_len, int po
                                      int n, float *out, void *stream);
 
 /* Device scratch (prior tables, work queue, per-ROI chain traces) that
- * grows on demand and is reused across calls on one stream. */
+ * grows on demand and is reused across calls on one stream; it also keeps
+ * the CTA shapes chosen by bamf_autotune. */
 typedef struct bamf_workspace bamf_workspace;
 bamf_status bamf_workspace_create(bamf_workspace **ws);
 void bamf_workspace_destroy(bamf_workspace *ws);
@@ -387,6 +388,19 @@ bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi_batch *roi
  * The work-queue counters are cleared at the start of every call; nothing
  * else in the scratch is assumed to start at zero.
  */
+/* Autotuner (no reference counterpart): for every ROI size class present
+ * in the (device) batch, times each CTA shape - 8, 4, 2 or 1 chains per CTA
+ * in fast arithmetic, 4, 2 or 1 in exact - on up to `sample` ROIs of the
+ * class with chains of `jumps` burn-in jumps, and keeps the fastest in the
+ * workspace; later bamf_rjmcmc_batch_device calls on that workspace launch
+ * each class with its tuned shape.  Results of a batch do not depend on
+ * the shape.  Synchronises `stream`. */
+bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *rois, const bamf_mcmc_params *p,
+                          const bamf_priors *priors, int arith, int jumps, int sample, void *stream);
+/* chains_per_cta[7]: the tuned shape per size class (sides (0,8], (8,12],
+ * ..., (28,32]); 0 where the class was not tuned. */
+bamf_status bamf_autotune_result(const bamf_workspace *ws, int arith, int32_t *chains_per_cta);
+
 #define BAMF_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *rois,
                                              const bamf_mcmc_params *p,

@@ -184,3 +184,35 @@ def test_fast_and_exact_posterior_counts_agree_on_uneven_rois(cuda_lib):
     pe, pf = np.mean([e[0] for e in ex]), np.mean([f[0] for f in fa])
     assert abs(pf - pe) < 0.03, (pf, pe)
     assert abs(np.mean([e[1] for e in ex]) - np.mean([f[1] for f in fa])) < 0.1
+
+
+def test_autotune_picks_a_shape_per_class_and_keeps_results(cuda_lib):
+    """The autotuner times every CTA shape per size class; batches after it
+    use the tuned shapes and give the same chains as before."""
+    import torch
+    b = synth.roi_batch_uneven(3000, seed=23)
+    rj = rjstruct.uneven_rjstruct()
+    rj.N_Burnin = rj.N_Trials = 300
+    p = rjstruct.mcmc_params(rj)
+    bg0 = rjstruct.initial_bg(rj)
+    dev = {"data": torch.from_numpy(b.data).cuda(), "offsets": torch.from_numpy(b.offsets).cuda(),
+           "xsize": torch.from_numpy(b.xsize).cuda(), "ysize": torch.from_numpy(b.ysize).cuda(),
+           "psf_sigma": torch.from_numpy(b.sigma).cuda(), "side_max": 24}
+    s = sampler.Sampler()
+
+    def run():
+        outs = {k: torch.zeros(3000, dtype=torch.int32, device="cuda") for k in ("map_n", "final_n", "status")}
+        outs["final_state"] = torch.zeros((3000, 4 + 4 * 32), dtype=torch.float32, device="cuda")
+        s.run_device(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=3, arith="fast", outs=outs, bg0=bg0)
+        torch.cuda.synchronize()
+        return {k: v.cpu().numpy() for k, v in outs.items()}
+
+    before = run()
+    tuned = s.autotune(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, arith="fast", jumps=100,
+                       sample=1000, bg0=bg0)
+    print("chains per CTA by size class:", tuned)
+    assert [t > 0 for t in tuned[:5]] == [True] * 5 and tuned[5:] == [0, 0]
+    assert all(t in (1, 2, 4, 8) for t in tuned[:5])
+    after = run()
+    for k in before:
+        np.testing.assert_array_equal(before[k], after[k], err_msg=k)
