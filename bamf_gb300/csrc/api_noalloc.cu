@@ -231,6 +231,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     K.bg0 = rois->bg0;
     K.sync_moves = arith == BAMF_ARITH_FAST ? 1 : 0;
     K.proposal = rois->proposal;
+    K.opt_model = rois->opt_model;
 
     SamplerBatch B;
     std::memset(&B, 0, sizeof B);
@@ -268,6 +269,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         B.x_trace = out->x_trace;
         B.x_cap = out->trace_len;
     }
+    B.sampled_psf = rois->opt_model == 1 ? rois->sampled_psf : nullptr;
     B.birth_cdf = rois->birth_cdf;
     B.birth_sub = rois->birth_sub;
     B.pgrid = out->pgrid;

@@ -152,6 +152,8 @@ struct bamf_workspace {
      * bamf_autotune; 0 = not tuned (occupancy rule) */
     int tuned_wpb[2][BAMF_N_CLASSES] = {};
     DevBuf tune_range; /* class ranges clipped to the tuning sample    */
+    std::vector<float> tables_host; /* what `tables` holds, to skip re-uploads */
+    DevStat tables_dev[3] = {};
     DevBuf tables;   /* the three prior tables                       */
     DevBuf queue;    /* work-queue counter                             */
     DevBuf trace;    /* per-ROI Signal==1 count per chain entry        */
@@ -176,10 +178,8 @@ static bamf_status upload_tables(bamf_workspace *ws, const HostStat st[3], DevSt
     size_t total = 0;
     for (int k = 0; k < 3; ++k)
         total += st[k].x.size() * 2 + st[k].ux.size() * 2;
-    bamf_status r = ws->tables.ensure(total * sizeof(float));
-    if (r) return r;
     std::vector<float> h;
-    h.reserve(total);
+    h.reserve(total + 12);
     size_t off[3][4];
     for (int k = 0; k < 3; ++k) {
         off[k][0] = h.size(); h.insert(h.end(), st[k].x.begin(), st[k].x.end());
@@ -187,8 +187,20 @@ static bamf_status upload_tables(bamf_workspace *ws, const HostStat st[3], DevSt
         off[k][2] = h.size(); h.insert(h.end(), st[k].ux.begin(), st[k].ux.end());
         off[k][3] = h.size(); h.insert(h.end(), st[k].uc.begin(), st[k].uc.end());
     }
+    /* the same tables as last time: nothing to upload (and no
+     * synchronisation, so a batch can be captured into a graph) */
+    for (int k = 0; k < 3; ++k) {
+        h.push_back((float)st[k].x.size());
+        h.push_back((float)st[k].ux.size());
+    }
+    if (ws->tables.p && h == ws->tables_host) {
+        for (int k = 0; k < 3; ++k) out[k] = ws->tables_dev[k];
+        return BAMF_OK;
+    }
+    bamf_status r = ws->tables.ensure(total * sizeof(float));
+    if (r) return r;
     /* synchronous: h is a temporary */
-    CU(cudaMemcpyAsync(ws->tables.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(ws->tables.p, h.data(), total * sizeof(float), cudaMemcpyHostToDevice, s));
     CU(cudaStreamSynchronize(s));
     float *base = (float *)ws->tables.p;
     for (int k = 0; k < 3; ++k) {
@@ -199,7 +211,9 @@ static bamf_status upload_tables(bamf_workspace *ws, const HostStat st[3], DevSt
         out[k].L = (int)st[k].x.size();
         out[k].nu = (int)st[k].ux.size();
         out[k].inv_dx = st[k].x.size() > 1 ? 1.0f / (st[k].x[1] - st[k].x[0]) : 0.0f; /* x[1] - x[0] = DX */
+        ws->tables_dev[k] = out[k];
     }
+    ws->tables_host.swap(h);
     return BAMF_OK;
 }
 
@@ -405,9 +419,30 @@ __global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__re
 
 /* Checks of the proposal fields of a batch and of the trace outputs, shared
  * with the allocation-free entry point. */
+/* OptModel 1 needs a sampled PSF whose four extents are positive and whose
+ * element count fits an int (NumModel indexes it with int, :81-84). */
+static int64_t psf_elems(const bamf_mcmc_params *p)
+{
+    int64_t n = 1;
+    for (int k = 0; k < 4; ++k) {
+        if (p->PSFsize[k] < 1) return -1;
+        n *= p->PSFsize[k];
+        if (n > INT32_MAX) return -1;
+    }
+    return n;
+}
+
+static bamf_status check_model(int32_t opt_model, const float *psf, const bamf_mcmc_params *p)
+{
+    if (opt_model == 0) return BAMF_OK;
+    if (opt_model != 1 || !psf || psf_elems(p) < 1) return BAMF_ERR_INVALID_ARG;
+    return BAMF_OK;
+}
+
 bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcmc_params *p, int arith,
                                       const bamf_batch_results *out)
 {
+    if (check_model(rois->opt_model, rois->sampled_psf, p)) return BAMF_ERR_INVALID_ARG;
     if (rois->proposal < BAMF_PROPOSAL_REFERENCE || rois->proposal > BAMF_PROPOSAL_LEARNED)
         return BAMF_ERR_INVALID_ARG;
     if (rois->proposal != BAMF_PROPOSAL_REFERENCE && arith != BAMF_ARITH_FAST) return BAMF_ERR_INVALID_ARG;
@@ -444,6 +479,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     bamf_status r = make_consts(ws, p, priors, seed, rois->bg0, K, s);
     if (r) return r;
     K.proposal = rois->proposal;
+    K.opt_model = rois->opt_model;
     int n = rois->n_rois;
     int64_t steps = (int64_t)p->N_Burnin + p->N_Trials;
     int trace_cap = (int)std::min<int64_t>(steps, INT32_MAX);
@@ -468,6 +504,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     B.llr_evals = out->llr_evals;
     B.birth_cdf = rois->birth_cdf;
     B.birth_sub = rois->birth_sub;
+    B.sampled_psf = rois->opt_model == 1 ? rois->sampled_psf : nullptr;
     B.pgrid = out->pgrid;
     B.pback = out->pback;
     B.grid_stride = out->grid_stride;
@@ -508,6 +545,66 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     return BAMF_OK;
 }
 
+/* ------------------------------------------------------------ graph capture */
+struct bamf_batch_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t stream = nullptr;
+};
+
+extern "C" void bamf_rjmcmc_batch_graph_destroy(bamf_batch_graph *g)
+{
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+/* One batch run on a private stream (prior tables uploaded, buffers sized,
+ * kernels configured), then the same batch captured into a CUDA graph. */
+extern "C" bamf_status bamf_rjmcmc_batch_graph_create(bamf_workspace *ws, const bamf_roi_batch *rois,
+                                                      const bamf_mcmc_params *p, const bamf_priors *priors,
+                                                      uint32_t seed, int arith, const bamf_batch_results *out,
+                                                      bamf_batch_graph **graph)
+{
+    if (!graph) return BAMF_ERR_INVALID_ARG;
+    *graph = nullptr;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    bamf_batch_graph *g = new bamf_batch_graph();
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        bamf_rjmcmc_batch_graph_destroy(g);
+        return BAMF_ERR_CUDA;
+    }
+    bamf_status r = bamf_rjmcmc_batch_device(ws, rois, p, priors, seed, arith, out, g->stream);
+    if (!r && cudaStreamSynchronize(g->stream) != cudaSuccess) r = cuda_fail(cudaGetLastError(), "warm-up batch");
+    if (!r && cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        r = cuda_fail(cudaGetLastError(), "cudaStreamBeginCapture");
+    if (!r) {
+        bamf_status rc = bamf_rjmcmc_batch_device(ws, rois, p, priors, seed, arith, out, g->stream);
+        cudaError_t e = cudaStreamEndCapture(g->stream, &g->graph);
+        if (rc) r = rc;
+        else if (e != cudaSuccess) r = cuda_fail(e, "cudaStreamEndCapture");
+    }
+    if (!r && cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess)
+        r = cuda_fail(cudaGetLastError(), "cudaGraphInstantiate");
+    if (r) {
+        cudaGetLastError();
+        bamf_rjmcmc_batch_graph_destroy(g);
+        return r;
+    }
+    *graph = g;
+    return BAMF_OK;
+}
+
+extern "C" bamf_status bamf_rjmcmc_batch_graph_launch(bamf_batch_graph *g, void *stream)
+{
+    if (!g || !g->exec) return BAMF_ERR_INVALID_ARG;
+    cudaError_t e = cudaGraphLaunch(g->exec, (cudaStream_t)stream);
+    return e == cudaSuccess ? BAMF_OK : cuda_fail(e, "cudaGraphLaunch");
+}
+
 /* ---------------------------------------------------------------- autotuner */
 /* Times every CTA shape (chains per CTA) on a sample of each size class of
  * the batch, with chains of `jumps` burn-in jumps, and keeps the fastest
@@ -532,6 +629,8 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
     bamf_status r = make_consts(ws, &pt, priors, 1u, rois->bg0, K, s);
     if (r) return r;
     K.sync_moves = arith == BAMF_ARITH_FAST ? 1 : 0;
+    if (check_model(rois->opt_model, rois->sampled_psf, p)) return BAMF_ERR_INVALID_ARG;
+    K.opt_model = rois->opt_model;
     const bool exact = arith == BAMF_ARITH_EXACT;
     const int n = rois->n_rois;
     SamplerBatch B;
@@ -543,6 +642,7 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
     B.ysize = rois->ysize;
     B.psf_sigma = rois->psf_sigma;
     B.scmos = rois->scmos;
+    B.sampled_psf = rois->opt_model == 1 ? rois->sampled_psf : nullptr;
     if ((r = ws->order.ensure((size_t)n * sizeof(int32_t) + 256))) return r;
     if ((r = ws->tune_range.ensure(sizeof(int32_t) * 2 * BAMF_N_CLASSES))) return r;
     if ((r = ws->queue.ensure(sizeof(int32_t) * BAMF_N_CLASSES))) return r;
@@ -692,6 +792,9 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if ((r = upload(o, (int32_t **)&d.init_n, rois->init_n, (size_t)n))) return r;
     if ((r = upload(o, (float **)&d.init_bg, rois->init_bg, (size_t)n))) return r;
     if ((r = upload(o, (float **)&d.init_ixy, rois->init_ixy, (size_t)n * 3 * BAMF_NMAX))) return r;
+    if (rois->opt_model == 1 &&
+        (r = upload(o, (float **)&d.sampled_psf, rois->sampled_psf, (size_t)psf_elems(p))))
+        return r;
     if (rois->proposal == BAMF_PROPOSAL_LEARNED) {
         if ((r = upload(o, (float **)&d.birth_cdf, rois->birth_cdf, (size_t)npix))) return r;
         if ((r = upload(o, (float **)&d.birth_sub, rois->birth_sub, (size_t)npix * 16))) return r;
@@ -734,7 +837,21 @@ extern "C" bamf_status bamf_crjmcmc_host(const float *data, int xsize, int ysize
                                          float *pgrid, float *pback, bamf_chain *chain,
                                          bamf_chain *chain_test, bamf_counters *counters)
 {
+    return bamf_crjmcmc_host_model(data, xsize, ysize, e0, p, off, off_len, sig, sig_len, back, back_len, scmos,
+                                   nullptr, 0, rng, arith, pgrid, pback, chain, chain_test, counters);
+}
+
+extern "C" bamf_status bamf_crjmcmc_host_model(const float *data, int xsize, int ysize,
+                                               const bamf_emitters *e0, const bamf_mcmc_params *p,
+                                               const float *off, int off_len, const float *sig,
+                                               int sig_len, const float *back, int back_len,
+                                               const float *scmos, const float *sampled_psf, int opt_model,
+                                               const bamf_rng *rng, int arith, float *pgrid, float *pback,
+                                               bamf_chain *chain, bamf_chain *chain_test,
+                                               bamf_counters *counters)
+{
     if (!data || !e0 || !p || !off || !sig || !back || !rng) return BAMF_ERR_INVALID_ARG;
+    if (check_model(opt_model, sampled_psf, p)) return BAMF_ERR_INVALID_ARG;
     if (xsize < 1 || ysize < 1 || off_len < 1 || sig_len < 1 || back_len < 1) return BAMF_ERR_INVALID_ARG;
     if (arith != BAMF_ARITH_EXACT && arith != BAMF_ARITH_FAST) return BAMF_ERR_INVALID_ARG;
     if ((pgrid == nullptr) != (pback == nullptr)) return BAMF_ERR_INVALID_ARG;
@@ -749,6 +866,7 @@ extern "C" bamf_status bamf_crjmcmc_host(const float *data, int xsize, int ysize
     SamplerConsts K;
     bamf_status r = make_consts(&ws, p, &pri, rng->seed, e0->BG, K, nullptr);
     if (r) return r;
+    K.opt_model = opt_model;
     Owned o;
     int npix = xsize * ysize;
     SamplerBatch B;
@@ -762,6 +880,7 @@ extern "C" bamf_status bamf_crjmcmc_host(const float *data, int xsize, int ysize
     if ((r = upload(o, (int32_t **)&B.xsize, &xs, 1))) return r;
     if ((r = upload(o, (int32_t **)&B.ysize, &ys, 1))) return r;
     if ((r = upload(o, (float **)&B.scmos, scmos, (size_t)npix))) return r;
+    if (opt_model == 1 && (r = upload(o, (float **)&B.sampled_psf, sampled_psf, (size_t)psf_elems(p)))) return r;
     std::vector<float> ixy(3 * BAMF_NMAX, 0.0f);
     for (int k = 0; k < e0->N; ++k) {
         ixy[k] = e0->I[k];

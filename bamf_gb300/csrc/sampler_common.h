@@ -34,6 +34,7 @@ struct SamplerConsts {
     float bg0;      /* starting BG when no per-ROI start state is given */
     int32_t sync_moves; /* fast mode: CTA-synchronous move choice (rjmcmc_kernel_sync) */
     int32_t proposal;   /* BAMF_PROPOSAL_* (fast mode only) */
+    int32_t opt_model;  /* 0 Gaussian PSF, 1 sampled PSF (p.PSFsize, SamplerBatch::sampled_psf) */
 };
 
 /* Per-ROI inputs and outputs of a batch.  Arrays indexed by ROI id. */
@@ -61,6 +62,7 @@ struct SamplerBatch {
     int32_t trace_cap;
     float *x_trace;               /* [roi][x_cap] mean X of the Signal==1 emitters */
     int32_t x_cap;
+    const float *sampled_psf;     /* OptModel 1: the batch's sampled PSF     */
     const float *birth_cdf;       /* learned birth density (bamf_roi_batch)  */
     const float *birth_sub;
     int32_t *n_entries;           /* [roi] recorded chain entries          */

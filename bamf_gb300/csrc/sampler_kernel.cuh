@@ -272,6 +272,10 @@ struct ChainWarp {
     float *D, *M, *Mt, *E, *NX, *NY, *logM;
     float *SXo, *SYo, *SXn, *SYn; /* fast mode: compact stencil rows */
     const float *scm; /* sCMOS: shared memory (exact) or global/null (fast) */
+    /* sampled PSF (OptModel 1): [P0 y][P1 x][P2 y-sub][P3 x-sub], y fastest;
+     * null for the Gaussian model */
+    const float *psf;
+    int pn0, pn01, pn012, ptot, pos;
     int *cnt, *cl;
     int rec_n[2];
     /* current state A (lane j = slot j) */
@@ -635,12 +639,150 @@ struct ChainWarp {
         __syncwarp();
     }
 
+    /* ------------------------------------------ sampled-PSF model */
+    /* NumModel (:67-170) places emitter (x, y) on four planes of the sampled
+     * PSF: pixel (xx, yy) of the ROI reads flat index b_i + yy + xx P0 of
+     * plane i and blends them bilinearly with weights wx (x) and wy (y).
+     * Exact mode repeats the reference's double arithmetic; fast mode takes
+     * the same steps in float. */
+    struct NumPlace {
+        int b1, b2, b3, b4;
+        float wx, wy;
+    };
+    __device__ __forceinline__ NumPlace num_place(float xf, float yf) const
+    {
+        const int c0 = pn0 / 2;
+        int sx, sy, ix, iy;
+        NumPlace q;
+        if (EXACT) {
+            const double xd = (double)xf, yd = (double)yf, os = (double)pos;
+            const double fx = dadd(xd, -floor(xd)), fy = dadd(yd, -floor(yd));
+            sx = (int)ceil(dadd((double)c0, -xd));
+            ix = (int)floor(dmul(os, fx));
+            sy = (int)ceil(dadd((double)c0, -yd));
+            iy = (int)floor(dmul(os, fy));
+            q.wy = (float)dadd(1.0, -dmul(dadd(fy, -__ddiv_rn((double)iy, os)), os));
+            q.wx = (float)dadd(1.0, -dmul(dadd(fx, -__ddiv_rn((double)ix, os)), os));
+        } else {
+            const float os = (float)pos;
+            const float fx = xf - floorf(xf), fy = yf - floorf(yf);
+            sx = (int)ceilf((float)c0 - xf);
+            ix = (int)floorf(os * fx);
+            sy = (int)ceilf((float)c0 - yf);
+            iy = (int)floorf(os * fy);
+            q.wy = 1.0f - (fy * os - (float)iy);
+            q.wx = 1.0f - (fx * os - (float)ix);
+        }
+        int sx2 = sx, ix2 = ix + 1, sy2 = sy, iy2 = iy + 1;
+        if (ix == pos - 1) {
+            sx2 = sx - 1;
+            ix2 = 0;
+        }
+        if (iy == pos - 1) {
+            sy2 = sy - 1;
+            iy2 = 0;
+        }
+        q.b1 = sy + sx * pn0 + iy * pn01 + ix * pn012;
+        q.b2 = sy + sx2 * pn0 + iy * pn01 + ix2 * pn012;
+        q.b3 = sy2 + sx * pn0 + iy2 * pn01 + ix * pn012;
+        q.b4 = sy2 + sx2 * pn0 + iy2 * pn01 + ix2 * pn012;
+        return q;
+    }
+    /* a flat index outside the array reads its last element (:131-157) */
+    __device__ __forceinline__ float psf_at(int i) const
+    {
+        return psf[(i >= ptot || i < 0) ? ptot - 1 : i];
+    }
+    /* the blended PSF value of pixel offset o = yy + xx P0 */
+    __device__ __forceinline__ float num_value(const NumPlace &q, int o) const
+    {
+        float a = q.wx * psf_at(q.b1 + o) + (1.0f - q.wx) * psf_at(q.b2 + o);
+        float b = q.wx * psf_at(q.b3 + o) + (1.0f - q.wx) * psf_at(q.b4 + o);
+        return q.wy * a + (1.0f - q.wy) * b;
+    }
+    __device__ __forceinline__ static NumPlace shfl_place(const NumPlace &q, int k)
+    {
+        NumPlace r;
+        r.b1 = __shfl_sync(BAMF_FULL, q.b1, k);
+        r.b2 = __shfl_sync(BAMF_FULL, q.b2, k);
+        r.b3 = __shfl_sync(BAMF_FULL, q.b3, k);
+        r.b4 = __shfl_sync(BAMF_FULL, q.b4, k);
+        r.wx = __shfl_sync(BAMF_FULL, q.wx, k);
+        r.wy = __shfl_sync(BAMF_FULL, q.wy, k);
+        return r;
+    }
+
+    /* NumModel of a lane-distributed state into out[] (both modes: the
+     * background plane, then the emitters in slot order, per pixel). */
+    __device__ __forceinline__ void model_num(int n, float I, float Xv, float Yv, float BG, float ABG, float BBG,
+                                              float *out)
+    {
+        NumPlace q = num_place(lane < n ? Xv : 0.0f, lane < n ? Yv : 0.0f);
+#pragma unroll 1
+        for (int b0 = 0; b0 < npix; b0 += 32) {
+            const int p = b0 + lane;
+            const bool v = p < npix;
+            const int x = p / Y, y = p - x * Y;
+            float m = v ? BG + ABG * (float)x + BBG * (float)y + (scm ? scm[p] : 0.0f) : 0.0f;
+            const int o = y + x * pn0;
+#pragma unroll 1
+            for (int k = 0; k < n; ++k) {
+                NumPlace r = shfl_place(q, k);
+                float Ik = __shfl_sync(BAMF_FULL, I, k);
+                if (v) m = m + Ik * num_value(r, o);
+            }
+            if (v) out[p] = m;
+        }
+        __syncwarp();
+    }
+
+    /* Fast mode, sampled PSF: Mt = M + the background change - the changed
+     * emitters of A + the changed emitters of T (lane q < na + nt holds
+     * changed slot q, intensity negated for A's); returns the pixel sum of
+     * D (ln Mt - ln M) - (Mt - M). */
+    __device__ __forceinline__ float llr_num_fast(int na, int nt)
+    {
+        const float LN2 = 0.69314718f;
+        const int nr = na + nt;
+        const bool isnew = lane >= na;
+        const int qq = isnew ? lane - na : lane;
+        int k = lane < nr ? nth_bit(isnew ? t_dirty : a_dirty, qq) : 0;
+        float Ia = __shfl_sync(BAMF_FULL, aI, k), It = __shfl_sync(BAMF_FULL, tI, k);
+        float Xa = __shfl_sync(BAMF_FULL, aX, k), Xt = __shfl_sync(BAMF_FULL, tX, k);
+        float Ya = __shfl_sync(BAMF_FULL, aY, k), Yt = __shfl_sync(BAMF_FULL, tY, k);
+        const float Iq = lane < nr ? (isnew ? It : -Ia) : 0.0f;
+        NumPlace q = num_place(isnew ? Xt : Xa, isnew ? Yt : Ya);
+        const float dBG = tBG - aBG, dABG = tABG - aABG, dBBG = tBBG - aBBG;
+        float acc = 0.0f;
+#pragma unroll 1
+        for (int b0 = 0; b0 < npix; b0 += 32) {
+            const int p = b0 + lane;
+            const bool v = p < npix;
+            const int x = p / Y, y = p - x * Y;
+            float d = dBG + dABG * (float)x + dBBG * (float)y;
+            const int o = y + x * pn0;
+#pragma unroll 1
+            for (int r = 0; r < nr; ++r) {
+                NumPlace g = shfl_place(q, r);
+                float Ir = __shfl_sync(BAMF_FULL, Iq, r);
+                if (v) d += Ir * num_value(g, o);
+            }
+            if (v) {
+                float mt = M[p] + d;
+                Mt[p] = mt;
+                acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - d;
+            }
+        }
+        return acc;
+    }
+
     /* likelihood_ratio (:1650-1686).  M always holds Model(A). */
     __device__ __forceinline__ float llr()
     {
         n_llr++;
         if (EXACT) {
-            model_full(tn, tI, tX, tY, tBG, tABG, tBBG, Mt, NX, NY);
+            if (psf) model_num(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
+            else model_full(tn, tI, tX, tY, tBG, tABG, tBBG, Mt, NX, NY);
             for (int p = lane; p < npix; p += 32)
                 E[p] = M[p] - Mt[p] + D[p] * MT::log_(Mt[p] / M[p]);
             __syncwarp();
@@ -656,7 +798,18 @@ struct ChainWarp {
             const float LN2 = 0.69314718f;
             int na = __popc(a_dirty), nt = __popc(t_dirty);
             float acc = 0.0f;
-            if (na <= FAST_ROWS && nt <= FAST_ROWS) {
+            if (psf) {
+                if (na <= FAST_ROWS && nt <= FAST_ROWS) {
+                    acc = llr_num_fast(na, nt);
+                } else {
+                    model_num(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
+#pragma unroll 1
+                    for (int p = lane; p < npix; p += 32) {
+                        float mt = Mt[p];
+                        acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - (mt - M[p]);
+                    }
+                }
+            } else if (na <= FAST_ROWS && nt <= FAST_ROWS) {
                 stencil_rows(na, nt);
                 /* lane -> row y = lane mod Y of column x0 + lane / Y; a pass
                  * covers 32 / Y columns.  The model change of a pixel is
@@ -733,9 +886,11 @@ struct ChainWarp {
     __device__ __forceinline__ void rebuild_model()
     {
         if (EXACT) {
-            model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NX, NY);
+            if (psf) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
+            else model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NX, NY);
         } else {
-            model_stream(an, aI, aX, aY, aBG, aABG, aBBG, M);
+            if (psf) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
+            else model_stream(an, aI, aX, aY, aBG, aABG, aBBG, M);
 #pragma unroll 1
             for (int p = lane; p < npix; p += 32) logM[p] = __log2f(M[p]);
             __syncwarp();
@@ -1636,6 +1791,17 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT> &w, const SamplerCons
     float s = Bt.psf_sigma ? Bt.psf_sigma[roi] : Kp->p.PSFsigma;
     w.sigma = s;
     w.Cst = 1.0f / (s * sqrtf(2.0f));
+    if (Kp->opt_model == 1) {
+        const int32_t *P = Kp->p.PSFsize;
+        w.psf = Bt.sampled_psf;
+        w.pn0 = P[0];
+        w.pn01 = P[0] * P[1];
+        w.pn012 = w.pn01 * P[2];
+        w.ptot = w.pn012 * P[3];
+        w.pos = P[3];
+    } else {
+        w.psf = nullptr;
+    }
     w.MeanN = Kp->p.Rho * (float)X * (float)Y;
     /* start state (cRJMCMC.cpp:120-133) */
     w.an = n0;

@@ -31,6 +31,11 @@ def _declare() -> C.CDLL:
         pf, C.c_int, C.c_int, C.POINTER(abi.Emitters), C.POINTER(abi.McmcParams),
         pf, C.c_int, pf, C.c_int, pf, C.c_int, pf, C.POINTER(abi.Rng), C.c_int,
         pf, pf, C.POINTER(abi.Chain), C.POINTER(abi.Chain), C.POINTER(abi.Counters)]
+    L.bamf_crjmcmc_host_model.restype = C.c_int
+    L.bamf_crjmcmc_host_model.argtypes = [
+        pf, C.c_int, C.c_int, C.POINTER(abi.Emitters), C.POINTER(abi.McmcParams),
+        pf, C.c_int, pf, C.c_int, pf, C.c_int, pf, pf, C.c_int, C.POINTER(abi.Rng), C.c_int,
+        pf, pf, C.POINTER(abi.Chain), C.POINTER(abi.Chain), C.POINTER(abi.Counters)]
     L.bamf_workspace_create.restype = C.c_int
     L.bamf_workspace_create.argtypes = [C.POINTER(C.c_void_p)]
     L.bamf_workspace_destroy.argtypes = [C.c_void_p]
@@ -47,6 +52,13 @@ def _declare() -> C.CDLL:
                                 C.c_int, C.c_int, C.c_int, C.c_void_p]
     L.bamf_autotune_result.restype = C.c_int
     L.bamf_autotune_result.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int32)]
+    L.bamf_rjmcmc_batch_graph_create.restype = C.c_int
+    L.bamf_rjmcmc_batch_graph_create.argtypes = [C.c_void_p, C.POINTER(RoiBatch), C.POINTER(abi.McmcParams),
+                                                 C.POINTER(Priors), C.c_uint32, C.c_int, C.POINTER(BatchResults),
+                                                 C.POINTER(C.c_void_p)]
+    L.bamf_rjmcmc_batch_graph_launch.restype = C.c_int
+    L.bamf_rjmcmc_batch_graph_launch.argtypes = [C.c_void_p, C.c_void_p]
+    L.bamf_rjmcmc_batch_graph_destroy.argtypes = [C.c_void_p]
     L.bamf_last_error.restype = C.c_char_p
     L._sampler_declared = True
     return L
@@ -63,7 +75,8 @@ class RoiBatch(C.Structure):
                 ("offsets", C.c_void_p), ("xsize", C.c_void_p), ("ysize", C.c_void_p),
                 ("psf_sigma", C.c_void_p), ("scmos", C.c_void_p), ("init_n", C.c_void_p),
                 ("init_bg", C.c_void_p), ("init_ixy", C.c_void_p), ("bg0", C.c_float),
-                ("proposal", C.c_int32), ("birth_cdf", C.c_void_p), ("birth_sub", C.c_void_p)]
+                ("proposal", C.c_int32), ("birth_cdf", C.c_void_p), ("birth_sub", C.c_void_p),
+                ("opt_model", C.c_int32), ("sampled_psf", C.c_void_p)]
 
 
 class BatchResults(C.Structure):
@@ -90,9 +103,16 @@ def _check(L, st: int, where: str) -> None:
 
 def crjmcmc_raw(roi: np.ndarray, params: abi.McmcParams, off, sig, back, e0=None,
                 rng=(0, 0, 0), scmos=None, arith: str = "exact", record: bool = True,
-                grids: bool = True) -> dict:
-    """One cRJMCMC call on a (Ysize, Xsize) ROI; raw outputs like oracle.run_chain."""
+                grids: bool = True, sampled_psf: np.ndarray | None = None) -> dict:
+    """One cRJMCMC call on a (Ysize, Xsize) ROI; raw outputs like oracle.run_chain.
+    sampled_psf: a 4-D (P0, P1, P2, P3) array selects OptModel 1 (params.PSFsize
+    must hold its shape); None the Gaussian model."""
     L = _declare()
+    psf = None
+    if sampled_psf is not None:
+        psf = np.ascontiguousarray(np.asarray(sampled_psf, np.float32).ravel(order="F"))
+        if tuple(params.PSFsize) != tuple(np.shape(sampled_psf)):
+            raise ValueError("params.PSFsize must be the sampled PSF's shape")
     ysize, xsize = roi.shape
     data = np.ascontiguousarray(np.asarray(roi, np.float32).ravel(order="F"))
     I, X, Y, BG = e0 if e0 is not None else ([], [], [], 0.0)
@@ -111,13 +131,14 @@ def crjmcmc_raw(roi: np.ndarray, params: abi.McmcParams, off, sig, back, e0=None
     pg = np.zeros(g, np.float32) if grids else None
     pb = np.zeros(g, np.float32) if grids else None
     cnt = abi.Counters()
-    st = L.bamf_crjmcmc_host(
+    st = L.bamf_crjmcmc_host_model(
         abi.fptr(data), xsize, ysize, C.byref(em), C.byref(params), abi.fptr(off), off.size,
         abi.fptr(sig), sig.size, abi.fptr(back), back.size, abi.fptr(sc) if sc is not None else None,
+        abi.fptr(psf) if psf is not None else None, 1 if psf is not None else 0,
         C.byref(r), ARITH[arith], abi.fptr(pg) if grids else None, abi.fptr(pb) if grids else None,
         C.byref(chains[0][0]) if record else None, C.byref(chains[1][0]) if record else None,
         C.byref(cnt))
-    _check(L, st, "bamf_crjmcmc_host")
+    _check(L, st, "bamf_crjmcmc_host_model")
     out = {"counters": cnt.as_dict()}
     if record:
         out["chain"] = abi.chain_to_dict(*chains[0])
@@ -201,6 +222,29 @@ def rjmcmc(Data, RJ: RJStruct, Ysize: int, Xsize: int, DriftY: float = 0.0, Drif
     return acc, stat, pg, pb, prop
 
 
+class BatchGraph:
+    """A captured batch (Sampler.capture); keeps its workspace and tensors alive."""
+
+    def __init__(self, sampler, handle, tensors):
+        self._s, self._h, self._t = sampler, handle, tensors
+
+    def launch(self, stream=None) -> None:
+        L = self._s._L
+        _check(L, L.bamf_rjmcmc_batch_graph_launch(self._h, C.c_void_p(stream) if stream else None),
+               "bamf_rjmcmc_batch_graph_launch")
+
+    def close(self) -> None:
+        if self._h:
+            self._s._L.bamf_rjmcmc_batch_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Sampler:
     """Batched sampler over device-resident ROIs (torch tensors on cuda)."""
 
@@ -237,14 +281,34 @@ class Sampler:
         outs: dict of torch CUDA tensors to fill (map_n, final_n, final_state,
         counters, n_entries, status, overflow, llr_evals, and the [n][T]
         traces n_trace (uint8) / x_trace (float32)).  Enqueues on `stream`."""
+        pr, keep, b, res = self._structs(dev, params, off, sig, back, outs, bg0, proposal)
+        st = self._L.bamf_rjmcmc_batch_device(self._ws, C.byref(b), C.byref(params), C.byref(pr),
+                                               int(seed), ARITH[arith], C.byref(res),
+                                               C.c_void_p(stream) if stream else None)
+        _check(self._L, st, "bamf_rjmcmc_batch_device")
+
+    def capture(self, dev: dict, params: abi.McmcParams, off, sig, back, seed: int, arith: str = "fast",
+                outs: dict | None = None, bg0: float = 0.0, proposal: str = "reference") -> "BatchGraph":
+        """bamf_rjmcmc_batch_graph_create: the batch of run_device as a CUDA
+        graph over the same tensors (one eager run first, then the capture).
+        BatchGraph.launch(stream) replays it on whatever the tensors then hold."""
+        pr, keep, b, res = self._structs(dev, params, off, sig, back, outs, bg0, proposal)
+        h = C.c_void_p()
+        _check(self._L, self._L.bamf_rjmcmc_batch_graph_create(self._ws, C.byref(b), C.byref(params), C.byref(pr),
+                                                               int(seed), ARITH[arith], C.byref(res), C.byref(h)),
+               "bamf_rjmcmc_batch_graph_create")
+        return BatchGraph(self, h, (dev, outs))
+
+    def _structs(self, dev, params, off, sig, back, outs, bg0, proposal):
         pr, keep = self._priors(off, sig, back)
         b = RoiBatch()
         b.n_rois = int(dev["xsize"].numel())
         b.side_max = int(dev.get("side_max", 0))
         for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos", "init_n", "init_bg",
-                  "init_ixy", "birth_cdf", "birth_sub"):
+                  "init_ixy", "birth_cdf", "birth_sub", "sampled_psf"):
             t = dev.get(k)
             setattr(b, k, t.data_ptr() if t is not None else None)
+        b.opt_model = 1 if dev.get("sampled_psf") is not None else 0
         b.bg0 = float(bg0)
         b.proposal = PROPOSAL[proposal]
         res = BatchResults()
@@ -266,10 +330,7 @@ class Sampler:
             if any(t.dim() != 2 or t.shape[1] != tr[0].shape[1] for t in tr):
                 raise ValueError("n_trace and x_trace must be [n_rois][trace_len] of one length")
             res.trace_len = int(tr[0].shape[1])
-        st = self._L.bamf_rjmcmc_batch_device(self._ws, C.byref(b), C.byref(params), C.byref(pr),
-                                               int(seed), ARITH[arith], C.byref(res),
-                                               C.c_void_p(stream) if stream else None)
-        _check(self._L, st, "bamf_rjmcmc_batch_device")
+        return pr, keep, b, res
 
     def autotune(self, dev: dict, params: abi.McmcParams, off, sig, back, arith: str = "fast", jumps: int = 200,
                  sample: int = 4864, stream=None, bg0: float = 0.0) -> list:
@@ -279,9 +340,10 @@ class Sampler:
         b = RoiBatch()
         b.n_rois = int(dev["xsize"].numel())
         b.side_max = int(dev.get("side_max", 0))
-        for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos"):
+        for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos", "sampled_psf"):
             t = dev.get(k)
             setattr(b, k, t.data_ptr() if t is not None else None)
+        b.opt_model = 1 if dev.get("sampled_psf") is not None else 0
         b.bg0 = float(bg0)
         L = self._L
         _check(L, L.bamf_autotune(self._ws, C.byref(b), C.byref(params), C.byref(pr), ARITH[arith], int(jumps),
@@ -292,10 +354,11 @@ class Sampler:
 
     def run_host(self, batch, params: abi.McmcParams, off, sig, back, seed: int,
                  arith: str = "fast", bg0: float = 0.0, init=None, proposal: str = "reference",
-                 birth=None, trace_len: int = 0) -> dict:
+                 birth=None, trace_len: int = 0, sampled_psf: np.ndarray | None = None) -> dict:
         """batch: synth.RoiBatch (host numpy); returns numpy results.
         birth: (cdf, sub) host arrays of the LEARNED proposal; trace_len > 0
-        adds the n_trace / x_trace outputs."""
+        adds the n_trace / x_trace outputs; sampled_psf: a 4-D array of shape
+        params.PSFsize selects the sampled-PSF model (OptModel 1)."""
         pr, keep = self._priors(off, sig, back)
         n = batch.n
         b = RoiBatch()
@@ -313,6 +376,11 @@ class Sampler:
         if birth is not None:
             arrays["birth_cdf"] = np.ascontiguousarray(birth[0], np.float32)
             arrays["birth_sub"] = np.ascontiguousarray(birth[1], np.float32)
+        if sampled_psf is not None:
+            if tuple(params.PSFsize) != tuple(np.shape(sampled_psf)):
+                raise ValueError("params.PSFsize must be the sampled PSF's shape")
+            arrays["sampled_psf"] = np.ascontiguousarray(np.asarray(sampled_psf, np.float32).ravel(order="F"))
+            b.opt_model = 1
         for k, a in arrays.items():
             setattr(b, k, a.ctypes.data)
         b.bg0 = float(bg0)

@@ -203,6 +203,17 @@ bamf_status bamf_crjmcmc_host(const float *data, int xsize, int ysize, const bam
                               float *pback, bamf_chain *chain, bamf_chain *chain_test,
                               bamf_counters *counters);
 
+/* cRJMCMC with its last two inputs (cRJMCMC.cpp:73-74): sampled_psf
+ * (host, bamf_mcmc_params.PSFsize extents) and opt_model (0 Gaussian PSF,
+ * 1 the sampled PSF; sampled_psf may be NULL for 0).  bamf_crjmcmc_host is
+ * this call with opt_model 0. */
+bamf_status bamf_crjmcmc_host_model(const float *data, int xsize, int ysize, const bamf_emitters *e0,
+                                    const bamf_mcmc_params *p, const float *off, int off_len,
+                                    const float *sig, int sig_len, const float *back, int back_len,
+                                    const float *scmos, const float *sampled_psf, int opt_model,
+                                    const bamf_rng *rng, int arith, float *pgrid, float *pback,
+                                    bamf_chain *chain, bamf_chain *chain_test, bamf_counters *counters);
+
 /* Prior PDF tables of a batch (host pointers; the library builds the
  * reference's CDF tables from them, LibRJMCMC.cpp:176-217). */
 typedef struct bamf_priors {
@@ -262,6 +273,19 @@ typedef struct bamf_roi_batch {
     int32_t proposal;
     const float *birth_cdf;
     const float *birth_sub;
+    /* Likelihood model (cRJMCMC.cpp:73-74, OptModel and SampledPSF):
+     *   0  the Gaussian PSF of sigma psf_sigma / PSFsigma (Model, LibRJMCMC.cpp:15-59)
+     *   1  the sampled PSF `sampled_psf` (NumModel, LibRJMCMC.cpp:67-170), one
+     *      for the whole batch, of extents bamf_mcmc_params.PSFsize =
+     *      [P0 y-pixels, P1 x-pixels, P2 y-sub-positions, P3 x-sub-positions],
+     *      y fastest (MATLAB order); an emitter at (x, y) is centred on PSF
+     *      pixel P0/2 and blends the sub-position planes floor(P3 * frac)
+     *      and the next one bilinearly; a flat index outside the array reads
+     *      its last element, as the reference does.
+     * sampled_psf is a device pointer for the device entry points, a host
+     * pointer for bamf_rjmcmc_batch_host. */
+    int32_t opt_model;
+    const float *sampled_psf;
 } bamf_roi_batch;
 
 #define BAMF_PROPOSAL_REFERENCE 0
@@ -388,6 +412,21 @@ bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi_batch *roi
  * The work-queue counters are cleared at the start of every call; nothing
  * else in the scratch is assumed to start at zero.
  */
+/* A batch as a CUDA graph (no reference counterpart): one run of the batch
+ * on a private stream (which uploads the prior tables, sizes the workspace
+ * and configures the kernels), then the same call captured into a graph:
+ * the size-class ordering, every class's persistent launch (burn-in and
+ * trial phases of all chains) on its forked stream, the MAP reduction.
+ * Each launch replays it on the buffers named at creation (new data may be
+ * written into them between launches; the seed is the one given here).
+ * The workspace must not be used by other calls while the graph lives. */
+typedef struct bamf_batch_graph bamf_batch_graph;
+bamf_status bamf_rjmcmc_batch_graph_create(bamf_workspace *ws, const bamf_roi_batch *rois,
+                                           const bamf_mcmc_params *p, const bamf_priors *priors, uint32_t seed,
+                                           int arith, const bamf_batch_results *out, bamf_batch_graph **graph);
+bamf_status bamf_rjmcmc_batch_graph_launch(bamf_batch_graph *graph, void *stream);
+void bamf_rjmcmc_batch_graph_destroy(bamf_batch_graph *graph);
+
 /* Autotuner (no reference counterpart): for every ROI size class present
  * in the (device) batch, times each CTA shape - 8, 4, 2 or 1 chains per CTA
  * in fast arithmetic, 4, 2 or 1 in exact - on up to `sample` ROIs of the

@@ -61,6 +61,10 @@ def load(kind: str = "port") -> C.CDLL:
     run.restype = C.c_void_p
     run.argtypes = [pf, C.c_int, C.c_int, C.POINTER(abi.Emitters), C.POINTER(abi.McmcParams),
                     pf, C.c_int, pf, C.c_int, pf, C.c_int, pf, C.POINTER(abi.Rng)]
+    run_m = getattr(L, f"{p}_rjmcmc_run_model")
+    run_m.restype = C.c_void_p
+    run_m.argtypes = [pf, C.c_int, C.c_int, C.POINTER(abi.Emitters), C.POINTER(abi.McmcParams),
+                      pf, C.c_int, pf, C.c_int, pf, C.c_int, pf, pf, C.c_int, C.POINTER(abi.Rng)]
     getattr(L, f"{p}_result_sizes").argtypes = [C.c_void_p, C.POINTER(C.c_int64)]
     getattr(L, f"{p}_result_chain").argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.Chain)]
     getattr(L, f"{p}_result_grids").argtypes = [C.c_void_p, pf, pf]
@@ -84,11 +88,12 @@ def load(kind: str = "port") -> C.CDLL:
 
 def run_chain(kind: str, roi: np.ndarray, params: abi.McmcParams, off: np.ndarray,
               sig: np.ndarray, back: np.ndarray, e0=None, rng=(0, 0, 0),
-              scmos: np.ndarray | None = None) -> dict:
+              scmos: np.ndarray | None = None, sampled_psf: np.ndarray | None = None) -> dict:
     """One cRJMCMC run on a (Ysize, Xsize) ROI; returns the raw outputs.
 
     e0 = (I, X, Y, BG) or None for the empty start of rjmcmc.m (BG taken
-    from the offset prior's maximum by the caller)."""
+    from the offset prior's maximum by the caller); sampled_psf, a 4-D array
+    of shape params.PSFsize, selects OptModel 1."""
     L = load(kind)
     p = PREFIX[kind]
     ysize, xsize = roi.shape
@@ -103,10 +108,17 @@ def run_chain(kind: str, roi: np.ndarray, params: abi.McmcParams, off: np.ndarra
     sc = None if scmos is None else np.ascontiguousarray(np.asarray(scmos).ravel(order="F"),
                                                          np.float32)
     r = abi.Rng(*rng)
-    h = getattr(L, f"{p}_rjmcmc_run")(abi.fptr(data), xsize, ysize, C.byref(em), C.byref(params),
-                                      abi.fptr(off), off.size, abi.fptr(sig), sig.size,
-                                      abi.fptr(back), back.size,
-                                      abi.fptr(sc) if sc is not None else None, C.byref(r))
+    psf = None
+    if sampled_psf is not None:
+        if tuple(params.PSFsize) != tuple(np.shape(sampled_psf)):
+            raise ValueError("params.PSFsize must be the sampled PSF's shape")
+        psf = np.ascontiguousarray(np.asarray(sampled_psf, np.float32).ravel(order="F"))
+    h = getattr(L, f"{p}_rjmcmc_run_model")(abi.fptr(data), xsize, ysize, C.byref(em), C.byref(params),
+                                            abi.fptr(off), off.size, abi.fptr(sig), sig.size,
+                                            abi.fptr(back), back.size,
+                                            abi.fptr(sc) if sc is not None else None,
+                                            abi.fptr(psf) if psf is not None else None,
+                                            1 if psf is not None else 0, C.byref(r))
     if not h:
         raise ValueError("oracle rejected the arguments")
     try:

@@ -28,6 +28,13 @@ void *oracle_rjmcmc_run(const float *data, int xsize, int ysize, const bamf_emit
                         const bamf_mcmc_params *p, const float *off, int loff, const float *sig,
                         int lsig, const float *back, int lback, const float *scmos,
                         const bamf_rng *rng);
+/* The same with cRJMCMC's last two inputs (cRJMCMC.cpp:73-74): the sampled
+ * PSF (p->PSFsize extents, first index fastest) and OptModel (0 Gaussian,
+ * 1 sampled PSF). */
+void *oracle_rjmcmc_run_model(const float *data, int xsize, int ysize, const bamf_emitters *e0,
+                              const bamf_mcmc_params *p, const float *off, int loff, const float *sig,
+                              int lsig, const float *back, int lback, const float *scmos,
+                              const float *sampled_psf, int opt_model, const bamf_rng *rng);
 int oracle_result_sizes(void *h, int64_t *sizes);
 int oracle_result_chain(void *h, int which, bamf_chain *out);
 int oracle_result_grids(void *h, float *pgrid, float *pback);

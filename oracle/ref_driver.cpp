@@ -65,14 +65,36 @@ void take_chain(RefResult &r, int w, const RJMCMCChain &c)
 
 }  // namespace
 
+extern "C" void *ref_rjmcmc_run_model(const float *data, int xsize, int ysize, const bamf_emitters *e0,
+                                      const bamf_mcmc_params *p, const float *off, int loff,
+                                      const float *sig, int lsig, const float *back, int lback,
+                                      const float *scmos, const float *sampled_psf, int opt_model,
+                                      const bamf_rng *rng);
+
 extern "C" void *ref_rjmcmc_run(const float *data, int xsize, int ysize, const bamf_emitters *e0,
                                 const bamf_mcmc_params *p, const float *off, int loff,
                                 const float *sig, int lsig, const float *back, int lback,
                                 const float *scmos, const bamf_rng *rng)
 {
+    return ref_rjmcmc_run_model(data, xsize, ysize, e0, p, off, loff, sig, lsig, back, lback, scmos, nullptr,
+                                0, rng);
+}
+
+/* cRJMCMC's SampledPSF (prhs[9]) and OptModel (prhs[10]) inputs
+ * (cRJMCMC.cpp:73-74); a null sampled_psf passes zeros, as rjmcmc.m:82-84
+ * does for the Gaussian model. */
+extern "C" void *ref_rjmcmc_run_model(const float *data, int xsize, int ysize, const bamf_emitters *e0,
+                                      const bamf_mcmc_params *p, const float *off, int loff,
+                                      const float *sig, int lsig, const float *back, int lback,
+                                      const float *scmos, const float *sampled_psf, int opt_model,
+                                      const bamf_rng *rng)
+{
     if (!data || !e0 || !p || !off || !sig || !back || !rng || xsize < 1 || ysize < 1 || loff < 1 ||
         lsig < 1 || lback < 1)
         return nullptr;
+    if ((opt_model != 0 && opt_model != 1) || (opt_model == 1 && !sampled_psf)) return nullptr;
+    for (int k = 0; k < 4; ++k)
+        if (p->PSFsize[k] < 1) return nullptr;
     g_seed = rng->seed;
     g_chain = rng->chain_id;
     g_index = rng->offset;
@@ -130,12 +152,13 @@ extern "C" void *ref_rjmcmc_run(const float *data, int xsize, int ysize, const b
         scmos = zeros_scmos.data();
     }
     size_t psfn = (size_t)psfsize[0] * psfsize[1] * psfsize[2] * psfsize[3];
-    std::vector<float> sampled_psf(psfn > 0 ? psfn : 1, 0.0f);
+    std::vector<float> psf_buf(psfn, 0.0f);
+    if (sampled_psf) psf_buf.assign(sampled_psf, sampled_psf + psfn);
 
     RefResult *res = new RefResult();
     {
         RJMCMC RJ = RJMCMC(const_cast<float *>(data), Params, xsize, ysize, const_cast<float *>(scmos),
-                           MeanN, sampled_psf.data(), 0);
+                           MeanN, psf_buf.data(), opt_model);
         RJ.IsBurnin = 0;
         RJ.E_Active = E_Active;
         RJ.OffgStat = OffgStat;

@@ -10,8 +10,9 @@
  * (include/bamf_parity_math.h); with -DBAMF_ORACLE_NATIVE_MATH glibc's
  * erff/logf/expf/powf, like the unmodified reference.
  *
- * Scope: OptModel = 0 (Gaussian PSF, Model/Stencil) only; the sampled-PSF
- * model (NumModel, LibRJMCMC.cpp:67-170) is not restated.
+ * Scope: both likelihood models of cRJMCMC.cpp:73-74: OptModel 0 (the
+ * Gaussian PSF, Model/Stencil) and OptModel 1 (the sampled PSF, NumModel,
+ * LibRJMCMC.cpp:67-170).
  */
 #include <math.h>
 #include <pthread.h>
@@ -230,6 +231,9 @@ typedef struct {
     ivec nsig_trace; /* per accepted-chain entry: emitters with Signal == 1 */
     float *pgrid, *pback;
     int messages;
+    int opt_model;     /* 0 Gaussian PSF, 1 sampled PSF */
+    int first_call;    /* Params.FirstCall of the reference (see likelihood_ratio) */
+    const float *psf;  /* [P0][P1][P2][P3] of p.PSFsize, first index fastest */
 } orj;
 
 static float urand(orj *r)
@@ -294,10 +298,70 @@ static void model(orj *r, const oem *E, float *M)
             for (int x = 0; x < X; ++x) M[y + x * Y] += r->NX[X * n + x] * r->NY[Y * n + y];
 }
 
-/* likelihood_ratio (:1650-1686).  r->M always equals Model(E_Active). */
+/* NumModel (:67-170).  The background plane, then per emitter, in order,
+ * I times a bilinear blend of four samples of the PSF array: the emitter
+ * sits on PSF pixel P0/2 (integer division), its fractional position picks
+ * the sub-position planes ix = floor(P3 frac x) and ix + 1 (the next pixel's
+ * plane 0 after the last), likewise in y, and the weights are the distance
+ * to the next plane in units of 1/P3.  Positions and weights are computed
+ * in double as there; the blend and the sum in float.  A flat index
+ * outside the array reads the last element (one message each). */
+static float psf_get(orj *r, int i, int total)
+{
+    if (i >= total || i < 0) {
+        r->messages++;
+        i = total - 1;
+    }
+    return r->psf[i];
+}
+
+static void num_model(orj *r, const oem *E, float *M)
+{
+    int X = r->X, Y = r->Y;
+    const int32_t *P = r->p.PSFsize;
+    const int s0 = P[0], s01 = P[0] * P[1], s012 = s01 * P[2], total = s012 * P[3];
+    const double os = (double)P[3];
+    const int c0 = P[0] / 2;
+    for (int x = 0; x < X; ++x)
+        for (int y = 0; y < Y; ++y)
+            M[y + x * Y] = E->BG + E->ABG * x + E->BBG * y + r->scmos[x * Y + y];
+    for (int n = 0; n < E->n; ++n) {
+        double xd = (double)E->X[n], yd = (double)E->Y[n];
+        double fx = xd - floor(xd), fy = yd - floor(yd);
+        int sx = (int)ceil(c0 - xd), ix = (int)floor(os * fx);
+        int sy = (int)ceil(c0 - yd), iy = (int)floor(os * fy);
+        int sx2 = sx, ix2 = ix + 1, sy2 = sy, iy2 = iy + 1;
+        if (ix == os - 1) { sx2 = sx - 1; ix2 = 0; }
+        if (iy == os - 1) { sy2 = sy - 1; iy2 = 0; }
+        float wy = (float)(1 - (fy - (double)iy / os) * os);
+        float wx = (float)(1 - (fx - (double)ix / os) * os);
+        for (int x = 0; x < X; ++x)
+            for (int y = 0; y < Y; ++y) {
+                float v1 = psf_get(r, (sy + y) + (sx + x) * s0 + iy * s01 + ix * s012, total);
+                float v2 = psf_get(r, (sy + y) + (sx2 + x) * s0 + iy * s01 + ix2 * s012, total);
+                float v3 = psf_get(r, (sy2 + y) + (sx + x) * s0 + iy2 * s01 + ix * s012, total);
+                float v4 = psf_get(r, (sy2 + y) + (sx2 + x) * s0 + iy2 * s01 + ix2 * s012, total);
+                float a = wx * v1 + (1.0f - wx) * v2;
+                float b = wx * v3 + (1.0f - wx) * v4;
+                M[y + x * Y] = M[y + x * Y] + E->I[n] * (wy * a + (1.0f - wy) * b);
+            }
+    }
+}
+
+static void state_model(orj *r, const oem *E, float *M)
+{
+    if (r->opt_model == 1) num_model(r, E, M);
+    else model(r, E, M);
+}
+
+/* likelihood_ratio (:1650-1686).  r->M always equals the model of
+ * E_Active.  The reference takes Params by value here, so until find_Birth
+ * clears FirstCall it rebuilds M from E_Active on every call: the same
+ * values, but the sampled-PSF model's index messages count each time. */
 static float likelihood_ratio(orj *r)
 {
-    model(r, &r->T, r->Mt);
+    if (r->first_call && r->opt_model == 1) state_model(r, &r->A, r->M);
+    state_model(r, &r->T, r->Mt);
     int N = r->X * r->Y;
     float tmp = 0;
     for (int n = 0; n < N; ++n) tmp += r->M[n] - r->Mt[n] + r->D[n] * O_LOG(r->Mt[n] / r->M[n]);
@@ -740,6 +804,8 @@ static void mv_merge(orj *r)
 static void find_birth(orj *r, float *x, float *y)
 {
     int N = r->X * r->Y;
+    if (r->first_call && r->opt_model == 1) state_model(r, &r->A, r->M);
+    r->first_call = 0;
     for (int n = 0; n < N; ++n) {
         float v = r->D[n] - r->M[n];
         r->resid[n] = (0.0f > v) ? 0.0f : v;
@@ -1025,7 +1091,7 @@ static void start_chain(orj *r)
 static int orj_init(orj *r, const float *data, int xsize, int ysize, const bamf_emitters *e0,
                     const bamf_mcmc_params *p, const float *off, int loff, const float *sig,
                     int lsig, const float *back, int lback, const float *scmos,
-                    const bamf_rng *rng, int record, int grids)
+                    const bamf_rng *rng, int record, int grids, const float *psf, int opt_model)
 {
     memset(r, 0, sizeof *r);
     r->X = xsize;
@@ -1077,7 +1143,13 @@ static int orj_init(orj *r, const float *data, int xsize, int ysize, const bamf_
     c->N_jump = c->N_split = c->N_merge = c->N_birth = c->N_death = 1;
     c->N_jumpFg = c->N_splitFg = c->N_mergeFg = c->N_birthFg = c->N_deathFg = 1;
     c->N_jumpBg = c->N_splitBg = c->N_mergeBg = c->N_birthBg = c->N_deathBg = 1;
-    model(r, &r->A, r->M);
+    /* M of the start state; the reference builds it at the first
+     * likelihood_ratio / find_Birth call, which count its messages */
+    r->first_call = 1;
+    r->opt_model = opt_model;
+    r->psf = psf;
+    state_model(r, &r->A, r->M);
+    r->messages = 0;
     return z != NULL; /* caller frees scmos if it was allocated here */
 }
 
@@ -1113,10 +1185,28 @@ void *oracle_rjmcmc_run(const float *data, int xsize, int ysize, const bamf_emit
                         int lsig, const float *back, int lback, const float *scmos,
                         const bamf_rng *rng)
 {
+    return oracle_rjmcmc_run_model(data, xsize, ysize, e0, p, off, loff, sig, lsig, back, lback, scmos,
+                                   NULL, 0, rng);
+}
+
+void *oracle_rjmcmc_run_model(const float *data, int xsize, int ysize, const bamf_emitters *e0,
+                              const bamf_mcmc_params *p, const float *off, int loff, const float *sig,
+                              int lsig, const float *back, int lback, const float *scmos,
+                              const float *sampled_psf, int opt_model, const bamf_rng *rng)
+{
     if (!args_ok(data, xsize, ysize, e0, p, off, loff, sig, lsig, back, lback, rng)) return NULL;
+    if (opt_model != 0 && opt_model != 1) return NULL;
+    if (opt_model == 1) {
+        long long total = 1;
+        for (int k = 0; k < 4; ++k) {
+            if (p->PSFsize[k] < 1) return NULL;
+            total *= p->PSFsize[k];
+        }
+        if (!sampled_psf || total > 0x7fffffffLL) return NULL;
+    }
     oresult *res = (oresult *)calloc(1, sizeof(oresult));
     int owned = orj_init(&res->r, data, xsize, ysize, e0, p, off, loff, sig, lsig, back, lback,
-                         scmos, rng, 1, 1);
+                         scmos, rng, 1, 1, sampled_psf, opt_model);
     if (owned) res->owned_scmos = (float *)res->r.scmos;
     res->rng_offset = rng->offset;
     start_chain(&res->r);
@@ -1245,7 +1335,7 @@ static void *batch_worker(void *arg)
         bamf_mcmc_params pi = *j->p;
         if (j->sigma) pi.PSFsigma = j->sigma[i];
         orj_init(&r, j->data + j->offsets[i], j->xs[i], j->ys[i], &e0, &pi, j->off, j->loff, j->sig,
-                 j->lsig, j->back, j->lback, NULL, &rng, 0, 0);
+                 j->lsig, j->back, j->lback, NULL, &rng, 0, 0, NULL, 0);
         float *owned = (float *)r.scmos;
         start_chain(&r);
         j->final_n[i] = r.A.n;

@@ -194,3 +194,96 @@ def test_batch_summary_matches_single_runs(c0):
         vals = np.array(ns[lo - 1:it])
         hist = np.bincount(vals)
         assert got["map_n"][k] == int(np.argmax(hist)), k
+
+
+NUMPSF_GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rjmcmc_ref_numpsf.npz")
+
+
+def _numpsf_cases():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_numpsf_golden", os.path.join(os.path.dirname(NUMPSF_GOLD), "make_numpsf_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.mark.parametrize("case", ["gauss64", "small10"])
+def test_port_sampled_psf_matches_reference_golden(case):
+    """OptModel 1 (NumModel): the restatement reproduces the reference's
+    chains, counters, uniforms and index messages bit for bit (fixtures from
+    the reference build, including a PSF whose indices leave the array)."""
+    with np.load(NUMPSF_GOLD) as z:
+        gold = {k: z[k] for k in z.files}
+    mod = _numpsf_cases()
+    psf, n = mod.cases()[case]
+    rj, p = mod.params(psf)
+    bg0 = rjstruct.initial_bg(rj)
+    b = synth.roi_batch_c0(40, seed=0)
+
+    def one(k):
+        r = oracle.run_chain("port", b.roi(k), p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons,
+                             e0=([], [], [], bg0), rng=(int(gold["seed"]), k, 0), sampled_psf=psf)
+        c = r["counters"]
+        return len(r["chain"]["N"]), r["uniforms_used"], [c[m] for m in sorted(c)], r["messages"], _digest(r)
+
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        rows = list(ex.map(one, range(n)))
+    np.testing.assert_array_equal([r[0] for r in rows], gold[f"{case}_entries"])
+    np.testing.assert_array_equal([r[1] for r in rows], gold[f"{case}_uniforms"])
+    np.testing.assert_array_equal([r[2] for r in rows], gold[f"{case}_counters"])
+    np.testing.assert_array_equal([r[3] for r in rows], gold[f"{case}_messages"])
+    assert [r[4] for r in rows] == list(gold[f"{case}_sha256"])
+    if case == "small10":
+        assert min(r[3] for r in rows) > 0
+
+
+@pytest.mark.skipif(not oracle.available("ref"), reason="reference tree not built here")
+@pytest.mark.parametrize("kind", ["port", "port_native"])
+def test_port_sampled_psf_matches_live_reference_other_settings(c0, kind):
+    """OptModel 1 with all 8 move types, a background-emitter prior, drift,
+    a start state and an anisotropic PSF (sigma_x 1.1, sigma_y 1.6)."""
+    b, rj, _, bg0 = c0
+    r2 = rjstruct.c0_rjstruct()
+    r2.N_Burnin = r2.N_Trials = 1000
+    r2.P_Burnin = [0.3, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1]
+    r2.P_Trials = [0.4, 0.0, 0.0, 0.05, 0.05, 0.15, 0.15, 0.2]
+    r2.IsBackg = 1
+    grid = np.arange(0, 12001, 10.0)
+    back = synth.lognormal_pdf(grid, 200.0, 0.5).astype(np.float32)
+    p = rjstruct.mcmc_params(r2, drift_x=0.3, drift_y=-0.2)
+    from bamf_gb300 import psf as psfmod
+    gx = psfmod._pixel_integrals(48, 24, 4, 1.1)
+    gy = psfmod._pixel_integrals(48, 24, 4, 1.6)
+    psf = (gy[:, None, :, None] * gx[None, :, None, :]).astype(np.float32)
+    for k, v in enumerate(psf.shape):
+        p.PSFsize[k] = v
+    refk = "ref" if kind == "port" else "ref_native"
+    for k in range(4):
+        e0 = (b.true_i[k].astype(np.float32), b.true_x[k].astype(np.float32),
+              b.true_y[k].astype(np.float32), 8.0)
+        a = oracle.run_chain(kind, b.roi(k), p, rj.P_Offset, rj.P_EmPhotons, back, e0=e0,
+                             rng=(5, 2000 + k, 9), sampled_psf=psf)
+        r = oracle.run_chain(refk, b.roi(k), p, rj.P_Offset, rj.P_EmPhotons, back, e0=e0,
+                             rng=(5, 2000 + k, 9), sampled_psf=psf)
+        assert _digest(a) == _digest(r), k
+        assert a["counters"] == r["counters"]
+        assert a["uniforms_used"] == r["uniforms_used"]
+        assert a["messages"] == r["messages"]
+
+
+def test_gaussian_sampled_psf_is_the_pixel_integrated_gaussian():
+    """psf.gaussian_sampled_psf: each sub-position plane sums to ~1 and its
+    centroid sits at the emitter offset NumModel assumes (pixel c0 plus the
+    sub-position, pixel centres at +0.5)."""
+    from bamf_gb300 import psf as psfmod
+    s = psfmod.gaussian_sampled_psf(1.3, pixels=32, oversampling=4)
+    assert s.shape == (32, 32, 4, 4) and s.dtype == np.float32
+    idx = np.arange(32) + 0.5
+    for iy in range(4):
+        for ix in range(4):
+            plane = s[:, :, iy, ix].astype(np.float64)
+            assert abs(plane.sum() - 1.0) < 1e-5
+            cy = (plane.sum(axis=1) * idx).sum() / plane.sum()
+            cx = (plane.sum(axis=0) * idx).sum() / plane.sum()
+            assert abs(cy - (16 + iy / 4)) < 1e-4 and abs(cx - (16 + ix / 4)) < 1e-4
