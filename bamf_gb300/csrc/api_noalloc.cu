@@ -270,6 +270,8 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         B.x_cap = out->trace_len;
     }
     B.sampled_psf = rois->opt_model == 1 ? rois->sampled_psf : nullptr;
+    B.psf_slot = rois->opt_model == 1 ? rois->psf_slot : nullptr;
+    B.n_psf = rois->n_psf > 1 ? rois->n_psf : 1;
     B.birth_cdf = rois->birth_cdf;
     B.birth_sub = rois->birth_sub;
     B.pgrid = out->pgrid;

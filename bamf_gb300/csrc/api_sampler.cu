@@ -442,7 +442,9 @@ static bamf_status check_model(int32_t opt_model, const float *psf, const bamf_m
 bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcmc_params *p, int arith,
                                       const bamf_batch_results *out)
 {
-    if (check_model(rois->opt_model, rois->sampled_psf, p)) return BAMF_ERR_INVALID_ARG;
+    if (check_model(rois->opt_model, rois->sampled_psf, p) || rois->n_psf < 0) return BAMF_ERR_INVALID_ARG;
+    if (rois->opt_model == 1 && (int64_t)std::max(rois->n_psf, 1) * psf_elems(p) > ((int64_t)1 << 40))
+        return BAMF_ERR_TOO_LARGE;
     if (rois->proposal < BAMF_PROPOSAL_REFERENCE || rois->proposal > BAMF_PROPOSAL_LEARNED)
         return BAMF_ERR_INVALID_ARG;
     if (rois->proposal != BAMF_PROPOSAL_REFERENCE && arith != BAMF_ARITH_FAST) return BAMF_ERR_INVALID_ARG;
@@ -505,6 +507,8 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     B.birth_cdf = rois->birth_cdf;
     B.birth_sub = rois->birth_sub;
     B.sampled_psf = rois->opt_model == 1 ? rois->sampled_psf : nullptr;
+    B.psf_slot = rois->opt_model == 1 ? rois->psf_slot : nullptr;
+    B.n_psf = std::max(rois->n_psf, 1);
     B.pgrid = out->pgrid;
     B.pback = out->pback;
     B.grid_stride = out->grid_stride;
@@ -643,6 +647,8 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
     B.psf_sigma = rois->psf_sigma;
     B.scmos = rois->scmos;
     B.sampled_psf = rois->opt_model == 1 ? rois->sampled_psf : nullptr;
+    B.psf_slot = rois->opt_model == 1 ? rois->psf_slot : nullptr;
+    B.n_psf = std::max(rois->n_psf, 1);
     if ((r = ws->order.ensure((size_t)n * sizeof(int32_t) + 256))) return r;
     if ((r = ws->tune_range.ensure(sizeof(int32_t) * 2 * BAMF_N_CLASSES))) return r;
     if ((r = ws->queue.ensure(sizeof(int32_t) * BAMF_N_CLASSES))) return r;
@@ -792,9 +798,11 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if ((r = upload(o, (int32_t **)&d.init_n, rois->init_n, (size_t)n))) return r;
     if ((r = upload(o, (float **)&d.init_bg, rois->init_bg, (size_t)n))) return r;
     if ((r = upload(o, (float **)&d.init_ixy, rois->init_ixy, (size_t)n * 3 * BAMF_NMAX))) return r;
-    if (rois->opt_model == 1 &&
-        (r = upload(o, (float **)&d.sampled_psf, rois->sampled_psf, (size_t)psf_elems(p))))
-        return r;
+    if (rois->opt_model == 1) {
+        const size_t npsf = (size_t)std::max(rois->n_psf, 1);
+        if ((r = upload(o, (float **)&d.sampled_psf, rois->sampled_psf, npsf * (size_t)psf_elems(p)))) return r;
+        if ((r = upload(o, (int32_t **)&d.psf_slot, rois->psf_slot, (size_t)n))) return r;
+    }
     if (rois->proposal == BAMF_PROPOSAL_LEARNED) {
         if ((r = upload(o, (float **)&d.birth_cdf, rois->birth_cdf, (size_t)npix))) return r;
         if ((r = upload(o, (float **)&d.birth_sub, rois->birth_sub, (size_t)npix * 16))) return r;
@@ -881,6 +889,7 @@ extern "C" bamf_status bamf_crjmcmc_host_model(const float *data, int xsize, int
     if ((r = upload(o, (int32_t **)&B.ysize, &ys, 1))) return r;
     if ((r = upload(o, (float **)&B.scmos, scmos, (size_t)npix))) return r;
     if (opt_model == 1 && (r = upload(o, (float **)&B.sampled_psf, sampled_psf, (size_t)psf_elems(p)))) return r;
+    B.n_psf = 1;
     std::vector<float> ixy(3 * BAMF_NMAX, 0.0f);
     for (int k = 0; k < e0->N; ++k) {
         ixy[k] = e0->I[k];

@@ -62,7 +62,9 @@ struct SamplerBatch {
     int32_t trace_cap;
     float *x_trace;               /* [roi][x_cap] mean X of the Signal==1 emitters */
     int32_t x_cap;
-    const float *sampled_psf;     /* OptModel 1: the batch's sampled PSF     */
+    const float *sampled_psf;     /* OptModel 1: n_psf sampled PSFs, one after another */
+    const int32_t *psf_slot;      /* [roi] which of them, or null: the first */
+    int32_t n_psf;
     const float *birth_cdf;       /* learned birth density (bamf_roi_batch)  */
     const float *birth_sub;
     int32_t *n_entries;           /* [roi] recorded chain entries          */

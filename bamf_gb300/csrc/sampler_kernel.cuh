@@ -1793,12 +1793,17 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT> &w, const SamplerCons
     w.Cst = 1.0f / (s * sqrtf(2.0f));
     if (Kp->opt_model == 1) {
         const int32_t *P = Kp->p.PSFsize;
-        w.psf = Bt.sampled_psf;
         w.pn0 = P[0];
         w.pn01 = P[0] * P[1];
         w.pn012 = w.pn01 * P[2];
         w.ptot = w.pn012 * P[3];
         w.pos = P[3];
+        const int slot = Bt.psf_slot ? Bt.psf_slot[roi] : 0;
+        if (slot < 0 || slot >= Bt.n_psf) {
+            if (lane == 0 && Bt.status) Bt.status[roi] = BAMF_ERR_INVALID_ARG;
+            return false;
+        }
+        w.psf = Bt.sampled_psf + (int64_t)slot * w.ptot;
     } else {
         w.psf = nullptr;
     }

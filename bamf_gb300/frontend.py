@@ -142,12 +142,15 @@ def gaussMLE(Data, FitType: str = "Basic", CameraType: str = "CCD", Sigma=1.3, *
                                         abi.fptr(P), abi.fptr(CR), abi.fptr(LL)), "bamf_gauss_mle_fit_host")
     P = P.reshape(npar, n).T
     CR = CR.reshape(npar, n).T
+    # a negative CRLB diagonal (an ill-conditioned fit) gives NaN here where
+    # MATLAB's sqrt returns a complex value
+    with np.errstate(invalid="ignore"):
+        SE = np.sqrt(CR)
     out = {"Y": P[:, 0], "X": P[:, 1], "Photons": P[:, 2], "BG": P[:, 3],
-           "Y_SE": np.sqrt(CR[:, 0]), "X_SE": np.sqrt(CR[:, 1]),
-           "Photons_SE": np.sqrt(CR[:, 2]), "BG_SE": np.sqrt(CR[:, 3])}
+           "Y_SE": SE[:, 0], "X_SE": SE[:, 1], "Photons_SE": SE[:, 2], "BG_SE": SE[:, 3]}
     for k, name in enumerate(FIT_EXTRA[FitType]):
         out[name] = P[:, 4 + k]
-        out[name + "_SE"] = np.sqrt(CR[:, 4 + k])
+        out[name + "_SE"] = SE[:, 4 + k]
     out["LogLikelihood"] = LL
     return out
 

@@ -74,6 +74,13 @@ def unpack(rec: np.ndarray) -> dict:
     return d
 
 
+def _set_psf_size(p, shape):
+    if shape is not None:
+        for k, v in enumerate(shape):
+            p.PSFsize[k] = int(v)
+    return p
+
+
 def _run(s, dev, params, rj, seed, arith, proposal, pos_len, bg0, extra=None):
     import torch
     n = int(dev["xsize"].numel())
@@ -91,14 +98,28 @@ def _run(s, dev, params, rj, seed, arith, proposal, pos_len, bg0, extra=None):
 
 
 def analyze(dev: dict, rj, seed: int = 1, arith: str = "fast", proposal: str = "reference", pos_len: int = 250,
-            refine: bool = True, s=None, grids: dict | None = None) -> dict:
+            refine: bool = True, s=None, grids: dict | None = None, sampled_psf=None, psf_slot=None) -> dict:
     """findMap + mcmc for every ROI of a device batch (sampler.run_device
     layout).  Returns numpy dicts 'map' (findMap SMD per ROI) and 'refined'
     (mcmc FoundMAP per ROI; NaN rows where the MAP count is 0), plus the
-    pass-1 map_n / n_entries."""
+    pass-1 map_n / n_entries.  sampled_psf (one 4-D PSF or a stack of them,
+    with psf_slot [n] torch int32 naming each ROI's) selects the sampled-PSF
+    model for both passes, as analyzeROIs.m:142-162 does."""
     import torch
     s = s or sampler.Sampler()
-    p1 = rjstruct.mcmc_params(rj)
+    psf_shape = None
+    if sampled_psf is not None:
+        a = np.asarray(sampled_psf, np.float32)
+        psf_shape = a.shape[-4:]
+        tmp = rjstruct.mcmc_params(rj)
+        _set_psf_size(tmp, psf_shape)
+        flat, npsf = sampler.pack_psfs(a, tmp)
+        dev = dict(dev)
+        dev["sampled_psf"] = torch.from_numpy(flat).cuda()
+        dev["n_psf"] = npsf
+        if psf_slot is not None:
+            dev["psf_slot"] = psf_slot
+    p1 = _set_psf_size(rjstruct.mcmc_params(rj), psf_shape)
     bg0 = rjstruct.initial_bg(rj)
     outs, thin = _run(s, dev, p1, rj, seed, arith, proposal, pos_len, bg0, extra=grids)
     km = map_kmeans(outs["pos_trace"], thin, outs["n_entries"], outs["map_n"])
@@ -115,6 +136,10 @@ def analyze(dev: dict, rj, seed: int = 1, arith: str = "fast", proposal: str = "
             if dev.get("psf_sigma") is not None:
                 sub["psf_sigma"] = dev["psf_sigma"].index_select(0, idx)
             sub["side_max"] = dev.get("side_max", 0)
+            if dev.get("sampled_psf") is not None:
+                sub["sampled_psf"], sub["n_psf"] = dev["sampled_psf"], dev["n_psf"]
+                if dev.get("psf_slot") is not None:
+                    sub["psf_slot"] = dev["psf_slot"].index_select(0, idx)
             m = int(idx.numel())
             kk = K.index_select(0, idx)
             ixy = torch.zeros((m, 3, 32), dtype=torch.float32, device="cuda")
@@ -126,7 +151,7 @@ def analyze(dev: dict, rj, seed: int = 1, arith: str = "fast", proposal: str = "
             sub["init_n"] = kk.contiguous()
             sub["init_ixy"] = ixy
             sub["init_bg"] = sel[:, 2].contiguous()
-            p2 = rjstruct.refine_params(rj)
+            p2 = _set_psf_size(rjstruct.refine_params(rj), psf_shape)
             outs2, thin2 = _run(s, sub, p2, rj, seed + 7919, arith, "reference", pos_len, bg0)
             rs = refine_stats(outs2["pos_trace"], thin2, outs2["n_entries"])
             refined[idx.cpu().numpy()] = rs.cpu().numpy()

@@ -95,7 +95,11 @@ def match(found_x, found_y, true_x, true_y, radius: float = 1.0):
 
 
 def analyze_frames(frames: np.ndarray, rj, box: int = 10, overlap: int = 3, proposal: str = "learned",
-                   net=None, seed: int = 1, pos_len: int = 200, grids: bool = True) -> dict:
+                   net=None, seed: int = 1, pos_len: int = 200, grids: bool = True, sampled_psf=None) -> dict:
+    """Frames (Y, X, Z) -> sub-regions -> sampler + MAP + refinement ->
+    stitched posterior image and global emitter list.  sampled_psf: None
+    (Gaussian PSF), one 4-D sampled PSF, or one per sub-region position
+    (psf.find_psf_sma's list), selects OptModel 1 (analyzeROIs.m:142-146)."""
     import torch
     Y, X, Z = frames.shape
     T = box + 2 * overlap
@@ -130,7 +134,15 @@ def analyze_frames(frames: np.ndarray, rj, box: int = 10, overlap: int = 3, prop
                  "grid_stride": Tz * Tz, "grid_ld": Tz,
                  "grid_slot": (sr["roi_ind"] - 1).contiguous()}
     t = time.perf_counter()
-    res = mapfit.analyze(dev, rj, seed=seed, proposal=proposal, pos_len=pos_len, grids=extra)
+    psf_kw = {}
+    if sampled_psf is not None:
+        stack = np.asarray(sampled_psf, np.float32)
+        psf_kw["sampled_psf"] = stack
+        if stack.ndim == 5:
+            if stack.shape[0] != per:
+                raise ValueError("one sampled PSF per sub-region position is needed")
+            psf_kw["psf_slot"] = (sr["roi_ind"] - 1).to(torch.int32).contiguous()
+    res = mapfit.analyze(dev, rj, seed=seed, proposal=proposal, pos_len=pos_len, grids=extra, **psf_kw)
     _sync()
     timing["sampler_map_refine"] = time.perf_counter() - t
     out = {"n_subregions": n, "timing": timing}

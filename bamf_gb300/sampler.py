@@ -76,7 +76,8 @@ class RoiBatch(C.Structure):
                 ("psf_sigma", C.c_void_p), ("scmos", C.c_void_p), ("init_n", C.c_void_p),
                 ("init_bg", C.c_void_p), ("init_ixy", C.c_void_p), ("bg0", C.c_float),
                 ("proposal", C.c_int32), ("birth_cdf", C.c_void_p), ("birth_sub", C.c_void_p),
-                ("opt_model", C.c_int32), ("sampled_psf", C.c_void_p)]
+                ("opt_model", C.c_int32), ("sampled_psf", C.c_void_p), ("n_psf", C.c_int32),
+                ("psf_slot", C.c_void_p)]
 
 
 class BatchResults(C.Structure):
@@ -222,6 +223,18 @@ def rjmcmc(Data, RJ: RJStruct, Ysize: int, Xsize: int, DriftY: float = 0.0, Drif
     return acc, stat, pg, pb, prop
 
 
+def pack_psfs(sampled_psf, params: abi.McmcParams):
+    """One sampled PSF (P0, P1, P2, P3) or a stack (n, P0, P1, P2, P3) ->
+    (float32 array of the PSFs one after another, each in MATLAB order, n)."""
+    a = np.asarray(sampled_psf, np.float32)
+    if a.ndim == 4:
+        a = a[None]
+    if a.ndim != 5 or tuple(a.shape[1:]) != tuple(params.PSFsize):
+        raise ValueError("params.PSFsize must be the sampled PSF's shape")
+    flat = np.concatenate([np.ravel(x, order="F") for x in a])
+    return np.ascontiguousarray(flat), int(a.shape[0])
+
+
 class BatchGraph:
     """A captured batch (Sampler.capture); keeps its workspace and tensors alive."""
 
@@ -305,10 +318,11 @@ class Sampler:
         b.n_rois = int(dev["xsize"].numel())
         b.side_max = int(dev.get("side_max", 0))
         for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos", "init_n", "init_bg",
-                  "init_ixy", "birth_cdf", "birth_sub", "sampled_psf"):
+                  "init_ixy", "birth_cdf", "birth_sub", "sampled_psf", "psf_slot"):
             t = dev.get(k)
             setattr(b, k, t.data_ptr() if t is not None else None)
         b.opt_model = 1 if dev.get("sampled_psf") is not None else 0
+        b.n_psf = int(dev.get("n_psf", 1))
         b.bg0 = float(bg0)
         b.proposal = PROPOSAL[proposal]
         res = BatchResults()
@@ -340,10 +354,11 @@ class Sampler:
         b = RoiBatch()
         b.n_rois = int(dev["xsize"].numel())
         b.side_max = int(dev.get("side_max", 0))
-        for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos", "sampled_psf"):
+        for k in ("data", "offsets", "xsize", "ysize", "psf_sigma", "scmos", "sampled_psf", "psf_slot"):
             t = dev.get(k)
             setattr(b, k, t.data_ptr() if t is not None else None)
         b.opt_model = 1 if dev.get("sampled_psf") is not None else 0
+        b.n_psf = int(dev.get("n_psf", 1))
         b.bg0 = float(bg0)
         L = self._L
         _check(L, L.bamf_autotune(self._ws, C.byref(b), C.byref(params), C.byref(pr), ARITH[arith], int(jumps),
@@ -354,11 +369,13 @@ class Sampler:
 
     def run_host(self, batch, params: abi.McmcParams, off, sig, back, seed: int,
                  arith: str = "fast", bg0: float = 0.0, init=None, proposal: str = "reference",
-                 birth=None, trace_len: int = 0, sampled_psf: np.ndarray | None = None) -> dict:
+                 birth=None, trace_len: int = 0, sampled_psf: np.ndarray | None = None,
+                 psf_slot: np.ndarray | None = None) -> dict:
         """batch: synth.RoiBatch (host numpy); returns numpy results.
         birth: (cdf, sub) host arrays of the LEARNED proposal; trace_len > 0
         adds the n_trace / x_trace outputs; sampled_psf: a 4-D array of shape
-        params.PSFsize selects the sampled-PSF model (OptModel 1)."""
+        params.PSFsize, or a stack (n_psf, *PSFsize) with psf_slot[k] naming
+        ROI k's, selects the sampled-PSF model (OptModel 1)."""
         pr, keep = self._priors(off, sig, back)
         n = batch.n
         b = RoiBatch()
@@ -377,9 +394,9 @@ class Sampler:
             arrays["birth_cdf"] = np.ascontiguousarray(birth[0], np.float32)
             arrays["birth_sub"] = np.ascontiguousarray(birth[1], np.float32)
         if sampled_psf is not None:
-            if tuple(params.PSFsize) != tuple(np.shape(sampled_psf)):
-                raise ValueError("params.PSFsize must be the sampled PSF's shape")
-            arrays["sampled_psf"] = np.ascontiguousarray(np.asarray(sampled_psf, np.float32).ravel(order="F"))
+            arrays["sampled_psf"], b.n_psf = pack_psfs(sampled_psf, params)
+            if psf_slot is not None:
+                arrays["psf_slot"] = np.ascontiguousarray(psf_slot, np.int32)
             b.opt_model = 1
         for k, a in arrays.items():
             setattr(b, k, a.ctypes.data)

@@ -282,10 +282,16 @@ typedef struct bamf_roi_batch {
      *      pixel P0/2 and blends the sub-position planes floor(P3 * frac)
      *      and the next one bilinearly; a flat index outside the array reads
      *      its last element, as the reference does.
-     * sampled_psf is a device pointer for the device entry points, a host
-     * pointer for bamf_rjmcmc_batch_host. */
+     * Several PSFs (analyzeROIs.m:142-146 uses one per sub-region position):
+     * n_psf arrays one after another in sampled_psf, and psf_slot[k] the
+     * one ROI k uses (NULL: all use the first; n_psf 0 counts as 1; a slot
+     * outside [0, n_psf) sets that ROI's status to BAMF_ERR_INVALID_ARG).
+     * sampled_psf and psf_slot are device pointers for the device entry
+     * points, host pointers for bamf_rjmcmc_batch_host. */
     int32_t opt_model;
     const float *sampled_psf;
+    int32_t n_psf;
+    const int32_t *psf_slot;
 } bamf_roi_batch;
 
 #define BAMF_PROPOSAL_REFERENCE 0
