@@ -38,8 +38,8 @@ cudaError_t launch_rjmcmc_exact(const SamplerConsts &K, const SamplerBatch &B, i
                                 int blocks, int warps_per_block, cudaStream_t stream);
 cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, int side_max,
                                int blocks, int warps_per_block, cudaStream_t stream);
-int blocks_per_sm_exact(int side_max, int warps_per_block);
-int blocks_per_sm_fast(int side_max, int warps_per_block);
+int blocks_per_sm_exact(int side_max, int warps_per_block, int opt_model);
+int blocks_per_sm_fast(int side_max, int warps_per_block, int opt_model);
 }  // namespace bamf
 
 /* defined in api_sampler.cu */
@@ -293,7 +293,8 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         Bc.queue = (int32_t *)S + c;
         Bc.cls = c;
         Bc.side_max = std::min(class_side(c), side_max);
-        int per_sm = exact ? blocks_per_sm_exact(Bc.side_max, wpb) : blocks_per_sm_fast(Bc.side_max, wpb);
+        int per_sm = exact ? blocks_per_sm_exact(Bc.side_max, wpb, K.opt_model)
+                           : blocks_per_sm_fast(Bc.side_max, wpb, K.opt_model);
         if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
         int blocks = std::min((n + wpb - 1) / wpb, per_sm * sms);
         cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, s)

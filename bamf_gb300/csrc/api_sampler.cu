@@ -19,8 +19,8 @@ cudaError_t launch_rjmcmc_exact(const SamplerConsts &K, const SamplerBatch &B, i
                                 int blocks, int warps_per_block, cudaStream_t stream);
 cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, int side_max,
                                int blocks, int warps_per_block, cudaStream_t stream);
-int blocks_per_sm_exact(int side_max, int warps_per_block);
-int blocks_per_sm_fast(int side_max, int warps_per_block);
+int blocks_per_sm_exact(int side_max, int warps_per_block, int opt_model);
+int blocks_per_sm_fast(int side_max, int warps_per_block, int opt_model);
 }  // namespace bamf
 
 using namespace bamf;
@@ -255,7 +255,7 @@ static int sm_count()
  * the work queue until it runs dry. */
 /* Warps per CTA for a class: the choice among 4, 2, 1 that keeps the most
  * warps resident per SM (shared memory per warp grows with the ROI side). */
-static int pick_wpb(bool exact, int side_max, int *per_sm_out)
+static int pick_wpb(bool exact, int side_max, int opt_model, int *per_sm_out)
 {
     /* fast arithmetic: CTAs of up to one move-stream group (8 chains);
      * exact: the per-warp kernel's 4 */
@@ -263,7 +263,8 @@ static int pick_wpb(bool exact, int side_max, int *per_sm_out)
     const int cand_f[3] = {8, 4, 2}, cand_e[3] = {4, 2, 1};
     const int *cand = exact ? cand_e : cand_f;
     for (int i = 0; i < 3; ++i) {
-        int per = exact ? blocks_per_sm_exact(side_max, cand[i]) : blocks_per_sm_fast(side_max, cand[i]);
+        int per = exact ? blocks_per_sm_exact(side_max, cand[i], opt_model)
+                        : blocks_per_sm_fast(side_max, cand[i], opt_model);
         if (per * cand[i] > best_w) {
             best_w = per * cand[i];
             best_wpb = cand[i];
@@ -302,11 +303,12 @@ static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, Samp
             Bc.side_max = std::min(class_side(c), B.side_max);
         }
         int per_sm = 0;
-        int wpb = pick_wpb(exact, Bc.side_max, &per_sm);
+        int wpb = pick_wpb(exact, Bc.side_max, K.opt_model, &per_sm);
         if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
         const int tw = ws->tuned_wpb[exact ? 0 : 1][c];
         if (tw > 0) {
-            int pt = exact ? blocks_per_sm_exact(Bc.side_max, tw) : blocks_per_sm_fast(Bc.side_max, tw);
+            int pt = exact ? blocks_per_sm_exact(Bc.side_max, tw, K.opt_model)
+                           : blocks_per_sm_fast(Bc.side_max, tw, K.opt_model);
             if (pt > 0) {
                 wpb = tw;
                 per_sm = pt;
@@ -687,7 +689,8 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
         int best = 0;
         for (int k = 0; k < ncand && !res; ++k) {
             int wpb = cand[k];
-            int per = exact ? blocks_per_sm_exact(Bc.side_max, wpb) : blocks_per_sm_fast(Bc.side_max, wpb);
+            int per = exact ? blocks_per_sm_exact(Bc.side_max, wpb, K.opt_model)
+                            : blocks_per_sm_fast(Bc.side_max, wpb, K.opt_model);
             if (per < 1) continue;
             int blocks = std::min((m + wpb - 1) / wpb, per * sms);
             for (int rep = 0; rep < 2 && !res; ++rep) { /* the first launch warms up */

@@ -11,24 +11,23 @@ cudaError_t launch_rjmcmc_exact(const SamplerConsts &K, const SamplerBatch &B, i
                                 int blocks, int warps_per_block, cudaStream_t stream)
 {
     size_t smem = (size_t)warp_smem_floats(side_max, true) * sizeof(float) * warps_per_block;
-    cudaError_t e = cudaFuncSetAttribute(rjmcmc_kernel<true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = K.opt_model == 1 ? rjmcmc_kernel<true, true> : rjmcmc_kernel<true, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    rjmcmc_kernel<true><<<blocks, 32 * warps_per_block, smem, stream>>>(K, B);
+    kern<<<blocks, 32 * warps_per_block, smem, stream>>>(K, B);
     return cudaGetLastError();
 }
 
-int blocks_per_sm_exact(int side_max, int warps_per_block)
+int blocks_per_sm_exact(int side_max, int warps_per_block, int opt_model)
 {
     size_t smem = (size_t)warp_smem_floats(side_max, true) * sizeof(float) * warps_per_block;
-    if (cudaFuncSetAttribute(rjmcmc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess) {
+    auto kern = opt_model == 1 ? rjmcmc_kernel<true, true> : rjmcmc_kernel<true, false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rjmcmc_kernel<true>, 32 * warps_per_block,
-                                                      smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, 32 * warps_per_block, smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }

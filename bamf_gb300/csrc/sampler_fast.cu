@@ -15,25 +15,26 @@ cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, in
 {
     if (warps_per_block < 1 || BAMF_SYNC_GROUP % warps_per_block != 0) return cudaErrorInvalidValue;
     size_t smem = (size_t)warp_smem_floats(side_max, false) * sizeof(float) * warps_per_block;
-    cudaError_t e = cudaFuncSetAttribute(rjmcmc_kernel_sync<0>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    /* one instantiation per likelihood model, so the Gaussian path carries
+     * no sampled-PSF code */
+    auto kern = K.opt_model == 1 ? rjmcmc_kernel_sync<true> : rjmcmc_kernel_sync<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     (void)K.sync_moves; /* always move-synchronous in fast arithmetic */
-    rjmcmc_kernel_sync<0><<<blocks, 32 * warps_per_block, smem, stream>>>(K, B);
+    kern<<<blocks, 32 * warps_per_block, smem, stream>>>(K, B);
     return cudaGetLastError();
 }
 
-int blocks_per_sm_fast(int side_max, int warps_per_block)
+int blocks_per_sm_fast(int side_max, int warps_per_block, int opt_model)
 {
     size_t smem = (size_t)warp_smem_floats(side_max, false) * sizeof(float) * warps_per_block;
-    if (cudaFuncSetAttribute(rjmcmc_kernel_sync<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess) {
+    auto kern = opt_model == 1 ? rjmcmc_kernel_sync<true> : rjmcmc_kernel_sync<false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rjmcmc_kernel_sync<0>, 32 * warps_per_block,
-                                                      smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, 32 * warps_per_block, smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }

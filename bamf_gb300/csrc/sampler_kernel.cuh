@@ -257,7 +257,7 @@ static __device__ __noinline__ float normpdf_f(float x, float u, float s)
     return 1.0f / (sq2pi * s) * SMath<EXACT>::exp_(-d * d / (2.0f * s * s));
 }
 
-template <bool EXACT>
+template <bool EXACT, bool NUM>
 struct ChainWarp {
     typedef SMath<EXACT> MT;
     const SamplerConsts *K;
@@ -781,7 +781,7 @@ struct ChainWarp {
     {
         n_llr++;
         if (EXACT) {
-            if (psf) model_num(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
+            if constexpr (NUM) model_num(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
             else model_full(tn, tI, tX, tY, tBG, tABG, tBBG, Mt, NX, NY);
             for (int p = lane; p < npix; p += 32)
                 E[p] = M[p] - Mt[p] + D[p] * MT::log_(Mt[p] / M[p]);
@@ -798,7 +798,7 @@ struct ChainWarp {
             const float LN2 = 0.69314718f;
             int na = __popc(a_dirty), nt = __popc(t_dirty);
             float acc = 0.0f;
-            if (psf) {
+            if constexpr (NUM) {
                 if (na <= FAST_ROWS && nt <= FAST_ROWS) {
                     acc = llr_num_fast(na, nt);
                 } else {
@@ -809,48 +809,50 @@ struct ChainWarp {
                         acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - (mt - M[p]);
                     }
                 }
-            } else if (na <= FAST_ROWS && nt <= FAST_ROWS) {
-                stencil_rows(na, nt);
-                /* lane -> row y = lane mod Y of column x0 + lane / Y; a pass
-                 * covers 32 / Y columns.  The model change of a pixel is
-                 * bg delta + sum_q w_q(y) SX_q[x] over the changed rows q
-                 * (old rows with weight -SYo, new with +SYn); each lane
-                 * holds its first four weights in registers. */
-                const int yl = lane % Y, xo = lane / Y, R = 32 / Y;
-                const int nr = na + nt;
-                float w[4];
-                const float *sx[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    bool old = q < na;
-                    int qq = old ? q : q - na;
-                    w[q] = q < nr ? (old ? -SYo[qq * Y + yl] : SYn[qq * Y + yl]) : 0.0f;
-                    sx[q] = old ? SXo + qq * X : SXn + qq * X;
-                }
-                const float base = (tBG - aBG) + (tBBG - aBBG) * (float)yl, dABG = tABG - aABG;
-                if (xo < R) {
-#pragma unroll 1
-                    for (int xx = xo; xx < X; xx += R) {
-                        float d = base + dABG * (float)xx;
-                        if (nr > 0) d += w[0] * sx[0][xx];
-                        if (nr > 1) d += w[1] * sx[1][xx];
-                        if (nr > 2) d += w[2] * sx[2][xx];
-                        if (nr > 3) d += w[3] * sx[3][xx];
-                        for (int q = 4; q < nr; ++q)
-                            d += q < na ? -SXo[q * X + xx] * SYo[q * Y + yl]
-                                        : SXn[(q - na) * X + xx] * SYn[(q - na) * Y + yl];
-                        int p = yl + Y * xx;
-                        float mt = M[p] + d;
-                        Mt[p] = mt;
-                        acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - d;
-                    }
-                }
             } else {
-                model_stream(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
+                if (na <= FAST_ROWS && nt <= FAST_ROWS) {
+                    stencil_rows(na, nt);
+                    /* lane -> row y = lane mod Y of column x0 + lane / Y; a pass
+                     * covers 32 / Y columns.  The model change of a pixel is
+                     * bg delta + sum_q w_q(y) SX_q[x] over the changed rows q
+                     * (old rows with weight -SYo, new with +SYn); each lane
+                     * holds its first four weights in registers. */
+                    const int yl = lane % Y, xo = lane / Y, R = 32 / Y;
+                    const int nr = na + nt;
+                    float w[4];
+                    const float *sx[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        bool old = q < na;
+                        int qq = old ? q : q - na;
+                        w[q] = q < nr ? (old ? -SYo[qq * Y + yl] : SYn[qq * Y + yl]) : 0.0f;
+                        sx[q] = old ? SXo + qq * X : SXn + qq * X;
+                    }
+                    const float base = (tBG - aBG) + (tBBG - aBBG) * (float)yl, dABG = tABG - aABG;
+                    if (xo < R) {
 #pragma unroll 1
-                for (int p = lane; p < npix; p += 32) {
-                    float mt = Mt[p];
-                    acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - (mt - M[p]);
+                        for (int xx = xo; xx < X; xx += R) {
+                            float d = base + dABG * (float)xx;
+                            if (nr > 0) d += w[0] * sx[0][xx];
+                            if (nr > 1) d += w[1] * sx[1][xx];
+                            if (nr > 2) d += w[2] * sx[2][xx];
+                            if (nr > 3) d += w[3] * sx[3][xx];
+                            for (int q = 4; q < nr; ++q)
+                                d += q < na ? -SXo[q * X + xx] * SYo[q * Y + yl]
+                                            : SXn[(q - na) * X + xx] * SYn[(q - na) * Y + yl];
+                            int p = yl + Y * xx;
+                            float mt = M[p] + d;
+                            Mt[p] = mt;
+                            acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - d;
+                        }
+                    }
+                } else {
+                    model_stream(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
+#pragma unroll 1
+                    for (int p = lane; p < npix; p += 32) {
+                        float mt = Mt[p];
+                        acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - (mt - M[p]);
+                    }
                 }
             }
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(BAMF_FULL, acc, o);
@@ -886,10 +888,10 @@ struct ChainWarp {
     __device__ __forceinline__ void rebuild_model()
     {
         if (EXACT) {
-            if (psf) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
+            if constexpr (NUM) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
             else model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NX, NY);
         } else {
-            if (psf) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
+            if constexpr (NUM) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
             else model_stream(an, aI, aX, aY, aBG, aABG, aBBG, M);
 #pragma unroll 1
             for (int p = lane; p < npix; p += 32) logM[p] = __log2f(M[p]);
@@ -1731,8 +1733,8 @@ struct ChainWarp {
 /* Loads ROI `roi` into a warp's carve-out and sets up its chain (the
  * set-up of cRJMCMC.cpp:103-148).  Returns false, with the ROI's status set,
  * when the ROI does not fit the launch. */
-template <bool EXACT>
-__device__ __forceinline__ bool begin_roi(ChainWarp<EXACT> &w, const SamplerConsts *Kp, const SamplerBatch &Bt,
+template <bool EXACT, bool NUM>
+__device__ __forceinline__ bool begin_roi(ChainWarp<EXACT, NUM> &w, const SamplerConsts *Kp, const SamplerBatch &Bt,
                                           float *sw, int roi)
 {
     const int lane = w.lane;
@@ -1791,7 +1793,7 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT> &w, const SamplerCons
     float s = Bt.psf_sigma ? Bt.psf_sigma[roi] : Kp->p.PSFsigma;
     w.sigma = s;
     w.Cst = 1.0f / (s * sqrtf(2.0f));
-    if (Kp->opt_model == 1) {
+    if (NUM) {
         const int32_t *P = Kp->p.PSFsize;
         w.pn0 = P[0];
         w.pn01 = P[0] * P[1];
@@ -1840,8 +1842,8 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT> &w, const SamplerCons
 }
 
 /* Writes the chain's per-ROI results. */
-template <bool EXACT>
-__device__ __forceinline__ void end_roi(ChainWarp<EXACT> &w, const SamplerBatch &Bt)
+template <bool EXACT, bool NUM>
+__device__ __forceinline__ void end_roi(ChainWarp<EXACT, NUM> &w, const SamplerBatch &Bt)
 {
     const int lane = w.lane, roi = w.roi;
     if (Bt.final_n && lane == 0) Bt.final_n[roi] = w.an;
@@ -1876,7 +1878,7 @@ __device__ __forceinline__ void end_roi(ChainWarp<EXACT> &w, const SamplerBatch 
 
 /* Persistent sampler: each warp pulls ROI ids from the work queue and runs
  * their chains one after another. */
-template <bool EXACT>
+template <bool EXACT, bool NUM>
 __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ SamplerConsts Kc,
                                                      const __grid_constant__ SamplerBatch Bc)
 {
@@ -1885,7 +1887,7 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ 
     int warp = threadIdx.x >> 5;
     int lane = threadIdx.x & 31;
     float *sw = smem_raw + (size_t)warp * warp_smem_floats(Bt.side_max, EXACT);
-    ChainWarp<EXACT> w;
+    ChainWarp<EXACT, NUM> w;
     w.K = &Kc;
     w.B = &Bc;
     w.lane = lane;
@@ -1910,7 +1912,7 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ 
  * ROI per warp at a time and its warps run their chains in lockstep, one
  * barrier per jump, with the move type and jump sub-branch shared across the
  * CTA (run_chain_sync). */
-template <int UNUSED>
+template <bool NUM>
 __global__ void __launch_bounds__(32 * BAMF_SYNC_GROUP, 2) rjmcmc_kernel_sync(const __grid_constant__ SamplerConsts Kc,
                                                           const __grid_constant__ SamplerBatch Bc)
 {
@@ -1921,7 +1923,7 @@ __global__ void __launch_bounds__(32 * BAMF_SYNC_GROUP, 2) rjmcmc_kernel_sync(co
     int warp = threadIdx.x >> 5;
     int lane = threadIdx.x & 31;
     float *sw = smem_raw + (size_t)warp * warp_smem_floats(Bt.side_max, false);
-    ChainWarp<false> w;
+    ChainWarp<false, NUM> w;
     w.K = &Kc;
     w.B = &Bc;
     w.lane = lane;
