@@ -28,7 +28,8 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-con
 # The exact sampler must round every float operation as the reference does;
 # the fast sampler promises no bitwise parity, and approximate division and
 # square root shrink its code (the chain loop is instruction-cache bound).
-PER_FILE = {"sampler_exact.cu": ["-fmad=false"], "sampler_fast.cu": ["-use_fast_math"]}
+PER_FILE = {"sampler_exact.cu": ["-fmad=false"], "sampler_exact_num.cu": ["-fmad=false"],
+            "sampler_fast.cu": ["-use_fast_math"], "sampler_fast_num.cu": ["-use_fast_math"]}
 
 
 def nvcc() -> str:

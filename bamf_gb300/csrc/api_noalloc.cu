@@ -32,15 +32,7 @@
 
 #include "bamf.h"
 #include "sampler_common.h"
-
-namespace bamf {
-cudaError_t launch_rjmcmc_exact(const SamplerConsts &K, const SamplerBatch &B, int side_max,
-                                int blocks, int warps_per_block, cudaStream_t stream);
-cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, int side_max,
-                               int blocks, int warps_per_block, cudaStream_t stream);
-int blocks_per_sm_exact(int side_max, int warps_per_block, int opt_model);
-int blocks_per_sm_fast(int side_max, int warps_per_block, int opt_model);
-}  // namespace bamf
+#include "sampler_launch.h"
 
 /* defined in api_sampler.cu */
 bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcmc_params *p, int arith,
@@ -285,7 +277,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     if (cudaGetLastError() != cudaSuccess) return BAMF_ERR_CUDA;
 
     const bool exact = arith == BAMF_ARITH_EXACT;
-    const int wpb = 4, sms = sm_count();
+    const int sms = sm_count();
     for (int c = BAMF_N_CLASSES - 1; c >= 0; --c) {
         int lo = c == 0 ? 1 : class_side(c - 1) + 1;
         if (lo > side_max) continue;
@@ -293,12 +285,13 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         Bc.queue = (int32_t *)S + c;
         Bc.cls = c;
         Bc.side_max = std::min(class_side(c), side_max);
+        int wpb = 4, mc = 2;
         int per_sm = exact ? blocks_per_sm_exact(Bc.side_max, wpb, K.opt_model)
-                           : blocks_per_sm_fast(Bc.side_max, wpb, K.opt_model);
+                           : best_fast_shape(Bc.side_max, K.opt_model, &wpb, &mc);
         if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
         int blocks = std::min((n + wpb - 1) / wpb, per_sm * sms);
         cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, s)
-                              : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, s);
+                              : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, mc, s);
         if (e != cudaSuccess) return BAMF_ERR_CUDA;
     }
     if (want_map) {

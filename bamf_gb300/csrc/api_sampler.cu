@@ -13,15 +13,7 @@
 
 #include "bamf.h"
 #include "sampler_common.h"
-
-namespace bamf {
-cudaError_t launch_rjmcmc_exact(const SamplerConsts &K, const SamplerBatch &B, int side_max,
-                                int blocks, int warps_per_block, cudaStream_t stream);
-cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, int side_max,
-                               int blocks, int warps_per_block, cudaStream_t stream);
-int blocks_per_sm_exact(int side_max, int warps_per_block, int opt_model);
-int blocks_per_sm_fast(int side_max, int warps_per_block, int opt_model);
-}  // namespace bamf
+#include "sampler_launch.h"
 
 using namespace bamf;
 
@@ -148,9 +140,11 @@ struct bamf_workspace {
         }
         return cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming) == cudaSuccess;
     }
-    /* CTA shape (chains per CTA) per arithmetic and size class chosen by
+    /* CTA shape (chains per CTA, and for fast arithmetic the register
+     * budget in CTAs per SM) per arithmetic and size class chosen by
      * bamf_autotune; 0 = not tuned (occupancy rule) */
     int tuned_wpb[2][BAMF_N_CLASSES] = {};
+    int tuned_min_ctas[BAMF_N_CLASSES] = {};
     DevBuf tune_range; /* class ranges clipped to the tuning sample    */
     std::vector<float> tables_host; /* what `tables` holds, to skip re-uploads */
     DevStat tables_dev[3] = {};
@@ -253,18 +247,15 @@ static int sm_count()
 /* Launch the chains of batch B as a persistent grid: as many CTAs as fit
  * on the GPU at once (or fewer for small batches); warps pull ROI ids from
  * the work queue until it runs dry. */
-/* Warps per CTA for a class: the choice among 4, 2, 1 that keeps the most
- * warps resident per SM (shared memory per warp grows with the ROI side). */
-static int pick_wpb(bool exact, int side_max, int opt_model, int *per_sm_out)
+/* Warps per CTA for an exact launch: the choice among 4, 2, 1 that keeps
+ * the most warps resident per SM (shared memory per warp grows with the ROI
+ * side). */
+static int pick_wpb_exact(int side_max, int opt_model, int *per_sm_out)
 {
-    /* fast arithmetic: CTAs of up to one move-stream group (8 chains);
-     * exact: the per-warp kernel's 4 */
-    int best_w = 0, best_wpb = exact ? 4 : 8, best_per = 0;
-    const int cand_f[3] = {8, 4, 2}, cand_e[3] = {4, 2, 1};
-    const int *cand = exact ? cand_e : cand_f;
+    int best_w = 0, best_wpb = 4, best_per = 0;
+    const int cand[3] = {4, 2, 1};
     for (int i = 0; i < 3; ++i) {
-        int per = exact ? blocks_per_sm_exact(side_max, cand[i], opt_model)
-                        : blocks_per_sm_fast(side_max, cand[i], opt_model);
+        int per = blocks_per_sm_exact(side_max, cand[i], opt_model);
         if (per * cand[i] > best_w) {
             best_w = per * cand[i];
             best_wpb = cand[i];
@@ -302,15 +293,17 @@ static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, Samp
             if (lo > B.side_max) continue;                /* no ROI of the batch is that large */
             Bc.side_max = std::min(class_side(c), B.side_max);
         }
-        int per_sm = 0;
-        int wpb = pick_wpb(exact, Bc.side_max, K.opt_model, &per_sm);
+        int per_sm = 0, wpb = 0, mc = 2;
+        if (exact) wpb = pick_wpb_exact(Bc.side_max, K.opt_model, &per_sm);
+        else per_sm = best_fast_shape(Bc.side_max, K.opt_model, &wpb, &mc);
         if (per_sm < 1) return BAMF_ERR_TOO_LARGE;
-        const int tw = ws->tuned_wpb[exact ? 0 : 1][c];
+        const int tw = ws->tuned_wpb[exact ? 0 : 1][c], tm = exact ? 0 : ws->tuned_min_ctas[c];
         if (tw > 0) {
             int pt = exact ? blocks_per_sm_exact(Bc.side_max, tw, K.opt_model)
-                           : blocks_per_sm_fast(Bc.side_max, tw, K.opt_model);
+                           : blocks_per_sm_fast(Bc.side_max, tw, tm, K.opt_model);
             if (pt > 0) {
                 wpb = tw;
+                mc = tm;
                 per_sm = pt;
             }
         }
@@ -323,7 +316,7 @@ static bamf_status launch_batch(bamf_workspace *ws, const SamplerConsts &K, Samp
             CU(cudaStreamWaitEvent(cs, ws->fork_ev, 0));
         }
         cudaError_t e = exact ? launch_rjmcmc_exact(Kl, Bc, Bc.side_max, blocks, wpb, cs)
-                              : launch_rjmcmc_fast(Kl, Bc, Bc.side_max, blocks, wpb, cs);
+                              : launch_rjmcmc_fast(Kl, Bc, Bc.side_max, blocks, wpb, mc, cs);
         if (e != cudaSuccess) return cuda_fail(e, "rjmcmc kernel launch");
         if (fork) {
             CU(cudaEventRecord(ws->join_ev[c], cs));
@@ -665,33 +658,40 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
     const int sms = sm_count();
-    const int cand_f[4] = {8, 4, 2, 1}, cand_e[3] = {4, 2, 1};
-    const int *cand = exact ? cand_e : cand_f;
-    const int ncand = exact ? 3 : 4;
+    /* (chains per CTA, register budget in CTAs per SM) */
+    const int cand_f[8][2] = {{8, 2}, {4, 2}, {2, 2}, {1, 2}, {8, 3}, {4, 3}, {2, 3}, {1, 3}};
+    const int cand_e[3][2] = {{4, 0}, {2, 0}, {1, 0}};
+    const int(*cand)[2] = exact ? cand_e : cand_f;
+    const int ncand = exact ? 3 : 8;
     bamf_status res = BAMF_OK;
     for (int c = 0; c < BAMF_N_CLASSES && !res; ++c) {
         int lo = cr[2 * c], hi = cr[2 * c + 1];
         if (hi <= lo) continue;
-        int32_t clip[2 * BAMF_N_CLASSES] = {};
-        clip[2 * c] = lo;
-        clip[2 * c + 1] = std::min(hi, lo + sample);
-        int m = clip[2 * c + 1] - lo;
-        if (cudaMemcpyAsync(ws->tune_range.p, clip, sizeof clip, cudaMemcpyHostToDevice, s) != cudaSuccess) {
-            res = BAMF_ERR_CUDA;
-            break;
-        }
         SamplerBatch Bc = B;
         Bc.class_range = (const int32_t *)ws->tune_range.p;
         Bc.cls = c;
         Bc.queue = (int32_t *)ws->queue.p + c;
         Bc.side_max = std::min(class_side(c), side_max);
         float best_ms = 0.0f;
-        int best = 0;
+        int best = 0, best_mc = 0;
         for (int k = 0; k < ncand && !res; ++k) {
-            int wpb = cand[k];
+            const int wpb = cand[k][0], mc = cand[k][1];
             int per = exact ? blocks_per_sm_exact(Bc.side_max, wpb, K.opt_model)
-                            : blocks_per_sm_fast(Bc.side_max, wpb, K.opt_model);
+                            : blocks_per_sm_fast(Bc.side_max, wpb, mc, K.opt_model);
             if (per < 1) continue;
+            /* a whole number of rounds of this shape's resident chains (at
+             * least one), so that no shape is timed with a partial last
+             * round; compared per ROI */
+            const int resident = per * sms * wpb;
+            int m = std::max(resident, (sample / resident) * resident);
+            m = std::min(m, hi - lo);
+            int32_t clip[2 * BAMF_N_CLASSES] = {};
+            clip[2 * c] = lo;
+            clip[2 * c + 1] = lo + m;
+            if (cudaMemcpyAsync(ws->tune_range.p, clip, sizeof clip, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+                res = BAMF_ERR_CUDA;
+                break;
+            }
             int blocks = std::min((m + wpb - 1) / wpb, per * sms);
             for (int rep = 0; rep < 2 && !res; ++rep) { /* the first launch warms up */
                 if (cudaMemsetAsync(Bc.queue, 0, sizeof(int32_t), s) != cudaSuccess ||
@@ -700,24 +700,37 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
                     break;
                 }
                 cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, s)
-                                      : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, s);
+                                      : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, mc, s);
                 float ms = 0.0f;
                 if (e != cudaSuccess || cudaEventRecord(e1, s) != cudaSuccess ||
                     cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
                     res = cuda_fail(e != cudaSuccess ? e : cudaGetLastError(), "autotune launch");
                     break;
                 }
+                ms /= (float)m;
                 if (rep == 1 && (best == 0 || ms < best_ms)) {
                     best_ms = ms;
                     best = wpb;
+                    best_mc = mc;
                 }
             }
         }
         ws->tuned_wpb[exact ? 0 : 1][c] = best;
+        if (!exact) ws->tuned_min_ctas[c] = best_mc;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return res;
+}
+
+extern "C" bamf_status bamf_autotune_shapes(const bamf_workspace *ws, int arith, int32_t *chains_per_cta,
+                                            int32_t *ctas_per_sm_budget)
+{
+    bamf_status r = bamf_autotune_result(ws, arith, chains_per_cta);
+    if (r || !ctas_per_sm_budget) return r ? r : BAMF_ERR_INVALID_ARG;
+    for (int c = 0; c < BAMF_N_CLASSES; ++c)
+        ctas_per_sm_budget[c] = arith == BAMF_ARITH_EXACT ? 4 * (ws->tuned_wpb[0][c] > 0) : ws->tuned_min_ctas[c];
+    return BAMF_OK;
 }
 
 extern "C" bamf_status bamf_autotune_result(const bamf_workspace *ws, int arith, int32_t *chains_per_cta)

@@ -1,44 +1,66 @@
 /*
- * sampler_fast.cu - the fast sampler: hardware SFU math, incremental model
- * updates, warp-tree reductions, and move-synchronous CTAs (the warps of a
- * CTA draw the move type and jump sub-branch from one shared stream and meet
- * at a barrier before each jump, so an SM's warps run the same code and the
- * instruction cache stops thrashing; each chain's move choice stays i.i.d.
- * with the configured probabilities and independent of its state).
+ * sampler_fast.cu - the fast sampler with the Gaussian PSF: hardware SFU
+ * math, incremental model updates, warp-tree reductions, and
+ * move-synchronous CTAs (the warps of a CTA draw the move type and jump
+ * sub-branch from one shared stream and meet at a barrier before each jump,
+ * so an SM's warps run the same code and the instruction cache stops
+ * thrashing; each chain's move choice stays i.i.d. with the configured
+ * probabilities and independent of its state).  Also the fast launchers,
+ * which pick the likelihood model's build.
  */
 #include "sampler_kernel.cuh"
+#include "sampler_launch.h"
 
 namespace bamf {
 
-cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, int side_max,
-                               int blocks, int warps_per_block, cudaStream_t stream)
+cudaError_t launch_fast_gauss(const SamplerConsts &K, const SamplerBatch &B, size_t smem, int blocks, int threads,
+                              int min_ctas, cudaStream_t stream)
 {
-    if (warps_per_block < 1 || BAMF_SYNC_GROUP % warps_per_block != 0) return cudaErrorInvalidValue;
-    size_t smem = (size_t)warp_smem_floats(side_max, false) * sizeof(float) * warps_per_block;
-    /* one instantiation per likelihood model, so the Gaussian path carries
-     * no sampled-PSF code */
-    auto kern = K.opt_model == 1 ? rjmcmc_kernel_sync<true> : rjmcmc_kernel_sync<false>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    (void)K.sync_moves; /* always move-synchronous in fast arithmetic */
-    kern<<<blocks, 32 * warps_per_block, smem, stream>>>(K, B);
-    return cudaGetLastError();
+    return min_ctas == 3 ? launch_kernel(rjmcmc_kernel_sync<false, 3>, K, B, smem, blocks, threads, stream)
+                         : launch_kernel(rjmcmc_kernel_sync<false, 2>, K, B, smem, blocks, threads, stream);
 }
 
-int blocks_per_sm_fast(int side_max, int warps_per_block, int opt_model)
+int occupancy_fast_gauss(size_t smem, int threads, int min_ctas)
+{
+    return min_ctas == 3 ? resident_ctas(rjmcmc_kernel_sync<false, 3>, smem, threads)
+                         : resident_ctas(rjmcmc_kernel_sync<false, 2>, smem, threads);
+}
+
+cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, int side_max, int blocks,
+                               int warps_per_block, int min_ctas, cudaStream_t stream)
+{
+    if (warps_per_block < 1 || BAMF_SYNC_GROUP % warps_per_block != 0) return cudaErrorInvalidValue;
+    if (min_ctas != 2 && min_ctas != 3) return cudaErrorInvalidValue;
+    size_t smem = (size_t)warp_smem_floats(side_max, false) * sizeof(float) * warps_per_block;
+    (void)K.sync_moves; /* always move-synchronous in fast arithmetic */
+    return K.opt_model == 1 ? launch_fast_num(K, B, smem, blocks, 32 * warps_per_block, min_ctas, stream)
+                            : launch_fast_gauss(K, B, smem, blocks, 32 * warps_per_block, min_ctas, stream);
+}
+
+int blocks_per_sm_fast(int side_max, int warps_per_block, int min_ctas, int opt_model)
 {
     size_t smem = (size_t)warp_smem_floats(side_max, false) * sizeof(float) * warps_per_block;
-    auto kern = opt_model == 1 ? rjmcmc_kernel_sync<true> : rjmcmc_kernel_sync<false>;
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, 32 * warps_per_block, smem) != cudaSuccess) {
-        cudaGetLastError();
-        return 0;
-    }
-    return n;
+    return opt_model == 1 ? occupancy_fast_num(smem, 32 * warps_per_block, min_ctas)
+                          : occupancy_fast_gauss(smem, 32 * warps_per_block, min_ctas);
+}
+
+int best_fast_shape(int side_max, int opt_model, int *warps_per_block, int *min_ctas)
+{
+    int best_w = 0, best_wpb = 8, best_mc = 2, best_per = 0;
+    const int cand[3] = {8, 4, 2};
+    for (int mc = 2; mc <= 3; ++mc)
+        for (int i = 0; i < 3; ++i) {
+            int per = blocks_per_sm_fast(side_max, cand[i], mc, opt_model);
+            if (per * cand[i] > best_w) {
+                best_w = per * cand[i];
+                best_wpb = cand[i];
+                best_mc = mc;
+                best_per = per;
+            }
+        }
+    *warps_per_block = best_wpb;
+    *min_ctas = best_mc;
+    return best_per;
 }
 
 }  // namespace bamf

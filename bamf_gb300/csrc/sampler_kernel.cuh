@@ -73,18 +73,21 @@ struct SMath<false> {
 
 /* Per-warp shared-memory carve-out, in floats.  Exact: data D, model M,
  * proposal model Mt, per-pixel work E, sCMOS, proposal stencils NX/NY.
- * Fast: D, M, Mt, log2 M and the compact stencil rows SXo/SYo (old, of A)
- * and SXn/SYn (new, of T); sCMOS is read from global memory at model
- * rebuilds only.  Both: counters and the neighbour pick list. */
+ * Fast: D, M, Mt and the compact stencil rows SXo/SYo (old, of A) and
+ * SXn/SYn (new, of T); log2 M is recomputed in each likelihood pass (the
+ * SFU has room; the smaller carve-out keeps 3 CTAs of 8 chains resident
+ * up to 24x24 ROIs); sCMOS is read from global memory at model rebuilds
+ * only.  Both: counters and the neighbour pick list. */
 /* Fast mode keeps stencil rows only for the emitters a proposal changes:
  * up to FAST_ROWS old rows (A) and FAST_ROWS new rows (T); larger proposals
- * and periodic rebuilds stream the model one emitter at a time. */
-#define FAST_ROWS 8
+ * (rare: a jump of a cluster of more than 4 emitters) and periodic rebuilds
+ * stream the model one emitter at a time. */
+#define FAST_ROWS 4
 __host__ __device__ inline int warp_smem_floats(int side_max, bool exact)
 {
     int npix = side_max * side_max, nxs = BAMF_NMAX * side_max;
     return exact ? 5 * npix + 2 * nxs + C_COUNT + BAMF_NMAX + 2                 /* D M Mt E sCMOS NX NY */
-                 : 4 * npix + 4 * FAST_ROWS * side_max + C_COUNT + BAMF_NMAX + 2; /* D M Mt log2M SXo SYo SXn SYn */
+                 : 3 * npix + 4 * FAST_ROWS * side_max + C_COUNT + BAMF_NMAX + 2; /* D M Mt SXo SYo SXn SYn */
 }
 
 /* double helpers that nvcc may not contract */
@@ -269,7 +272,7 @@ struct ChainWarp {
     int px_dx, px_dy; /* pixel p -> p+32 moves x by px_dx and y by px_dy (then wraps) */
     float sigma, Cst, MeanN;
     /* shared memory */
-    float *D, *M, *Mt, *E, *NX, *NY, *logM;
+    float *D, *M, *Mt, *E, *NX, *NY;
     float *SXo, *SYo, *SXn, *SYn; /* fast mode: compact stencil rows */
     const float *scm; /* sCMOS: shared memory (exact) or global/null (fast) */
     /* sampled PSF (OptModel 1): [P0 y][P1 x][P2 y-sub][P3 x-sub], y fastest;
@@ -770,7 +773,7 @@ struct ChainWarp {
             if (v) {
                 float mt = M[p] + d;
                 Mt[p] = mt;
-                acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - d;
+                acc += D[p] * (__log2f(mt) - __log2f(M[p])) * LN2 - d;
             }
         }
         return acc;
@@ -806,7 +809,7 @@ struct ChainWarp {
 #pragma unroll 1
                     for (int p = lane; p < npix; p += 32) {
                         float mt = Mt[p];
-                        acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - (mt - M[p]);
+                        acc += D[p] * (__log2f(mt) - __log2f(M[p])) * LN2 - (mt - M[p]);
                     }
                 }
             } else {
@@ -843,7 +846,7 @@ struct ChainWarp {
                             int p = yl + Y * xx;
                             float mt = M[p] + d;
                             Mt[p] = mt;
-                            acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - d;
+                            acc += D[p] * (__log2f(mt) - __log2f(M[p])) * LN2 - d;
                         }
                     }
                 } else {
@@ -851,7 +854,7 @@ struct ChainWarp {
 #pragma unroll 1
                     for (int p = lane; p < npix; p += 32) {
                         float mt = Mt[p];
-                        acc += D[p] * (__log2f(mt) - logM[p]) * LN2 - (mt - M[p]);
+                        acc += D[p] * (__log2f(mt) - __log2f(M[p])) * LN2 - (mt - M[p]);
                     }
                 }
             }
@@ -860,14 +863,13 @@ struct ChainWarp {
         }
     }
 
-    /* fast mode: fold the accepted proposal into M and log2 M */
+    /* fast mode: fold the accepted proposal into M */
     __device__ __forceinline__ void commit_fast()
     {
 #pragma unroll 1
         for (int p = lane; p < npix; p += 32) {
             float m = Mt[p];
             M[p] = m;
-            logM[p] = __log2f(m);
         }
         __syncwarp();
     }
@@ -884,7 +886,7 @@ struct ChainWarp {
         }
     }
 
-    /* Full rebuild of M (and, in fast mode, log2 M). */
+    /* Full rebuild of M. */
     __device__ __forceinline__ void rebuild_model()
     {
         if (EXACT) {
@@ -893,8 +895,6 @@ struct ChainWarp {
         } else {
             if constexpr (NUM) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
             else model_stream(an, aI, aX, aY, aBG, aABG, aBBG, M);
-#pragma unroll 1
-            for (int p = lane; p < npix; p += 32) logM[p] = __log2f(M[p]);
             __syncwarp();
         }
     }
@@ -1754,7 +1754,6 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT, NUM> &w, const Sample
     if (EXACT) {
         w.E = sw + 3 * npix_max;
         scm_smem = sw + 4 * npix_max;
-        w.logM = nullptr;
         w.NX = sw + 5 * npix_max;
         w.NY = w.NX + nxs;
         w.SXo = w.SYo = w.SXn = w.SYn = nullptr;
@@ -1762,9 +1761,8 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT, NUM> &w, const Sample
     } else {
         const int rs = FAST_ROWS * Bt.side_max;
         w.E = nullptr;
-        w.logM = sw + 3 * npix_max;
         w.NX = w.NY = nullptr;
-        w.SXo = sw + 4 * npix_max;
+        w.SXo = sw + 3 * npix_max;
         w.SYo = w.SXo + rs;
         w.SXn = w.SYo + rs;
         w.SYn = w.SXn + rs;
@@ -1912,8 +1910,8 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ 
  * ROI per warp at a time and its warps run their chains in lockstep, one
  * barrier per jump, with the move type and jump sub-branch shared across the
  * CTA (run_chain_sync). */
-template <bool NUM>
-__global__ void __launch_bounds__(32 * BAMF_SYNC_GROUP, 2) rjmcmc_kernel_sync(const __grid_constant__ SamplerConsts Kc,
+template <bool NUM, int MIN_CTAS>
+__global__ void __launch_bounds__(32 * BAMF_SYNC_GROUP, MIN_CTAS) rjmcmc_kernel_sync(const __grid_constant__ SamplerConsts Kc,
                                                           const __grid_constant__ SamplerBatch Bc)
 {
     extern __shared__ float smem_raw[];

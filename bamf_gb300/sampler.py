@@ -52,6 +52,8 @@ def _declare() -> C.CDLL:
                                 C.c_int, C.c_int, C.c_int, C.c_void_p]
     L.bamf_autotune_result.restype = C.c_int
     L.bamf_autotune_result.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int32)]
+    L.bamf_autotune_shapes.restype = C.c_int
+    L.bamf_autotune_shapes.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.bamf_rjmcmc_batch_graph_create.restype = C.c_int
     L.bamf_rjmcmc_batch_graph_create.argtypes = [C.c_void_p, C.POINTER(RoiBatch), C.POINTER(abi.McmcParams),
                                                  C.POINTER(Priors), C.c_uint32, C.c_int, C.POINTER(BatchResults),
@@ -366,6 +368,13 @@ class Sampler:
         out = (C.c_int32 * 7)()
         _check(L, L.bamf_autotune_result(self._ws, ARITH[arith], out), "bamf_autotune_result")
         return list(out)
+
+    def tuned_shapes(self, arith: str = "fast") -> tuple:
+        """(chains per CTA, CTAs per SM of the register budget) per size class."""
+        L = self._L
+        a, b = (C.c_int32 * 7)(), (C.c_int32 * 7)()
+        _check(L, L.bamf_autotune_shapes(self._ws, ARITH[arith], a, b), "bamf_autotune_shapes")
+        return list(a), list(b)
 
     def run_host(self, batch, params: abi.McmcParams, off, sig, back, seed: int,
                  arith: str = "fast", bg0: float = 0.0, init=None, proposal: str = "reference",

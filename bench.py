@@ -335,8 +335,9 @@ def main():
                      outs=outs, stream=stream.cuda_stream, bg0=bg0)
 
     # CTA shape per size class by the project's autotuner (short chains on a sample of each class)
-    tuned = s.autotune(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, arith="fast", jumps=200,
+    tuned = s.autotune(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, arith="fast", jumps=400,
                        sample=4864, stream=stream.cuda_stream, bg0=bg0)
+    budget = s.tuned_shapes("fast")[1]
     for _ in range(a.warmup):
         step()
     torch.cuda.synchronize()
@@ -435,7 +436,8 @@ def main():
             "config": {"workload": workload_label(n, a.jumps), "n_rois": n, "jumps": [a.jumps, a.jumps],
                        "arith": "fast", "parallelism": f"replicas x{world}",
                        "l2": "flushed between timed steps (512 MB write)",
-                       "chains_per_cta_by_size_class": tuned},
+                       "chains_per_cta_by_size_class": tuned,
+                       "ctas_per_sm_register_budget_by_size_class": budget},
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": mufu.value / 1e9,
                          "unit": "Gop/s (MUFU log2)", "frac": achieved / mufu.value,
                          "traffic": None,

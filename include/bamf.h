@@ -189,8 +189,8 @@ const char *bamf_last_error(void);
  *                   (plhs[2], plhs[3] before marshalling)
  *   counters        the 30 counters behind the Stat output  (plhs[4]); may be NULL
  *
- * The sampled-PSF model (prhs[9], prhs[10] = OptModel 1) is not supported:
- * this entry point always uses the Gaussian PSF (OptModel 0).
+ * This entry point uses the Gaussian PSF (OptModel 0); the sampled-PSF
+ * model (prhs[9], prhs[10] = OptModel 1) is bamf_crjmcmc_host_model.
  * Errors: BAMF_ERR_INVALID_ARG (null input, size < 1, pdf length < 1),
  * BAMF_ERR_TOO_LARGE (side > BAMF_MAX_ROI_SIDE or N > BAMF_NMAX),
  * BAMF_ERR_BAD_PRIOR (NaN/negative pdf, non-increasing grid),
@@ -435,9 +435,11 @@ void bamf_rjmcmc_batch_graph_destroy(bamf_batch_graph *graph);
 
 /* Autotuner (no reference counterpart): for every ROI size class present
  * in the (device) batch, times each CTA shape - 8, 4, 2 or 1 chains per CTA
- * in fast arithmetic, 4, 2 or 1 in exact - on up to `sample` ROIs of the
- * class with chains of `jumps` burn-in jumps, and keeps the fastest in the
- * workspace; later bamf_rjmcmc_batch_device calls on that workspace launch
+ * in fast arithmetic, each with the kernel build whose registers are sized
+ * for 2 or for 3 CTAs per SM; 4, 2 or 1 in exact - on about `sample` ROIs
+ * of the class (a whole number of rounds of the shape's resident chains,
+ * at least one, at most the class) with chains of `jumps` burn-in jumps,
+ * and keeps the shape with the least time per ROI in the workspace; later bamf_rjmcmc_batch_device calls on that workspace launch
  * each class with its tuned shape.  Results of a batch do not depend on
  * the shape.  Synchronises `stream`. */
 bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *rois, const bamf_mcmc_params *p,
@@ -445,6 +447,11 @@ bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *rois, const 
 /* chains_per_cta[7]: the tuned shape per size class (sides (0,8], (8,12],
  * ..., (28,32]); 0 where the class was not tuned. */
 bamf_status bamf_autotune_result(const bamf_workspace *ws, int arith, int32_t *chains_per_cta);
+/* The tuned shapes with the fast kernel's register budget: chains_per_cta
+ * as bamf_autotune_result, ctas_per_sm_budget[c] the CTAs per SM the chosen
+ * build's registers are sized for (fast: 2 or 3; exact: 4; 0 untuned). */
+bamf_status bamf_autotune_shapes(const bamf_workspace *ws, int arith, int32_t *chains_per_cta,
+                                 int32_t *ctas_per_sm_budget);
 
 #define BAMF_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *rois,

@@ -213,6 +213,8 @@ def test_autotune_picks_a_shape_per_class_and_keeps_results(cuda_lib):
     print("chains per CTA by size class:", tuned)
     assert [t > 0 for t in tuned[:5]] == [True] * 5 and tuned[5:] == [0, 0]
     assert all(t in (1, 2, 4, 8) for t in tuned[:5])
+    shapes, budget = s.tuned_shapes("fast")
+    assert shapes == tuned and all(b in (2, 3) for b in budget[:5]) and budget[5:] == [0, 0]
     after = run()
     for k in before:
         np.testing.assert_array_equal(before[k], after[k], err_msg=k)
