@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--jumps", type=int, default=3000)
     ap.add_argument("--cpu-sample", type=int, default=0, help="ROIs per CPU-baseline sample (0: auto)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="launch each size class with the occupancy rule's CTA shape (for profiling)")
     ap.add_argument("--no-learned", action="store_true",
                     help="skip the learned-vs-uniform proposal evaluation (16x16 ROIs)")
     ap.add_argument("--learned-train-rois", type=int, default=2_000_000)
@@ -335,9 +337,12 @@ def main():
                      outs=outs, stream=stream.cuda_stream, bg0=bg0)
 
     # CTA shape per size class by the project's autotuner (short chains on a sample of each class)
-    tuned = s.autotune(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, arith="fast", jumps=400,
-                       sample=4864, stream=stream.cuda_stream, bg0=bg0)
-    budget = s.tuned_shapes("fast")[1]
+    if a.no_autotune:
+        tuned = budget = "occupancy rule"
+    else:
+        tuned = s.autotune(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, arith="fast", jumps=400,
+                           sample=4864, stream=stream.cuda_stream, bg0=bg0)
+        budget = s.tuned_shapes("fast")[1]
     for _ in range(a.warmup):
         step()
     torch.cuda.synchronize()
