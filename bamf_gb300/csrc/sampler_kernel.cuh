@@ -303,6 +303,7 @@ struct ChainWarp {
     int n_llr;
     /* incremental-model bookkeeping (fast mode) */
     uint32_t a_dirty, t_dirty;
+    int llr_box; /* pixels the last likelihood pass changed: x0 | x1 << 8 | y0 << 16 | y1 << 24 */
     /* move-synchronous mode: the jump sub-branch uniform comes from the CTA */
     bool use_shared_ub;
     float shared_ub;
@@ -802,6 +803,7 @@ struct ChainWarp {
             int na = __popc(a_dirty), nt = __popc(t_dirty);
             float acc = 0.0f;
             if constexpr (NUM) {
+                llr_box = full_box();
                 if (na <= FAST_ROWS && nt <= FAST_ROWS) {
                     acc = llr_num_fast(na, nt);
                 } else {
@@ -815,13 +817,41 @@ struct ChainWarp {
             } else {
                 if (na <= FAST_ROWS && nt <= FAST_ROWS) {
                     stencil_rows(na, nt);
-                    /* lane -> row y = lane mod Y of column x0 + lane / Y; a pass
-                     * covers 32 / Y columns.  The model change of a pixel is
-                     * bg delta + sum_q w_q(y) SX_q[x] over the changed rows q
-                     * (old rows with weight -SYo, new with +SYn); each lane
-                     * holds its first four weights in registers. */
-                    const int yl = lane % Y, xo = lane / Y, R = 32 / Y;
                     const int nr = na + nt;
+                    /* Support box: unless the background changes, a pixel
+                     * outside the union of the changed rows' nonzero x- and
+                     * y-stencil entries has d = 0 exactly (Mt = M, a zero
+                     * term), so the pass covers only the box.  Stencils of
+                     * sigma ~1.3 vanish in float ~7 px from the emitter. */
+                    int x0 = 0, x1 = X - 1, y0 = 0, y1 = Y - 1;
+                    if (tBG == aBG && tABG == aABG && tBBG == aBBG) {
+                        bool nzx = false, nzy = false;
+#pragma unroll 1
+                        for (int q = 0; q < nr; ++q) {
+                            const bool old = q < na;
+                            const int qq = old ? q : q - na;
+                            nzx |= lane < X && (old ? SXo : SXn)[qq * X + lane] != 0.0f;
+                            nzy |= lane < Y && (old ? SYo : SYn)[qq * Y + lane] != 0.0f;
+                        }
+                        const uint32_t mx = __ballot_sync(BAMF_FULL, nzx), my = __ballot_sync(BAMF_FULL, nzy);
+                        if (mx == 0u || my == 0u) {
+                            llr_box = 1; /* empty: Mt = M everywhere, LLR = 1 */
+                            return 1.0f;
+                        }
+                        x0 = __ffs(mx) - 1;
+                        x1 = 31 - __clz(mx);
+                        y0 = __ffs(my) - 1;
+                        y1 = 31 - __clz(my);
+                    }
+                    llr_box = x0 | (x1 << 8) | (y0 << 16) | (y1 << 24);
+                    /* lane -> row y = y0 + lane mod h of column x0 + lane / h
+                     * (h the box height); a pass covers 32 / h columns.  The
+                     * model change of a pixel is bg delta + sum_q w_q(y)
+                     * SX_q[x] over the changed rows q (old rows with weight
+                     * -SYo, new with +SYn); each lane holds its first four
+                     * weights in registers. */
+                    const int h = y1 - y0 + 1;
+                    const int yl = y0 + lane % h, xo = lane / h, R = 32 / h;
                     float w[4];
                     const float *sx[4];
 #pragma unroll
@@ -834,7 +864,7 @@ struct ChainWarp {
                     const float base = (tBG - aBG) + (tBBG - aBBG) * (float)yl, dABG = tABG - aABG;
                     if (xo < R) {
 #pragma unroll 1
-                        for (int xx = xo; xx < X; xx += R) {
+                        for (int xx = x0 + xo; xx <= x1; xx += R) {
                             float d = base + dABG * (float)xx;
                             if (nr > 0) d += w[0] * sx[0][xx];
                             if (nr > 1) d += w[1] * sx[1][xx];
@@ -851,6 +881,7 @@ struct ChainWarp {
                     }
                 } else {
                     model_stream(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
+                    llr_box = full_box();
 #pragma unroll 1
                     for (int p = lane; p < npix; p += 32) {
                         float mt = Mt[p];
@@ -863,13 +894,18 @@ struct ChainWarp {
         }
     }
 
-    /* fast mode: fold the accepted proposal into M */
+    /* fast mode: fold the accepted proposal into M (Mt differs from M only
+     * inside the box of the last likelihood pass) */
+    __device__ __forceinline__ int full_box() const { return (X - 1) << 8 | (Y - 1) << 24; }
     __device__ __forceinline__ void commit_fast()
     {
+        const int x0 = llr_box & 255, x1 = (llr_box >> 8) & 255, y0 = (llr_box >> 16) & 255, y1 = llr_box >> 24;
+        if (x0 <= x1) {
+            const int h = y1 - y0 + 1, R = 32 / h, yy = y0 + lane % h, xo = lane / h;
+            if (xo < R) {
 #pragma unroll 1
-        for (int p = lane; p < npix; p += 32) {
-            float m = Mt[p];
-            M[p] = m;
+                for (int xx = x0 + xo; xx <= x1; xx += R) M[yy + Y * xx] = Mt[yy + Y * xx];
+            }
         }
         __syncwarp();
     }
