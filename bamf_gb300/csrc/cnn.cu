@@ -725,6 +725,21 @@ __global__ void adam_kernel(float *__restrict__ P, float *__restrict__ G, float 
 
 __global__ void step_inc_kernel(int *step_dev) { *step_dev += 1; }
 
+/* Training batch `step` from caller-provided examples: ROI b of the batch is
+ * example (step * batch + b) mod n_examples; counts clipped to the target
+ * capacity.  One CTA of NPX threads per ROI. */
+__global__ void gather_examples_kernel(const float *__restrict__ data, const int32_t *__restrict__ n_em,
+                                       const float *__restrict__ xyi, int n_examples, const int *step_dev,
+                                       int batch, float *__restrict__ gdata, int32_t *__restrict__ gn,
+                                       float *__restrict__ gxyi)
+{
+    const int b = blockIdx.x, t = threadIdx.x;
+    const int64_t k = ((int64_t)(*step_dev) * batch + b) % n_examples;
+    gdata[(size_t)b * NPX + t] = data[(size_t)k * NPX + t];
+    if (t == 0) gn[b] = min(max(n_em[k], 0), BAMF_SYNTH_NMAX);
+    if (t < BAMF_SYNTH_NMAX * 3) gxyi[(size_t)b * BAMF_SYNTH_NMAX * 3 + t] = xyi[(size_t)k * BAMF_SYNTH_NMAX * 3 + t];
+}
+
 }  // namespace
 
 /* ================================================================ host */
@@ -951,11 +966,12 @@ extern "C" bamf_status bamf_cnn_loss_grad(bamf_cnn *net, const float *data, cons
     return BAMF_OK;
 }
 
-extern "C" bamf_status bamf_cnn_train(bamf_cnn *net, const bamf_synth_params *sp, int steps, int batch, float lr,
-                                      uint32_t data_seed, float *loss_trace)
+/* `steps` Adam steps, each one replay of a CUDA graph of: produce(s) (the
+ * step's batch into gdata / gn / gxyi), forward, backward, Adam, weight
+ * packing, step counter.  Optimiser state starts from zero. */
+template <typename Produce>
+static bamf_status train_graph(bamf_cnn *net, int steps, int batch, float lr, float *loss_trace, Produce produce)
 {
-    if (!net || !sp || steps < 0 || batch < 1 || batch > MAX_BATCH || !(lr > 0.0f)) return BAMF_ERR_INVALID_ARG;
-    if (steps == 0) return BAMF_OK;
     bamf_status r;
     if ((r = ensure_loss(net, steps))) return r;
     cudaStream_t s;
@@ -976,7 +992,7 @@ extern "C" bamf_status bamf_cnn_train(bamf_cnn *net, const bamf_synth_params *sp
             res = BAMF_ERR_CUDA;
             break;
         }
-        synth_kernel<<<batch, 256, 0, s>>>(*sp, data_seed, 0, net->step, batch, batch, net->gdata, net->gn, net->gxyi);
+        produce(s);
         bamf_status r1 = forward(net, net->gdata, batch, s);
         bamf_status r2 = r1 ? r1 : backward(net, net->gn, net->gxyi, batch, 1.0f / (float)batch, s);
         adam_kernel<<<(NPARAM + 255) / 256, 256, 0, s>>>(net->P, net->G, net->M, net->V, net->step, steps, lr);
@@ -1010,6 +1026,32 @@ extern "C" bamf_status bamf_cnn_train(bamf_cnn *net, const bamf_synth_params *sp
     cudaStreamDestroy(s);
     if (res) cudaGetLastError();
     return res;
+}
+
+extern "C" bamf_status bamf_cnn_train(bamf_cnn *net, const bamf_synth_params *sp, int steps, int batch, float lr,
+                                      uint32_t data_seed, float *loss_trace)
+{
+    if (!net || !sp || steps < 0 || batch < 1 || batch > MAX_BATCH || !(lr > 0.0f)) return BAMF_ERR_INVALID_ARG;
+    if (steps == 0) return BAMF_OK;
+    const bamf_synth_params spv = *sp;
+    return train_graph(net, steps, batch, lr, loss_trace, [&](cudaStream_t s) {
+        synth_kernel<<<batch, 256, 0, s>>>(spv, data_seed, 0, net->step, batch, batch, net->gdata, net->gn,
+                                           net->gxyi);
+    });
+}
+
+extern "C" bamf_status bamf_cnn_train_examples(bamf_cnn *net, const float *data, const int32_t *n_em,
+                                               const float *xyi, int n_examples, int steps, int batch, float lr,
+                                               float *loss_trace)
+{
+    if (!net || !data || !n_em || !xyi || n_examples < 1 || steps < 0 || batch < 1 || batch > MAX_BATCH ||
+        !(lr > 0.0f))
+        return BAMF_ERR_INVALID_ARG;
+    if (steps == 0) return BAMF_OK;
+    return train_graph(net, steps, batch, lr, loss_trace, [&](cudaStream_t s) {
+        gather_examples_kernel<<<batch, NPX, 0, s>>>(data, n_em, xyi, n_examples, net->step, batch, net->gdata,
+                                                     net->gn, net->gxyi);
+    });
 }
 
 extern "C" bamf_status bamf_cnn_init_states(const float *cdf, const float *sub, const float *count_logits, int n,

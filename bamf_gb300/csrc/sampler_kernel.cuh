@@ -304,6 +304,7 @@ struct ChainWarp {
     /* incremental-model bookkeeping (fast mode) */
     uint32_t a_dirty, t_dirty;
     int llr_box; /* pixels the last likelihood pass changed: x0 | x1 << 8 | y0 << 16 | y1 << 24 */
+    float pdf_aBG; /* fast mode: offset-prior density of aBG */
     /* move-synchronous mode: the jump sub-branch uniform comes from the CTA */
     bool use_shared_ub;
     float shared_ub;
@@ -912,7 +913,10 @@ struct ChainWarp {
 
     __device__ __forceinline__ void accept_T()
     {
-        if (!EXACT) commit_fast();
+        if (!EXACT) {
+            commit_fast();
+            if (tBG != aBG) pdf_aBG = findPDF(K->off, tBG);
+        }
         an = tn; aI = tI; aX = tX; aY = tY; aS = tS;
         aBG = tBG; aABG = tABG; aBBG = tBBG;
         if (EXACT) {
@@ -1180,6 +1184,15 @@ struct ChainWarp {
     }
     __device__ __forceinline__ float finish_jump(float LLR)
     {
+        if (!EXACT) {
+            /* fast: the offset prior of the current BG is cached, and the
+             * factors of an unchanged BG / slope are 1 (x / x, exp(0)) */
+            float BgPDFtest = tBG == aBG ? pdf_aBG : findPDF(K->off, tBG);
+            float PrBg = BgPDFtest / pdf_aBG;
+            if (tBBG != aBBG) PrBg *= MT::exp_(-(tBBG * tBBG - aBBG * aBBG) / 2.0f);
+            if (tABG != aABG) PrBg *= MT::exp_(-(tABG * tABG - aABG * aABG) / 2.0f);
+            return LLR * pk_f0 * PrBg;
+        }
         float BgPDF = findPDF(K->off, aBG);
         float BgPDFtest = findPDF(K->off, tBG);
         float PrBg = (BgPDFtest / BgPDF) * MT::exp_(-(tBBG * tBBG - aBBG * aBBG) / 2.0f) *
@@ -1856,6 +1869,7 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT, NUM> &w, const Sample
     }
     w.aBG = Bt.init_bg ? Bt.init_bg[roi] : Kp->bg0;
     if (w.aBG == 0.0f) w.aBG = 1.0f;
+    if (!EXACT) w.pdf_aBG = w.findPDF(Kp->off, w.aBG);
     w.aABG = 0.0f;
     w.aBBG = 0.0f;
     w.seed = Kp->seed;

@@ -43,6 +43,7 @@ def _lib() -> C.CDLL:
     L.bamf_cnn_set_params.argtypes = [vp, f32p]
     L.bamf_cnn_loss_grad.argtypes = [vp, vp, vp, vp, i32, f32p, f32p]
     L.bamf_cnn_train.argtypes = [vp, C.POINTER(SynthParams), i32, i32, C.c_float, C.c_uint32, f32p]
+    L.bamf_cnn_train_examples.argtypes = [vp, vp, vp, vp, i32, i32, i32, C.c_float, f32p]
     L.bamf_cnn_infer.argtypes = [vp, vp, i32, vp, vp, vp, vp]
     L.bamf_cnn_init_states.argtypes = [vp, vp, vp, i32, C.c_float, i32, vp, vp, vp]
     for f in ("bamf_synth_generate", "bamf_cnn_create", "bamf_cnn_get_params", "bamf_cnn_set_params",
@@ -128,6 +129,17 @@ class ProposalNet:
         _check(self._L, st, "bamf_cnn_train")
         return trace[:steps]
 
+    def train_examples(self, ex: dict, steps: int, batch: int = 512, lr: float = 1e-3) -> np.ndarray:
+        """Adam on caller examples (torch CUDA: data [n][256], n_em [n] int32,
+        xyi [n][16][3]), e.g. from `examples_from_states`; per-step loss."""
+        n = int(ex["n_em"].numel())
+        trace = np.zeros(max(steps, 1), np.float32)
+        st = self._L.bamf_cnn_train_examples(self._h, ex["data"].contiguous().data_ptr(),
+                                             ex["n_em"].contiguous().data_ptr(), ex["xyi"].contiguous().data_ptr(),
+                                             n, int(steps), int(batch), float(lr), abi.fptr(trace))
+        _check(self._L, st, "bamf_cnn_train_examples")
+        return trace[:steps]
+
     def infer(self, data, stream=None) -> dict:
         """data: torch CUDA float32 [n][256] (16x16 ROIs, y fastest) ->
         birth tables cdf [n*256], sub [n*256*16] and count logits [n][11]."""
@@ -157,3 +169,31 @@ def init_states(tables: dict, intensity: float = 1000.0, max_n: int = 10, stream
                                 C.c_void_p(stream) if stream else None)
     _check(L, st, "bamf_cnn_init_states")
     return out
+
+
+def examples_from_states(data, pos_trace, n_entries, pos_thin: int, seed: int = 0) -> dict:
+    """Training examples from states the sampler accepted: for every ROI one
+    recorded state (bamf_batch_results.pos_trace) drawn uniformly from the
+    second half of its chain (the trial phase when burn-in and trials are
+    equally long), as targets: n_em = its Signal==1 count (clipped to
+    BAMF_SYNTH_NMAX), xyi = the X, Y, I of those emitters.  data [n][256]
+    are the ROIs the sampler ran on.  Torch CUDA in, torch CUDA out."""
+    import torch
+    n, pos_len, rec = pos_trace.shape
+    S = (rec - 5) // 3
+    ent = n_entries.to(torch.int64)
+    nrec = torch.clamp((ent - 1) // pos_thin + 1, min=1, max=pos_len)
+    lo = torch.minimum((ent // 2 + pos_thin - 1) // pos_thin, nrec - 1)
+    g = torch.Generator(device=pos_trace.device)
+    g.manual_seed(int(seed))
+    u = torch.rand(n, generator=g, device=pos_trace.device)
+    j = torch.minimum(lo + (u * (nrec - lo).to(torch.float32)).to(torch.int64), nrec - 1)
+    r = pos_trace[torch.arange(n, device=pos_trace.device), j]
+    ns = torch.nan_to_num(r[:, 1]).to(torch.int64).clamp(0, SYNTH_NMAX)
+    k = torch.arange(SYNTH_NMAX, device=pos_trace.device)
+    keep = (k[None, :] < ns[:, None]).to(torch.float32)
+    xyi = torch.stack([r[:, 5:5 + SYNTH_NMAX], r[:, 5 + S:5 + S + SYNTH_NMAX],
+                       r[:, 5 + 2 * S:5 + 2 * S + SYNTH_NMAX]], dim=2)
+    xyi = torch.nan_to_num(xyi) * keep[:, :, None]
+    return {"data": data.reshape(n, NPX).contiguous(), "n_em": ns.to(torch.int32).contiguous(),
+            "xyi": xyi.contiguous()}

@@ -90,6 +90,15 @@ bamf_status bamf_cnn_loss_grad(bamf_cnn *net, const float *data, const int32_t *
 bamf_status bamf_cnn_train(bamf_cnn *net, const bamf_synth_params *sp, int steps, int batch, float lr,
                            uint32_t data_seed, float *loss_trace);
 
+/* `steps` Adam steps (as bamf_cnn_train, optimiser state from zero) on
+ * caller-provided examples: n_examples device ROIs in the layout of
+ * bamf_synth_generate (data [n][256], n_em [n], xyi [n][BAMF_SYNTH_NMAX][3];
+ * counts above BAMF_SYNTH_NMAX are clipped), step i training on examples
+ * i*batch .. i*batch+batch-1 modulo n_examples.  This is how the network
+ * learns from states the sampler accepted (bamf_batch_results.pos_trace)
+ * on data the generator does not describe. */
+bamf_status bamf_cnn_train_examples(bamf_cnn *net, const float *data, const int32_t *n_em, const float *xyi,
+                                    int n_examples, int steps, int batch, float lr, float *loss_trace);
 /* Inference on n device ROIs of 16x16 (data [n][256]), into the sampler's
  * LEARNED tables for ROIs laid out back to back (ROI k at pixel 256 k):
  * cdf [n][256], sub [n][256][16], and count logits [n][11] (may be NULL). */

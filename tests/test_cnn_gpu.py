@@ -133,3 +133,57 @@ def test_start_states_follow_the_count_logits_and_density(cuda_lib):
     print("start emitters within 0.5 px of a true one:", np.mean(near))
     assert np.mean(near) > 0.6
     print("count accuracy of the start state:", np.mean(n0 == np.minimum(h["n_em"], 10)))
+
+
+def test_training_on_accepted_states_adapts_to_data_the_generator_misdescribes(cuda_lib):
+    """The network learns from states the sampler accepted.  Trained on
+    generator ROIs of PSF sigma 1.3 and median intensity 1000, it meets ROIs
+    of sigma 1.7 and median 600.  The uniform-birth sampler (given the true
+    PSF) runs on 16k of those ROIs; one accepted state per ROI from the
+    trial phase becomes a training example (no ground truth is used) and the
+    network is fine-tuned on them (bamf_cnn_train_examples).  On fresh
+    shifted ROIs the fine-tuned network's loss on the true emitters falls
+    and its count head is right more often."""
+    import torch
+    from bamf_gb300 import learned, mapfit, rjstruct, sampler
+    net = learned.ProposalNet(seed=3)
+    net.train(300, batch=512, lr=2e-3, data_seed=5, mean_n=5.0, sigma=1.3, i_median=1000.0, i_logsd=0.3,
+              bg=10.0)
+    shift = dict(mean_n=5.0, sigma=1.7, i_median=600.0, i_logsd=0.3, bg=10.0)
+    n = 16384
+    tr = learned.generate(n, seed=77, **shift)
+    rj = rjstruct.c0_rjstruct()
+    rj.Rho = 5.0 / 256.0
+    rj.PSF_Sigma = 1.7
+    rj.N_Burnin = rj.N_Trials = 1000
+    p = rjstruct.mcmc_params(rj)
+    pos_len = 64
+    thin = mapfit.thinning(2000, pos_len)
+    dev = {"data": tr["data"].reshape(-1), "offsets": torch.arange(n, dtype=torch.int64, device="cuda") * 256,
+           "xsize": torch.full((n,), 16, dtype=torch.int32, device="cuda"),
+           "ysize": torch.full((n,), 16, dtype=torch.int32, device="cuda"), "side_max": 16}
+    outs = {k: torch.zeros(n, dtype=torch.int32, device="cuda") for k in ("status", "n_entries")}
+    outs["pos_trace"] = torch.zeros((n, pos_len, mapfit.POS_RECORD), dtype=torch.float32, device="cuda")
+    outs["pos_thin"] = thin
+    sampler.Sampler().run_device(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=11, arith="fast",
+                                 outs=outs, bg0=rjstruct.initial_bg(rj), proposal="uniform")
+    torch.cuda.synchronize()
+    assert int((outs["status"] != 0).sum()) == 0
+    ex = learned.examples_from_states(tr["data"], outs["pos_trace"], outs["n_entries"], thin, seed=1)
+    agree = float((ex["n_em"] == tr["n_em"].clamp(max=16)).float().mean())
+    ev = learned.generate(4096, seed=99, **shift)
+
+    def score():
+        loss, _ = net.loss_grad(ev)
+        cnt = net.infer(ev["data"])["count_logits"].argmax(dim=1)
+        acc = float((cnt == ev["n_em"].clamp(max=10).to(cnt.dtype)).float().mean())
+        return loss, acc
+
+    loss_a, acc_a = score()
+    trace = net.train_examples(ex, steps=300, batch=512, lr=1e-3)
+    loss_b, acc_b = score()
+    print(f"sampler states match the true count on {agree:.3f} of ROIs; loss {loss_a:.3f} -> {loss_b:.3f}, "
+          f"count accuracy {acc_a:.3f} -> {acc_b:.3f}; example loss {trace[0]:.3f} -> {trace[-1]:.3f}")
+    assert np.isfinite(trace).all()
+    assert loss_b < loss_a - 0.05
+    assert acc_b > acc_a
