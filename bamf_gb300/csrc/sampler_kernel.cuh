@@ -233,21 +233,31 @@ __device__ __forceinline__ float shared_uniform(uint32_t seed, uint32_t grp, uin
 /* (1 / A) / q(x, y) for the LEARNED birth proposal q = (learned + uniform)/2
  * on a box of area A; the learned part is the ROI's pixel running sum cdf
  * times the pixel's 16 sub-cell probabilities sub (16 cells per px^2). */
+/* The learned position density at (x, y) per px^2 (pixel probability from
+ * the running sum, sub-cell probability, 16 sub-cells per px^2); 0 outside
+ * the ROI. */
+static __device__ __noinline__ float learned_density(float x, float y, int X, int Y, int npix,
+                                                     const float *__restrict__ cdf,
+                                                     const float *__restrict__ sub)
+{
+    if (!(x >= 0.0f && y >= 0.0f && x < (float)X && y < (float)Y)) return 0.0f;
+    int px = min((int)x, X - 1), py = min((int)y, Y - 1);
+    int pix = py + px * Y;
+    int sc = min((int)((y - (float)py) * 4.0f), 3) + 4 * min((int)((x - (float)px) * 4.0f), 3);
+    float pp = __ldg(&cdf[pix]) - (pix > 0 ? __ldg(&cdf[pix - 1]) : 0.0f);
+    const float *sp = sub + 16 * pix;
+    float ps = 0.0f;
+    for (int k = 0; k < 16; ++k) ps += __ldg(&sp[k]);
+    return (pp / __ldg(&cdf[npix - 1])) * (__ldg(&sp[sc]) / ps) * 16.0f;
+}
+
+/* (1 / A) / q(x, y) for the birth mixture q = 1/2 learned + 1/2 uniform on
+ * the extended box of area A. */
 static __device__ __noinline__ float learned_q_ratio(float x, float y, int X, int Y, int npix, float A,
                                                      const float *__restrict__ cdf,
                                                      const float *__restrict__ sub)
 {
-    float qa = 0.0f; /* learned density times box area */
-    if (x >= 0.0f && y >= 0.0f && x < (float)X && y < (float)Y) {
-        int px = min((int)x, X - 1), py = min((int)y, Y - 1);
-        int pix = py + px * Y;
-        int sc = min((int)((y - (float)py) * 4.0f), 3) + 4 * min((int)((x - (float)px) * 4.0f), 3);
-        float pp = __ldg(&cdf[pix]) - (pix > 0 ? __ldg(&cdf[pix - 1]) : 0.0f);
-        const float *sp = sub + 16 * pix;
-        float ps = 0.0f;
-        for (int k = 0; k < 16; ++k) ps += __ldg(&sp[k]);
-        qa = (pp / __ldg(&cdf[npix - 1])) * (__ldg(&sp[sc]) / ps) * 16.0f * A;
-    }
+    const float qa = learned_density(x, y, X, Y, npix, cdf, sub) * A; /* learned density times box area */
     return 1.0f / (0.5f * qa + 0.5f);
 }
 
@@ -1213,8 +1223,21 @@ struct ChainWarp {
         int BF = A_S(jj);
         cinc(BF == 1 ? C_N_splitFg : C_N_splitBg);
         float u1 = urand();
-        float u2 = p.Split_std * randn();
-        float u3 = p.Split_std * randn();
+        float u2, u3;
+        if (!EXACT && K->proposal == BAMF_PROPOSAL_LEARNED && urand() < 0.5f) {
+            /* learned split: the first emitter's position from the learned
+             * density and the intensity fraction from a triangular density on
+             * [0.3, 0.7] (the mixture density of (u1, offset) enters
+             * finish_split) */
+            float lx, ly;
+            learned_position(&lx, &ly);
+            u1 = 0.3f + 0.2f * (urand() + urand());
+            u2 = lx - mux;
+            u3 = ly - muy;
+        } else {
+            u2 = p.Split_std * randn();
+            u3 = p.Split_std * randn();
+        }
         setT(jj, u1 * Ijp, mux + u2, muy + u3);
         if (!EXACT) a_dirty |= 1u << jj;
         addT((1.0f - u1) * Ijp, mux - u1 * u2 / (1.0f - u1), muy - u1 * u3 / (1.0f - u1), BF);
@@ -1252,8 +1275,24 @@ struct ChainWarp {
         float Us = 1.0f / (Norm1 * Norm2);
         float om = 1.0f - u1;
         float Jacob = EXACT ? (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om))) : Ijp / (om * om);
-        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE)
-            return LLR * PrI * (1.0f / box_area()) * Us * Jacob * (P[2] / P[1]) * PrM;
+        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE) {
+            /* exact split/merge pair accounting: the merge proposes this pair
+             * with probability (1/k_a + 1/k_b) / (n + 1) (a random partner
+             * within 3 sigma of a random emitter; k = such partners), the
+             * split draws it from either emitter as the first:
+             * (1/n) (q_a / J_a + q_b / J_b) */
+            const float xa = __shfl_sync(BAMF_FULL, tX, jj), ya = __shfl_sync(BAMF_FULL, tY, jj);
+            const float xb = __shfl_sync(BAMF_FULL, tX, tn - 1), yb = __shfl_sync(BAMF_FULL, tY, tn - 1);
+            const float dmax = 3.0f * sigma;
+            const float dx = xa - xb, dy = ya - yb;
+            if (!(sqrtf(dx * dx + dy * dy) < dmax)) return 0.0f; /* no merge undoes it */
+            const float ka = (float)near_count_T(jj, dmax), kb = (float)near_count_T(tn - 1, dmax);
+            const float mux = A_X(jj), muy = A_Y(jj);
+            const float qa = pair_density(u1, xa - mux, ya - muy, xa, ya, Ijp);
+            const float qb = pair_density(1.0f - u1, xb - mux, yb - muy, xb, yb, Ijp);
+            return LLR * PrI * (1.0f / box_area()) * (P[2] / P[1]) * PrM * (float)an * (1.0f / ka + 1.0f / kb) /
+                   (qa + qb);
+        }
         return LLR * PrI * PrX * Us * Jacob * (P[1] / P[2]) * PrM;
     }
 
@@ -1323,9 +1362,46 @@ struct ChainWarp {
         float om = 1.0f - u1;
         float Jacob = EXACT ? (float)(__ddiv_rn((double)Ijp, dmul((double)om, (double)om))) : Ijp / (om * om);
         float PrM = MeanN / NEm;
-        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE)
-            return LLR / (PrI * (1.0f / box_area()) * Jacob * Us * PrM * P[2] / P[1]);
+        if (!EXACT && K->proposal != BAMF_PROPOSAL_REFERENCE) {
+            /* the inverse of the split ratio that would undo this merge
+             * (pair accounting as in finish_split) */
+            const float dmax = 3.0f * sigma;
+            const float kj = (float)__popc(near_mask(jj, dmax)), ki = (float)__popc(near_mask(ii, dmax));
+            const float muxjp = __shfl_sync(BAMF_FULL, tX, jj > ii ? jj - 1 : jj);
+            const float muyjp = __shfl_sync(BAMF_FULL, tY, jj > ii ? jj - 1 : jj);
+            const float xa = A_X(jj), ya = A_Y(jj), xb = A_X(ii), yb = A_Y(ii);
+            const float qa = pair_density(u1, xa - muxjp, ya - muyjp, xa, ya, Ijp);
+            const float qb = pair_density(1.0f - u1, xb - muxjp, yb - muyjp, xb, yb, Ijp);
+            return LLR / (PrI * (1.0f / box_area()) * (P[2] / P[1]) * PrM * (float)(an - 1) *
+                          (1.0f / kj + 1.0f / ki) / (qa + qb));
+        }
         return LLR / (PrI * PrX * Jacob * Us * PrM * P[1] / P[2]);
+    }
+
+    /* Density of a split that makes (x1, y1) the first emitter, over the
+     * Jacobian: q(u1, u) (1 - u1)^2 / I for intensity fraction u1 and offset
+     * u = (first emitter) - (split emitter).  q: UNIFORM, U(0, 1) x
+     * N(0, Split_std^2)^2; LEARNED, half of that and half the triangular
+     * density on [0.3, 0.7] x the learned density at (x1, y1). */
+    __device__ __forceinline__ float pair_density(float u1, float u2, float u3, float x1, float y1, float I) const
+    {
+        const float s = K->p.Split_std;
+        float q = normpdf(u2, 0.0f, s) * normpdf(u3, 0.0f, s);
+        if (K->proposal == BAMF_PROPOSAL_LEARNED) {
+            const int64_t off = B->offsets[roi];
+            const float ql = learned_density(x1, y1, X, Y, npix, B->birth_cdf + off, B->birth_sub + 16 * off);
+            const float tri = fmaxf(0.0f, 1.0f - fabsf(u1 - 0.5f) * 5.0f) * 5.0f;
+            q = 0.5f * q + 0.5f * tri * ql;
+        }
+        const float om = 1.0f - u1;
+        return q * om * om / I;
+    }
+    /* emitters of T within dmin of T's emitter k (k excluded) */
+    __device__ __forceinline__ int near_count_T(int k, float dmin) const
+    {
+        const float xk = __shfl_sync(BAMF_FULL, tX, k), yk = __shfl_sync(BAMF_FULL, tY, k);
+        const float dx = tX - xk, dy = tY - yk;
+        return __popc(__ballot_sync(BAMF_FULL, lane < tn && lane != k && sqrtf(dx * dx + dy * dy) < dmin));
     }
 
     /* Area of the extended box [-Bnd, X+Bnd] x [-Bnd, Y+Bnd] that test()
@@ -1349,6 +1425,14 @@ struct ChainWarp {
             *by = (float)(-bnd) + (float)(Y + 2 * bnd) * urand();
             return;
         }
+        learned_position(bx, by);
+    }
+
+    /* A position drawn from the learned density: a pixel from the ROI's
+     * running sum birth_cdf, a sub-cell from birth_sub, a uniform point in
+     * the sub-cell.  Call with the whole warp. */
+    __device__ __forceinline__ void learned_position(float *bx, float *by)
+    {
         const int64_t off = B->offsets[roi];
         const float *cdf = B->birth_cdf + off;
         float rr = urand() * __ldg(&cdf[npix - 1]);
