@@ -258,11 +258,17 @@ typedef struct bamf_roi_batch {
      *                            LLR * MeanN/(NEm+1) * P_death/P_birth and death
      *                            its inverse; raw phase probabilities in every
      *                            ratio; split/merge position prior 1/area of
-     *                            the extended box
+     *                            the extended box, and the exact split/merge
+     *                            pair accounting (the merge's pick of the pair,
+     *                            both orderings of a split, unmergeable splits
+     *                            rejected), which the reference's ratio omits
      *   BAMF_PROPOSAL_LEARNED    UNIFORM, with the birth position drawn half of
      *                            the time from a per-ROI density over 4x4
-     *                            sub-cells of each pixel; its exact density
-     *                            enters the birth and death ratios
+     *                            sub-cells of each pixel, and half of the
+     *                            splits placing the first emitter from that
+     *                            density (intensity fraction triangular on
+     *                            [0.3, 0.7]); the exact mixture densities enter
+     *                            the birth, death, split and merge ratios
      * Anything but REFERENCE needs BAMF_ARITH_FAST.  LEARNED reads
      *   birth_cdf   [pixel] running sum of the pixel probabilities, laid out
      *               like data (ROI k at offsets[k], y fastest)
