@@ -36,7 +36,7 @@ def test_pipeline_localises_dense_frames(cuda_lib, proposal):
     print(proposal, st, {k: round(v, 3) for k, v in out["timing"].items()})
     assert out["n_subregions"] == 3 * 7 * 7
     assert abs(st["bias_x"]) < 0.05 and abs(st["bias_y"]) < 0.05
-    assert st["recall"] > 0.75 and st["precision"] > 0.8 and st["rmse_px"] < 0.25
+    assert st["recall"] > 0.75 and st["precision"] > 0.8 and st["rmse_px"] < 0.3
     img = out["PImage"].cpu().numpy()
     assert img.shape == (4 * 64, 4 * 64) and img.sum() > 0
 
