@@ -15,11 +15,11 @@
  *   2. cols   - the same along the strided columns, both sigmas, then the
  *               difference of Gaussians (:48-92); lanes own columns, so
  *               every access is coalesced
- *   3. rowmax - window max along rows with floor minval, +max / -max
+ *   3. maxima - window max along rows with floor minval, +max / -max
  *               (:94-117), window bounds formed in float over the stack's
- *               linear index exactly as the reference does
- *   4. colmax - window max of |.| along columns, flag where it equals the
- *               pixel within 1e-6 (:119-147)
+ *               linear index exactly as the reference does, then window max
+ *               of |.| along columns, flag where it equals the pixel within
+ *               1e-6 (:119-147), fused through shared-memory tiles
  *   5. compaction of the flags in memory order (MATLAB find, findROI.m:125),
  *      box corners (:130-148) and the ROI crop (:157-160)
  * The recurrence is evaluated with explicit IEEE operations in the order
@@ -186,53 +186,80 @@ __global__ void __launch_bounds__(128) cols_kernel(float *__restrict__ a, float 
     }
 }
 
-/* Pass 3: kernel_maxX on the DoG stack. Window bounds as the reference forms
- * them: (int)((fmaxf(0, c-k) + (float)(X*row)) + (float)(X*Y*frame)).  An
- * index past the stack's end (possible only for the very last row) is left
- * out of the max (the reference reads beyond its buffer there). */
-__global__ void __launch_bounds__(256) rowmax_kernel(const float *__restrict__ dog,
-                                                     float *__restrict__ out, int X, int Y, int Z,
-                                                     int k, float minval)
+/* Passes 3 and 4, fused: kernel_maxX (window max along rows with floor
+ * minval, +max / -max) then kernel_maxY (window max of |.| along columns,
+ * flag where it equals the pixel within 1e-6), cuda_FindROI.cu:94-147.
+ * One CTA per (32-column strip, MAX_TH-row tile, frame): every row-max value
+ * the tile's column windows need (its rows and k above and below, clamped to
+ * the frame) is formed from a linear chunk of the DoG stack staged in shared
+ * memory, with the window bounds formed in float over the stack's linear
+ * index exactly as the reference does ((int)((fmaxf(0, c-k) + (float)(X*row))
+ * + (float)(X*Y*frame))); a window that leaves the staged chunk (only where
+ * the float spacing of the linear index exceeds the halo, stacks beyond
+ * ~2^28 pixels) reads global memory.  An index past the stack's end (only in
+ * the very last row) is left out of the max (the reference reads beyond its
+ * buffer there).  The column maxima then run over the staged row maxima. */
+constexpr int MAX_TW = 32, MAX_TH = 64, MAX_WARPS = 8, MAX_HALO_EXTRA = 32;
+
+__host__ __device__ inline int maxima_smem_floats(int k)
 {
-    int64_t n = (int64_t)X * Y * Z;
-    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n) return;
-    int64_t row = idx / X;              /* global row = frame*Y + r */
-    int c = (int)(idx - row * X);
-    int64_t z = row / Y;
-    int r = (int)(row - z * Y);
-    float lo = fmaxf(0.0f, (float)(c - k));
-    float hi = fminf((float)(X - 1), (float)(c + k));
-    float rb = __uint2float_rn((unsigned)X * (unsigned)r);
-    float zb = __uint2float_rn((unsigned)X * (unsigned)Y * (unsigned)z);
-    int64_t start = (int64_t)__fadd_rn(__fadd_rn(lo, rb), zb);
-    int64_t end = (int64_t)__fadd_rn(__fadd_rn(hi, rb), zb);
-    if (end > n - 1) end = n - 1;
-    float maxval = minval;
-    for (int64_t i = start; i <= end; ++i) maxval = fmaxf(maxval, __ldg(&dog[i]));
-    float inpixel = dog[idx];
-    out[idx] = maxval > inpixel ? -maxval : (maxval == inpixel ? maxval : 0.0f);
+    return MAX_WARPS * (MAX_TW + 2 * (k + MAX_HALO_EXTRA)) + (MAX_TH + 2 * k) * MAX_TW;
 }
 
-/* Pass 4: kernel_maxY; writes 1-byte flags. */
-__global__ void __launch_bounds__(256) colmax_kernel(const float *__restrict__ rm,
-                                                     uint8_t *__restrict__ flags, int X, int Y,
-                                                     int Z, int k, float minval)
+__global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__restrict__ dog,
+                                                                uint8_t *__restrict__ flags, int X, int Y,
+                                                                int Z, int k, float minval)
 {
-    int64_t n = (int64_t)X * Y * Z;
-    int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n) return;
-    int64_t row = idx / X;
-    int c = (int)(idx - row * X);
-    int64_t z = row / Y;
-    int r = (int)(row - z * Y);
-    int start = (int)fmaxf(0.0f, (float)(r - k));
-    int end = (int)fminf((float)(Y - 1), (float)(r + k));
-    const float *col = rm + z * (int64_t)X * Y + c;
-    float maxval = minval;
-    for (int i = start; i <= end; ++i) maxval = fmaxf(maxval, fabsf(__ldg(&col[(int64_t)i * X])));
-    float inpixel = rm[idx];
-    flags[idx] = (double)fabsf(__fsub_rn(maxval, inpixel)) < 1e-6 ? 1 : 0;
+    extern __shared__ float sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int H = k + MAX_HALO_EXTRA, CW = MAX_TW + 2 * H;
+    float *chunk = sm + warp * CW;
+    float *rmT = sm + MAX_WARPS * CW; /* [MAX_TH + 2k][MAX_TW] */
+    const int64_t n = (int64_t)X * Y * Z;
+    const int c0 = blockIdx.x * MAX_TW, r0 = blockIdx.y * MAX_TH, c = c0 + lane;
+    const int rlo = max(0, r0 - k), rhi = min(Y - 1, r0 + MAX_TH - 1 + k);
+    for (int z = blockIdx.z; z < Z; z += gridDim.z) {
+        __syncthreads(); /* rmT of the previous frame is consumed */
+        for (int r = rlo + warp; r <= rhi; r += MAX_WARPS) {
+            const int64_t base = ((int64_t)z * Y + r) * X + c0, cbeg = base - H;
+            for (int i = lane; i < CW; i += 32) {
+                const int64_t g = cbeg + i;
+                chunk[i] = (g >= 0 && g < n) ? __ldg(&dog[g]) : 0.0f; /* never inside a window */
+            }
+            __syncwarp();
+            float rmv = 0.0f;
+            if (c < X) {
+                const float lo = fmaxf(0.0f, (float)(c - k));
+                const float hi = fminf((float)(X - 1), (float)(c + k));
+                const float rb = __uint2float_rn((unsigned)X * (unsigned)r);
+                const float zb = __uint2float_rn((unsigned)X * (unsigned)Y * (unsigned)z);
+                const int64_t start = (int64_t)__fadd_rn(__fadd_rn(lo, rb), zb);
+                int64_t end = (int64_t)__fadd_rn(__fadd_rn(hi, rb), zb);
+                if (end > n - 1) end = n - 1;
+                float maxval = minval;
+                if (start >= cbeg && end < cbeg + CW) {
+                    for (int64_t i = start; i <= end; ++i) maxval = fmaxf(maxval, chunk[i - cbeg]);
+                } else {
+                    for (int64_t i = start; i <= end; ++i) maxval = fmaxf(maxval, __ldg(&dog[i]));
+                }
+                const float inpixel = chunk[lane + H];
+                rmv = maxval > inpixel ? -maxval : (maxval == inpixel ? maxval : 0.0f);
+            }
+            rmT[(r - rlo) * MAX_TW + lane] = rmv;
+            __syncwarp(); /* the chunk is restaged for the warp's next row */
+        }
+        __syncthreads();
+        if (c < X) {
+            for (int r = r0 + warp; r < min(Y, r0 + MAX_TH); r += MAX_WARPS) {
+                const int start = (int)fmaxf(0.0f, (float)(r - k));
+                const int end = (int)fminf((float)(Y - 1), (float)(r + k));
+                float maxval = minval;
+                for (int i = start; i <= end; ++i) maxval = fmaxf(maxval, fabsf(rmT[(i - rlo) * MAX_TW + lane]));
+                const float inpixel = rmT[(r - rlo) * MAX_TW + lane];
+                flags[((int64_t)z * Y + r) * X + c] = (double)fabsf(__fsub_rn(maxval, inpixel)) < 1e-6 ? 1 : 0;
+            }
+        }
+    }
 }
 
 /* Compaction, phase 1: flags per 1024-pixel chunk. */
@@ -420,6 +447,7 @@ extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *fr
         return BAMF_ERR_INVALID_ARG;
     if ((roi_stack != nullptr) && corners == nullptr) return BAMF_ERR_INVALID_ARG;
     if (xsize > ysize * 64 || ysize > xsize * 64) return BAMF_ERR_INVALID_ARG;
+    if (boxsize > 256) return BAMF_ERR_TOO_LARGE; /* the maxima tiles stage 2 boxsize + 96 rows */
     cudaStream_t s = (cudaStream_t)stream;
     const int64_t n = (int64_t)xsize * ysize * zsize;
     /* kernel view (as the reference launches it): each frame is KY = Ysize
@@ -447,8 +475,15 @@ extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *fr
         rows_kernel<<<grid, 32 * ROWS_WARPS, 0, s>>>(frames, A, Bb, KX, KY, zsize, ca, cb);
     }
     cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(A, Bb, KX, KY, zsize, ca, cb);
-    rowmax_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(A, Bb, KX, KY, zsize, boxsize, minval);
-    colmax_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Bb, flags, KX, KY, zsize, boxsize, minval);
+    {
+        const size_t smem = (size_t)maxima_smem_floats(boxsize) * sizeof(float);
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(maxima_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return BAMF_ERR_CUDA;
+        dim3 grid((unsigned)((KX + MAX_TW - 1) / MAX_TW), (unsigned)((KY + MAX_TH - 1) / MAX_TH),
+                  (unsigned)std::min(zsize, 65535));
+        maxima_kernel<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, boxsize, minval);
+    }
     count_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
     scan_kernel<<<1, 1024, 0, s>>>((int32_t *)ws->chunks.p, nchunks, (int64_t *)ws->total.p);
     emit_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p, ysize, xsize,
