@@ -167,7 +167,28 @@ __global__ void __launch_bounds__(128) cols_kernel(float *__restrict__ a, float 
     float a1, a2, a3, b1, b2, b3;
     a1 = a2 = a3 = pa[0];
     b1 = b2 = b3 = pb[0];
-    for (int i = 0; i < Y; ++i) {
+    /* the loads of a block of COLS_PF rows are issued before its
+     * recurrence steps (they do not depend on it), hiding their latency */
+    constexpr int COLS_PF = 8;
+    int i = 0;
+    for (; i + COLS_PF <= Y; i += COLS_PF) {
+        float va[COLS_PF], vb[COLS_PF];
+#pragma unroll
+        for (int u = 0; u < COLS_PF; ++u) {
+            va[u] = pa[(int64_t)(i + u) * X];
+            vb[u] = pb[(int64_t)(i + u) * X];
+        }
+#pragma unroll
+        for (int u = 0; u < COLS_PF; ++u) {
+            float ta = iir_step(va[u], a1, a2, a3, ca);
+            float tb = iir_step(vb[u], b1, b2, b3, cb);
+            pa[(int64_t)(i + u) * X] = ta;
+            pb[(int64_t)(i + u) * X] = tb;
+            a3 = a2; a2 = a1; a1 = ta;
+            b3 = b2; b2 = b1; b1 = tb;
+        }
+    }
+    for (; i < Y; ++i) {
         float ta = iir_step(pa[(int64_t)i * X], a1, a2, a3, ca);
         float tb = iir_step(pb[(int64_t)i * X], b1, b2, b3, cb);
         pa[(int64_t)i * X] = ta;
@@ -177,7 +198,24 @@ __global__ void __launch_bounds__(128) cols_kernel(float *__restrict__ a, float 
     }
     a1 = a2 = a3 = pa[(int64_t)(Y - 1) * X];
     b1 = b2 = b3 = pb[(int64_t)(Y - 1) * X];
-    for (int i = Y - 1; i >= 0; --i) {
+    i = Y - 1;
+    for (; i - COLS_PF + 1 >= 0; i -= COLS_PF) {
+        float va[COLS_PF], vb[COLS_PF];
+#pragma unroll
+        for (int u = 0; u < COLS_PF; ++u) {
+            va[u] = pa[(int64_t)(i - u) * X];
+            vb[u] = pb[(int64_t)(i - u) * X];
+        }
+#pragma unroll
+        for (int u = 0; u < COLS_PF; ++u) {
+            float ta = iir_step(va[u], a1, a2, a3, ca);
+            float tb = iir_step(vb[u], b1, b2, b3, cb);
+            pa[(int64_t)(i - u) * X] = __fsub_rn(ta, tb); /* kernel_subtract */
+            a3 = a2; a2 = a1; a1 = ta;
+            b3 = b2; b2 = b1; b1 = tb;
+        }
+    }
+    for (; i >= 0; --i) {
         float ta = iir_step(pa[(int64_t)i * X], a1, a2, a3, ca);
         float tb = iir_step(pb[(int64_t)i * X], b1, b2, b3, cb);
         pa[(int64_t)i * X] = __fsub_rn(ta, tb); /* kernel_subtract */
@@ -199,7 +237,7 @@ __global__ void __launch_bounds__(128) cols_kernel(float *__restrict__ a, float 
  * ~2^28 pixels) reads global memory.  An index past the stack's end (only in
  * the very last row) is left out of the max (the reference reads beyond its
  * buffer there).  The column maxima then run over the staged row maxima. */
-constexpr int MAX_TW = 32, MAX_TH = 64, MAX_WARPS = 8, MAX_HALO_EXTRA = 32;
+constexpr int MAX_TW = 32, MAX_TH = 128, MAX_WARPS = 8, MAX_HALO_EXTRA = 32;
 
 __host__ __device__ inline int maxima_smem_floats(int k)
 {
@@ -208,7 +246,7 @@ __host__ __device__ inline int maxima_smem_floats(int k)
 
 __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__restrict__ dog,
                                                                 uint8_t *__restrict__ flags, int X, int Y,
-                                                                int Z, int k, float minval)
+                                                                int Z, int k, float minval, float eps_hi)
 {
     extern __shared__ float sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -238,7 +276,9 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
                 if (end > n - 1) end = n - 1;
                 float maxval = minval;
                 if (start >= cbeg && end < cbeg + CW) {
-                    for (int64_t i = start; i <= end; ++i) maxval = fmaxf(maxval, chunk[i - cbeg]);
+                    const int s0 = (int)(start - cbeg), s1 = (int)(end - cbeg);
+#pragma unroll 4
+                    for (int i = s0; i <= s1; ++i) maxval = fmaxf(maxval, chunk[i]);
                 } else {
                     for (int64_t i = start; i <= end; ++i) maxval = fmaxf(maxval, __ldg(&dog[i]));
                 }
@@ -254,9 +294,13 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
                 const int start = (int)fmaxf(0.0f, (float)(r - k));
                 const int end = (int)fminf((float)(Y - 1), (float)(r + k));
                 float maxval = minval;
-                for (int i = start; i <= end; ++i) maxval = fmaxf(maxval, fabsf(rmT[(i - rlo) * MAX_TW + lane]));
+                const float *col = rmT + (start - rlo) * MAX_TW + lane;
+#pragma unroll 4
+                for (int i = 0; i <= end - start; ++i) maxval = fmaxf(maxval, fabsf(col[i * MAX_TW]));
                 const float inpixel = rmT[(r - rlo) * MAX_TW + lane];
-                flags[((int64_t)z * Y + r) * X + c] = (double)fabsf(__fsub_rn(maxval, inpixel)) < 1e-6 ? 1 : 0;
+                /* (double)d < 1e-6 for a float d is d < eps_hi, the float
+                 * just above the double 1e-6 */
+                flags[((int64_t)z * Y + r) * X + c] = fabsf(__fsub_rn(maxval, inpixel)) < eps_hi ? 1 : 0;
             }
         }
     }
@@ -482,7 +526,10 @@ extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *fr
             return BAMF_ERR_CUDA;
         dim3 grid((unsigned)((KX + MAX_TW - 1) / MAX_TW), (unsigned)((KY + MAX_TH - 1) / MAX_TH),
                   (unsigned)std::min(zsize, 65535));
-        maxima_kernel<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, boxsize, minval);
+        /* the smallest float above the double 1e-6 */
+        float eps_hi = (float)1e-6;
+        if ((double)eps_hi <= 1e-6) eps_hi = std::nextafter(eps_hi, 1.0f);
+        maxima_kernel<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, boxsize, minval, eps_hi);
     }
     count_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
     scan_kernel<<<1, 1024, 0, s>>>((int32_t *)ws->chunks.p, nchunks, (int64_t *)ws->total.p);
