@@ -74,7 +74,7 @@ __device__ __forceinline__ float iir_step(float w0, float w1, float w2, float w3
  * grid is persistent with ROWS_CTAS_PER_SM CTAs per SM so that the rows in
  * flight (and their forward results) stay within L2. */
 constexpr int ROWS_WARPS = 3;
-constexpr int ROWS_CTAS_PER_SM = 3;
+constexpr int ROWS_CTAS_PER_SM = 5;
 
 __global__ void __launch_bounds__(32 * ROWS_WARPS) rows_kernel(const float *__restrict__ in,
                                                                float *__restrict__ out_a,
