@@ -316,7 +316,8 @@ def main():
     L.bamf_probe_peaks.restype = C.c_int
     L.bamf_probe_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
 
-    b, rj, p, bg0 = workload(a.n_rois, 2 + rank, a.jumps)
+    from bamf_gb300 import replicas
+    b, rj, p, bg0 = workload(a.n_rois, replicas.rank_seed(2, rank), a.jumps)
     dev = {
         "data": torch.from_numpy(b.data).cuda(), "offsets": torch.from_numpy(b.offsets).cuda(),
         "xsize": torch.from_numpy(b.xsize).cuda(), "ysize": torch.from_numpy(b.ysize).cuda(),
@@ -365,12 +366,8 @@ def main():
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    total = sum(times)
-    if dist:
-        t = torch.tensor([total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
-    value = world * a.steps * n / total
+    total = replicas.max_over_ranks(sum(times), dist, "cuda")
+    value = replicas.whole_job_rate(a.steps * n, world, total)
     step_s = total / a.steps
 
     # roofline: one MUFU log2 per ROI pixel per scored proposal
@@ -387,13 +384,15 @@ def main():
         host_out = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=1234,
                               arith="fast", bg0=bg0)  # warm
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         t0 = time.perf_counter()
         host_out = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=1234,
                               arith="fast", bg0=bg0)
-        dt = time.perf_counter() - t0
+        dt = replicas.max_over_ranks(time.perf_counter() - t0, dist, "cuda")
         h2d = b.data.nbytes + b.offsets.nbytes + b.xsize.nbytes + b.ysize.nbytes + b.sigma.nbytes
         d2h = sum(v.nbytes for v in host_out.values())
-        e2e = {"value": world * n / dt, "unit": "ROIs/s", "h2d_bytes_per_step": int(h2d),
+        e2e = {"value": replicas.whole_job_rate(n, world, dt), "unit": "ROIs/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
 
     # per step: order_kernel, one sampler launch per non-empty size class, map_n_kernel
