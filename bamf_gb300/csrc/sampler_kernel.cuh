@@ -235,20 +235,24 @@ __device__ __forceinline__ float shared_uniform(uint32_t seed, uint32_t grp, uin
  * times the pixel's 16 sub-cell probabilities sub (16 cells per px^2). */
 /* The learned position density at (x, y) per px^2 (pixel probability from
  * the running sum, sub-cell probability, 16 sub-cells per px^2); 0 outside
- * the ROI. */
+ * the ROI.  Call with the whole warp on the same arguments: lanes 0..15 load
+ * the pixel's sub-cell probabilities and a butterfly sums them. */
 static __device__ __noinline__ float learned_density(float x, float y, int X, int Y, int npix,
                                                      const float *__restrict__ cdf,
                                                      const float *__restrict__ sub)
 {
     if (!(x >= 0.0f && y >= 0.0f && x < (float)X && y < (float)Y)) return 0.0f;
+    const int lane = threadIdx.x & 31;
     int px = min((int)x, X - 1), py = min((int)y, Y - 1);
     int pix = py + px * Y;
     int sc = min((int)((y - (float)py) * 4.0f), 3) + 4 * min((int)((x - (float)px) * 4.0f), 3);
     float pp = __ldg(&cdf[pix]) - (pix > 0 ? __ldg(&cdf[pix - 1]) : 0.0f);
     const float *sp = sub + 16 * pix;
-    float ps = 0.0f;
-    for (int k = 0; k < 16; ++k) ps += __ldg(&sp[k]);
-    return (pp / __ldg(&cdf[npix - 1])) * (__ldg(&sp[sc]) / ps) * 16.0f;
+    const float v = lane < 16 ? __ldg(&sp[lane]) : 0.0f;
+    float ps = v;
+    for (int o = 1; o < 32; o <<= 1) ps += __shfl_xor_sync(0xffffffffu, ps, o);
+    const float vs = __shfl_sync(0xffffffffu, v, sc);
+    return (pp / __ldg(&cdf[npix - 1])) * (vs / ps) * 16.0f;
 }
 
 /* (1 / A) / q(x, y) for the birth mixture q = 1/2 learned + 1/2 uniform on
@@ -1436,16 +1440,16 @@ struct ChainWarp {
         const int64_t off = B->offsets[roi];
         const float *cdf = B->birth_cdf + off;
         float rr = urand() * __ldg(&cdf[npix - 1]);
-        int pix = npix - 1;
-#pragma unroll 1
-        for (int b0 = 0; b0 < npix; b0 += 32) {
-            int q = b0 + lane;
-            uint32_t m = __ballot_sync(BAMF_FULL, q < npix && rr <= __ldg(&cdf[min(q, npix - 1)]));
-            if (m) {
-                pix = b0 + __ffs(m) - 1;
-                break;
-            }
-        }
+        /* the first pixel whose running sum reaches rr, in two rounds of
+         * loads: the first 32-pixel block whose last sum reaches it (npix <=
+         * 1024, so one lane per block), then the pixel inside it */
+        const int nblk = (npix + 31) >> 5;
+        const uint32_t mb =
+            __ballot_sync(BAMF_FULL, lane < nblk && rr <= __ldg(&cdf[min(32 * lane + 31, npix - 1)]));
+        const int blk = mb ? __ffs(mb) - 1 : nblk - 1;
+        const int q = 32 * blk + lane;
+        const uint32_t mp = __ballot_sync(BAMF_FULL, q < npix && rr <= __ldg(&cdf[min(q, npix - 1)]));
+        const int pix = mp ? 32 * blk + __ffs(mp) - 1 : npix - 1;
         const float *sub = B->birth_sub + 16 * (off + pix);
         float v = lane < 16 ? __ldg(&sub[lane]) : 0.0f;
         for (int o = 1; o < 16; o <<= 1) {
