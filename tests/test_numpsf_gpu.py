@@ -43,18 +43,23 @@ def test_exact_chain_sampled_psf_matches_oracle(cuda_lib, oracle_port, case, k):
 
 
 def test_exact_chain_sampled_psf_start_state_all_moves(cuda_lib, oracle_port):
-    """All 8 move types, drift, a start state and a nonzero stream offset."""
+    """All 8 move types, background emitters (IsBackg = 1, a background
+    prior), an sCMOS map, drift, a start state and a nonzero stream offset."""
     b, rj, p, _ = _setup(4, 800, GAUSS, seed=3)
     rj.P_Burnin = [0.3, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1]
     rj.P_Trials = [0.4, 0.0, 0.0, 0.05, 0.05, 0.15, 0.15, 0.2]
+    rj.IsBackg = 1
     p = rjstruct.mcmc_params(rj, drift_x=0.3, drift_y=-0.2)
     for i, v in enumerate(GAUSS.shape):
         p.PSFsize[i] = v
     k = 2
+    back = synth.lognormal_pdf(np.arange(0, 12001, 10.0), 200.0, 0.5).astype(np.float32)
+    scmos = np.random.default_rng(4).uniform(0.0, 3.0, b.roi(k).shape).astype(np.float32)
     e0 = (b.true_i[k].astype(np.float32), b.true_x[k].astype(np.float32), b.true_y[k].astype(np.float32), 8.0)
-    args = (p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons)
-    ref = oracle_port.run_chain("port", b.roi(k), *args, e0=e0, rng=(5, 77, 21), sampled_psf=GAUSS)
-    got = sampler.crjmcmc_raw(b.roi(k), *args, e0=e0, rng=(5, 77, 21), arith="exact", sampled_psf=GAUSS)
+    args = (p, rj.P_Offset, rj.P_EmPhotons, back)
+    ref = oracle_port.run_chain("port", b.roi(k), *args, e0=e0, rng=(5, 77, 21), sampled_psf=GAUSS, scmos=scmos)
+    got = sampler.crjmcmc_raw(b.roi(k), *args, e0=e0, rng=(5, 77, 21), arith="exact", sampled_psf=GAUSS,
+                              scmos=scmos)
     assert_same_chain(got, ref)
 
 

@@ -270,3 +270,27 @@ def test_captured_batch_graph_replays_eager_results_on_new_data(cuda_lib, arith)
     for k, v in ref2.items():
         np.testing.assert_array_equal(outs[k].cpu().numpy(), v, err_msg=k)
     g.close()
+
+
+@pytest.mark.parametrize("k", [0, 3])
+def test_exact_chain_all_moves_background_emitters_and_scmos(cuda_lib, oracle_port, k):
+    """Settings the plain workload does not reach, bit for bit against the
+    oracle: all 8 move types (gSplit, gMerge, backFore on), IsBackg = 1 with
+    a background-emitter prior, an sCMOS correction map, drift, a start
+    state and a nonzero stream offset."""
+    b, rj = _c0(6, steps=1000, seed=5)
+    rj.P_Burnin = [0.3, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1, 0.1]
+    rj.P_Trials = [0.4, 0.0, 0.0, 0.05, 0.05, 0.15, 0.15, 0.2]
+    rj.IsBackg = 1
+    p = rjstruct.mcmc_params(rj, drift_x=0.3, drift_y=-0.2)
+    grid = np.arange(0, 12001, 10.0)
+    back = synth.lognormal_pdf(grid, 200.0, 0.5).astype(np.float32)
+    rng = np.random.default_rng(k)
+    roi = b.roi(k)
+    scmos = rng.uniform(0.0, 3.0, roi.shape).astype(np.float32)
+    e0 = (b.true_i[k].astype(np.float32), b.true_x[k].astype(np.float32), b.true_y[k].astype(np.float32), 8.0)
+    args = (p, rj.P_Offset, rj.P_EmPhotons, back)
+    ref = oracle_port.run_chain("port", roi, *args, e0=e0, rng=(3, 500 + k, 11), scmos=scmos)
+    got = sampler.crjmcmc_raw(roi, *args, e0=e0, rng=(3, 500 + k, 11), scmos=scmos, arith="exact")
+    assert ref["counters"]["N_birthBg"] > 1 or ref["counters"]["N_jumpBg"] > 1   # background emitters appear
+    assert_same_chain(got, ref)
