@@ -294,3 +294,55 @@ def test_exact_chain_all_moves_background_emitters_and_scmos(cuda_lib, oracle_po
     got = sampler.crjmcmc_raw(roi, *args, e0=e0, rng=(3, 500 + k, 11), scmos=scmos, arith="exact")
     assert ref["counters"]["N_birthBg"] > 1 or ref["counters"]["N_jumpBg"] > 1   # background emitters appear
     assert_same_chain(got, ref)
+
+
+def test_fast_sampler_matches_the_reference_posterior_ks(cuda_lib, oracle_port):
+    """With its own RNG and move-synchronous CTAs, the fast sampler draws
+    from the posterior of the reference algorithm: on one ROI, the final
+    states of 384 independent GPU chains and of 192 oracle chains (the C
+    restatement, bit-identical to the reference build; independent streams)
+    agree in the emitter count (total variation) and in the emitters' X and
+    Y positions (two-sample Kolmogorov-Smirnov)."""
+    import concurrent.futures as cf
+    from scipy.stats import ks_2samp
+    b0, rj = _c0(8, steps=2000, seed=6)
+    k = int(np.argsort(b0.true_n)[len(b0.true_n) // 2])
+    p = rjstruct.mcmc_params(rj)
+    bg0 = rjstruct.initial_bg(rj)
+    roi = b0.roi(k)
+    args = (p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons)
+
+    def oracle_final(c):
+        r = oracle_port.run_chain("port", roi, *args, e0=([], [], [], bg0), rng=(77, 10000 + c, 0))
+        ch = r["chain"]
+        n, I, X, Y, S = sampler._emitters_of(ch, len(ch["N"]) - 1)
+        keep = (S == 1) if int(ch["N"][-1]) > 0 else np.zeros(0, bool)
+        return int(ch["N"][-1]), X[keep], Y[keep]
+
+    with cf.ThreadPoolExecutor(16) as ex:
+        ora = list(ex.map(oracle_final, range(192)))
+    copies = 384
+    b = synth._pack([roi] * copies, [b0.sigma[k]] * copies, [b0.bg[k]] * copies, [b0.true_n[k]] * copies,
+                    [b0.true_x[k]] * copies, [b0.true_y[k]] * copies, [b0.true_i[k]] * copies)
+    s = sampler.Sampler()
+    got = s.run_host(b, *args, seed=41, arith="fast", bg0=bg0)
+    assert (got["status"] == 0).all()
+    fs, fn = got["final_state"], got["final_n"]
+    nmax = (fs.shape[1] - 4) // 4
+    gx = np.concatenate([fs[i, 4 + nmax:4 + nmax + fn[i]][fs[i, 4 + 3 * nmax:4 + 3 * nmax + fn[i]] == 1]
+                         for i in range(copies)])
+    gy = np.concatenate([fs[i, 4 + 2 * nmax:4 + 2 * nmax + fn[i]][fs[i, 4 + 3 * nmax:4 + 3 * nmax + fn[i]] == 1]
+                         for i in range(copies)])
+    on = np.array([o[0] for o in ora])
+    ox = np.concatenate([o[1] for o in ora])
+    oy = np.concatenate([o[2] for o in ora])
+    K = 12
+    hg = np.bincount(np.minimum(fn, K - 1), minlength=K) / copies
+    ho = np.bincount(np.minimum(on, K - 1), minlength=K) / len(on)
+    tv = 0.5 * np.abs(hg - ho).sum()
+    px = ks_2samp(gx, ox).pvalue
+    py = ks_2samp(gy, oy).pvalue
+    print(f"ROI {k} (true N {b0.true_n[k]}): count TV {tv:.3f}; KS p-values X {px:.3f}, Y {py:.3f}; "
+          f"mean N gpu {fn.mean():.2f} oracle {on.mean():.2f}")
+    assert tv < 0.12
+    assert px > 0.001 and py > 0.001
