@@ -131,6 +131,7 @@ def analyze_frames(frames: np.ndarray, rj, box: int = 10, overlap: int = 3, prop
     per = sr["Xsub"] * sr["Ysub"]
     if grids:
         extra = {"pgrid": torch.zeros(per * Tz * Tz, dtype=torch.float32, device="cuda"),
+                 "pback": torch.zeros(per * Tz * Tz, dtype=torch.float32, device="cuda"),
                  "grid_stride": Tz * Tz, "grid_ld": Tz,
                  "grid_slot": (sr["roi_ind"] - 1).contiguous()}
     t = time.perf_counter()
@@ -149,13 +150,14 @@ def analyze_frames(frames: np.ndarray, rj, box: int = 10, overlap: int = 3, prop
     t = time.perf_counter()
     if grids:
         # one grid per sub-region position, summed over frames; frame 1's ROI_Struct rows describe them
-        g = extra["pgrid"]
         xs, ys = sr["xsize"][:per].contiguous(), sr["ysize"][:per].contiguous()
         ri = sr["roi_ind"][:per].contiguous()
-        tiles.remove_overlapping_device(g, per, Tz, xs, ys, ri, sr["Xsub"], sr["Ysub"], overlap, Zm)
-        img, bad = tiles.stitch_rois_device(g, per, Tz, xs, ys, sr["frame_num"][:per].contiguous(), ri,
-                                            (Y, X, 1), box, overlap, Zm)
-        out["PImage"] = img.view(Zm * X, Zm * Y).t()
+        for key, name in (("pgrid", "PImage"), ("pback", "PBg")):
+            g = extra[key]
+            tiles.remove_overlapping_device(g, per, Tz, xs, ys, ri, sr["Xsub"], sr["Ysub"], overlap, Zm)
+            img, bad = tiles.stitch_rois_device(g, per, Tz, xs, ys, sr["frame_num"][:per].contiguous(), ri,
+                                                (Y, X, 1), box, overlap, Zm)
+            out[name] = img.view(Zm * X, Zm * Y).t()
     _sync()
     timing["stitch"] = time.perf_counter() - t
     rec = res["refined"]
