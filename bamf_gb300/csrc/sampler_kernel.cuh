@@ -1490,26 +1490,51 @@ struct ChainWarp {
             __syncwarp();
             total = E[npix - 1];
         } else {
-            /* contiguous chunk per lane, lane-local serial sum, warp scan */
-            int per = (npix + 31) >> 5;
-            int p0 = min(lane * per, npix), p1 = min(p0 + per, npix);
+            /* Fast: the residual's running sum is never stored.  Lane j sums
+             * the contiguous chunk j of ceil(npix/32) pixels, a warp scan
+             * gives the chunk ends, a ballot finds the chunk that reaches
+             * rr, and that chunk's pixels (one per lane) are scanned again
+             * to find the pixel: the same draw (the first pixel whose
+             * running sum reaches rr), two passes over the chunk's pixels
+             * instead of three over all. */
+            const int per = (npix + 31) >> 5;
+            const int p0 = min(lane * per, npix), p1 = min(p0 + per, npix);
             float s = 0.0f;
 #pragma unroll 1
             for (int p = p0; p < p1; ++p) {
                 float v = D[p] - M[p];
                 s += v > 0.0f ? v : 0.0f;
-                Pf[p] = s;
             }
             float incl = s;
             for (int o = 1; o < 32; o <<= 1) {
                 float t = __shfl_up_sync(BAMF_FULL, incl, o);
                 if (lane >= o) incl += t;
             }
-            float excl = incl - s;
-#pragma unroll 1
-            for (int p = p0; p < p1; ++p) Pf[p] += excl;
-            __syncwarp();
             total = __shfl_sync(BAMF_FULL, incl, 31);
+            const float rr = total * urand();
+            const uint32_t mc = __ballot_sync(BAMF_FULL, p0 < p1 && rr <= incl);
+            int ii;
+            if (mc) {
+                const int cj = __ffs(mc) - 1;
+                const float base = __shfl_sync(BAMF_FULL, incl - s, cj);
+                const int q0 = cj * per, q = q0 + lane;
+                float v = 0.0f;
+                if (lane < per && q < npix) {
+                    v = D[q] - M[q];
+                    v = v > 0.0f ? v : 0.0f;
+                }
+                for (int o = 1; o < 32; o <<= 1) {
+                    float t = __shfl_up_sync(BAMF_FULL, v, o);
+                    if (lane >= o) v += t;
+                }
+                const uint32_t mq = __ballot_sync(BAMF_FULL, lane < per && q < npix && rr <= base + v);
+                ii = mq ? q0 + __ffs(mq) - 1 : min(q0 + per, npix) - 1;
+            } else {
+                ii = npix; /* rr beyond the total (total 0: every pixel zero) */
+            }
+            *by = (float)(ii - Y * (ii / Y)) + urand() - 0.5f;
+            *bx = (float)(int)floorf((float)ii / (float)Y) + urand() - 0.5f;
+            return;
         }
         float rr = total * urand();
         int first = npix;
