@@ -566,6 +566,13 @@ bamf_status bamf_gauss_mle_fit_host(const float *rois, int sz, int nfits, int fi
  * roofline denominators of the sampler.  Not used by any sampler path. */
 bamf_status bamf_probe_peaks(double *fp32_flops, double *mufu_ops);
 
+/* Known-answer check of the 5th-generation tensor-core path (tcgen05 MMA
+ * from shared-memory descriptors into TMEM, read back with tcgen05.ld): a
+ * 128 x 32 x 16 BF16 product of small integers.  *max_abs_err = the largest
+ * deviation from the exact product (0 when the path works), *timed_out = 1
+ * if the MMA's completion did not arrive within the kernel's bounded wait. */
+bamf_status bamf_tcgen05_selftest(double *max_abs_err, int *timed_out);
+
 #ifdef __cplusplus
 }
 #endif
