@@ -4,17 +4,18 @@
  * training step, and inference into the sampler's LEARNED birth tables.
  *
  * Layouts.  Activations are channels-last BF16, [roi][p][32] with pixel
- * p = y + 16 x.  The three 32 -> 32 convolutions are implicit GEMMs on the
- * tensor cores (mma.sync m16n8k16, BF16 in, FP32 accumulate): a CTA stages
- * one ROI's activations in shared memory as an 18 x 18 zero-bordered tile
- * with a 40-channel pixel stride (80 bytes: the eight rows an ldmatrix phase
- * reads fall in eight different 16-byte bank groups), an M tile is one image
- * row x (16 pixels along y), N = 32 output channels (4 tiles of 8), and
- * K = 9 taps x 32 input channels (18 steps of 16).  The input gradient of a
- * convolution is the same kernel run with the taps flipped and the channel
- * roles swapped (packed once per step); the weight gradient is a GEMM with
- * M = (tap, input channel) = 288 and K = the pixels of every ROI of the
- * CTA, with both operands read transposed by ldmatrix.trans.
+ * p = y + 16 x.  The three 32 -> 32 convolutions (forward and input
+ * gradient) run on the 5th-generation tensor cores (tcgen05.mma from
+ * shared-memory descriptors into TMEM, conv_tc_kernel): per ROI an implicit
+ * GEMM with M = 256 pixels (two tiles of 128), N = 32, K = 9 taps x 32
+ * channels.  The input gradient of a convolution is the same kernel run with
+ * the taps flipped and the channel roles swapped (packed once per step).
+ * The weight gradient is a GEMM with M = (tap, input channel) = 288 and
+ * K = the pixels of every ROI of the CTA, on mma.sync m16n8k16 with both
+ * operands read transposed by ldmatrix.trans: a CTA stages a ROI's
+ * activations as an 18 x 18 zero-bordered tile with a 40-channel pixel
+ * stride (80 bytes: the eight rows an ldmatrix phase reads fall in eight
+ * different 16-byte bank groups).
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -27,6 +28,7 @@
 #include "bamf.h"
 #include "bamf_cnn.h"
 #include "bamf_philox.h"
+#include "tc_ptx.cuh"
 
 namespace {
 
@@ -46,7 +48,7 @@ static_assert(NPARAM == BAMF_CNN_NPARAM, "parameter count");
 static_assert(O_B1 == O_W1 + 288 && O_BC + NC == NPARAM, "conv1 block and head layout");
 constexpr int O_W[3] = {O_W2, O_W3, O_W4};
 constexpr int O_B[3] = {O_B2, O_B3, O_B4};
-constexpr int PK = 9 * CH * CP; /* packed bf16 weights of one layer */
+constexpr int PKT = 9 * CH * CH; /* tensor-core operand weights of one layer */
 
 typedef __nv_bfloat16 bf16;
 
@@ -54,12 +56,6 @@ typedef __nv_bfloat16 bf16;
 __device__ __forceinline__ uint32_t smem_addr(const void *p)
 {
     return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_addr(p)));
 }
 __device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void *p)
 {
@@ -185,18 +181,21 @@ __global__ void synth_kernel(bamf_synth_params sp, uint32_t seed, uint64_t first
 }
 
 /* -------------------------------------------------------- weight packing */
-/* Wf[l][tap][co][ci] (forward) and Wb[l][tap][ci][co] = W_l[co][ci][8 - tap]
- * (input gradient), BF16, channel stride CP. */
+/* The B operands of the 32 -> 32 convolutions for the tensor cores, per
+ * layer [tap][ci group g][n][8] BF16 (K-major core matrices: 8 n x 8 k):
+ * forward Wf: B[n = co][k = ci] = W_l[co][ci][tap]; input gradient Wb:
+ * B[n = ci][k = co] = W_l[co][ci][8 - tap]. */
 __global__ void pack_kernel(const float *__restrict__ P, bf16 *__restrict__ Wf, bf16 *__restrict__ Wb)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= 3 * 9 * CH * CH) return;
-    int l = i / (9 * CH * CH), rem = i - l * 9 * CH * CH;
+    if (i >= 3 * PKT) return;
+    int l = i / PKT, rem = i - l * PKT;
     int tap = rem / (CH * CH), nk = rem - tap * CH * CH;
     int nn = nk / CH, kk = nk - nn * CH;
     const float *W = P + (l == 0 ? O_W2 : (l == 1 ? O_W3 : O_W4));
-    Wf[l * PK + (tap * CH + nn) * CP + kk] = __float2bfloat16_rn(W[(nn * CH + kk) * 9 + tap]);
-    Wb[l * PK + (tap * CH + nn) * CP + kk] = __float2bfloat16_rn(W[(kk * CH + nn) * 9 + (8 - tap)]);
+    const int o = l * PKT + tap * CH * CH + (kk >> 3) * (CH * 8) + nn * 8 + (kk & 7);
+    Wf[o] = __float2bfloat16_rn(W[(nn * CH + kk) * 9 + tap]);
+    Wb[o] = __float2bfloat16_rn(W[(kk * CH + nn) * 9 + (8 - tap)]);
 }
 
 /* --------------------------------------------------------------- conv1 */
@@ -277,88 +276,135 @@ __global__ void conv1_bwd_kernel(const float *__restrict__ x0, const bf16 *__res
 }
 
 /* -------------------------------------------------- 32 -> 32 convolution */
-/* MODE 0: out = relu(conv(in, Wpk) + bias).  MODE 1 (input gradient):
- * out = conv(in, Wpk) * (mask > 0).  One ROI per CTA iteration, 8 warps,
- * warp w computes image rows x = 2w, 2w+1. */
+/* MODE 0: out = relu(conv(in, W) + bias).  MODE 1 (input gradient):
+ * out = conv(in, W) * (mask > 0).  On the 5th-generation tensor cores: per
+ * ROI an implicit GEMM D[pixel][co] = sum over 9 taps of A_tap[pixel][ci]
+ * B_tap[co][ci], M = 256 pixels as two tiles of 128, N = 32, K = 32 per tap
+ * as two MMAs of 16: 36 tcgen05.mma (BF16 x BF16 -> FP32) issued by one
+ * thread into TMEM (64 columns), completion through an mbarrier, epilogue
+ * from tcgen05.ld.
+ *
+ * A operands straight from shared memory: the ROI is staged as three copies
+ * shifted by ky - 1 along y, each [ci group g][padded x 0..17][y 0..15][8 ci]
+ * BF16, so that for tap (kx, ky) the 128 rows of M tile t (pixels p = 128 t
+ * + m, x = p / 16, y = p mod 16) are 16-byte rows at consecutive addresses
+ * from (8 t + kx) * 16 rows into copy ky: K-major core matrices with SBO =
+ * 128 B and LBO = one ci group.  Borders stay zero.  One ROI per iteration
+ * of a persistent CTA of 128 threads (thread m owns pixels m and 128 + m in
+ * the epilogue).  The mbarrier wait is bounded; a timeout is recorded in
+ * *status and the kernel frees its TMEM and returns. */
+constexpr int TC_GSTRIDE = PS * S * 16;            /* bytes of one ci group of one copy */
+constexpr int TC_COPY = 4 * TC_GSTRIDE;            /* bytes of one shifted copy */
+constexpr size_t SMEM_TC = (size_t)PKT * 2 + 3 * TC_COPY + 16;
+constexpr uint32_t TC_IDESC = bamf::tc::idesc_bf16_f32(128, 32);
+
 template <int MODE>
-__global__ void __launch_bounds__(256) conv_mma_kernel(const bf16 *__restrict__ in, const bf16 *__restrict__ Wpk,
-                                                       const float *__restrict__ bias,
-                                                       const bf16 *__restrict__ mask, bf16 *__restrict__ out,
-                                                       int n)
+__global__ void __launch_bounds__(128) conv_tc_kernel(const bf16 *__restrict__ in, const bf16 *__restrict__ Wt,
+                                                      const float *__restrict__ bias,
+                                                      const bf16 *__restrict__ mask, bf16 *__restrict__ out, int n,
+                                                      int *__restrict__ status)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    bf16 *Ws = (bf16 *)smem_raw;      /* [9][32][CP] */
-    bf16 *T = Ws + PK;                /* [PS][PS][CP] */
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned char *Ws = smem_raw;                    /* [9][4][32][8] bf16 */
+    unsigned char *Cp = smem_raw + PKT * 2;          /* 3 copies */
+    uint64_t *mbar = (uint64_t *)(Cp + 3 * TC_COPY);
+    __shared__ uint32_t tslot;
+    const int t = threadIdx.x, warp = t >> 5;
+    if (warp == 0) bamf::tc::tmem_alloc(&tslot, 64);
     {
-        const uint4 *src = (const uint4 *)Wpk;
+        const uint4 *src = (const uint4 *)Wt;
         uint4 *dst = (uint4 *)Ws;
-        for (int i = t; i < PK * 2 / 16; i += blockDim.x) dst[i] = src[i];
-        /* zero the whole tile once; the interior is overwritten per ROI */
-        uint4 z = make_uint4(0, 0, 0, 0);
-        uint4 *tt = (uint4 *)T;
-        for (int i = t; i < PS * PS * CP * 2 / 16; i += blockDim.x) tt[i] = z;
+        for (int i = t; i < PKT * 2 / 16; i += blockDim.x) dst[i] = src[i];
+        const uint4 z = make_uint4(0, 0, 0, 0);
+        uint4 *cc = (uint4 *)Cp;
+        for (int i = t; i < 3 * TC_COPY / 16; i += blockDim.x) cc[i] = z;
     }
-    const int g = lane >> 2, q = lane & 3;
-    for (int r = blockIdx.x; r < n; r += gridDim.x) {
-        __syncthreads();
-        /* interior: 256 pixels x 64 bytes */
+    if (t == 0) bamf::tc::mbar_init(mbar, 1);
+    bamf::tc::fence_before_sync();
+    __syncthreads();
+    bamf::tc::fence_after_sync();
+    const uint32_t tbase = tslot;
+    const uint32_t ws_addr = bamf::tc::smem_addr(Ws), cp_addr = bamf::tc::smem_addr(Cp);
+    uint32_t phase = 0;
+    bool alive = true;
+    for (int r = blockIdx.x; r < n && alive; r += gridDim.x) {
+        /* stage the ROI: each 16-byte chunk (8 channels of one pixel) goes to
+         * the three shifted copies where it lands inside */
         const uint4 *src = (const uint4 *)(in + (size_t)r * NPX * CH);
         for (int i = t; i < NPX * 4; i += blockDim.x) {
-            int p = i >> 2, c = i & 3;
-            int x = p / S, y = p - (p / S) * S;
-            *(uint4 *)(T + ((x + 1) * PS + (y + 1)) * CP + c * 8) = src[i];
+            const uint4 v = src[i];
+            const int p = i >> 2, g = i & 3, x = p >> 4, y = p & 15;
+#pragma unroll
+            for (int ky = 0; ky < 3; ++ky) {
+                const int yo = y - ky + 1;
+                if (yo >= 0 && yo < S)
+                    *(uint4 *)(Cp + ky * TC_COPY + g * TC_GSTRIDE + ((x + 1) * S + yo) * 16) = v;
+            }
         }
+        bamf::tc::fence_proxy_async();
+        bamf::tc::fence_before_sync();
         __syncthreads();
-        for (int mt = 0; mt < 2; ++mt) {
-            const int x = 2 * warp + mt;
-            float acc[4][4];
-            for (int a = 0; a < 4; ++a)
-                for (int b = 0; b < 4; ++b) acc[a][b] = 0.0f;
-#pragma unroll
-            for (int tap = 0; tap < 9; ++tap) {
-                const int kx = tap / 3, ky = tap - (tap / 3) * 3;
-#pragma unroll
-                for (int cb = 0; cb < 2; ++cb) {
-                    uint32_t A[4];
-                    {
-                        int j = lane >> 3, rr = lane & 7;
-                        int y = rr + 8 * (j & 1), ch = cb * 16 + 8 * (j >> 1);
-                        ldsm_x4(A, T + ((x + kx) * PS + (y + ky)) * CP + ch);
-                    }
-#pragma unroll
-                    for (int np = 0; np < 2; ++np) {
-                        uint32_t Bf[4];
-                        int j = lane >> 3, rr = lane & 7;
-                        int co = np * 16 + 8 * (j >> 1) + rr, ci = cb * 16 + 8 * (j & 1);
-                        ldsm_x4(Bf, Ws + (tap * CH + co) * CP + ci);
-                        mma16816(acc[2 * np], A, Bf[0], Bf[1]);
-                        mma16816(acc[2 * np + 1], A, Bf[2], Bf[3]);
+        bamf::tc::fence_after_sync();
+        if (t == 0) {
+            uint32_t acc = 0;
+#pragma unroll 1
+            for (int mt = 0; mt < 2; ++mt) {
+                acc = 0;
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int kx = tap / 3, ky = tap - kx * 3;
+                    for (int cb = 0; cb < 2; ++cb) {
+                        const uint32_t a = cp_addr + ky * TC_COPY + (2 * cb) * TC_GSTRIDE + (8 * mt + kx) * S * 16;
+                        const uint32_t b = ws_addr + tap * (CH * CH * 2) + (2 * cb) * (CH * 16);
+                        bamf::tc::mma_bf16(tbase + 32 * mt, bamf::tc::smem_desc(a, TC_GSTRIDE, 128),
+                                           bamf::tc::smem_desc(b, CH * 16, 128), TC_IDESC, acc);
+                        acc = 1;
                     }
                 }
             }
-            /* epilogue */
+            bamf::tc::commit(mbar);
+        }
+        const bool ok = bamf::tc::mbar_wait(mbar, phase, 1u << 24);
+        phase ^= 1u;
+        bamf::tc::fence_after_sync();
+        if (!ok) {
+            if (t == 0) atomicExch(status, 1);
+            alive = false;
+        } else {
+#pragma unroll 1
+            for (int mt = 0; mt < 2; ++mt) {
+                float v[32];
+                bamf::tc::tmem_ld32(tbase + ((uint32_t)(warp * 32) << 16) + 32 * mt, v);
+                const int p = 128 * mt + t;
+                const size_t off = ((size_t)r * NPX + p) * CH;
+                __align__(16) __nv_bfloat162 o[16];
+                if (MODE == 0) {
 #pragma unroll
-            for (int nt = 0; nt < 4; ++nt) {
-                int co = nt * 8 + 2 * q;
+                    for (int c = 0; c < 16; ++c)
+                        o[c] = __floats2bfloat162_rn(fmaxf(v[2 * c] + bias[2 * c], 0.0f),
+                                                     fmaxf(v[2 * c + 1] + bias[2 * c + 1], 0.0f));
+                } else {
+                    __align__(16) __nv_bfloat162 mk[16];
+                    const uint4 *ms = (const uint4 *)(mask + off);
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    int y = g + 8 * h;
-                    size_t off = ((size_t)r * NPX + x * S + y) * CH + co;
-                    float v0 = acc[nt][2 * h], v1 = acc[nt][2 * h + 1];
-                    if (MODE == 0) {
-                        v0 = fmaxf(v0 + bias[co], 0.0f);
-                        v1 = fmaxf(v1 + bias[co + 1], 0.0f);
-                    } else {
-                        __nv_bfloat162 m = *(const __nv_bfloat162 *)(mask + off);
-                        v0 = __bfloat162float(m.x) > 0.0f ? v0 : 0.0f;
-                        v1 = __bfloat162float(m.y) > 0.0f ? v1 : 0.0f;
-                    }
-                    *(__nv_bfloat162 *)(out + off) = __floats2bfloat162_rn(v0, v1);
+                    for (int q = 0; q < 4; ++q) ((uint4 *)mk)[q] = ms[q];
+#pragma unroll
+                    for (int c = 0; c < 16; ++c)
+                        o[c] = __floats2bfloat162_rn(__bfloat162float(mk[c].x) > 0.0f ? v[2 * c] : 0.0f,
+                                                     __bfloat162float(mk[c].y) > 0.0f ? v[2 * c + 1] : 0.0f);
                 }
+                uint4 *dst = (uint4 *)(out + off);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) dst[q] = ((uint4 *)o)[q];
             }
         }
+        bamf::tc::fence_before_sync();
+        __syncthreads(); /* TMEM read and copies consumed before the next ROI */
+        bamf::tc::fence_after_sync();
+        alive = __syncthreads_and(alive);
     }
+    bamf::tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) bamf::tc::tmem_dealloc(tbase, 64);
 }
 
 /* Weight and bias gradient of a 32 -> 32 convolution: dW[co][ci][tap] +=
@@ -753,6 +799,7 @@ struct bamf_cnn {
     float *gdata = nullptr, *gxyi = nullptr;
     int32_t *gn = nullptr;
     int *step = nullptr;
+    int *tc_status = nullptr; /* set by a convolution whose tensor-core wait timed out */
     float *loss = nullptr;
     int loss_cap = 0;
     int sms = 1;
@@ -764,7 +811,6 @@ namespace {
 std::mutex g_attr_mutex;
 bool g_attr_done = false;
 
-const size_t SMEM_CONV = (size_t)(PK + PS * PS * CP) * sizeof(bf16);
 const size_t SMEM_DW = (size_t)(PS * PS * CP + NPX * CP) * sizeof(bf16);
 const size_t SMEM_HEAD = (size_t)(NPX * (CH + 1) + NPX * (NSUB + 1)) * sizeof(float);
 
@@ -773,9 +819,9 @@ cudaError_t set_attrs()
     std::lock_guard<std::mutex> lock(g_attr_mutex);
     if (g_attr_done) return cudaSuccess;
     cudaError_t e;
-    if ((e = cudaFuncSetAttribute(conv_mma_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CONV)))
+    if ((e = cudaFuncSetAttribute(conv_tc_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC)))
         return e;
-    if ((e = cudaFuncSetAttribute(conv_mma_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_CONV)))
+    if ((e = cudaFuncSetAttribute(conv_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC)))
         return e;
     if ((e = cudaFuncSetAttribute(conv_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_DW)))
         return e;
@@ -803,8 +849,9 @@ bamf_status forward(bamf_cnn *net, const float *data, int n, cudaStream_t s)
 {
     conv1_fwd_kernel<<<n, 256, 0, s>>>(data, n, net->P, net->x0, net->a[0]);
     for (int l = 0; l < 3; ++l)
-        conv_mma_kernel<0><<<grid_for(n, 4, net->sms), 256, SMEM_CONV, s>>>(net->a[l], net->Wf + l * PK,
-                                                                           net->P + O_B[l], nullptr, net->a[l + 1], n);
+        conv_tc_kernel<0><<<grid_for(n, 3, net->sms), 128, SMEM_TC, s>>>(net->a[l], net->Wf + l * PKT,
+                                                                         net->P + O_B[l], nullptr, net->a[l + 1], n,
+                                                                         net->tc_status);
     CK(cudaGetLastError());
     return BAMF_OK;
 }
@@ -819,8 +866,8 @@ bamf_status backward(bamf_cnn *net, const int32_t *n_em, const float *xyi, int n
         /* layer l+2: input a[l], output a[l+1]; dz = dL/dz_{l+2} */
         conv_dw_kernel<<<grid_for(n, 3, net->sms), 288, SMEM_DW, s>>>(net->a[l], dz, n, net->G + O_W[l],
                                                                      net->G + O_B[l]);
-        conv_mma_kernel<1><<<grid_for(n, 4, net->sms), 256, SMEM_CONV, s>>>(dz, net->Wb + l * PK, nullptr,
-                                                                           net->a[l], dzn, n);
+        conv_tc_kernel<1><<<grid_for(n, 3, net->sms), 128, SMEM_TC, s>>>(dz, net->Wb + l * PKT, nullptr,
+                                                                         net->a[l], dzn, n, net->tc_status);
         bf16 *tmp = dz;
         dz = dzn;
         dzn = tmp;
@@ -856,7 +903,8 @@ extern "C" void bamf_cnn_destroy(bamf_cnn *net)
 {
     if (!net) return;
     void *ps[] = {net->P, net->G, net->M, net->V, net->Wf, net->Wb, net->x0, net->a[0], net->a[1], net->a[2],
-                  net->a[3], net->dzA, net->dzB, net->gdata, net->gxyi, net->gn, net->step, net->loss};
+                  net->a[3], net->dzA, net->dzB, net->gdata, net->gxyi, net->gn, net->step, net->loss,
+                  net->tc_status};
     for (void *p : ps)
         if (p) cudaFree(p);
     delete net;
@@ -875,7 +923,8 @@ extern "C" bamf_status bamf_cnn_create(bamf_cnn **out, uint32_t seed)
     const size_t B = MAX_BATCH;
     bool ok = cudaMalloc(&net->P, NPARAM * 4) == cudaSuccess && cudaMalloc(&net->G, NPARAM * 4) == cudaSuccess &&
               cudaMalloc(&net->M, NPARAM * 4) == cudaSuccess && cudaMalloc(&net->V, NPARAM * 4) == cudaSuccess &&
-              cudaMalloc(&net->Wf, 3 * PK * 2) == cudaSuccess && cudaMalloc(&net->Wb, 3 * PK * 2) == cudaSuccess &&
+              cudaMalloc(&net->Wf, 3 * PKT * 2) == cudaSuccess && cudaMalloc(&net->Wb, 3 * PKT * 2) == cudaSuccess &&
+              cudaMalloc(&net->tc_status, sizeof(int)) == cudaSuccess &&
               cudaMalloc(&net->x0, B * NPX * 4) == cudaSuccess && cudaMalloc(&net->dzA, B * NPX * CH * 2) == cudaSuccess &&
               cudaMalloc(&net->dzB, B * NPX * CH * 2) == cudaSuccess &&
               cudaMalloc(&net->gdata, B * NPX * 4) == cudaSuccess &&
@@ -907,7 +956,8 @@ extern "C" bamf_status bamf_cnn_create(bamf_cnn **out, uint32_t seed)
     fill(O_WC, 352, 32);
     bool ok2 = cudaMemcpy(net->P, h.data(), NPARAM * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
                cudaMemset(net->G, 0, NPARAM * 4) == cudaSuccess && cudaMemset(net->M, 0, NPARAM * 4) == cudaSuccess &&
-               cudaMemset(net->V, 0, NPARAM * 4) == cudaSuccess && cudaMemset(net->step, 0, sizeof(int)) == cudaSuccess;
+               cudaMemset(net->V, 0, NPARAM * 4) == cudaSuccess && cudaMemset(net->step, 0, sizeof(int)) == cudaSuccess &&
+               cudaMemset(net->tc_status, 0, sizeof(int)) == cudaSuccess;
     if (!ok2 || pack(net, nullptr) != BAMF_OK || cudaDeviceSynchronize() != cudaSuccess) {
         cudaGetLastError();
         bamf_cnn_destroy(net);
@@ -931,6 +981,19 @@ extern "C" bamf_status bamf_cnn_set_params(bamf_cnn *net, const float *params)
     bamf_status r = pack(net, nullptr);
     if (r) return r;
     CK(cudaDeviceSynchronize());
+    return BAMF_OK;
+}
+
+/* after a synchronisation: a convolution whose tensor-core completion wait
+ * ran out left garbage outputs; report it */
+static bamf_status check_tc(bamf_cnn *net)
+{
+    int st = 0;
+    CK(cudaMemcpy(&st, net->tc_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st) {
+        cudaMemset(net->tc_status, 0, sizeof(int));
+        return BAMF_ERR_CUDA;
+    }
     return BAMF_OK;
 }
 
@@ -959,6 +1022,7 @@ extern "C" bamf_status bamf_cnn_loss_grad(bamf_cnn *net, const float *data, cons
     if ((r = forward(net, data, n, nullptr))) return r;
     if ((r = backward(net, n_em, xyi, n, 1.0f / (float)n, nullptr))) return r;
     CK(cudaDeviceSynchronize());
+    if ((r = check_tc(net))) return r;
     if (loss) CK(cudaMemcpy(loss, net->loss, sizeof(float), cudaMemcpyDeviceToHost));
     if (grad) CK(cudaMemcpy(grad, net->G, NPARAM * 4, cudaMemcpyDeviceToHost));
     CK(cudaMemset(net->G, 0, NPARAM * 4));
@@ -1017,6 +1081,7 @@ static bamf_status train_graph(bamf_cnn *net, int steps, int batch, float lr, fl
             res = BAMF_ERR_CUDA;
             break;
         }
+        if ((res = check_tc(net))) break;
         if (loss_trace &&
             cudaMemcpy(loss_trace, net->loss, (size_t)steps * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
             res = BAMF_ERR_CUDA;
