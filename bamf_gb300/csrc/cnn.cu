@@ -327,20 +327,34 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const bf16 *__restrict__ i
     const uint32_t ws_addr = bamf::tc::smem_addr(Ws), cp_addr = bamf::tc::smem_addr(Cp);
     uint32_t phase = 0;
     bool alive = true;
-    for (int r = blockIdx.x; r < n && alive; r += gridDim.x) {
-        /* stage the ROI: each 16-byte chunk (8 channels of one pixel) goes to
-         * the three shifted copies where it lands inside */
+    /* each thread carries 8 of the ROI's 1024 16-byte chunks (8 channels of
+     * one pixel); the next ROI's chunks are loaded while the current ROI's
+     * MMAs run, and staged once they completed */
+    constexpr int CPT = NPX * 4 / 128;
+    uint4 pre[CPT];
+    auto load = [&](int r) {
         const uint4 *src = (const uint4 *)(in + (size_t)r * NPX * CH);
-        for (int i = t; i < NPX * 4; i += blockDim.x) {
-            const uint4 v = src[i];
-            const int p = i >> 2, g = i & 3, x = p >> 4, y = p & 15;
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) pre[k] = src[t + 128 * k];
+    };
+    /* each chunk goes to the three shifted copies where it lands inside */
+    auto stage = [&]() {
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            const int i = t + 128 * k, p = i >> 2, g = i & 3, x = p >> 4, y = p & 15;
 #pragma unroll
             for (int ky = 0; ky < 3; ++ky) {
                 const int yo = y - ky + 1;
                 if (yo >= 0 && yo < S)
-                    *(uint4 *)(Cp + ky * TC_COPY + g * TC_GSTRIDE + ((x + 1) * S + yo) * 16) = v;
+                    *(uint4 *)(Cp + ky * TC_COPY + g * TC_GSTRIDE + ((x + 1) * S + yo) * 16) = pre[k];
             }
         }
+    };
+    if (blockIdx.x < n) {
+        load(blockIdx.x);
+        stage();
+    }
+    for (int r = blockIdx.x; r < n && alive; r += gridDim.x) {
         bamf::tc::fence_proxy_async();
         bamf::tc::fence_before_sync();
         __syncthreads();
@@ -363,6 +377,8 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const bf16 *__restrict__ i
             }
             bamf::tc::commit(mbar);
         }
+        const int rn = r + gridDim.x;
+        if (rn < n) load(rn);
         const bool ok = bamf::tc::mbar_wait(mbar, phase, 1u << 24);
         phase ^= 1u;
         bamf::tc::fence_after_sync();
@@ -401,6 +417,7 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const bf16 *__restrict__ i
         __syncthreads(); /* TMEM read and copies consumed before the next ROI */
         bamf::tc::fence_after_sync();
         alive = __syncthreads_and(alive);
+        if (alive && rn < n) stage();
     }
     bamf::tc::fence_before_sync();
     __syncthreads();
