@@ -16,6 +16,12 @@ roofline  the sampler kernel against the measured MUFU log2 rate: one log2 per
           ROI pixel per scored proposal (the likelihood-ratio pass)
 cpu_baseline  the CPU restatement of the reference sampler (glibc math, bit-
           identical to the reference build) on the host cores, on a sample
+plain_exact  (rank 0, outside the timed region) the plain-RJMCMC
+          configuration (200 ROIs 16x16, 3000+3000 jumps) in exact
+          arithmetic, whose chains equal the reference sampler's bit for bit:
+          end to end through the host API, throughput at 4,864 ROIs (two
+          rounds of the GPU's resident chains), and
+          the CPU restatement on the same 200 ROIs with all host threads
 frontend  (rank 0, outside the timed region) FindROI + gaussMLE on the
           2000-frame 256x256 front-end workload: frames/s, FindROI against the
           measured HBM bandwidth (one 4-byte read per pixel), fits/s, and an
@@ -68,6 +74,8 @@ def parse():
     ap.add_argument("--learned-train-rois", type=int, default=2_000_000)
     ap.add_argument("--learned-eval-rois", type=int, default=50_000)
     ap.add_argument("--no-frontend", action="store_true", help="skip the FindROI + gaussMLE measurement")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain-RJMCMC exact-arithmetic measurement (200 ROIs 16x16)")
     ap.add_argument("--frontend-frames", type=int, default=2000)
     ap.add_argument("--no-dense", action="store_true", help="skip the dense end-to-end frame analysis")
     ap.add_argument("--dense-frames", type=int, default=20)
@@ -117,6 +125,51 @@ def measured_hbm_gbs():
             return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback 6.8 TB/s (of fallback)"
+
+
+def plain_exact_bench(n_large: int = 4864) -> dict:
+    """The plain-RJMCMC configuration (200 ROIs of 16x16, 3000+3000 jumps,
+    the reference proposal) in exact arithmetic, the path whose chains equal
+    the reference sampler's bit for bit: the 200-ROI batch end to end through
+    the host API, the same generator at n_large ROIs for throughput (device
+    inputs), and the CPU restatement (bit-identical to the reference build)
+    on all host threads over the 200 ROIs."""
+    import torch
+
+    from bamf_gb300 import rjstruct, sampler, synth
+    rj = rjstruct.c0_rjstruct()
+    p = rjstruct.mcmc_params(rj)
+    bg0 = rjstruct.initial_bg(rj)
+    s = sampler.Sampler()
+    out = {"workload": "plain RJMCMC, exact arithmetic: 200 ROIs 16x16, 3000+3000 jumps (and the same "
+                       f"generator at {n_large} ROIs)"}
+    b = synth.roi_batch_c0(200, seed=0)
+    s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=7, arith="exact", bg0=bg0)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    r = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=7, arith="exact", bg0=bg0)
+    out["seconds_200"] = time.perf_counter() - t
+    out["rois_per_s_200_e2e"] = 200 / out["seconds_200"]
+    assert (r["status"] == 0).all()
+    bl = synth.roi_batch_c0(n_large, seed=1)
+    dev = {"data": torch.from_numpy(bl.data).cuda(), "offsets": torch.from_numpy(bl.offsets).cuda(),
+           "xsize": torch.from_numpy(bl.xsize).cuda(), "ysize": torch.from_numpy(bl.ysize).cuda(),
+           "psf_sigma": torch.from_numpy(bl.sigma).cuda(), "side_max": 16}
+    outs = {k: torch.zeros(n_large, dtype=torch.int32, device="cuda") for k in ("map_n", "status")}
+    s.run_device(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=7, arith="exact", outs=outs, bg0=bg0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    s.run_device(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=7, arith="exact", outs=outs, bg0=bg0)
+    e1.record()
+    torch.cuda.synchronize()
+    out["rois_per_s_large"] = n_large / (e0.elapsed_time(e1) * 1e-3)
+    threads = os.cpu_count() or 1
+    rate, secs = cpu_sample_rate(b, rj, p, bg0, 200, threads)
+    out["cpu_rois_per_s_200"] = rate
+    out["cpu_cores"] = threads
+    out["cpu_seconds_200"] = secs
+    return out
 
 
 def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3) -> dict:
@@ -415,6 +468,10 @@ def main():
             "equal_accuracy": r["equal_accuracy_vs_uniform_at_full_length"],
         }
 
+    plain_block = None
+    if rank == 0 and not a.no_plain:
+        plain_block = plain_exact_bench()
+
     frontend_block = None
     if rank == 0 and not a.no_frontend:
         frontend_block = frontend_bench(a.frontend_frames)
@@ -451,6 +508,7 @@ def main():
             "gpu_launches": launches_per_step * a.steps,
             "clocks": clk.summary(),
             "learned_proposal": learned_block,
+            "plain_exact": plain_block,
             "frontend": frontend_block,
             "dense_e2e": dense_block,
             "map_n_mean": float(outs["map_n"].float().mean().item()),
