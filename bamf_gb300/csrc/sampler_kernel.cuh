@@ -86,7 +86,7 @@ struct SMath<false> {
 __host__ __device__ inline int warp_smem_floats(int side_max, bool exact)
 {
     int npix = side_max * side_max, nxs = BAMF_NMAX * side_max;
-    return exact ? 5 * npix + 2 * nxs + C_COUNT + BAMF_NMAX + 2                 /* D M Mt E sCMOS NX NY */
+    return exact ? 5 * npix + 4 * nxs + C_COUNT + BAMF_NMAX + 2 /* D M Mt E sCMOS, NX NY of A and of T */
                  : 3 * npix + 4 * FAST_ROWS * side_max + C_COUNT + BAMF_NMAX + 2; /* D M Mt SXo SYo SXn SYn */
 }
 
@@ -287,6 +287,8 @@ struct ChainWarp {
     float sigma, Cst, MeanN;
     /* shared memory */
     float *D, *M, *Mt, *E, *NX, *NY;
+    float *NXt, *NYt; /* exact mode: stencil rows of T (NX, NY hold A's) */
+    int tsrc;         /* exact mode: the A slot T's emitter in this lane came from, -1 if changed */
     float *SXo, *SYo, *SXn, *SYn; /* fast mode: compact stencil rows */
     const float *scm; /* sCMOS: shared memory (exact) or global/null (fast) */
     /* sampled PSF (OptModel 1): [P0 y][P1 x][P2 y-sub][P3 x-sub], y fastest;
@@ -376,6 +378,7 @@ struct ChainWarp {
             tI = I;
             tX = x;
             tY = y;
+            if (EXACT) tsrc = -1;
         }
         if (!EXACT) t_dirty |= 1u << k;
     }
@@ -390,6 +393,7 @@ struct ChainWarp {
             tX = x;
             tY = y;
             tS = s;
+            if (EXACT) tsrc = -1;
         }
         if (!EXACT) t_dirty |= 1u << tn;
         tn++;
@@ -401,8 +405,10 @@ struct ChainWarp {
         float vX = __shfl_down_sync(BAMF_FULL, tX, 1);
         float vY = __shfl_down_sync(BAMF_FULL, tY, 1);
         int vS = __shfl_down_sync(BAMF_FULL, tS, 1);
+        int vsrc = EXACT ? __shfl_down_sync(BAMF_FULL, tsrc, 1) : 0;
         if (lane >= id) {
             tI = vI; tX = vX; tY = vY; tS = vS;
+            if (EXACT) tsrc = vsrc;
         }
         if (!EXACT) {
             uint32_t lo = t_dirty & ((1u << id) - 1u);
@@ -416,6 +422,7 @@ struct ChainWarp {
         tn = an; tI = aI; tX = aX; tY = aY; tS = aS;
         tBG = aBG; tABG = aABG; tBBG = aBBG;
         t_overflow = false;
+        if (EXACT) tsrc = lane;
         if (!EXACT) {
             a_dirty = 0u;
             t_dirty = 0u;
@@ -557,6 +564,57 @@ struct ChainWarp {
         for (int p = lane; p < npix; p += 32) {
             float m = BG + ABG * (float)x + BBG * (float)y + (scm ? scm[p] : 0.0f);
             for (int k = 0; k < n; ++k) m += nx[k * X + x] * ny[k * Y + y];
+            out[p] = m;
+            x += px_dx;
+            y += px_dy;
+            if (y >= Y) {
+                y -= Y;
+                x++;
+            }
+        }
+        __syncwarp();
+    }
+
+    /* Exact mode, the proposal's model: as model_full for T, but the
+     * stencil rows of the emitters the proposal left unchanged are copied
+     * from A's rows (the same function of the same inputs, so the same
+     * bits) instead of evaluated again; only changed or new emitters pay
+     * the erf evaluations.  Rows go to NXt / NYt. */
+    __device__ __forceinline__ void model_cached(int n, float I, float Xv, float Yv, float BG, float ABG, float BBG,
+                                                 float *out)
+    {
+        int totx = n * X, toty = n * Y;
+#pragma unroll 1
+        for (int b0 = 0; b0 < totx; b0 += 32) {
+            int item = b0 + lane;
+            int k = min(item / X, n - 1);
+            int x = item - k * X;
+            float Ik = __shfl_sync(BAMF_FULL, I, k);
+            float Xk = __shfl_sync(BAMF_FULL, Xv, k);
+            int src = __shfl_sync(BAMF_FULL, tsrc, k);
+            if (item < totx)
+                NXt[k * X + x] = src >= 0 ? NX[src * X + x]
+                                          : Ik * 0.5f * (MT::erf_(((float)x - Xk + 1.0f) * Cst) -
+                                                         MT::erf_(((float)x - Xk) * Cst));
+        }
+#pragma unroll 1
+        for (int b0 = 0; b0 < toty; b0 += 32) {
+            int item = b0 + lane;
+            int k = min(item / Y, n - 1);
+            int y = item - k * Y;
+            float Yk = __shfl_sync(BAMF_FULL, Yv, k);
+            int src = __shfl_sync(BAMF_FULL, tsrc, k);
+            if (item < toty)
+                NYt[k * Y + y] = src >= 0 ? NY[src * Y + y]
+                                          : 0.5f * (MT::erf_(((float)y - Yk + 1.0f) * Cst) -
+                                                    MT::erf_(((float)y - Yk) * Cst));
+        }
+        __syncwarp();
+        int x = lane / Y, y = lane - (lane / Y) * Y;
+#pragma unroll 1
+        for (int p = lane; p < npix; p += 32) {
+            float m = BG + ABG * (float)x + BBG * (float)y + (scm ? scm[p] : 0.0f);
+            for (int k = 0; k < n; ++k) m += NXt[k * X + x] * NYt[k * Y + y];
             out[p] = m;
             x += px_dx;
             y += px_dy;
@@ -801,7 +859,7 @@ struct ChainWarp {
         n_llr++;
         if (EXACT) {
             if constexpr (NUM) model_num(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
-            else model_full(tn, tI, tX, tY, tBG, tABG, tBBG, Mt, NX, NY);
+            else model_cached(tn, tI, tX, tY, tBG, tABG, tBBG, Mt);
             for (int p = lane; p < npix; p += 32)
                 E[p] = M[p] - Mt[p] + D[p] * MT::log_(Mt[p] / M[p]);
             __syncwarp();
@@ -937,6 +995,8 @@ struct ChainWarp {
             float *t = M;
             M = Mt;
             Mt = t;
+            t = NX; NX = NXt; NXt = t;
+            t = NY; NY = NYt; NYt = t;
         }
     }
 
@@ -1918,12 +1978,14 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT, NUM> &w, const Sample
         scm_smem = sw + 4 * npix_max;
         w.NX = sw + 5 * npix_max;
         w.NY = w.NX + nxs;
+        w.NXt = w.NY + nxs;
+        w.NYt = w.NXt + nxs;
         w.SXo = w.SYo = w.SXn = w.SYn = nullptr;
-        w.cnt = (int *)(w.NY + nxs);
+        w.cnt = (int *)(w.NYt + nxs);
     } else {
         const int rs = FAST_ROWS * Bt.side_max;
         w.E = nullptr;
-        w.NX = w.NY = nullptr;
+        w.NX = w.NY = w.NXt = w.NYt = nullptr;
         w.SXo = sw + 3 * npix_max;
         w.SYo = w.SXo + rs;
         w.SXn = w.SYo + rs;
