@@ -10,12 +10,9 @@
  * GEMM with M = 256 pixels (two tiles of 128), N = 32, K = 9 taps x 32
  * channels.  The input gradient of a convolution is the same kernel run with
  * the taps flipped and the channel roles swapped (packed once per step).
- * The weight gradient is a GEMM with M = (tap, input channel) = 288 and
- * K = the pixels of every ROI of the CTA, on mma.sync m16n8k16 with both
- * operands read transposed by ldmatrix.trans: a CTA stages a ROI's
- * activations as an 18 x 18 zero-bordered tile with a 40-channel pixel
- * stride (80 bytes: the eight rows an ldmatrix phase reads fall in eight
- * different 16-byte bank groups).
+ * The weight gradient is a GEMM with K = the pixels of every ROI of the
+ * CTA, also on tcgen05, with MN-major operands so that the channels-last
+ * activations stage without a transpose (conv_dw_tc_kernel).
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -35,7 +32,6 @@ namespace {
 constexpr int S = BAMF_CNN_SIDE;  /* 16 */
 constexpr int NPX = S * S;        /* 256 */
 constexpr int CH = BAMF_CNN_CH;   /* 32 */
-constexpr int CP = 40;            /* smem channel stride (bf16) */
 constexpr int PS = S + 2;         /* padded side */
 constexpr int NC = BAMF_CNN_COUNTS;
 constexpr int NSUB = 16;
@@ -46,30 +42,14 @@ constexpr int O_W1 = 0, O_B1 = 288, O_W2 = 320, O_B2 = 9536, O_W3 = 9568, O_B3 =
               O_B4 = 28032, O_WL = 28064, O_BL = 28576, O_WC = 28592, O_BC = 28944, NPARAM = 28955;
 static_assert(NPARAM == BAMF_CNN_NPARAM, "parameter count");
 static_assert(O_B1 == O_W1 + 288 && O_BC + NC == NPARAM, "conv1 block and head layout");
+constexpr int HEAD_NPARAM = NPARAM - O_WL; /* WL, BL, WC, BC: the heads' parameters, contiguous */
+static_assert(O_BL == O_WL + NSUB * CH && O_WC == O_BL + NSUB && O_BC == O_WC + NC * CH, "head layout");
+constexpr int C1_NPARAM = O_W2;            /* W1, B1 */
 constexpr int O_W[3] = {O_W2, O_W3, O_W4};
 constexpr int O_B[3] = {O_B2, O_B3, O_B4};
 constexpr int PKT = 9 * CH * CH; /* tensor-core operand weights of one layer */
 
 typedef __nv_bfloat16 bf16;
-
-/* ------------------------------------------------------------ PTX helpers */
-__device__ __forceinline__ uint32_t smem_addr(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void *p)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_addr(p)));
-}
-__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
-{
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
-                 "{%8,%9}, {%0,%1,%2,%3};\n"
-                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
 
 __device__ __forceinline__ float u01(uint32_t w)
 {
@@ -237,7 +217,8 @@ __global__ void conv1_fwd_kernel(const float *__restrict__ data, int n, const fl
     for (int q = 0; q < 4; ++q) dst[q] = src[q];
 }
 
-/* dW1, db1 from dz1 (= dL/d pre-activation of conv1) and x0. */
+/* dW1, db1 from dz1 (= dL/d pre-activation of conv1) and x0: each CTA's
+ * sums over its ROIs into row blockIdx.x of G (C1_NPARAM floats). */
 __global__ void conv1_bwd_kernel(const float *__restrict__ x0, const bf16 *__restrict__ dz1, int n,
                                  float *__restrict__ G)
 {
@@ -271,8 +252,9 @@ __global__ void conv1_bwd_kernel(const float *__restrict__ x0, const bf16 *__res
             else acc0 += acc;
         }
     }
-    if (o0 < 320) atomicAdd(&G[O_W1 + o0], acc0);
-    if (o1 < 320) atomicAdd(&G[O_W1 + o1], acc1);
+    float *row = G + (size_t)blockIdx.x * C1_NPARAM;
+    if (o0 < C1_NPARAM) row[o0] = acc0;
+    if (o1 < C1_NPARAM) row[o1] = acc1;
 }
 
 /* -------------------------------------------------- 32 -> 32 convolution */
@@ -328,20 +310,24 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const bf16 *__restrict__ i
     uint32_t phase = 0;
     bool alive = true;
     /* each thread carries 8 of the ROI's 1024 16-byte chunks (8 channels of
-     * one pixel); the next ROI's chunks are loaded while the current ROI's
-     * MMAs run, and staged once they completed */
+     * one pixel): pixels (t & 7) + 8 (t >> 5) + 32 k, channel group
+     * (t >> 3) & 3, so that the 8 lanes of a 16-byte store phase write 8
+     * consecutive pixels of one group (one bank group each); the next ROI's
+     * chunks are loaded while the current ROI's MMAs run, and staged once
+     * they completed */
     constexpr int CPT = NPX * 4 / 128;
+    const int cg = (t >> 3) & 3, p0 = (t & 7) + 8 * (t >> 5);
     uint4 pre[CPT];
     auto load = [&](int r) {
         const uint4 *src = (const uint4 *)(in + (size_t)r * NPX * CH);
 #pragma unroll
-        for (int k = 0; k < CPT; ++k) pre[k] = src[t + 128 * k];
+        for (int k = 0; k < CPT; ++k) pre[k] = src[(p0 + 32 * k) * 4 + cg];
     };
     /* each chunk goes to the three shifted copies where it lands inside */
     auto stage = [&]() {
 #pragma unroll
         for (int k = 0; k < CPT; ++k) {
-            const int i = t + 128 * k, p = i >> 2, g = i & 3, x = p >> 4, y = p & 15;
+            const int p = p0 + 32 * k, g = cg, x = p >> 4, y = p & 15;
 #pragma unroll
             for (int ky = 0; ky < 3; ++ky) {
                 const int yo = y - ky + 1;
@@ -424,84 +410,228 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const bf16 *__restrict__ i
     if (warp == 0) bamf::tc::tmem_dealloc(tbase, 64);
 }
 
-/* Weight and bias gradient of a 32 -> 32 convolution: dW[co][ci][tap] +=
- * sum over ROIs and pixels of act[p + tap][ci] * dz[p][co].  9 warps; warp
- * w owns M tiles 2w, 2w+1 of M = (tap, ci block) = 18 tiles of 16. */
-__global__ void __launch_bounds__(288) conv_dw_kernel(const bf16 *__restrict__ act, const bf16 *__restrict__ dz,
-                                                      int n, float *__restrict__ dW, float *__restrict__ db)
+/* Weight and bias gradient of a 32 -> 32 convolution on the tensor cores:
+ * dW[co][ci][tap] += sum over ROIs and pixels p of act[p + tap][ci] dz[p][co]
+ * with tap = 3 kx + ky the shift (kx - 1, ky - 1) in (x, y).  Substituting
+ * q = p + 16 (kx - 1) (the x shift moves a pixel index by 16),
+ *   D[(ky, ci)][(kx, co)] = sum over q in [0, 256) of
+ *                           A[(ky, ci)][q] * B[(kx, co)][q],
+ *   A[(ky, ci)][q] = act[q + ky - 1][ci] (zero where y(q) + ky - 1 leaves
+ *                    the ROI),
+ *   B[(kx, co)][q] = dz[q - 16 (kx - 1)][co] (zero outside the ROI),
+ * an M = 128 (96 rows (ky, ci), the last 32 rows ignored) x N = 96 x K = 256
+ * GEMM per ROI: 16 tcgen05.mma of K = 16, accumulated in TMEM over all ROIs
+ * of the CTA (column 32 kx + co).
+ *
+ * Both operands MN-major, so that a 16-byte chunk of the channels-last
+ * tensors (8 channels of one pixel) is one row of a core matrix and staging
+ * is plain 16-byte copies: A as three y-shifted copies of act, B as three
+ * x-shifted copies of dz, core matrix (k group j, row block 4 s + g) at
+ * j * 1536 + (4 s + g) * 128 (s = ky for A, kx for B).  The ignored rows
+ * 96..127 of A read the next k group's rows (in bounds: B follows A).  One
+ * ROI per iteration of a persistent CTA of 128 threads, the next ROI's
+ * chunks loaded into registers while the MMAs run; the bias gradient (sum of
+ * dz over pixels) is formed from the staged chunks.  A lane's chunks are
+ * pixel (t & 7) + 8 (t >> 5) + 32 k, channel group (t >> 3) & 3: the 8 lanes
+ * of a 16-byte store phase write 8 consecutive pixels of one block, one
+ * shared-memory bank group each.  Each CTA writes its partial sums (D, then
+ * the 32 bias sums) to its own slice of `part`, coalesced; dw_reduce_kernel
+ * adds the slices in a fixed order (no atomics, the same bits every run).
+ * The mbarrier wait is bounded; a timeout is recorded in *status, the CTA
+ * writes zeros, frees its TMEM and returns. */
+constexpr int DW_KS = 12 * 128;                /* bytes of one k group (8 pixels) */
+constexpr int DW_PART = 96 * 96 + CH;          /* floats of one CTA's partial sums */
+constexpr int DW_ABYTES = 32 * DW_KS;          /* 256 pixels */
+constexpr size_t SMEM_DW = (size_t)2 * DW_ABYTES + 16;
+constexpr uint32_t DW_IDESC = bamf::tc::idesc_bf16_f32_mn(128, 96);
+
+__global__ void __launch_bounds__(128) conv_dw_tc_kernel(const bf16 *__restrict__ act, const bf16 *__restrict__ dz,
+                                                         int n, float *__restrict__ part, int *__restrict__ status)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    bf16 *A = (bf16 *)smem_raw;       /* [PS][PS][CP] */
-    bf16 *D = A + PS * PS * CP;       /* [S][S][CP]   */
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    unsigned char *As = smem_raw;
+    unsigned char *Bs = smem_raw + DW_ABYTES;
+    uint64_t *mbar = (uint64_t *)(Bs + DW_ABYTES);
+    __shared__ uint32_t tslot;
+    const int t = threadIdx.x, warp = t >> 5;
+    if (warp == 0) bamf::tc::tmem_alloc(&tslot, 128);
     {
-        uint4 z = make_uint4(0, 0, 0, 0);
-        uint4 *aa = (uint4 *)A;
-        for (int i = t; i < PS * PS * CP * 2 / 16; i += blockDim.x) aa[i] = z;
+        const uint4 z = make_uint4(0, 0, 0, 0);
+        uint4 *dst = (uint4 *)smem_raw;
+        for (int i = t; i < 2 * DW_ABYTES / 16; i += blockDim.x) dst[i] = z;
     }
-    float acc[2][4][4];
-    for (int a = 0; a < 2; ++a)
-        for (int b = 0; b < 4; ++b)
-            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.0f;
-    float accb = 0.0f;
-    for (int r = blockIdx.x; r < n; r += gridDim.x) {
-        __syncthreads();
+    if (t == 0) bamf::tc::mbar_init(mbar, 1);
+    bamf::tc::fence_before_sync();
+    __syncthreads();
+    bamf::tc::fence_after_sync();
+    const uint32_t tbase = tslot;
+    const uint32_t a_addr = bamf::tc::smem_addr(As), b_addr = bamf::tc::smem_addr(Bs);
+    /* each thread carries 8 of the ROI's 1024 chunks of act and of dz */
+    constexpr int CPT = NPX * 4 / 128;
+    const int g = (t >> 3) & 3, p0 = (t & 7) + 8 * (t >> 5);
+    uint4 pa[CPT], pd[CPT];
+    float bsum[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) bsum[c] = 0.0f;
+    auto load = [&](int r) {
         const uint4 *sa = (const uint4 *)(act + (size_t)r * NPX * CH);
         const uint4 *sd = (const uint4 *)(dz + (size_t)r * NPX * CH);
-        for (int i = t; i < NPX * 4; i += blockDim.x) {
-            int p = i >> 2, c = i & 3;
-            int x = p / S, y = p - (p / S) * S;
-            *(uint4 *)(A + ((x + 1) * PS + (y + 1)) * CP + c * 8) = sa[i];
-            *(uint4 *)(D + p * CP + c * 8) = sd[i];
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            pa[k] = sa[(p0 + 32 * k) * 4 + g];
+            pd[k] = sd[(p0 + 32 * k) * 4 + g];
         }
+    };
+    auto stage = [&]() {
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) {
+            const int p = p0 + 32 * k, y = p & 15;
+#pragma unroll
+            for (int sh = 0; sh < 3; ++sh) {
+                const int yq = y - sh + 1, qa = p - sh + 1; /* A[(sh, .)][qa] = act[p] */
+                if (yq >= 0 && yq < S)
+                    *(uint4 *)(As + (qa >> 3) * DW_KS + (4 * sh + g) * 128 + (qa & 7) * 16) = pa[k];
+                const int qb = p + 16 * (sh - 1); /* B[(sh, .)][qb] = dz[p] */
+                if (qb >= 0 && qb < NPX)
+                    *(uint4 *)(Bs + (qb >> 3) * DW_KS + (4 * sh + g) * 128 + (qb & 7) * 16) = pd[k];
+            }
+            const __nv_bfloat162 *h = (const __nv_bfloat162 *)&pd[k];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float2 f = __bfloat1622float2(h[c]);
+                bsum[2 * c] += f.x;
+                bsum[2 * c + 1] += f.y;
+            }
+        }
+    };
+    bool alive = true, first = true;
+    uint32_t phase = 0;
+    if (blockIdx.x < n) {
+        load(blockIdx.x);
+        stage();
+    }
+    for (int r = blockIdx.x; r < n && alive; r += gridDim.x) {
+        bamf::tc::fence_proxy_async();
+        bamf::tc::fence_before_sync();
         __syncthreads();
-        if (t < CH)
-            for (int p = 0; p < NPX; ++p) accb += __bfloat162float(D[p * CP + t]);
-        for (int x = 0; x < S; ++x) {
-            uint32_t Bf[2][4];
+        bamf::tc::fence_after_sync();
+        if (t == 0) {
+#pragma unroll 1
+            for (int sk = 0; sk < 16; ++sk)
+                bamf::tc::mma_bf16(tbase, bamf::tc::smem_desc(a_addr + 2 * sk * DW_KS, DW_KS, 128),
+                                   bamf::tc::smem_desc(b_addr + 2 * sk * DW_KS, DW_KS, 128), DW_IDESC,
+                                   (first && sk == 0) ? 0u : 1u);
+            bamf::tc::commit(mbar);
+        }
+        first = false;
+        const int rn = r + gridDim.x;
+        if (rn < n) load(rn);
+        const bool ok = bamf::tc::mbar_wait(mbar, phase, 1u << 24);
+        phase ^= 1u;
+        bamf::tc::fence_after_sync();
+        if (!ok) {
+            if (t == 0) atomicExch(status, 1);
+            alive = false;
+        }
+        bamf::tc::fence_before_sync();
+        __syncthreads(); /* the MMAs have read the tiles before they are restaged */
+        bamf::tc::fence_after_sync();
+        alive = __syncthreads_and(alive);
+        if (alive && rn < n) stage();
+    }
+    if (blockIdx.x < n) {
+        float *mine = part + (size_t)blockIdx.x * DW_PART;
+        if (warp < 3) {
+            /* warp ky, lane ci: D[(ky, ci)][(kx, co)] in column 32 kx + co,
+             * stored at (32 kx + co) * 96 + 32 ky + ci */
+#pragma unroll 1
+            for (int kx = 0; kx < 3; ++kx) {
+                float v[32];
+                if (alive) {
+                    bamf::tc::tmem_ld32(tbase + ((uint32_t)(warp * 32) << 16) + 32 * kx, v);
+                } else {
 #pragma unroll
-            for (int np = 0; np < 2; ++np) {
-                int j = lane >> 3, rr = lane & 7;
-                int y = rr + 8 * (j & 1), co = (2 * np + (j >> 1)) * 8;
-                ldsm_x4_t(Bf[np], D + (x * S + y) * CP + co);
-            }
-#pragma unroll
-            for (int mi = 0; mi < 2; ++mi) {
-                int mt = 2 * warp + mi;
-                int tap = mt >> 1, cib = (mt & 1) * 16;
-                int kx = tap / 3, ky = tap - (tap / 3) * 3;
-                uint32_t Af[4];
-                int j = lane >> 3, rr = lane & 7;
-                int y = rr + 8 * (j >> 1), ci = cib + 8 * (j & 1);
-                ldsm_x4_t(Af, A + ((x + kx) * PS + (y + ky)) * CP + ci);
-#pragma unroll
-                for (int np = 0; np < 2; ++np) {
-                    mma16816(acc[mi][2 * np], Af, Bf[np][0], Bf[np][1]);
-                    mma16816(acc[mi][2 * np + 1], Af, Bf[np][2], Bf[np][3]);
+                    for (int co = 0; co < CH; ++co) v[co] = 0.0f;
                 }
+#pragma unroll
+                for (int co = 0; co < CH; ++co) mine[(32 * kx + co) * 96 + t] = v[co];
             }
         }
+        /* bias: lanes with equal (lane >> 3) hold the same 8 channels */
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            float v = bsum[c];
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            v += __shfl_xor_sync(0xffffffffu, v, 2);
+            v += __shfl_xor_sync(0xffffffffu, v, 4);
+            bsum[c] = v;
+        }
+        __shared__ float bred[4][CH];
+        if ((t & 7) == 0)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) bred[warp][8 * g + c] = bsum[c];
+        __syncthreads();
+        if (t < CH) mine[96 * 96 + t] = alive ? (bred[0][t] + bred[1][t]) + (bred[2][t] + bred[3][t]) : 0.0f;
     }
-    const int g = lane >> 2, q = lane & 3;
-#pragma unroll
-    for (int mi = 0; mi < 2; ++mi) {
-        int mt = 2 * warp + mi;
-        int tap = mt >> 1, cib = (mt & 1) * 16;
-#pragma unroll
-        for (int nt = 0; nt < 4; ++nt)
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                int ci = cib + g + 8 * (e >> 1), co = nt * 8 + 2 * q + (e & 1);
-                atomicAdd(&dW[(co * CH + ci) * 9 + tap], acc[mi][nt][e]);
-            }
+    bamf::tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) bamf::tc::tmem_dealloc(tbase, 128);
+}
+
+/* Column sums of a row-major [nrows][width] array of partial sums, in a
+ * fixed order (no atomics: the same bits every run).  A CTA of 32 warps owns
+ * 32 consecutive columns (lane = column, coalesced): warp w adds rows w,
+ * w + 32, ...; then warp 0 adds the 32 warp sums in order.  The result is
+ * valid in warp 0. */
+__device__ __forceinline__ float column_sum(const float *__restrict__ part, int nrows, int width, int j,
+                                            float (*red)[33])
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float acc = 0.0f;
+    if (j < width)
+        for (int c = w; c < nrows; c += 32) acc += part[(size_t)c * width + j];
+    red[w][lane] = acc;
+    __syncthreads();
+    float sum = 0.0f;
+    if (w == 0)
+        for (int k = 0; k < 32; ++k) sum += red[k][lane];
+    return sum;
+}
+
+/* out[j] += sum over rows of part[row][j], j < width */
+__global__ void __launch_bounds__(1024) reduce_rows_kernel(const float *__restrict__ part, int nrows, int width,
+                                                           float *__restrict__ out)
+{
+    __shared__ float red[32][33];
+    const int j = blockIdx.x * 32 + (threadIdx.x & 31);
+    const float sum = column_sum(part, nrows, width, j, red);
+    if (threadIdx.x < 32 && j < width) out[j] += sum;
+}
+
+/* dW[co][ci][3 kx + ky] += sum over CTAs of part[cta][(32 kx + co) * 96 +
+ * 32 ky + ci], db[c] += sum of part[cta][96 * 96 + c] */
+__global__ void __launch_bounds__(1024) dw_reduce_kernel(const float *__restrict__ part, int nparts,
+                                                         float *__restrict__ dW, float *__restrict__ db)
+{
+    __shared__ float red[32][33];
+    const int j = blockIdx.x * 32 + (threadIdx.x & 31);
+    const float sum = column_sum(part, nparts, DW_PART, j, red);
+    if (threadIdx.x < 32 && j < DW_PART) {
+        if (j < 96 * 96) {
+            const int col = j / 96, row = j - col * 96;
+            const int kx = col >> 5, co = col & 31, ky = row >> 5, ci = row & 31;
+            dW[(co * CH + ci) * 9 + 3 * kx + ky] += sum;
+        } else {
+            db[j - 96 * 96] += sum;
+        }
     }
-    if (t < CH) atomicAdd(&db[t], accb);
 }
 
 /* ----------------------------------------------------------------- heads */
 /* One CTA (256 threads, thread = pixel) per ROI.  TRAIN: loss, head
- * gradients (atomics into G), dz4 = dL/d(pre-activation of conv4).  INFER:
- * the sampler's birth tables and the count logits. */
+ * gradients (row r of G, HEAD_NPARAM floats per ROI), dz4 = dL/d(pre-
+ * activation of conv4).  INFER: the sampler's birth tables and the count
+ * logits. */
 template <bool TRAIN>
 __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, int n, const float *__restrict__ P,
                                                    const int32_t *__restrict__ n_em, const float *__restrict__ xyi,
@@ -668,20 +798,23 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
         const uint4 *src = (const uint4 *)o;
         for (int qd = 0; qd < 4; ++qd) dst[qd] = src[qd];
     }
-    /* head parameter gradients */
+    /* head parameter gradients of this ROI, in the parameter order from O_WL
+     * (WL, BL, WC, BC), into its row of G (one row per ROI; reduce_rows_kernel
+     * adds the rows) */
+    float *row = G + (size_t)r * HEAD_NPARAM;
     for (int o = t; o < NSUB * CH; o += 256) {
         int s = o / CH, c = o - (o / CH) * CH;
         float v = 0.0f;
         for (int p = 0; p < NPX; ++p) v += DZ[p * (NSUB + 1) + s] * H[p * (CH + 1) + c];
-        atomicAdd(&G[O_WL + o], v);
+        row[o] = v;
     }
     if (t < NSUB) {
         float v = 0.0f;
         for (int p = 0; p < NPX; ++p) v += DZ[p * (NSUB + 1) + t];
-        atomicAdd(&G[O_BL + t], v);
+        row[O_BL - O_WL + t] = v;
     }
-    for (int o = t; o < NC * CH; o += 256) atomicAdd(&G[O_WC + o], dzc[o / CH] * gmean[o - (o / CH) * CH]);
-    if (t < NC) atomicAdd(&G[O_BC + t], dzc[t]);
+    for (int o = t; o < NC * CH; o += 256) row[O_WC - O_WL + o] = dzc[o / CH] * gmean[o - (o / CH) * CH];
+    if (t < NC) row[O_BC - O_WL + t] = dzc[t];
 }
 
 /* --------------------------------------------------------- start states */
@@ -817,6 +950,9 @@ struct bamf_cnn {
     int32_t *gn = nullptr;
     int *step = nullptr;
     int *tc_status = nullptr; /* set by a convolution whose tensor-core wait timed out */
+    float *dwpart = nullptr;  /* per-CTA partial weight gradients, 2 CTAs per SM */
+    float *hpart = nullptr;   /* per-ROI head gradients (MAX_BATCH rows) */
+    float *c1part = nullptr;  /* per-CTA conv1 gradients, 4 CTAs per SM */
     float *loss = nullptr;
     int loss_cap = 0;
     int sms = 1;
@@ -828,7 +964,6 @@ namespace {
 std::mutex g_attr_mutex;
 bool g_attr_done = false;
 
-const size_t SMEM_DW = (size_t)(PS * PS * CP + NPX * CP) * sizeof(bf16);
 const size_t SMEM_HEAD = (size_t)(NPX * (CH + 1) + NPX * (NSUB + 1)) * sizeof(float);
 
 cudaError_t set_attrs()
@@ -840,7 +975,7 @@ cudaError_t set_attrs()
         return e;
     if ((e = cudaFuncSetAttribute(conv_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_TC)))
         return e;
-    if ((e = cudaFuncSetAttribute(conv_dw_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_DW)))
+    if ((e = cudaFuncSetAttribute(conv_dw_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_DW)))
         return e;
     if ((e = cudaFuncSetAttribute(head_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM_HEAD)))
         return e;
@@ -876,20 +1011,24 @@ bamf_status forward(bamf_cnn *net, const float *data, int n, cudaStream_t s)
 /* loss and gradients (accumulated into G) of the batch whose forward ran */
 bamf_status backward(bamf_cnn *net, const int32_t *n_em, const float *xyi, int n, float inv_batch, cudaStream_t s)
 {
-    head_kernel<true><<<n, 256, SMEM_HEAD, s>>>(net->a[3], n, net->P, n_em, xyi, inv_batch, net->G, net->dzA,
+    head_kernel<true><<<n, 256, SMEM_HEAD, s>>>(net->a[3], n, net->P, n_em, xyi, inv_batch, net->hpart, net->dzA,
                                                 net->loss, net->step, nullptr, nullptr, nullptr);
     bf16 *dz = net->dzA, *dzn = net->dzB;
     for (int l = 2; l >= 0; --l) {
         /* layer l+2: input a[l], output a[l+1]; dz = dL/dz_{l+2} */
-        conv_dw_kernel<<<grid_for(n, 3, net->sms), 288, SMEM_DW, s>>>(net->a[l], dz, n, net->G + O_W[l],
-                                                                     net->G + O_B[l]);
+        const int gdw = grid_for(n, 2, net->sms);
+        conv_dw_tc_kernel<<<gdw, 128, SMEM_DW, s>>>(net->a[l], dz, n, net->dwpart, net->tc_status);
+        dw_reduce_kernel<<<(DW_PART + 31) / 32, 1024, 0, s>>>(net->dwpart, gdw, net->G + O_W[l], net->G + O_B[l]);
         conv_tc_kernel<1><<<grid_for(n, 3, net->sms), 128, SMEM_TC, s>>>(dz, net->Wb + l * PKT, nullptr,
                                                                          net->a[l], dzn, n, net->tc_status);
         bf16 *tmp = dz;
         dz = dzn;
         dzn = tmp;
     }
-    conv1_bwd_kernel<<<grid_for(n, 4, net->sms), 256, 0, s>>>(net->x0, dz, n, net->G);
+    reduce_rows_kernel<<<(HEAD_NPARAM + 31) / 32, 1024, 0, s>>>(net->hpart, n, HEAD_NPARAM, net->G + O_WL);
+    const int g1 = grid_for(n, 4, net->sms);
+    conv1_bwd_kernel<<<g1, 256, 0, s>>>(net->x0, dz, n, net->c1part);
+    reduce_rows_kernel<<<(C1_NPARAM + 31) / 32, 1024, 0, s>>>(net->c1part, g1, C1_NPARAM, net->G + O_W1);
     CK(cudaGetLastError());
     return BAMF_OK;
 }
@@ -921,7 +1060,7 @@ extern "C" void bamf_cnn_destroy(bamf_cnn *net)
     if (!net) return;
     void *ps[] = {net->P, net->G, net->M, net->V, net->Wf, net->Wb, net->x0, net->a[0], net->a[1], net->a[2],
                   net->a[3], net->dzA, net->dzB, net->gdata, net->gxyi, net->gn, net->step, net->loss,
-                  net->tc_status};
+                  net->tc_status, net->dwpart, net->hpart, net->c1part};
     for (void *p : ps)
         if (p) cudaFree(p);
     delete net;
@@ -942,6 +1081,9 @@ extern "C" bamf_status bamf_cnn_create(bamf_cnn **out, uint32_t seed)
               cudaMalloc(&net->M, NPARAM * 4) == cudaSuccess && cudaMalloc(&net->V, NPARAM * 4) == cudaSuccess &&
               cudaMalloc(&net->Wf, 3 * PKT * 2) == cudaSuccess && cudaMalloc(&net->Wb, 3 * PKT * 2) == cudaSuccess &&
               cudaMalloc(&net->tc_status, sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&net->dwpart, (size_t)2 * net->sms * DW_PART * 4) == cudaSuccess &&
+              cudaMalloc(&net->hpart, B * HEAD_NPARAM * 4) == cudaSuccess &&
+              cudaMalloc(&net->c1part, (size_t)4 * net->sms * C1_NPARAM * 4) == cudaSuccess &&
               cudaMalloc(&net->x0, B * NPX * 4) == cudaSuccess && cudaMalloc(&net->dzA, B * NPX * CH * 2) == cudaSuccess &&
               cudaMalloc(&net->dzB, B * NPX * CH * 2) == cudaSuccess &&
               cudaMalloc(&net->gdata, B * NPX * 4) == cudaSuccess &&

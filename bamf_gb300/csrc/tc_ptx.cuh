@@ -4,10 +4,13 @@
  * commit to an mbarrier, TMEM loads) and the mbarrier / proxy fences they
  * need, for sm_103a.  Written from the PTX ISA's descriptions.
  *
- * Operand layout used throughout: K-major, no swizzle.  An operand tile is a
- * grid of "core matrices" of 8 rows x 16 bytes (8 bf16 along K), each stored
- * as 128 contiguous bytes; LBO is the byte distance between core matrices
- * adjacent along K, SBO between core matrices adjacent along M (or N).
+ * Operand layouts, no swizzle.  An operand tile is a grid of "core
+ * matrices" of 128 contiguous bytes.  K-major: a core matrix is 8 rows of M
+ * (or N) x 16 bytes (8 bf16 along K).  MN-major: 8 rows of K x 16 bytes (8
+ * bf16 along M or N).  In both, LBO is the byte distance between core
+ * matrices adjacent along K and SBO between core matrices adjacent along M
+ * (or N); the MN-major reading is pinned by a known-answer check
+ * (tc_selftest.cu).
  */
 #ifndef BAMF_TC_PTX_CUH
 #define BAMF_TC_PTX_CUH
@@ -34,6 +37,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+/* The same with both A and B MN-major (the descriptor's transpose bits). */
+__host__ __device__ constexpr uint32_t idesc_bf16_f32_mn(int M, int N)
+{
+    return idesc_bf16_f32(M, N) | (1u << 15) | (1u << 16);
 }
 
 /* TMEM allocation by one full warp; the address lands in *slot (shared). */

@@ -573,6 +573,11 @@ bamf_status bamf_probe_peaks(double *fp32_flops, double *mufu_ops);
  * if the MMA's completion did not arrive within the kernel's bounded wait. */
 bamf_status bamf_tcgen05_selftest(double *max_abs_err, int *timed_out);
 
+/* The same check for one operand layout: 0 = both operands K-major (as
+ * bamf_tcgen05_selftest), 1 = both MN-major (the layout of the
+ * convolutions' weight-gradient GEMM). */
+bamf_status bamf_tcgen05_selftest_layout(int layout, double *max_abs_err, int *timed_out);
+
 #ifdef __cplusplus
 }
 #endif

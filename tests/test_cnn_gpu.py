@@ -60,13 +60,16 @@ def test_forward_matches_the_torch_oracle(cuda_lib):
     assert torch.allclose(sub.reshape(-1, 16).sum(1), torch.ones(48 * 256), atol=1e-4)
 
 
-def test_gradients_match_torch_autograd(cuda_lib):
+@pytest.mark.parametrize("n", [32, 600])
+def test_gradients_match_torch_autograd(cuda_lib, n):
+    """n = 600 puts several ROIs on each CTA of the weight-gradient kernel
+    (accumulation in TMEM across ROIs, next-ROI prefetch)."""
     import torch
 
     from bamf_gb300 import learned
     from oracle import cnn_torch
     net = learned.ProposalNet(seed=4)
-    b = learned.generate(32, seed=11)
+    b = learned.generate(n, seed=11)
     loss, grad = net.loss_grad(b)
     h = _host(b)
     theta = torch.tensor(net.get_params()).requires_grad_(True)
