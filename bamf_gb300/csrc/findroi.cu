@@ -306,23 +306,48 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
     }
 }
 
-/* Compaction, phase 1: flags per 1024-pixel chunk. */
+/* Compaction: chunks of CHUNK pixels, one block of 256 threads each, a
+ * thread owning 32 consecutive pixels (two 16-byte loads of flags where the
+ * 32 lie inside the stack and are 16-byte aligned). */
+constexpr int CHUNK = 256 * 32;
+
+/* the flags of pixels [j0, j0 + 32) as a bit mask, bit q = pixel j0 + q
+ * (flags are 0 or 1: byte i of a little-endian word holds pixel i's flag in
+ * its lowest bit) */
+__device__ __forceinline__ uint32_t flag_bits(const uint8_t *__restrict__ flags, int64_t n, int64_t j0)
+{
+    uint32_t m = 0;
+    if (j0 + 32 <= n && (reinterpret_cast<uintptr_t>(flags + j0) & 15) == 0) {
+        const uint4 *v = reinterpret_cast<const uint4 *>(flags + j0);
+        const uint4 a = v[0], b = v[1];
+        const uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t x = w[k];
+            m |= ((x & 1u) | ((x >> 7) & 2u) | ((x >> 14) & 4u) | ((x >> 21) & 8u)) << (4 * k);
+        }
+    } else {
+        for (int q = 0; q < 32; ++q)
+            if (j0 + q < n && flags[j0 + q]) m |= 1u << q;
+    }
+    return m;
+}
+
+/* phase 1: flags per chunk. */
 __global__ void __launch_bounds__(256) count_kernel(const uint8_t *__restrict__ flags, int64_t n,
                                                     int32_t *__restrict__ counts)
 {
-    __shared__ int s;
-    if (threadIdx.x == 0) s = 0;
-    __syncthreads();
-    int64_t base = (int64_t)blockIdx.x * 1024;
-    int local = 0;
-    for (int i = threadIdx.x; i < 1024; i += 256) {
-        int64_t j = base + i;
-        if (j < n) local += flags[j];
-    }
+    __shared__ int wsum[8];
+    const int64_t j0 = (int64_t)blockIdx.x * CHUNK + (int64_t)threadIdx.x * 32;
+    int local = __popc(flag_bits(flags, n, j0));
     for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&s, local);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = local;
     __syncthreads();
-    if (threadIdx.x == 0) counts[blockIdx.x] = s;
+    if (threadIdx.x == 0) {
+        int s = 0;
+        for (int k = 0; k < 8; ++k) s += wsum[k];
+        counts[blockIdx.x] = s;
+    }
 }
 
 /* phase 2: exclusive scan of the chunk counts (one block, serial tiles). */
@@ -372,16 +397,11 @@ __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ f
                                                    int32_t *__restrict__ corners)
 {
     __shared__ int wsum[8];
-    int64_t base = (int64_t)blockIdx.x * 1024;
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    /* each thread owns 4 consecutive pixels: keeps memory order */
-    int64_t j0 = base + threadIdx.x * 4;
-    int f[4], cnt = 0;
-    for (int q = 0; q < 4; ++q) {
-        int64_t j = j0 + q;
-        f[q] = (j < n) ? flags[j] : 0;
-        cnt += f[q];
-    }
+    /* each thread owns 32 consecutive pixels: keeps memory order */
+    const int64_t j0 = (int64_t)blockIdx.x * CHUNK + (int64_t)threadIdx.x * 32;
+    uint32_t bits = flag_bits(flags, n, j0);
+    const int cnt = __popc(bits);
     int x = cnt;
     for (int o = 1; o < 32; o <<= 1) {
         int t = __shfl_up_sync(0xffffffffu, x, o);
@@ -393,8 +413,9 @@ __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ f
     for (int i = 0; i < w; ++i) before += wsum[i];
     int64_t pos = (int64_t)offs[blockIdx.x] + before + x - cnt;
     const int half = (int)floor(box / 2.0 + 0.5);
-    for (int q = 0; q < 4; ++q) {
-        if (!f[q]) continue;
+    while (bits) {
+        const int q = __ffs(bits) - 1;
+        bits &= bits - 1;
         if (pos < capacity) {
             int64_t m = j0 + q;
             int64_t plane = (int64_t)Ysz * Xsz;
@@ -504,7 +525,7 @@ extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *fr
         if (!ws->flags.ensure(n)) return BAMF_ERR_CUDA;
         flags = (uint8_t *)ws->flags.p;
     }
-    int64_t nchunks = (n + 1023) / 1024;
+    int64_t nchunks = (n + CHUNK - 1) / CHUNK;
     if (!ws->chunks.ensure(nchunks * sizeof(int32_t)) || !ws->total.ensure(sizeof(int64_t)))
         return BAMF_ERR_CUDA;
     float *A = (float *)ws->a.p, *Bb = (float *)ws->b.p;
