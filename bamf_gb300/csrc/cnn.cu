@@ -45,6 +45,9 @@ static_assert(O_B1 == O_W1 + 288 && O_BC + NC == NPARAM, "conv1 block and head l
 constexpr int HEAD_NPARAM = NPARAM - O_WL; /* WL, BL, WC, BC: the heads' parameters, contiguous */
 static_assert(O_BL == O_WL + NSUB * CH && O_WC == O_BL + NSUB && O_BC == O_WC + NC * CH, "head layout");
 constexpr int C1_NPARAM = O_W2;            /* W1, B1 */
+constexpr int HS = CH + 4;                 /* head kernel: floats per pixel row of H (16-byte rows) */
+/* the WC part of ROI r's head-gradient row */
+__device__ __forceinline__ float *row_wc(float *G, int r) { return G + (size_t)r * HEAD_NPARAM + (O_WC - O_WL); }
 constexpr int O_W[3] = {O_W2, O_W3, O_W4};
 constexpr int O_B[3] = {O_B2, O_B3, O_B4};
 constexpr int PKT = 9 * CH * CH; /* tensor-core operand weights of one layer */
@@ -218,43 +221,74 @@ __global__ void conv1_fwd_kernel(const float *__restrict__ data, int n, const fl
 }
 
 /* dW1, db1 from dz1 (= dL/d pre-activation of conv1) and x0: each CTA's
- * sums over its ROIs into row blockIdx.x of G (C1_NPARAM floats). */
-__global__ void conv1_bwd_kernel(const float *__restrict__ x0, const bf16 *__restrict__ dz1, int n,
-                                 float *__restrict__ G)
+ * sums over its ROIs into row blockIdx.x of G (C1_NPARAM floats).  Warp w
+ * owns output channels 4w .. 4w + 3 (all 9 taps and the bias), lane l the
+ * pixels l + 32 i: per pixel 9 neighbours and 4 dz values from shared
+ * memory feed 40 register accumulators, kept over all the CTA's ROIs and
+ * reduced over the warp once at the end. */
+__global__ void __launch_bounds__(256) conv1_bwd_kernel(const float *__restrict__ x0, const bf16 *__restrict__ dz1,
+                                                        int n, float *__restrict__ G)
 {
     __shared__ float xp[PS * PS];
     __shared__ float dz[NPX * (CH + 1)];
-    int t = threadIdx.x;
-    float acc0 = 0.0f, acc1 = 0.0f;
-    const int o0 = t, o1 = t + 256; /* outputs: co*9+tap (288), then 288+co */
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    float acc[4][9], accb[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        accb[j] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[j][k] = 0.0f;
+    }
     for (int i = t; i < PS * PS; i += blockDim.x) xp[i] = 0.0f;
     for (int r = blockIdx.x; r < n; r += gridDim.x) {
         __syncthreads();
-        int x = t / S, y = t - (t / S) * S;
-        xp[(x + 1) * PS + (y + 1)] = x0[(size_t)r * NPX + t];
-        for (int c = 0; c < CH; ++c) dz[t * (CH + 1) + c] = __bfloat162float(dz1[((size_t)r * NPX + t) * CH + c]);
-        __syncthreads();
-        for (int h = 0; h < 2; ++h) {
-            int o = h ? o1 : o0;
-            if (o >= 320) continue;
-            float acc = 0.0f;
-            if (o < 288) {
-                int co = o / 9, tp = o - co * 9, kx = tp / 3, ky = tp - kx * 3;
-                for (int p = 0; p < NPX; ++p) {
-                    int px = p / S, py = p - px * S;
-                    acc += dz[p * (CH + 1) + co] * xp[(px + kx) * PS + (py + ky)];
+        {
+            const int x = t / S, y = t - (t / S) * S;
+            xp[(x + 1) * PS + (y + 1)] = x0[(size_t)r * NPX + t];
+            const uint4 *src = (const uint4 *)(dz1 + ((size_t)r * NPX + t) * CH);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const uint4 u = src[q];
+                const __nv_bfloat162 *b = (const __nv_bfloat162 *)&u;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const float2 f = __bfloat1622float2(b[e]);
+                    dz[t * (CH + 1) + 8 * q + 2 * e] = f.x;
+                    dz[t * (CH + 1) + 8 * q + 2 * e + 1] = f.y;
                 }
-            } else {
-                int co = o - 288;
-                for (int p = 0; p < NPX; ++p) acc += dz[p * (CH + 1) + co];
             }
-            if (h) acc1 += acc;
-            else acc0 += acc;
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int i = 0; i < NPX / 32; ++i) {
+            const int p = lane + 32 * i, x = p >> 4, y = p & 15;
+            float nb[9];
+#pragma unroll
+            for (int kx = 0; kx < 3; ++kx)
+#pragma unroll
+                for (int ky = 0; ky < 3; ++ky) nb[kx * 3 + ky] = xp[(x + kx) * PS + (y + ky)];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float d = dz[p * (CH + 1) + 4 * warp + j];
+                accb[j] += d;
+#pragma unroll
+                for (int k = 0; k < 9; ++k) acc[j][k] += d * nb[k];
+            }
         }
     }
     float *row = G + (size_t)blockIdx.x * C1_NPARAM;
-    if (o0 < C1_NPARAM) row[o0] = acc0;
-    if (o1 < C1_NPARAM) row[o1] = acc1;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            float v = acc[j][k];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) row[(4 * warp + j) * 9 + k] = v;
+        }
+        float v = accb[j];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) row[288 + 4 * warp + j] = v;
+    }
 }
 
 /* -------------------------------------------------- 32 -> 32 convolution */
@@ -641,9 +675,10 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
                                                    float *__restrict__ cnt_out)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *H = (float *)smem_raw;             /* [256][33] */
-    float *DZ = H + NPX * (CH + 1);           /* [256][17] */
-    __shared__ float Wl[NSUB * CH], bl[NSUB], Wc[NC * CH], bc[NC];
+    float *H = (float *)smem_raw;             /* [256][HS] */
+    float *DZ = H + NPX * HS;                 /* [256][17] */
+    __shared__ __align__(16) float Wl[NSUB * CH];
+    __shared__ float bl[NSUB], Wc[NC * CH], bc[NC];
     __shared__ float red[8], gmean[CH], part[8][CH], zc[NC], dzc[NC], dg[CH];
     __shared__ float ex[BAMF_SYNTH_NMAX], ey[BAMF_SYNTH_NMAX];
     __shared__ float sm_max, sm_sum, loss_loc_sh;
@@ -662,13 +697,22 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
             for (int e = 0; e < 8; ++e) h[qd * 8 + e] = __bfloat162float(b[e]);
         }
     }
-    for (int c = 0; c < CH; ++c) H[t * (CH + 1) + c] = h[c];
+#pragma unroll
+    for (int q = 0; q < CH / 4; ++q)
+        ((float4 *)H)[t * (HS / 4) + q] = make_float4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
     __syncthreads();
     float z[NSUB];
     float mx = -INFINITY;
     for (int s = 0; s < NSUB; ++s) {
         float v = bl[s];
-        for (int c = 0; c < CH; ++c) v += Wl[s * CH + c] * h[c];
+#pragma unroll
+        for (int q = 0; q < CH / 4; ++q) {
+            const float4 w = ((const float4 *)Wl)[s * (CH / 4) + q];
+            v += w.x * h[4 * q];
+            v += w.y * h[4 * q + 1];
+            v += w.z * h[4 * q + 2];
+            v += w.w * h[4 * q + 3];
+        }
         z[s] = v;
         mx = fmaxf(mx, v);
     }
@@ -678,7 +722,7 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
     {
         int c = t & 31, grp = t >> 5;
         float sacc = 0.0f;
-        for (int p = grp; p < NPX; p += 8) sacc += H[p * (CH + 1) + c];
+        for (int p = grp; p < NPX; p += 8) sacc += H[p * HS + c];
         part[grp][c] = sacc;
     }
     __syncthreads();
@@ -788,11 +832,25 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
     __syncthreads();
     /* dz4 of this pixel */
     {
+        float dzr[NSUB];
+#pragma unroll
+        for (int k = 0; k < NSUB; ++k) dzr[k] = DZ[t * (NSUB + 1) + k];
         __align__(16) bf16 o[CH];
-        for (int c = 0; c < CH; ++c) {
-            float v = dg[c];
-            for (int s = 0; s < NSUB; ++s) v += DZ[t * (NSUB + 1) + s] * Wl[s * CH + c];
-            o[c] = __float2bfloat16_rn(h[c] > 0.0f ? v : 0.0f);
+#pragma unroll
+        for (int q = 0; q < CH / 4; ++q) {
+            float v0 = dg[4 * q], v1 = dg[4 * q + 1], v2 = dg[4 * q + 2], v3 = dg[4 * q + 3];
+#pragma unroll
+            for (int k = 0; k < NSUB; ++k) {
+                const float4 w = ((const float4 *)Wl)[k * (CH / 4) + q];
+                v0 += dzr[k] * w.x;
+                v1 += dzr[k] * w.y;
+                v2 += dzr[k] * w.z;
+                v3 += dzr[k] * w.w;
+            }
+            o[4 * q] = __float2bfloat16_rn(h[4 * q] > 0.0f ? v0 : 0.0f);
+            o[4 * q + 1] = __float2bfloat16_rn(h[4 * q + 1] > 0.0f ? v1 : 0.0f);
+            o[4 * q + 2] = __float2bfloat16_rn(h[4 * q + 2] > 0.0f ? v2 : 0.0f);
+            o[4 * q + 3] = __float2bfloat16_rn(h[4 * q + 3] > 0.0f ? v3 : 0.0f);
         }
         uint4 *dst = (uint4 *)(dz4 + ((size_t)r * NPX + t) * CH);
         const uint4 *src = (const uint4 *)o;
@@ -800,21 +858,47 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
     }
     /* head parameter gradients of this ROI, in the parameter order from O_WL
      * (WL, BL, WC, BC), into its row of G (one row per ROI; reduce_rows_kernel
-     * adds the rows) */
-    float *row = G + (size_t)r * HEAD_NPARAM;
-    for (int o = t; o < NSUB * CH; o += 256) {
-        int s = o / CH, c = o - (o / CH) * CH;
-        float v = 0.0f;
-        for (int p = 0; p < NPX; ++p) v += DZ[p * (NSUB + 1) + s] * H[p * (CH + 1) + c];
-        row[o] = v;
+     * adds the rows).  dWL[s][c] = sum over pixels of DZ[p][s] H[p][c] and
+     * dBL[s] = sum of DZ[p][s]: thread t owns the 2 x 4 block (s0, c0) of
+     * tile t & 63 over the pixel quarter t >> 6; the four quarters are added
+     * through shared memory (over H, once every thread has read it). */
+    {
+        const int tile = t & 63, quarter = t >> 6;
+        const int s0 = 2 * (tile >> 3), c0 = 4 * (tile & 7);
+        float g0[4] = {0.0f, 0.0f, 0.0f, 0.0f}, g1[4] = {0.0f, 0.0f, 0.0f, 0.0f}, gb0 = 0.0f, gb1 = 0.0f;
+#pragma unroll 4
+        for (int p = 64 * quarter; p < 64 * quarter + 64; ++p) {
+            const float4 hv = ((const float4 *)H)[p * (HS / 4) + (c0 >> 2)];
+            const float d0 = DZ[p * (NSUB + 1) + s0], d1 = DZ[p * (NSUB + 1) + s0 + 1];
+            g0[0] += d0 * hv.x;
+            g0[1] += d0 * hv.y;
+            g0[2] += d0 * hv.z;
+            g0[3] += d0 * hv.w;
+            g1[0] += d1 * hv.x;
+            g1[1] += d1 * hv.y;
+            g1[2] += d1 * hv.z;
+            g1[3] += d1 * hv.w;
+            gb0 += d0;
+            gb1 += d1;
+        }
+        __syncthreads();
+        constexpr int QW = NSUB * CH + NSUB; /* one quarter's WL and BL sums */
+        float *red = H + quarter * QW;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            red[s0 * CH + c0 + k] = g0[k];
+            red[(s0 + 1) * CH + c0 + k] = g1[k];
+        }
+        if ((tile & 7) == 0) {
+            red[NSUB * CH + s0] = gb0;
+            red[NSUB * CH + s0 + 1] = gb1;
+        }
+        __syncthreads();
+        float *row = G + (size_t)r * HEAD_NPARAM;
+        for (int o = t; o < QW; o += 256) row[o] = (H[o] + H[QW + o]) + (H[2 * QW + o] + H[3 * QW + o]);
     }
-    if (t < NSUB) {
-        float v = 0.0f;
-        for (int p = 0; p < NPX; ++p) v += DZ[p * (NSUB + 1) + t];
-        row[O_BL - O_WL + t] = v;
-    }
-    for (int o = t; o < NC * CH; o += 256) row[O_WC - O_WL + o] = dzc[o / CH] * gmean[o - (o / CH) * CH];
-    if (t < NC) row[O_BC - O_WL + t] = dzc[t];
+    for (int o = t; o < NC * CH; o += 256) row_wc(G, r)[o] = dzc[o / CH] * gmean[o - (o / CH) * CH];
+    if (t < NC) row_wc(G, r)[NC * CH + t] = dzc[t];
 }
 
 /* --------------------------------------------------------- start states */
@@ -964,7 +1048,7 @@ namespace {
 std::mutex g_attr_mutex;
 bool g_attr_done = false;
 
-const size_t SMEM_HEAD = (size_t)(NPX * (CH + 1) + NPX * (NSUB + 1)) * sizeof(float);
+const size_t SMEM_HEAD = (size_t)(NPX * HS + NPX * (NSUB + 1)) * sizeof(float);
 
 cudaError_t set_attrs()
 {
