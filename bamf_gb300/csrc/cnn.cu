@@ -399,6 +399,17 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const bf16 *__restrict__ i
         }
         const int rn = r + gridDim.x;
         if (rn < n) load(rn);
+        /* MODE 1: this thread's two pixels of the ReLU mask, loaded while
+         * the MMAs run */
+        uint4 mk[2][4];
+        if (MODE == 1) {
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                const uint4 *ms = (const uint4 *)(mask + ((size_t)r * NPX + 128 * mt + t) * CH);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) mk[mt][q] = ms[q];
+            }
+        }
         const bool ok = bamf::tc::mbar_wait(mbar, phase, 1u << 24);
         phase ^= 1u;
         bamf::tc::fence_after_sync();
@@ -419,14 +430,14 @@ __global__ void __launch_bounds__(128) conv_tc_kernel(const bf16 *__restrict__ i
                         o[c] = __floats2bfloat162_rn(fmaxf(v[2 * c] + bias[2 * c], 0.0f),
                                                      fmaxf(v[2 * c + 1] + bias[2 * c + 1], 0.0f));
                 } else {
-                    __align__(16) __nv_bfloat162 mk[16];
-                    const uint4 *ms = (const uint4 *)(mask + off);
+                    __align__(16) uint4 m4[4];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) ((uint4 *)mk)[q] = ms[q];
+                    for (int q = 0; q < 4; ++q) m4[q] = mt == 0 ? mk[0][q] : mk[1][q];
+                    const __nv_bfloat162 *m2 = (const __nv_bfloat162 *)m4;
 #pragma unroll
                     for (int c = 0; c < 16; ++c)
-                        o[c] = __floats2bfloat162_rn(__bfloat162float(mk[c].x) > 0.0f ? v[2 * c] : 0.0f,
-                                                     __bfloat162float(mk[c].y) > 0.0f ? v[2 * c + 1] : 0.0f);
+                        o[c] = __floats2bfloat162_rn(__bfloat162float(m2[c].x) > 0.0f ? v[2 * c] : 0.0f,
+                                                     __bfloat162float(m2[c].y) > 0.0f ? v[2 * c + 1] : 0.0f);
                 }
                 uint4 *dst = (uint4 *)(out + off);
 #pragma unroll
