@@ -47,7 +47,7 @@ static_assert(O_BL == O_WL + NSUB * CH && O_WC == O_BL + NSUB && O_BC == O_WC + 
 constexpr int C1_NPARAM = O_W2;            /* W1, B1 */
 constexpr int HS = CH + 4;                 /* head kernel: floats per pixel row of H (16-byte rows) */
 /* the WC part of ROI r's head-gradient row */
-__device__ __forceinline__ float *row_wc(float *G, int r) { return G + (size_t)r * HEAD_NPARAM + (O_WC - O_WL); }
+__device__ __forceinline__ float *row_wc(float *rows, int r) { return rows + (size_t)r * HEAD_NPARAM + (O_WC - O_WL); }
 constexpr int O_W[3] = {O_W2, O_W3, O_W4};
 constexpr int O_B[3] = {O_B2, O_B3, O_B4};
 constexpr int PKT = 9 * CH * CH; /* tensor-core operand weights of one layer */
@@ -221,13 +221,13 @@ __global__ void conv1_fwd_kernel(const float *__restrict__ data, int n, const fl
 }
 
 /* dW1, db1 from dz1 (= dL/d pre-activation of conv1) and x0: each CTA's
- * sums over its ROIs into row blockIdx.x of G (C1_NPARAM floats).  Warp w
+ * sums over its ROIs into row blockIdx.x of `rows` (C1_NPARAM floats).  Warp w
  * owns output channels 4w .. 4w + 3 (all 9 taps and the bias), lane l the
  * pixels l + 32 i: per pixel 9 neighbours and 4 dz values from shared
  * memory feed 40 register accumulators, kept over all the CTA's ROIs and
  * reduced over the warp once at the end. */
 __global__ void __launch_bounds__(256) conv1_bwd_kernel(const float *__restrict__ x0, const bf16 *__restrict__ dz1,
-                                                        int n, float *__restrict__ G)
+                                                        int n, float *__restrict__ rows)
 {
     __shared__ float xp[PS * PS];
     __shared__ float dz[NPX * (CH + 1)];
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(256) conv1_bwd_kernel(const float *__restrict_
             }
         }
     }
-    float *row = G + (size_t)blockIdx.x * C1_NPARAM;
+    float *row = rows + (size_t)blockIdx.x * C1_NPARAM;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
 #pragma unroll
@@ -626,16 +626,24 @@ __global__ void __launch_bounds__(128) conv_dw_tc_kernel(const bf16 *__restrict_
 /* Column sums of a row-major [nrows][width] array of partial sums, in a
  * fixed order (no atomics: the same bits every run).  A CTA of 32 warps owns
  * 32 consecutive columns (lane = column, coalesced): warp w adds rows w,
- * w + 32, ...; then warp 0 adds the 32 warp sums in order.  The result is
- * valid in warp 0. */
+ * w + 32, ... into four interleaved accumulators; then warp 0 adds the 32
+ * warp sums in order.  The result is valid in warp 0. */
 __device__ __forceinline__ float column_sum(const float *__restrict__ part, int nrows, int width, int j,
                                             float (*red)[33])
 {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    float acc = 0.0f;
-    if (j < width)
-        for (int c = w; c < nrows; c += 32) acc += part[(size_t)c * width + j];
-    red[w][lane] = acc;
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f; /* four loads in flight */
+    if (j < width) {
+        int c = w;
+        for (; c + 96 < nrows; c += 128) {
+            a0 += part[(size_t)c * width + j];
+            a1 += part[(size_t)(c + 32) * width + j];
+            a2 += part[(size_t)(c + 64) * width + j];
+            a3 += part[(size_t)(c + 96) * width + j];
+        }
+        for (; c < nrows; c += 32) a0 += part[(size_t)c * width + j];
+    }
+    red[w][lane] = (a0 + a1) + (a2 + a3);
     __syncthreads();
     float sum = 0.0f;
     if (w == 0)
@@ -674,13 +682,13 @@ __global__ void __launch_bounds__(1024) dw_reduce_kernel(const float *__restrict
 
 /* ----------------------------------------------------------------- heads */
 /* One CTA (256 threads, thread = pixel) per ROI.  TRAIN: loss, head
- * gradients (row r of G, HEAD_NPARAM floats per ROI), dz4 = dL/d(pre-
+ * gradients (row r of `hrows`, HEAD_NPARAM floats per ROI), dz4 = dL/d(pre-
  * activation of conv4).  INFER: the sampler's birth tables and the count
  * logits. */
 template <bool TRAIN>
 __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, int n, const float *__restrict__ P,
                                                    const int32_t *__restrict__ n_em, const float *__restrict__ xyi,
-                                                   float inv_batch, float *__restrict__ G, bf16 *__restrict__ dz4,
+                                                   float inv_batch, float *__restrict__ hrows, bf16 *__restrict__ dz4,
                                                    float *__restrict__ loss_buf, const int *__restrict__ step_dev,
                                                    float *__restrict__ cdf, float *__restrict__ sub,
                                                    float *__restrict__ cnt_out)
@@ -868,7 +876,7 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
         for (int qd = 0; qd < 4; ++qd) dst[qd] = src[qd];
     }
     /* head parameter gradients of this ROI, in the parameter order from O_WL
-     * (WL, BL, WC, BC), into its row of G (one row per ROI; reduce_rows_kernel
+     * (WL, BL, WC, BC), into its row of `hrows` (one row per ROI; reduce_rows_kernel
      * adds the rows).  dWL[s][c] = sum over pixels of DZ[p][s] H[p][c] and
      * dBL[s] = sum of DZ[p][s]: thread t owns the 2 x 4 block (s0, c0) of
      * tile t & 63 over the pixel quarter t >> 6; the four quarters are added
@@ -905,11 +913,11 @@ __global__ void __launch_bounds__(256) head_kernel(const bf16 *__restrict__ a4, 
             red[NSUB * CH + s0 + 1] = gb1;
         }
         __syncthreads();
-        float *row = G + (size_t)r * HEAD_NPARAM;
+        float *row = hrows + (size_t)r * HEAD_NPARAM;
         for (int o = t; o < QW; o += 256) row[o] = (H[o] + H[QW + o]) + (H[2 * QW + o] + H[3 * QW + o]);
     }
-    for (int o = t; o < NC * CH; o += 256) row_wc(G, r)[o] = dzc[o / CH] * gmean[o - (o / CH) * CH];
-    if (t < NC) row_wc(G, r)[NC * CH + t] = dzc[t];
+    for (int o = t; o < NC * CH; o += 256) row_wc(hrows, r)[o] = dzc[o / CH] * gmean[o - (o / CH) * CH];
+    if (t < NC) row_wc(hrows, r)[NC * CH + t] = dzc[t];
 }
 
 /* --------------------------------------------------------- start states */
