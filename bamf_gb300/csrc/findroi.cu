@@ -490,6 +490,13 @@ bamf_status launch_err()
 
 struct bamf_findroi_ws {
     Scratch a, b, flags, chunks, total;
+    cudaStream_t copy = nullptr; /* host-to-device chunks of bamf_find_roi_pinned */
+    cudaEvent_t landed = nullptr;
+    ~bamf_findroi_ws()
+    {
+        if (landed) cudaEventDestroy(landed);
+        if (copy) cudaStreamDestroy(copy);
+    }
 };
 
 extern "C" bamf_status bamf_findroi_workspace_create(bamf_findroi_ws **ws)
@@ -501,11 +508,18 @@ extern "C" bamf_status bamf_findroi_workspace_create(bamf_findroi_ws **ws)
 
 extern "C" void bamf_findroi_workspace_destroy(bamf_findroi_ws *ws) { delete ws; }
 
-extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *frames, int ysize,
-                                            int xsize, int zsize, double sigma1, double sigma2,
-                                            int boxsize, float minval, int64_t capacity,
-                                            int32_t *coords, int32_t *corners, float *roi_stack,
-                                            int64_t *count, uint8_t *flags_out, void *stream)
+namespace {
+
+/* Passes 1-5 on `frames` (device).  With host_frames, the frames are first
+ * copied from there in chunks of chunk_frames on the workspace's copy
+ * stream, and each chunk's row and column filters start on `s` as soon as
+ * its copy has landed (the filters are frame-local, so a chunk is filtered
+ * exactly as inside the whole stack); the window maxima and everything after
+ * them run on the whole stack once every chunk is filtered. */
+bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_frames, const float *frames,
+                     int ysize, int xsize, int zsize, double sigma1, double sigma2, int boxsize, float minval,
+                     int64_t capacity, int32_t *coords, int32_t *corners, float *roi_stack, int64_t *count,
+                     uint8_t *flags_out, cudaStream_t s)
 {
     if (!ws || !frames || !coords || !count || ysize < 1 || xsize < 1 || zsize < 1 || boxsize < 1 ||
         capacity < 0)
@@ -513,7 +527,6 @@ extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *fr
     if ((roi_stack != nullptr) && corners == nullptr) return BAMF_ERR_INVALID_ARG;
     if (xsize > ysize * 64 || ysize > xsize * 64) return BAMF_ERR_INVALID_ARG;
     if (boxsize > 256) return BAMF_ERR_TOO_LARGE; /* the maxima tiles stage 2 boxsize + 96 rows */
-    cudaStream_t s = (cudaStream_t)stream;
     const int64_t n = (int64_t)xsize * ysize * zsize;
     /* kernel view (as the reference launches it): each frame is KY = Ysize
      * runs of KX = Xsize contiguous floats (size(Image,2), findROI.m:186-189) */
@@ -529,17 +542,37 @@ extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *fr
     if (!ws->chunks.ensure(nchunks * sizeof(int32_t)) || !ws->total.ensure(sizeof(int64_t)))
         return BAMF_ERR_CUDA;
     float *A = (float *)ws->a.p, *Bb = (float *)ws->b.p;
-    int64_t nrows = (int64_t)KY * zsize, ncols = (int64_t)KX * zsize;
-    {
-        int dev = 0, sms = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        int64_t groups = (nrows + 31) / 32;
-        unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((groups + ROWS_WARPS - 1) / ROWS_WARPS,
-                                                                         (int64_t)sms * ROWS_CTAS_PER_SM));
-        rows_kernel<<<grid, 32 * ROWS_WARPS, 0, s>>>(frames, A, Bb, KX, KY, zsize, ca, cb);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (host_frames) {
+        if (!ws->copy && cudaStreamCreateWithFlags(&ws->copy, cudaStreamNonBlocking) != cudaSuccess)
+            return BAMF_ERR_CUDA;
+        if (!ws->landed && cudaEventCreateWithFlags(&ws->landed, cudaEventDisableTiming) != cudaSuccess)
+            return BAMF_ERR_CUDA;
+        /* the copies start after the work already enqueued on s */
+        if (cudaEventRecord(ws->landed, s) != cudaSuccess || cudaStreamWaitEvent(ws->copy, ws->landed, 0) != cudaSuccess)
+            return BAMF_ERR_CUDA;
     }
-    cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(A, Bb, KX, KY, zsize, ca, cb);
+    const int step = host_frames ? std::max(1, chunk_frames) : zsize;
+    const int64_t plane = (int64_t)KX * KY;
+    for (int z0 = 0; z0 < zsize; z0 += step) {
+        const int zc = std::min(step, zsize - z0);
+        const int64_t off = z0 * plane;
+        if (host_frames) {
+            if (cudaMemcpyAsync((float *)frames + off, host_frames + off, (size_t)(zc * plane) * sizeof(float),
+                                cudaMemcpyHostToDevice, ws->copy) != cudaSuccess ||
+                cudaEventRecord(ws->landed, ws->copy) != cudaSuccess ||
+                cudaStreamWaitEvent(s, ws->landed, 0) != cudaSuccess)
+                return BAMF_ERR_CUDA;
+        }
+        const int64_t nrows = (int64_t)KY * zc, ncols = (int64_t)KX * zc;
+        const int64_t groups = (nrows + 31) / 32;
+        const unsigned grid = (unsigned)std::max<int64_t>(
+            1, std::min<int64_t>((groups + ROWS_WARPS - 1) / ROWS_WARPS, (int64_t)sms * ROWS_CTAS_PER_SM));
+        rows_kernel<<<grid, 32 * ROWS_WARPS, 0, s>>>(frames + off, A + off, Bb + off, KX, KY, zc, ca, cb);
+        cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(A + off, Bb + off, KX, KY, zc, ca, cb);
+    }
     {
         const size_t smem = (size_t)maxima_smem_floats(boxsize) * sizeof(float);
         if (smem > 48 * 1024 &&
@@ -566,6 +599,29 @@ extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *fr
                                                                       roi_stack, capacity);
     }
     return launch_err();
+}
+
+}  // namespace
+
+extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *frames, int ysize,
+                                            int xsize, int zsize, double sigma1, double sigma2,
+                                            int boxsize, float minval, int64_t capacity,
+                                            int32_t *coords, int32_t *corners, float *roi_stack,
+                                            int64_t *count, uint8_t *flags_out, void *stream)
+{
+    return find_roi(ws, nullptr, 0, frames, ysize, xsize, zsize, sigma1, sigma2, boxsize, minval, capacity,
+                    coords, corners, roi_stack, count, flags_out, (cudaStream_t)stream);
+}
+
+extern "C" bamf_status bamf_find_roi_pinned(bamf_findroi_ws *ws, const float *host_frames, float *dev_frames,
+                                            int chunk_frames, int ysize, int xsize, int zsize, double sigma1,
+                                            double sigma2, int boxsize, float minval, int64_t capacity,
+                                            int32_t *coords, int32_t *corners, float *roi_stack,
+                                            int64_t *count, uint8_t *flags_out, void *stream)
+{
+    if (!host_frames || chunk_frames < 1) return BAMF_ERR_INVALID_ARG;
+    return find_roi(ws, host_frames, chunk_frames, dev_frames, ysize, xsize, zsize, sigma1, sigma2, boxsize,
+                    minval, capacity, coords, corners, roi_stack, count, flags_out, (cudaStream_t)stream);
 }
 
 extern "C" bamf_status bamf_find_roi_host(const float *frames, int ysize, int xsize, int zsize,

@@ -32,6 +32,10 @@ def _declare():
     L.bamf_find_roi_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                        C.c_double, C.c_int, C.c_float, C.c_int64, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.bamf_find_roi_pinned.restype = C.c_int
+    L.bamf_find_roi_pinned.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, C.c_double, C.c_int, C.c_float, C.c_int64, C.c_void_p,
+                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     L.bamf_gauss_mle_device.restype = C.c_int
     L.bamf_gauss_mle_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_int, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_void_p]
@@ -198,6 +202,36 @@ class FindRoiDevice:
             out["stack"].data_ptr() if want_stack else None, out["count"].data_ptr(),
             out["flags"].data_ptr() if want_flags else None, C.c_void_p(stream) if stream else None)
         abi.check(st, "bamf_find_roi_device")
+        return out
+
+    def run_pinned(self, host_frames, ysize, xsize, zsize, sigma1=1.3, sigma2=2.6, boxsize=7, minval=None,
+                   capacity=None, stream=None, chunk_frames=250, dev_frames=None):
+        """`run` on frames in (pinned) host memory: a torch CPU tensor of
+        ysize*xsize*zsize floats, y fastest.  The frames are copied in chunks
+        whose filters start as each chunk lands; the dict adds `frames` (the
+        device copy).  Enqueued on `stream`; keep host_frames alive until it
+        has been synchronised."""
+        import torch
+        if minval is None:
+            minval = default_minval()
+        n = ysize * xsize * zsize
+        if host_frames.device.type != "cpu" or host_frames.dtype != torch.float32 or host_frames.numel() != n:
+            raise ValueError("host_frames: a CPU float32 tensor of ysize*xsize*zsize values")
+        host_frames = host_frames.contiguous()
+        cap = capacity if capacity is not None else max(1024, n // 64)
+        if dev_frames is None:
+            dev_frames = torch.empty(n, dtype=torch.float32, device="cuda")
+        out = {"coords": torch.empty((cap, 3), dtype=torch.int32, device="cuda"),
+               "corners": torch.empty((cap, 2), dtype=torch.int32, device="cuda"),
+               "count": torch.zeros(1, dtype=torch.int64, device="cuda"),
+               "stack": torch.empty((cap, boxsize * boxsize), dtype=torch.float32, device="cuda"),
+               "frames": dev_frames}
+        st = self._L.bamf_find_roi_pinned(
+            self._ws, host_frames.data_ptr(), dev_frames.data_ptr(), int(chunk_frames), ysize, xsize, zsize,
+            float(sigma1), float(sigma2), int(boxsize), float(np.float32(minval)), cap, out["coords"].data_ptr(),
+            out["corners"].data_ptr(), out["stack"].data_ptr(), out["count"].data_ptr(), None,
+            C.c_void_p(stream) if stream else None)
+        abi.check(st, "bamf_find_roi_pinned")
         return out
 
 

@@ -81,3 +81,23 @@ def test_gaussmle_matches_float_restatement_and_fp64(cuda_lib, frames):
         relc = np.abs(crlb[good] - ref["CRLB"][good]) / np.abs(ref["CRLB"][good])
         assert np.percentile(relc, 99) < 1e-3
         np.testing.assert_allclose(res["LogLikelihood"], ref["LL"], rtol=1e-3, atol=1e-2)
+
+
+@pytest.mark.parametrize("chunk", [64, 37])
+def test_findroi_from_pinned_host_in_chunks_matches_the_device_call(cuda_lib, chunk):
+    """bamf_find_roi_pinned (frames copied in chunks, each chunk's filters
+    started as it lands) gives the device call's outputs bit for bit, on a
+    300-frame stack whose row-max window bounds round from frame 256 on."""
+    import torch
+    st, _ = synth.frames(300, seed=5)
+    host = torch.from_numpy(np.asfortranarray(st).ravel(order="F")).pin_memory()
+    fr = frontend.FindRoiDevice()
+    a = fr.run(host.cuda(), 256, 256, 300, boxsize=7)
+    b = fr.run_pinned(host, 256, 256, 300, boxsize=7, chunk_frames=chunk)
+    torch.cuda.synchronize()
+    c = int(a["count"].item())
+    assert c > 0 and int(b["count"].item()) == c
+    assert torch.equal(a["coords"][:c], b["coords"][:c])
+    assert torch.equal(a["corners"][:c], b["corners"][:c])
+    assert torch.equal(a["stack"][:c], b["stack"][:c])
+    assert torch.equal(b["frames"], host.cuda())
