@@ -486,6 +486,14 @@ bamf_status launch_err()
     return cudaGetLastError() == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;
 }
 
+/* a failed runtime call: clear its error so that it is not reported again
+ * by a later call on this thread */
+bamf_status cuda_fail()
+{
+    cudaGetLastError();
+    return BAMF_ERR_CUDA;
+}
+
 }  // namespace
 
 struct bamf_findroi_ws {
@@ -547,12 +555,12 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (host_frames) {
         if (!ws->copy && cudaStreamCreateWithFlags(&ws->copy, cudaStreamNonBlocking) != cudaSuccess)
-            return BAMF_ERR_CUDA;
+            return cuda_fail();
         if (!ws->landed && cudaEventCreateWithFlags(&ws->landed, cudaEventDisableTiming) != cudaSuccess)
-            return BAMF_ERR_CUDA;
+            return cuda_fail();
         /* the copies start after the work already enqueued on s */
         if (cudaEventRecord(ws->landed, s) != cudaSuccess || cudaStreamWaitEvent(ws->copy, ws->landed, 0) != cudaSuccess)
-            return BAMF_ERR_CUDA;
+            return cuda_fail();
     }
     const int step = host_frames ? std::max(1, chunk_frames) : zsize;
     const int64_t plane = (int64_t)KX * KY;
@@ -564,7 +572,7 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
                                 cudaMemcpyHostToDevice, ws->copy) != cudaSuccess ||
                 cudaEventRecord(ws->landed, ws->copy) != cudaSuccess ||
                 cudaStreamWaitEvent(s, ws->landed, 0) != cudaSuccess)
-                return BAMF_ERR_CUDA;
+                return cuda_fail();
         }
         const int64_t nrows = (int64_t)KY * zc, ncols = (int64_t)KX * zc;
         const int64_t groups = (nrows + 31) / 32;
