@@ -34,6 +34,14 @@
 #include "sampler_common.h"
 #include "sampler_launch.h"
 
+/* a failed CUDA runtime call: clear its error so that a later call on this
+ * thread does not report it again */
+static inline bamf_status clear_cuda_error()
+{
+    cudaGetLastError();
+    return BAMF_ERR_CUDA;
+}
+
 /* defined in api_sampler.cu */
 bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcmc_params *p, int arith,
                                       const bamf_batch_results *out);
@@ -188,11 +196,11 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     if (r) return r;
     cudaStream_t s = (cudaStream_t)stream;
     /* what must start at zero: the work-queue counters */
-    if (cudaMemsetAsync(S, 0, 256, s) != cudaSuccess) return BAMF_ERR_CUDA;
+    if (cudaMemsetAsync(S, 0, 256, s) != cudaSuccess) return clear_cuda_error();
     for (int k = 0; k < 3; ++k)
         if (cudaMemcpyAsync(S + tab_off[k] + (size_t)L[k] * sizeof(float), pdf[k], (size_t)L[k] * sizeof(float),
                             cudaMemcpyHostToDevice, s) != cudaSuccess)
-            return BAMF_ERR_CUDA;
+            return clear_cuda_error();
     build_tables_kernel<<<3, 32, 0, s>>>((float *)(S + tab_off[0]), (float *)(S + tab_off[1]),
                                          (float *)(S + tab_off[2]), L[0], L[1], L[2], p->DX);
 
@@ -292,7 +300,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         int blocks = std::min((n + wpb - 1) / wpb, per_sm * sms);
         cudaError_t e = exact ? launch_rjmcmc_exact(K, Bc, Bc.side_max, blocks, wpb, s)
                               : launch_rjmcmc_fast(K, Bc, Bc.side_max, blocks, wpb, mc, s);
-        if (e != cudaSuccess) return BAMF_ERR_CUDA;
+        if (e != cudaSuccess) return clear_cuda_error();
     }
     if (want_map) {
         map_n_kernel<<<(n + 7) / 8, 256, 0, s>>>(B.nsig_trace, B.trace_cap, entries, n, out->map_n);

@@ -22,6 +22,7 @@ static thread_local std::string g_last_error;
 static bamf_status cuda_fail(cudaError_t e, const char *where)
 {
     g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+    cudaGetLastError(); /* not reported again by a later call on this thread */
     return BAMF_ERR_CUDA;
 }
 

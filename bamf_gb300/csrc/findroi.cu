@@ -475,7 +475,10 @@ struct Scratch {
         if (p) cudaFree(p);
         p = nullptr;
         n = 0;
-        if (cudaMalloc(&p, bytes) != cudaSuccess) return false;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
         n = bytes;
         return true;
     }
@@ -585,7 +588,7 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
         const size_t smem = (size_t)maxima_smem_floats(boxsize) * sizeof(float);
         if (smem > 48 * 1024 &&
             cudaFuncSetAttribute(maxima_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return BAMF_ERR_CUDA;
+            return cuda_fail();
         dim3 grid((unsigned)((KX + MAX_TW - 1) / MAX_TW), (unsigned)((KY + MAX_TH - 1) / MAX_TH),
                   (unsigned)std::min(zsize, 65535));
         /* the smallest float above the double 1e-6 */
@@ -598,7 +601,7 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
     emit_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p, ysize, xsize,
                                                   boxsize, capacity, coords, corners);
     if (cudaMemcpyAsync(count, ws->total.p, sizeof(int64_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
-        return BAMF_ERR_CUDA;
+        return cuda_fail();
     if (roi_stack) {
         int64_t work = capacity * boxsize * boxsize;
         if (work > 0)
@@ -649,13 +652,13 @@ extern "C" bamf_status bamf_find_roi_host(const float *frames, int ysize, int xs
         return BAMF_ERR_CUDA;
     if (roi_stack && !dstack.ensure(cap * boxsize * boxsize * sizeof(float))) return BAMF_ERR_CUDA;
     if (cudaMemcpy(dframes.p, frames, n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
-        return BAMF_ERR_CUDA;
+        return cuda_fail();
     bamf_status r = bamf_find_roi_device(&ws, (float *)dframes.p, ysize, xsize, zsize, sigma1, sigma2,
                                          boxsize, minval, capacity, (int32_t *)dcoords.p,
                                          (int32_t *)dcorners.p, roi_stack ? (float *)dstack.p : nullptr,
                                          (int64_t *)dcount.p, nullptr, nullptr);
     if (r) return r;
-    if (cudaDeviceSynchronize() != cudaSuccess) return BAMF_ERR_CUDA;
+    if (cudaDeviceSynchronize() != cudaSuccess) return cuda_fail();
     int64_t c = 0;
     cudaMemcpy(&c, dcount.p, sizeof c, cudaMemcpyDeviceToHost);
     *count = c;

@@ -19,6 +19,14 @@
 
 #include "bamf.h"
 
+/* a failed CUDA runtime call: clear its error so that a later call on this
+ * thread does not report it again */
+static inline bamf_status clear_cuda_error()
+{
+    cudaGetLastError();
+    return BAMF_ERR_CUDA;
+}
+
 namespace {
 
 constexpr int MAXSZ = 21;        /* IMSZBIG of definitions.h: largest fit window */
@@ -218,7 +226,7 @@ extern "C" bamf_status bamf_gauss_mle_device(const float *rois, int sz, int nfit
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(mle_xynb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
-        return BAMF_ERR_CUDA;
+        return clear_cuda_error();
     int blocks = (nfits + FITS_PER_BLOCK - 1) / FITS_PER_BLOCK;
     mle_xynb_kernel<<<blocks, FITS_PER_BLOCK, smem, (cudaStream_t)stream>>>(
         rois, psf_sigma, sz, iterations, params, crlb, loglik, nfits);

@@ -29,6 +29,14 @@
 
 #include "bamf.h"
 
+/* a failed CUDA runtime call: clear its error so that a later call on this
+ * thread does not report it again */
+static inline bamf_status clear_cuda_error()
+{
+    cudaGetLastError();
+    return BAMF_ERR_CUDA;
+}
+
 namespace {
 
 constexpr int S = BAMF_POS_SLOTS;
@@ -268,7 +276,7 @@ extern "C" bamf_status bamf_map_kmeans_device(const float *pos_trace, int pos_le
     size_t smem = (size_t)MAX_POS_LEN * S * (3 * sizeof(float) + sizeof(int));
     if (cudaFuncSetAttribute(map_kmeans_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
-        return BAMF_ERR_CUDA;
+        return clear_cuda_error();
     map_kmeans_kernel<<<n, THREADS, smem, (cudaStream_t)stream>>>(pos_trace, pos_len, pos_thin, n_entries, map_n,
                                                                   n, max_iter, out);
     return cudaGetLastError() == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;

@@ -7,6 +7,14 @@
 
 #include "bamf.h"
 
+/* a failed CUDA runtime call: clear its error so that a later call on this
+ * thread does not report it again */
+static inline bamf_status clear_cuda_error()
+{
+    cudaGetLastError();
+    return BAMF_ERR_CUDA;
+}
+
 namespace {
 
 __global__ void fma_probe(float *out, int iters, float a, float b)
@@ -41,7 +49,7 @@ extern "C" bamf_status bamf_probe_peaks(double *fp32_flops, double *mufu_ops)
     if (cudaGetDevice(&dev) != cudaSuccess) return BAMF_ERR_NO_DEVICE;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     float *out = nullptr;
-    if (cudaMalloc(&out, 65536 * sizeof(float)) != cudaSuccess) return BAMF_ERR_CUDA;
+    if (cudaMalloc(&out, 65536 * sizeof(float)) != cudaSuccess) return clear_cuda_error();
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

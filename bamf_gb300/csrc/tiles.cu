@@ -19,6 +19,14 @@
 #include "bamf.h"
 #include "bamf_tiles.h"
 
+/* a failed CUDA runtime call: clear its error so that a later call on this
+ * thread does not report it again */
+static inline bamf_status clear_cuda_error()
+{
+    cudaGetLastError();
+    return BAMF_ERR_CUDA;
+}
+
 namespace {
 
 struct Geom {
@@ -228,10 +236,10 @@ extern "C" bamf_status bamf_make_subregions_device(const float *frames, int ysiz
     if (packed == 0) {
         /* the padding of every tile is zero, as in the reference's zeros() */
         if (cudaMemsetAsync(out, 0, (size_t)n_sub * T * T * sizeof(float), (cudaStream_t)stream) != cudaSuccess)
-            return BAMF_ERR_CUDA;
+            return clear_cuda_error();
         if (out_var &&
             cudaMemsetAsync(out_var, 0, (size_t)n_sub * T * T * sizeof(float), (cudaStream_t)stream) != cudaSuccess)
-            return BAMF_ERR_CUDA;
+            return clear_cuda_error();
     }
     int64_t work = n_sub * T * T;
     subregions_kernel<<<blocks_for(work, 256), 256, 0, (cudaStream_t)stream>>>(
@@ -264,8 +272,8 @@ extern "C" bamf_status bamf_stitch_rois_device(const float *grids, int n, int ti
     cudaStream_t s = (cudaStream_t)stream;
     const int per = g.Xsub * g.Ysub;
     const int64_t nslot = (int64_t)im_z * per;
-    if (cudaMemsetAsync(scratch, 0xff, (size_t)nslot * sizeof(int32_t), s) != cudaSuccess) return BAMF_ERR_CUDA;
-    if (cudaMemsetAsync(scratch + nslot, 0, sizeof(int32_t), s) != cudaSuccess) return BAMF_ERR_CUDA;
+    if (cudaMemsetAsync(scratch, 0xff, (size_t)nslot * sizeof(int32_t), s) != cudaSuccess) return clear_cuda_error();
+    if (cudaMemsetAsync(scratch + nslot, 0, sizeof(int32_t), s) != cudaSuccess) return clear_cuda_error();
     if (n > 0)
         stitch_slots_kernel<<<blocks_for(n, 256), 256, 0, s>>>(frame_num, roi_ind, n, per, im_z, scratch,
                                                                scratch + nslot);
