@@ -96,3 +96,27 @@ def test_batch_proposal_and_trace_arguments_are_checked_before_the_gpu():
     # well-formed calls get past the checks (and stop at the missing GPU here)
     ok = call(proposal=1, trace_len=8, n_trace=tr.ctypes.data)
     assert ok in (abi.BAMF_OK, abi.BAMF_ERR_NO_DEVICE)
+
+
+def test_find_roi_pinned_rejects_bad_arguments_before_touching_the_device():
+    """bamf_find_roi_pinned: no host frames or chunk_frames < 1 is
+    BAMF_ERR_INVALID_ARG (checked on the host, no CUDA call); the Python
+    wrapper rejects a host tensor of the wrong size."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    from bamf_gb300 import abi, frontend
+    fr = frontend.FindRoiDevice()
+    L = fr._L
+    buf = np.zeros(16, np.float32)
+    out = np.zeros(3, np.int32)
+    cnt = np.zeros(1, np.int64)
+    common = (4, 4, 1, 1.3, 2.6, 7, 1.0, 1, out.ctypes.data, None, None, cnt.ctypes.data, None, None)
+    assert L.bamf_find_roi_pinned(fr._ws, None, buf.ctypes.data, 8, *common) == abi.BAMF_ERR_INVALID_ARG
+    assert L.bamf_find_roi_pinned(fr._ws, buf.ctypes.data, buf.ctypes.data, 0, *common) == \
+        abi.BAMF_ERR_INVALID_ARG
+    with pytest.raises(ValueError):
+        fr.run_pinned(torch.zeros(10), 4, 4, 1)
+    fr.close()
