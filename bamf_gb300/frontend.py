@@ -209,8 +209,8 @@ class FindRoiDevice:
         """`run` on frames in (pinned) host memory: a torch CPU tensor of
         ysize*xsize*zsize floats, y fastest.  The frames are copied in chunks
         whose filters start as each chunk lands; the dict adds `frames` (the
-        device copy).  Enqueued on `stream`; keep host_frames alive until it
-        has been synchronised."""
+        device copy) and `host_frames` (the host tensor the copies read,
+        kept referenced).  Enqueued on `stream`."""
         import torch
         if minval is None:
             minval = default_minval()
@@ -225,7 +225,8 @@ class FindRoiDevice:
                "corners": torch.empty((cap, 2), dtype=torch.int32, device="cuda"),
                "count": torch.zeros(1, dtype=torch.int64, device="cuda"),
                "stack": torch.empty((cap, boxsize * boxsize), dtype=torch.float32, device="cuda"),
-               "frames": dev_frames}
+               "frames": dev_frames,
+               "host_frames": host_frames}  # the copies read it until the stream gets there
         st = self._L.bamf_find_roi_pinned(
             self._ws, host_frames.data_ptr(), dev_frames.data_ptr(), int(chunk_frames), ysize, xsize, zsize,
             float(sigma1), float(sigma2), int(boxsize), float(np.float32(minval)), cap, out["coords"].data_ptr(),
