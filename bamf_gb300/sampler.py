@@ -201,14 +201,23 @@ def cRJMCMC(Data, E_active: dict, MCMC: abi.McmcParams, Xsize: int, Ysize: int, 
             SignalPDF, BackPDF, sCMOScorr=None, SampledPSF=None, OptModel: int = 0,
             rng=(0, 0, 0), arith: str = "exact"):
     """The MEX call of rjmcmc.m:102 / mcmc.m:142 with the same five outputs:
-    PGrid, PBack, accepted chain, proposed chain, Stat."""
-    if OptModel not in (0, None):
-        raise abi.BamfError(abi.BAMF_ERR_UNSUPPORTED, "cRJMCMC(OptModel=1)")
+    PGrid, PBack, accepted chain, proposed chain, Stat.  OptModel 0 is the
+    Gaussian model, 1 the sampled PSF `SampledPSF` (4-D, MATLAB order, its
+    shape in MCMC.PSFsize; cRJMCMC.cpp:74); other values are rejected."""
+    if OptModel is None:
+        OptModel = 0
+    if OptModel not in (0, 1):
+        raise abi.BamfError(abi.BAMF_ERR_INVALID_ARG, f"cRJMCMC(OptModel={OptModel})")
+    psf = None
+    if OptModel == 1:
+        if SampledPSF is None:
+            raise abi.BamfError(abi.BAMF_ERR_INVALID_ARG, "cRJMCMC(OptModel=1) needs SampledPSF")
+        psf = np.asarray(SampledPSF, np.float32)
     data = np.asarray(Data, np.float32)[:Ysize, :Xsize]
     e0 = (np.asarray(E_active.get("I", []), np.float32), np.asarray(E_active.get("X", []), np.float32),
           np.asarray(E_active.get("Y", []), np.float32), float(E_active["BG"]))
     raw = crjmcmc_raw(data, MCMC, OffSetPDF, SignalPDF, BackPDF, e0=e0, rng=rng, scmos=sCMOScorr,
-                      arith=arith)
+                      arith=arith, sampled_psf=psf)
     acc = mex_chain(raw["chain"])
     prop = mex_chain(raw["chain_test"], accepted=raw["chain"])
     return raw["pgrid"], raw["pback"], acc, prop, mex_stat(raw["counters"], MCMC)

@@ -120,3 +120,18 @@ def test_find_roi_pinned_rejects_bad_arguments_before_touching_the_device():
     with pytest.raises(ValueError):
         fr.run_pinned(torch.zeros(10), 4, 4, 1)
     fr.close()
+
+
+def test_crjmcmc_mirror_checks_the_model_option_on_the_host():
+    """sampler.cRJMCMC (the MEX call, cRJMCMC.cpp:74): OptModel 0 or 1 only,
+    and OptModel 1 needs a SampledPSF; both refused before any GPU call."""
+    import numpy as np
+
+    from bamf_gb300 import abi, sampler
+    p = abi.McmcParams()
+    E = {"N": 0, "I": [], "X": [], "Y": [], "BG": 10.0}
+    pdf = np.ones(8, np.float32)
+    with pytest.raises(abi.BamfError):
+        sampler.cRJMCMC(np.zeros((8, 8), np.float32), E, p, 8, 8, pdf, pdf, pdf, OptModel=2)
+    with pytest.raises(abi.BamfError):
+        sampler.cRJMCMC(np.zeros((8, 8), np.float32), E, p, 8, 8, pdf, pdf, pdf, OptModel=1)
