@@ -325,7 +325,7 @@ def run_reference(a, rank, world):
         return
     b, rj, p, bg0 = workload(a.n_rois, 2, a.jumps)
     threads = os.cpu_count() or 1
-    n = a.cpu_sample or max(threads * 8, 64)
+    n = a.cpu_sample or max(threads * 24, 96)  # ~1 s per step on 16 Grace cores
     for _ in range(a.warmup):
         cpu_sample_rate(b, rj, p, bg0, min(n, 32), threads)
     rates, secs = [], []
@@ -483,7 +483,7 @@ def main():
     cpu = None
     if rank == 0:
         threads = os.cpu_count() or 1
-        ns = a.cpu_sample or max(threads * 6, 48)
+        ns = a.cpu_sample or max(threads * 24, 96)  # ~20 thread-seconds of CPU work
         rate, secs = cpu_sample_rate(b, rj, p, bg0, ns, threads)
         cpu = {"value": rate, "unit": "ROIs/s", "cores": threads, "kind": "port",
                "sample": f"first {ns} ROIs of the workload, {secs:.1f} s on {threads} host threads; "
