@@ -4,13 +4,11 @@
  * bamf_rjmcmc_batch_device needs device scratch (work-queue counters, the
  * size-class ordering of the ROIs, the prior tables, one byte per chain step
  * per ROI for the MAP count) and takes it from a bamf_workspace that grows
- * with cudaMalloc.  Some callers cannot do that: code that records the call
- * into a CUDA graph (cudaMalloc is not allowed while a stream is being
- * captured), hosts that hand all device memory out through their own pool
- * (MATLAB's gpuArray allocator, a framework's caching allocator) and must not
- * see the driver's free memory change underneath them, and latency-sensitive
- * loops that cannot afford the device-wide synchronisation cudaMalloc and
- * cudaFree imply.  bamf_rjmcmc_batch_device_noalloc serves them: its scratch
+ * with cudaMalloc.  Some callers cannot do that: hosts that hand all device
+ * memory out through their own pool (MATLAB's gpuArray allocator, a
+ * framework's caching allocator) and must not see the driver's free memory
+ * change underneath them, and latency-sensitive loops that cannot afford the
+ * device-wide synchronisation cudaMalloc and cudaFree imply.  bamf_rjmcmc_batch_device_noalloc serves them: its scratch
  * is the fixed array below, which the CUDA runtime reserves on every device
  * when the library's device code is loaded there and keeps until the process
  * exits.
@@ -252,6 +250,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     B.status = out->status;
     B.overflow = out->overflow;
     B.llr_evals = out->llr_evals;
+    B.model_drift = arith == BAMF_ARITH_FAST ? out->model_drift : nullptr;
     B.order = (int32_t *)(S + off_order);
     B.class_range = (int32_t *)(S + 256);
     order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)B.order, (int32_t *)B.class_range);

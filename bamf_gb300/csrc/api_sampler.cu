@@ -500,6 +500,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
     B.status = out->status;
     B.overflow = out->overflow;
     B.llr_evals = out->llr_evals;
+    B.model_drift = arith == BAMF_ARITH_FAST ? out->model_drift : nullptr;
     B.birth_cdf = rois->birth_cdf;
     B.birth_sub = rois->birth_sub;
     B.sampled_psf = rois->opt_model == 1 ? rois->sampled_psf : nullptr;
@@ -835,6 +836,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if (out->status && (r = dalloc(o.v, &dout.status, n))) return r;
     if (out->overflow && (r = dalloc(o.v, &dout.overflow, n))) return r;
     if (out->llr_evals && (r = dalloc(o.v, &dout.llr_evals, n))) return r;
+    if (out->model_drift && (r = dalloc(o.v, &dout.model_drift, n))) return r;
     const size_t tl = out->trace_len > 0 ? (size_t)out->trace_len : 0;
     dout.trace_len = out->trace_len;
     if (out->n_trace && tl && (r = dalloc(o.v, &dout.n_trace, (size_t)n * tl))) return r;
@@ -849,6 +851,8 @@ extern "C" bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi
     if ((r = download(out->status, dout.status, n))) return r;
     if ((r = download(out->overflow, dout.overflow, n))) return r;
     if ((r = download(out->llr_evals, dout.llr_evals, n))) return r;
+    if (arith == BAMF_ARITH_FAST && (r = download(out->model_drift, dout.model_drift, n))) return r;
+    if (arith != BAMF_ARITH_FAST && out->model_drift) std::memset(out->model_drift, 0, sizeof(float) * (size_t)n);
     if ((r = download(out->n_trace, dout.n_trace, (size_t)n * tl))) return r;
     if ((r = download(out->x_trace, dout.x_trace, (size_t)n * tl))) return r;
     return BAMF_OK;
@@ -986,6 +990,196 @@ extern "C" bamf_status bamf_crjmcmc_host_model(const float *data, int xsize, int
                 return r;
             h->n_entries = ne;
             h->n_records = got[w].n_records;
+        }
+    }
+    return BAMF_OK;
+}
+
+/* Many cRJMCMC calls as one launch: the ROIs of the batch share the MCMC
+ * struct and the priors, each keeps its own start state, uniform stream and
+ * full MEX outputs.  One persistent launch over all ROIs (no size-class
+ * split: the launch is sized for the largest side). */
+extern "C" bamf_status bamf_crjmcmc_batch_host(int n_rois, const float *data, const int64_t *offsets,
+                                               const int32_t *xsize, const int32_t *ysize,
+                                               const bamf_emitters *e0, const bamf_mcmc_params *p,
+                                               const bamf_priors *priors, const float *scmos, uint32_t seed,
+                                               const uint32_t *chain_id, const uint32_t *rng_offset, int arith,
+                                               float *pgrids, float *pbacks, bamf_chain *chains,
+                                               bamf_counters *counters, uint32_t *uniforms_used,
+                                               int32_t *status)
+{
+    if (n_rois < 0 || !p || !priors || !status) return BAMF_ERR_INVALID_ARG;
+    if (n_rois == 0) return BAMF_OK;
+    if (!data || !offsets || !xsize || !ysize || !e0) return BAMF_ERR_INVALID_ARG;
+    if (arith != BAMF_ARITH_EXACT && arith != BAMF_ARITH_FAST) return BAMF_ERR_INVALID_ARG;
+    if ((pgrids == nullptr) != (pbacks == nullptr)) return BAMF_ERR_INVALID_ARG;
+    if (p->N_Burnin < 0 || p->N_Trials < 0 || p->Grid_Zoom < 0) return BAMF_ERR_INVALID_ARG;
+    if (pgrids && p->Grid_Zoom < 1) return BAMF_ERR_INVALID_ARG;
+    const int n = n_rois;
+    int64_t npix = 0, gmax = 0;
+    int side_max = 0;
+    const int64_t zz = (int64_t)p->Grid_Zoom * p->Grid_Zoom;
+    for (int k = 0; k < n; ++k) {
+        if (xsize[k] < 1 || ysize[k] < 1 || offsets[k] < 0) return BAMF_ERR_INVALID_ARG;
+        if (e0[k].N < 0 || (e0[k].N > 0 && (!e0[k].I || !e0[k].X || !e0[k].Y))) return BAMF_ERR_INVALID_ARG;
+        if (e0[k].N > BAMF_NMAX) return BAMF_ERR_TOO_LARGE;
+        if (chains && (chains[2 * k].capacity_entries < 0 || chains[2 * k].capacity_records < 0 ||
+                       chains[2 * k + 1].capacity_entries < 0 || chains[2 * k + 1].capacity_records < 0))
+            return BAMF_ERR_INVALID_ARG;
+        npix = std::max<int64_t>(npix, offsets[k] + (int64_t)xsize[k] * ysize[k]);
+        gmax = std::max<int64_t>(gmax, (int64_t)xsize[k] * ysize[k] * zz);
+        side_max = std::max(side_max, (int)std::max(xsize[k], ysize[k]));
+    }
+    if (side_max > BAMF_MAX_ROI_SIDE) return BAMF_ERR_TOO_LARGE;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+
+    bamf_workspace ws;
+    SamplerConsts K;
+    bamf_status r = make_consts(&ws, p, priors, seed, 0.0f, K, nullptr);
+    if (r) return r;
+    Owned o;
+    SamplerBatch B;
+    std::memset(&B, 0, sizeof B);
+    B.n_rois = n;
+    B.side_max = side_max;
+    B.n_psf = 1;
+    if ((r = upload(o, (float **)&B.data, data, (size_t)npix))) return r;
+    if ((r = upload(o, (int64_t **)&B.offsets, offsets, (size_t)n))) return r;
+    if ((r = upload(o, (int32_t **)&B.xsize, xsize, (size_t)n))) return r;
+    if ((r = upload(o, (int32_t **)&B.ysize, ysize, (size_t)n))) return r;
+    if ((r = upload(o, (float **)&B.scmos, scmos, (size_t)npix))) return r;
+    std::vector<int32_t> n0(n);
+    std::vector<float> bg(n), ixy((size_t)n * 3 * BAMF_NMAX, 0.0f);
+    std::vector<uint32_t> cid(n), roff(n);
+    for (int k = 0; k < n; ++k) {
+        n0[k] = e0[k].N;
+        bg[k] = e0[k].BG;
+        float *row = &ixy[(size_t)k * 3 * BAMF_NMAX];
+        for (int j = 0; j < e0[k].N; ++j) {
+            row[j] = e0[k].I[j];
+            row[BAMF_NMAX + j] = e0[k].X[j];
+            row[2 * BAMF_NMAX + j] = e0[k].Y[j];
+        }
+        cid[k] = chain_id ? chain_id[k] : (uint32_t)k;
+        roff[k] = rng_offset ? rng_offset[k] : 0u;
+    }
+    if ((r = upload(o, (int32_t **)&B.init_n, n0.data(), (size_t)n))) return r;
+    if ((r = upload(o, (float **)&B.init_bg, bg.data(), (size_t)n))) return r;
+    if ((r = upload(o, (float **)&B.init_ixy, ixy.data(), ixy.size()))) return r;
+    if ((r = upload(o, (uint32_t **)&B.chain_ids, cid.data(), (size_t)n))) return r;
+    if ((r = upload(o, (uint32_t **)&B.rng_offset, roff.data(), (size_t)n))) return r;
+    int32_t *d_counters = nullptr, *d_status = nullptr, *d_entries = nullptr;
+    uint32_t *d_unif = nullptr;
+    if ((r = dalloc(o.v, &d_counters, (size_t)n * 30))) return r;
+    if ((r = dalloc(o.v, &d_status, (size_t)n))) return r;
+    if ((r = dalloc(o.v, &d_entries, (size_t)n))) return r;
+    if ((r = dalloc(o.v, &d_unif, (size_t)n))) return r;
+    B.counters = d_counters;
+    B.status = d_status;
+    B.n_entries = d_entries;
+    B.uniforms_used = d_unif;
+    if (pgrids) {
+        if ((r = dalloc(o.v, &B.pgrid, (size_t)(n * gmax)))) return r;
+        if ((r = dalloc(o.v, &B.pback, (size_t)(n * gmax)))) return r;
+        CU(cudaMemset(B.pgrid, 0, (size_t)(n * gmax) * sizeof(float)));
+        CU(cudaMemset(B.pback, 0, (size_t)(n * gmax) * sizeof(float)));
+        B.grid_stride = gmax;
+    }
+    /* every chain field of all ROIs in one device buffer per field, ROI k's
+     * arrays at the running sum of the capacities before it */
+    std::vector<bamf_chain> dch;
+    std::vector<int64_t> ebase(2 * (size_t)n + 1, 0), rbase(2 * (size_t)n + 1, 0);
+    bamf_chain all;
+    std::memset(&all, 0, sizeof all);
+    if (chains) {
+        for (int i = 0; i < 2 * n; ++i) {
+            ebase[i + 1] = ebase[i] + chains[i].capacity_entries;
+            rbase[i + 1] = rbase[i] + chains[i].capacity_records;
+        }
+        const size_t ce = (size_t)std::max<int64_t>(ebase[2 * n], 1), cr = (size_t)std::max<int64_t>(rbase[2 * n], 1);
+        if ((r = dalloc(o.v, &all.N, ce)) || (r = dalloc(o.v, &all.LLR, ce)) || (r = dalloc(o.v, &all.PR, ce)) ||
+            (r = dalloc(o.v, &all.JumpType, ce)) || (r = dalloc(o.v, &all.Accepted, ce)) ||
+            (r = dalloc(o.v, &all.BG, ce)) || (r = dalloc(o.v, &all.ABG, ce)) || (r = dalloc(o.v, &all.BBG, ce)) ||
+            (r = dalloc(o.v, &all.Index, cr)) || (r = dalloc(o.v, &all.Photons, cr)) || (r = dalloc(o.v, &all.X, cr)) ||
+            (r = dalloc(o.v, &all.Y, cr)) || (r = dalloc(o.v, &all.Signal, cr)))
+            return r;
+        dch.resize(2 * (size_t)n);
+        for (int i = 0; i < 2 * n; ++i) {
+            bamf_chain &c = dch[i];
+            std::memset(&c, 0, sizeof c);
+            c.capacity_entries = chains[i].capacity_entries;
+            c.capacity_records = chains[i].capacity_records;
+            const int64_t e = ebase[i], q = rbase[i];
+            c.N = all.N + e; c.LLR = all.LLR + e; c.PR = all.PR + e; c.JumpType = all.JumpType + e;
+            c.Accepted = all.Accepted + e; c.BG = all.BG + e; c.ABG = all.ABG + e; c.BBG = all.BBG + e;
+            c.Index = all.Index + q; c.Photons = all.Photons + q; c.X = all.X + q; c.Y = all.Y + q;
+            c.Signal = all.Signal + q;
+        }
+        bamf_chain *d = nullptr;
+        if ((r = upload(o, &d, dch.data(), dch.size()))) return r;
+        B.chains = d;
+    }
+    if ((r = launch_batch(&ws, K, B, arith, nullptr))) return r;
+    CU(cudaDeviceSynchronize());
+    if ((r = download(status, d_status, (size_t)n))) return r;
+    std::vector<int32_t> ne(n);
+    if ((r = download(ne.data(), d_entries, (size_t)n))) return r;
+    if (counters && (r = download((int32_t *)counters, d_counters, (size_t)n * 30))) return r;
+    if (uniforms_used && (r = download(uniforms_used, d_unif, (size_t)n))) return r;
+    if (pgrids) {
+        std::vector<float> g((size_t)(n * gmax));
+        for (int w = 0; w < 2; ++w) {
+            if ((r = download(g.data(), w ? B.pback : B.pgrid, g.size()))) return r;
+            float *dst = w ? pbacks : pgrids;
+            for (int k = 0; k < n; ++k)
+                std::memcpy(dst + offsets[k] * zz, g.data() + k * gmax,
+                            sizeof(float) * (size_t)((int64_t)xsize[k] * ysize[k] * zz));
+        }
+    }
+    if (chains) {
+        std::vector<bamf_chain> got(2 * (size_t)n);
+        CU(cudaMemcpy(got.data(), B.chains, got.size() * sizeof(bamf_chain), cudaMemcpyDeviceToHost));
+        const size_t ce = (size_t)ebase[2 * n], cr = (size_t)rbase[2 * n];
+        std::vector<int32_t> hi(std::max(ce, cr));
+        std::vector<float> hf(std::max(ce, cr));
+        /* one download per field, then each ROI's part into its own arrays */
+        auto scatter_i = [&](int32_t *bamf_chain::*f, const std::vector<int64_t> &base, bool rec) -> bamf_status {
+            bamf_status rr = download(hi.data(), all.*f, rec ? cr : ce);
+            if (rr) return rr;
+            for (int i = 0; i < 2 * n; ++i) {
+                if (status[i / 2] != BAMF_OK) continue;
+                const int32_t cnt = rec ? got[i].n_records : std::min(ne[i / 2], chains[i].capacity_entries);
+                if (cnt > 0) std::memcpy(chains[i].*f, hi.data() + base[i], sizeof(int32_t) * (size_t)cnt);
+            }
+            return BAMF_OK;
+        };
+        auto scatter_f = [&](float *bamf_chain::*f, const std::vector<int64_t> &base, bool rec) -> bamf_status {
+            bamf_status rr = download(hf.data(), all.*f, rec ? cr : ce);
+            if (rr) return rr;
+            for (int i = 0; i < 2 * n; ++i) {
+                if (status[i / 2] != BAMF_OK) continue;
+                const int32_t cnt = rec ? got[i].n_records : std::min(ne[i / 2], chains[i].capacity_entries);
+                if (cnt > 0) std::memcpy(chains[i].*f, hf.data() + base[i], sizeof(float) * (size_t)cnt);
+            }
+            return BAMF_OK;
+        };
+        for (int i = 0; i < 2 * n; ++i) {
+            if (status[i / 2] != BAMF_OK) continue;
+            if (ne[i / 2] > chains[i].capacity_entries || got[i].n_records > chains[i].capacity_records)
+                status[i / 2] = BAMF_ERR_CAPACITY;
+        }
+        if ((r = scatter_i(&bamf_chain::N, ebase, false)) || (r = scatter_f(&bamf_chain::LLR, ebase, false)) ||
+            (r = scatter_f(&bamf_chain::PR, ebase, false)) || (r = scatter_i(&bamf_chain::JumpType, ebase, false)) ||
+            (r = scatter_i(&bamf_chain::Accepted, ebase, false)) || (r = scatter_f(&bamf_chain::BG, ebase, false)) ||
+            (r = scatter_f(&bamf_chain::ABG, ebase, false)) || (r = scatter_f(&bamf_chain::BBG, ebase, false)) ||
+            (r = scatter_i(&bamf_chain::Index, rbase, true)) || (r = scatter_f(&bamf_chain::Photons, rbase, true)) ||
+            (r = scatter_f(&bamf_chain::X, rbase, true)) || (r = scatter_f(&bamf_chain::Y, rbase, true)) ||
+            (r = scatter_i(&bamf_chain::Signal, rbase, true)))
+            return r;
+        for (int i = 0; i < 2 * n; ++i) {
+            if (status[i / 2] != BAMF_OK) continue;
+            chains[i].n_entries = ne[i / 2];
+            chains[i].n_records = got[i].n_records;
         }
     }
     return BAMF_OK;

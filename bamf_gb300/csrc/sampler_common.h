@@ -72,6 +72,7 @@ struct SamplerBatch {
     int32_t *status;              /* [roi] 0 ok, else BAMF_ERR_*           */
     int32_t *overflow;            /* [roi] proposals rejected at BAMF_NMAX */
     int32_t *llr_evals;           /* [roi] likelihood-ratio evaluations     */
+    float *model_drift;           /* [roi] largest relative model drift at the periodic rebuilds (fast) */
     float *pgrid;                 /* [slot][grid_stride] or null           */
     float *pback;
     int64_t grid_stride;

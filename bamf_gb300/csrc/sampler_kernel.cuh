@@ -1007,9 +1007,26 @@ struct ChainWarp {
             if constexpr (NUM) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
             else model_full(an, aI, aX, aY, aBG, aABG, aBBG, M, NX, NY);
         } else {
-            if constexpr (NUM) model_num(an, aI, aX, aY, aBG, aABG, aBBG, M);
-            else model_stream(an, aI, aX, aY, aBG, aABG, aBBG, M);
+            /* with a drift output, a periodic rebuild goes to Mt (free
+             * between proposals) first, to measure how far the incrementally
+             * updated M has moved from the model of its state */
+            const bool chk = B->model_drift != nullptr && entries > 0;
+            float *dst = chk ? Mt : M;
+            if constexpr (NUM) model_num(an, aI, aX, aY, aBG, aABG, aBBG, dst);
+            else model_stream(an, aI, aX, aY, aBG, aABG, aBBG, dst);
             __syncwarp();
+            if (chk) {
+                float d = 0.0f;
+                for (int p = lane; p < npix; p += 32) {
+                    const float m = Mt[p];
+                    d = fmaxf(d, fabsf(M[p] - m) / m);
+                    M[p] = m;
+                }
+                for (int o = 16; o > 0; o >>= 1) d = fmaxf(d, __shfl_xor_sync(BAMF_FULL, d, o));
+                /* non-negative floats order like their bit patterns */
+                if (lane == 0) atomicMax((int *)&B->model_drift[roi], __float_as_int(d));
+                __syncwarp();
+            }
         }
     }
 
@@ -2059,6 +2076,7 @@ __device__ __forceinline__ bool begin_roi(ChainWarp<EXACT, NUM> &w, const Sample
     w.use_shared_ub = false;
     w.shared_ub = 0.0f;
     w.rec_n[0] = w.rec_n[1] = 0;
+    if (!EXACT && Bt.model_drift && lane == 0) Bt.model_drift[roi] = 0.0f;
     __syncwarp();
     w.rebuild_model();
     return true;

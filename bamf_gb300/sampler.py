@@ -36,6 +36,11 @@ def _declare() -> C.CDLL:
         pf, C.c_int, C.c_int, C.POINTER(abi.Emitters), C.POINTER(abi.McmcParams),
         pf, C.c_int, pf, C.c_int, pf, C.c_int, pf, pf, C.c_int, C.POINTER(abi.Rng), C.c_int,
         pf, pf, C.POINTER(abi.Chain), C.POINTER(abi.Chain), C.POINTER(abi.Counters)]
+    L.bamf_crjmcmc_batch_host.restype = C.c_int
+    L.bamf_crjmcmc_batch_host.argtypes = [
+        C.c_int, pf, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(abi.Emitters), C.POINTER(abi.McmcParams),
+        C.c_void_p, pf, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int, pf, pf, C.POINTER(abi.Chain),
+        C.POINTER(abi.Counters), C.c_void_p, C.c_void_p]
     L.bamf_workspace_create.restype = C.c_int
     L.bamf_workspace_create.argtypes = [C.POINTER(C.c_void_p)]
     L.bamf_workspace_destroy.argtypes = [C.c_void_p]
@@ -88,7 +93,8 @@ class BatchResults(C.Structure):
                 ("overflow", C.c_void_p), ("llr_evals", C.c_void_p), ("trace_len", C.c_int32),
                 ("n_trace", C.c_void_p), ("x_trace", C.c_void_p), ("pgrid", C.c_void_p), ("pback", C.c_void_p),
                 ("grid_stride", C.c_int64), ("grid_ld", C.c_int32), ("grid_slot", C.c_void_p),
-                ("pos_trace", C.c_void_p), ("pos_len", C.c_int32), ("pos_thin", C.c_int32)]
+                ("pos_trace", C.c_void_p), ("pos_len", C.c_int32), ("pos_thin", C.c_int32),
+                ("model_drift", C.c_void_p)]
 
 POS_SLOTS = 32
 POS_RECORD = 5 + 3 * POS_SLOTS
@@ -149,6 +155,77 @@ def crjmcmc_raw(roi: np.ndarray, params: abi.McmcParams, off, sig, back, e0=None
     if grids:
         out["pgrid"] = pg.reshape(xsize * Z, ysize * Z).T.copy()
         out["pback"] = pb.reshape(xsize * Z, ysize * Z).T.copy()
+    return out
+
+
+def crjmcmc_batch_raw(rois: list, params: abi.McmcParams, off, sig, back, e0s=None, seed: int = 0,
+                      chain_ids=None, rng_offsets=None, arith: str = "exact", record: bool = True,
+                      grids: bool = True, records_per_entry: int = 12) -> list[dict]:
+    """Many cRJMCMC calls in one launch (bamf_crjmcmc_batch_host): ROI k is
+    rois[k] (Ysize, Xsize), start state e0s[k] = (I, X, Y, BG), stream
+    (seed, chain_ids[k], rng_offsets[k]).  Returns one dict per ROI like
+    crjmcmc_raw (plus "uniforms_used").  Chains are given
+    records_per_entry records per entry of room; a ROI that needs more is
+    run again alone with room for BAMF_NMAX (the same stream gives the same
+    chain)."""
+    L = _declare()
+    n = len(rois)
+    if n == 0:
+        return []
+    xs = np.array([r.shape[1] for r in rois], np.int32)
+    ys = np.array([r.shape[0] for r in rois], np.int32)
+    sizes = xs.astype(np.int64) * ys
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    data = np.ascontiguousarray(np.concatenate([np.asarray(r, np.float32).ravel(order="F") for r in rois]))
+    keep = []
+    ems = (abi.Emitters * n)()
+    for k in range(n):
+        I, X, Y, BG = e0s[k] if e0s is not None else ([], [], [], 0.0)
+        e, kp = abi.make_emitters(len(I), I, X, Y, BG)
+        ems[k] = e
+        keep.append(kp)
+    pr, arrs = Sampler._priors(off, sig, back)
+    cid = None if chain_ids is None else np.ascontiguousarray(chain_ids, np.uint32)
+    rof = None if rng_offsets is None else np.ascontiguousarray(rng_offsets, np.uint32)
+    steps = int(params.N_Burnin) + int(params.N_Trials)
+    chains = None
+    if record:
+        bufs = [abi.alloc_chain(steps + 1, (steps + 1) * records_per_entry) for _ in range(2 * n)]
+        chains = (abi.Chain * (2 * n))(*[b[0] for b in bufs])
+    Z = int(params.Grid_Zoom)
+    pg = np.zeros(int(sizes.sum()) * Z * Z, np.float32) if grids else None
+    pb = np.zeros(int(sizes.sum()) * Z * Z, np.float32) if grids else None
+    cnt = (abi.Counters * n)()
+    unif = np.zeros(n, np.uint32)
+    status = np.zeros(n, np.int32)
+    st = L.bamf_crjmcmc_batch_host(
+        n, abi.fptr(data), offs.ctypes.data, xs.ctypes.data, ys.ctypes.data, ems, C.byref(params), C.byref(pr),
+        None, seed, cid.ctypes.data if cid is not None else None, rof.ctypes.data if rof is not None else None,
+        ARITH[arith], abi.fptr(pg) if grids else None, abi.fptr(pb) if grids else None, chains, cnt,
+        unif.ctypes.data, status.ctypes.data)
+    _check(L, st, "bamf_crjmcmc_batch_host")
+    out = []
+    for k in range(n):
+        if status[k] == abi.BAMF_ERR_CAPACITY and record:
+            I, X, Y, BG = e0s[k] if e0s is not None else ([], [], [], 0.0)
+            one = crjmcmc_batch_raw([rois[k]], params, off, sig, back, e0s=[(I, X, Y, BG)], seed=seed,
+                                    chain_ids=[int(cid[k]) if cid is not None else k],
+                                    rng_offsets=[int(rof[k]) if rof is not None else 0], arith=arith,
+                                    record=True, grids=grids, records_per_entry=abi.BAMF_NMAX)
+            out.append(one[0])
+            continue
+        if status[k] != abi.BAMF_OK:
+            raise abi.BamfError(int(status[k]), f"bamf_crjmcmc_batch_host: ROI {k}")
+        d = {"counters": cnt[k].as_dict(), "uniforms_used": int(unif[k])}
+        if record:
+            d["chain"] = abi.chain_to_dict(chains[2 * k], bufs[2 * k][1])
+            d["chain_test"] = abi.chain_to_dict(chains[2 * k + 1], bufs[2 * k + 1][1])
+        if grids:
+            g0 = int(offs[k]) * Z * Z
+            gz = int(sizes[k]) * Z * Z
+            d["pgrid"] = pg[g0:g0 + gz].reshape(int(xs[k]) * Z, int(ys[k]) * Z).T.copy()
+            d["pback"] = pb[g0:g0 + gz].reshape(int(xs[k]) * Z, int(ys[k]) * Z).T.copy()
+        out.append(d)
     return out
 
 
@@ -339,7 +416,7 @@ class Sampler:
         res = BatchResults()
         outs = outs or {}
         for k in ("map_n", "final_n", "final_state", "counters", "n_entries", "status", "overflow",
-                  "llr_evals", "n_trace", "x_trace"):
+                  "llr_evals", "n_trace", "x_trace", "model_drift"):
             t = outs.get(k)
             setattr(res, k, t.data_ptr() if t is not None else None)
         for k in ("pgrid", "pback", "grid_slot", "pos_trace"):
@@ -388,10 +465,12 @@ class Sampler:
     def run_host(self, batch, params: abi.McmcParams, off, sig, back, seed: int,
                  arith: str = "fast", bg0: float = 0.0, init=None, proposal: str = "reference",
                  birth=None, trace_len: int = 0, sampled_psf: np.ndarray | None = None,
-                 psf_slot: np.ndarray | None = None) -> dict:
+                 psf_slot: np.ndarray | None = None, model_drift: bool = False) -> dict:
         """batch: synth.RoiBatch (host numpy); returns numpy results.
         birth: (cdf, sub) host arrays of the LEARNED proposal; trace_len > 0
-        adds the n_trace / x_trace outputs; sampled_psf: a 4-D array of shape
+        adds the n_trace / x_trace outputs; model_drift adds the per-ROI
+        largest relative drift of the incremental model (fast arithmetic);
+        sampled_psf: a 4-D array of shape
         params.PSFsize, or a stack (n_psf, *PSFsize) with psf_slot[k] naming
         ROI k's, selects the sampled-PSF model (OptModel 1)."""
         pr, keep = self._priors(off, sig, back)
@@ -428,6 +507,8 @@ class Sampler:
         if trace_len > 0:
             outs["n_trace"] = np.zeros((n, trace_len), np.uint8)
             outs["x_trace"] = np.zeros((n, trace_len), np.float32)
+        if model_drift:
+            outs["model_drift"] = np.zeros(n, np.float32)
         res = BatchResults()
         for k, a in outs.items():
             setattr(res, k, a.ctypes.data)

@@ -226,6 +226,35 @@ typedef struct bamf_priors {
 } bamf_priors;
 
 /*
+ * Many cRJMCMC calls in one launch: the per-ROI loop of analyzeROIs.m:126-159
+ * (each iteration rjmcmc.m:102 -> MEX cRJMCMC, cRJMCMC.cpp:52-308) with the
+ * full per-call outputs of bamf_crjmcmc_host for every ROI.  Host buffers,
+ * synchronous; Gaussian PSF (OptModel 0).
+ *   n_rois, data, offsets, xsize, ysize   ROI k at data[offsets[k]], y fastest
+ *   e0          [n_rois] start states (prhs[1] of each call)
+ *   p, priors   shared by all ROIs (prhs[2], prhs[5..7])
+ *   scmos       laid out like data, or NULL (zeros)
+ *   seed, chain_id[k] (NULL: k), rng_offset[k] (NULL: 0)  ROI k's uniform
+ *               stream, as bamf_rng {seed, chain_id, offset}
+ *   pgrids, pbacks  ROI k's (Ysize*Zoom)*(Xsize*Zoom) grid at
+ *               Zoom*Zoom*offsets[k]; may be NULL together
+ *   chains      [n_rois][2] (Chain, Chain_Test) with the caller's capacities,
+ *               or NULL
+ *   counters    [n_rois] or NULL;  uniforms_used [n_rois] uniforms each
+ *               chain drew, or NULL
+ *   status      [n_rois]: BAMF_OK, or that ROI's error (BAMF_ERR_CAPACITY
+ *               when its chain arrays were too small; its outputs are then
+ *               not written)
+ * Errors of the call itself as bamf_crjmcmc_host.
+ */
+bamf_status bamf_crjmcmc_batch_host(int n_rois, const float *data, const int64_t *offsets,
+                                    const int32_t *xsize, const int32_t *ysize, const bamf_emitters *e0,
+                                    const bamf_mcmc_params *p, const bamf_priors *priors, const float *scmos,
+                                    uint32_t seed, const uint32_t *chain_id, const uint32_t *rng_offset,
+                                    int arith, float *pgrids, float *pbacks, bamf_chain *chains,
+                                    bamf_counters *counters, uint32_t *uniforms_used, int32_t *status);
+
+/*
  * A batch of independent ROIs of possibly different sizes, packed back to
  * back (the per-ROI calls of analyzeROIs.m:126-159 as one launch).
  * ROI k occupies data[offsets[k] .. offsets[k] + ysize[k]*xsize[k]), y fastest.
@@ -334,7 +363,13 @@ typedef struct bamf_roi_batch {
  *                index, Signal==1 count, BG, ABG, BBG, then X, Y, I of up
  *                to BAMF_POS_SLOTS Signal==1 emitters in slot order (NaN
  *                past the count); the input of bamf_map_kmeans_device and
- *                bamf_refine_stats_device (findMap.m, mcmc.m) */
+ *                bamf_refine_stats_device (findMap.m, mcmc.m)
+ *   model_drift  [k] fast arithmetic only: the largest relative difference
+ *                max_p |M_p - M'_p| / M'_p between the incrementally
+ *                updated model image M and the model M' rebuilt from the
+ *                chain's state, over the periodic rebuilds (every 512
+ *                jumps); 0 when the chain had none.  No counterpart in the
+ *                reference, which rebuilds the model for every proposal. */
 typedef struct bamf_batch_results {
     int32_t *map_n;
     int32_t *final_n;
@@ -355,6 +390,7 @@ typedef struct bamf_batch_results {
     float *pos_trace;
     int32_t pos_len;
     int32_t pos_thin;
+    float *model_drift;
 } bamf_batch_results;
 
 #define BAMF_POS_SLOTS 32
@@ -398,32 +434,6 @@ bamf_status bamf_rjmcmc_batch_host(bamf_workspace *ws, const bamf_roi_batch *roi
                                    const bamf_mcmc_params *p, const bamf_priors *priors,
                                    uint32_t seed, int arith, const bamf_batch_results *out);
 
-/*
- * Allocation-free variant of bamf_rjmcmc_batch_device.  It has no
- * counterpart in the reference (which is a single-ROI CPU sampler); it is
- * for callers that must not allocate device memory: code recorded into a
- * CUDA graph (no cudaMalloc during stream capture), hosts whose own pool
- * owns the device memory (MATLAB's gpuArray allocator, a framework's caching
- * allocator), loops that cannot take the device-wide synchronisation of
- * cudaMalloc/cudaFree.  Same arguments and results as
- * bamf_rjmcmc_batch_device minus the workspace; it calls no cudaMalloc,
- * cudaFree or other allocating routine.
- *
- * Its scratch is one fixed array of BAMF_NOALLOC_SCRATCH_BYTES compiled into
- * the library: every GPU that loads the library holds it until the process
- * exits, and every call shares it.  A call needs
- *   512 + sum over the 3 priors of 16*len (each rounded up to 256)
- *   + 4*n_rois (rounded up to 256)
- *   + [map_n wanted] n_rois*(N_Burnin+N_Trials) (+ 4*n_rois if n_entries is NULL)
- * bytes; a call needing more returns BAMF_ERR_TOO_LARGE before any GPU work
- * (split the batch).  The first call on each device looks up the array's
- * device address with that device current; make that first call before any
- * stream capture begins.  Calls that overlap on the GPU (different streams,
- * or different host threads, not ordered by the caller) race on the shared
- * scratch and corrupt each other's results; calls on one stream are safe.
- * The work-queue counters are cleared at the start of every call; nothing
- * else in the scratch is assumed to start at zero.
- */
 /* A batch as a CUDA graph (no reference counterpart): one run of the batch
  * on a private stream (which uploads the prior tables, sizes the workspace
  * and configures the kernels), then the same call captured into a graph:
@@ -459,6 +469,46 @@ bamf_status bamf_autotune_result(const bamf_workspace *ws, int arith, int32_t *c
 bamf_status bamf_autotune_shapes(const bamf_workspace *ws, int arith, int32_t *chains_per_cta,
                                  int32_t *ctas_per_sm_budget);
 
+/*
+ * Allocation-free variant of bamf_rjmcmc_batch_device.  It has no
+ * counterpart in the reference (which is a single-ROI CPU sampler).  It is
+ * for callers that must not allocate device memory: hosts whose own pool
+ * owns the device memory (MATLAB's gpuArray allocator, a framework's caching
+ * allocator) and must not see the free memory change under them, and loops
+ * that cannot take the device-wide synchronisation of cudaMalloc/cudaFree.
+ * Same arguments and results as bamf_rjmcmc_batch_device minus the
+ * workspace; it calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * Its scratch is one fixed array of BAMF_NOALLOC_SCRATCH_BYTES compiled into
+ * the library: every GPU that loads the library holds it until the process
+ * exits, and every call shares it.  A call needs
+ *   512 + sum over the 3 priors of 16*len (each rounded up to 256)
+ *   + 4*n_rois (rounded up to 256)
+ *   + [map_n wanted] n_rois*(N_Burnin+N_Trials) (+ 4*n_rois if n_entries is NULL)
+ * bytes; a call needing more returns BAMF_ERR_TOO_LARGE before any GPU work
+ * (split the batch).
+ *
+ * Set-up: the first call on each device looks up the array's device address
+ * with that device current and keeps it for the life of the process; make
+ * that first call before any stream capture begins.  The address belongs to
+ * the device's context: after cudaDeviceReset of a device, this entry point
+ * must not be called on that device again in the same process.
+ *
+ * Priors: the three prior PDF arrays (priors->*_pdf) are host memory that
+ * the call copies into the scratch with copies enqueued on `stream`.  From
+ * ordinary (pageable) memory they are read before the call returns; from
+ * page-locked memory (cudaHostAlloc / cudaHostRegister) the copies read them
+ * when the stream reaches them, so such arrays must stay valid and unchanged
+ * until then.
+ *
+ * Calls that overlap on the GPU (different streams, or different host
+ * threads, not ordered by the caller) race on the shared scratch and
+ * corrupt each other's results; calls on one stream are safe.  The
+ * work-queue counters are cleared at the start of every call; nothing else
+ * in the scratch is assumed to start at zero.  The size classes of a batch
+ * run one after another on `stream` (the workspace entry point overlaps
+ * them on side streams), so a batch of mixed ROI sizes takes somewhat longer.
+ */
 #define BAMF_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *rois,
                                              const bamf_mcmc_params *p,
