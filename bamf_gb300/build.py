@@ -65,9 +65,18 @@ def _compile(src: str, extra: list[str], verbose: bool) -> str:
     return obj
 
 
+def build_boundary() -> None:
+    """The MEX gateways (mex/, against the project's mx stub) and the
+    standalone C++ driver (driver/), both linking the library."""
+    for d in ("mex", "driver"):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, d)], check=True)
+
+
 def build(force: bool = False, verbose: bool = False, extra: list[str] | None = None) -> str:
-    """Compile every .cu under csrc/ and link the shared library; returns its path."""
+    """Compile every .cu under csrc/ and link the shared library, then the
+    MEX gateways and the driver that link it; returns the library's path."""
     if not force and not _stale():
+        build_boundary()
         return OUT
     os.makedirs(OBJDIR, exist_ok=True)
     extra = extra or []
@@ -79,6 +88,7 @@ def build(force: bool = False, verbose: bool = False, extra: list[str] | None = 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, OUT)
+    build_boundary()
     return OUT
 
 
