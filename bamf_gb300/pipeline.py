@@ -95,78 +95,107 @@ def match(found_x, found_y, true_x, true_y, radius: float = 1.0):
 
 
 def analyze_frames(frames: np.ndarray, rj, box: int = 10, overlap: int = 3, proposal: str = "learned",
-                   net=None, seed: int = 1, pos_len: int = 200, grids: bool = True, sampled_psf=None) -> dict:
+                   net=None, seed: int = 1, pos_len: int = 200, grids: bool = True, sampled_psf=None,
+                   chunk_frames: int | None = None) -> dict:
     """Frames (Y, X, Z) -> sub-regions -> sampler + MAP + refinement ->
     stitched posterior image and global emitter list.  sampled_psf: None
     (Gaussian PSF), one 4-D sampled PSF, or one per sub-region position
-    (psf.find_psf_sma's list), selects OptModel 1 (analyzeROIs.m:142-146)."""
+    (psf.find_psf_sma's list), selects OptModel 1 (analyzeROIs.m:142-146).
+    chunk_frames: analyse the stack chunk_frames frames at a time (device
+    memory for the chain traces stays bounded; the posterior grids of each
+    sub-region position accumulate over all chunks, as over all frames in
+    analyzeROIs.m:153), then stitch once.  Every chunk's sampler streams
+    are keyed by its first frame, so chunking changes which uniforms a
+    sub-region's chain draws but not its law."""
     import torch
     Y, X, Z = frames.shape
     T = box + 2 * overlap
-    timing = {}
-    _sync()
-    t0 = time.perf_counter()
-    dev_frames = torch.from_numpy(np.asfortranarray(frames, np.float32).ravel(order="F")).cuda()
-    _sync()
-    timing["h2d"] = time.perf_counter() - t0
-    t = time.perf_counter()
-    sr = tiles.make_subregions_device(dev_frames, Y, X, Z, box, overlap, packed=True)
-    dev = {"data": sr["data"], "offsets": sr["offsets"], "xsize": sr["xsize"], "ysize": sr["ysize"],
-           "side_max": T}
-    _sync()
-    timing["subregions"] = time.perf_counter() - t
-    n = sr["n"]
-    if proposal == "learned":
-        if T != learned.SIDE:
-            raise ValueError("the learned proposal needs 16x16 sub-regions (box + 2 overlap = 16)")
-        t = time.perf_counter()
-        tab = net.infer(sr["data"].view(n, T * T))
-        uniform_fill(tab["cdf"], tab["sub"], sr["xsize"], sr["ysize"], T)
-        dev["birth_cdf"], dev["birth_sub"] = tab["cdf"], tab["sub"]
-        _sync()
-        timing["network"] = time.perf_counter() - t
-    extra = None
     Zm = int(rj.SRZoom)
     Tz = Zm * T
-    per = sr["Xsub"] * sr["Ysub"]
-    if grids:
-        extra = {"pgrid": torch.zeros(per * Tz * Tz, dtype=torch.float32, device="cuda"),
-                 "pback": torch.zeros(per * Tz * Tz, dtype=torch.float32, device="cuda"),
-                 "grid_stride": Tz * Tz, "grid_ld": Tz,
-                 "grid_slot": (sr["roi_ind"] - 1).contiguous()}
-    t = time.perf_counter()
-    psf_kw = {}
-    if sampled_psf is not None:
-        stack = np.asarray(sampled_psf, np.float32)
-        psf_kw["sampled_psf"] = stack
-        if stack.ndim == 5:
-            if stack.shape[0] != per:
-                raise ValueError("one sampled PSF per sub-region position is needed")
-            psf_kw["psf_slot"] = (sr["roi_ind"] - 1).to(torch.int32).contiguous()
-    res = mapfit.analyze(dev, rj, seed=seed, proposal=proposal, pos_len=pos_len, grids=extra, **psf_kw)
-    _sync()
-    timing["sampler_map_refine"] = time.perf_counter() - t
-    out = {"n_subregions": n, "timing": timing}
+    chunk = Z if not chunk_frames else max(1, min(int(chunk_frames), Z))
+    timing = {"h2d": 0.0, "subregions": 0.0, "network": 0.0, "sampler_map_refine": 0.0}
+    extra = None
+    cis, map_ns, n_total, geom = [], [], 0, None
+    for f0 in range(0, Z, chunk):
+        part = frames[:, :, f0:f0 + chunk]
+        zc = part.shape[2]
+        _sync()
+        t0 = time.perf_counter()
+        dev_frames = torch.from_numpy(np.asfortranarray(part, np.float32).ravel(order="F")).cuda()
+        _sync()
+        timing["h2d"] += time.perf_counter() - t0
+        t = time.perf_counter()
+        sr = tiles.make_subregions_device(dev_frames, Y, X, zc, box, overlap, packed=True)
+        dev = {"data": sr["data"], "offsets": sr["offsets"], "xsize": sr["xsize"], "ysize": sr["ysize"],
+               "side_max": T}
+        _sync()
+        timing["subregions"] += time.perf_counter() - t
+        n = sr["n"]
+        n_total += n
+        if proposal == "learned":
+            if T != learned.SIDE:
+                raise ValueError("the learned proposal needs 16x16 sub-regions (box + 2 overlap = 16)")
+            t = time.perf_counter()
+            tab = net.infer(sr["data"].view(n, T * T))
+            uniform_fill(tab["cdf"], tab["sub"], sr["xsize"], sr["ysize"], T)
+            dev["birth_cdf"], dev["birth_sub"] = tab["cdf"], tab["sub"]
+            _sync()
+            timing["network"] += time.perf_counter() - t
+        per = sr["Xsub"] * sr["Ysub"]
+        if geom is None:
+            geom = {k: sr[k][:per].contiguous() for k in ("xsize", "ysize", "roi_ind", "frame_num")}
+            geom.update(Xsub=sr["Xsub"], Ysub=sr["Ysub"], per=per)
+            if grids:
+                extra = {"pgrid": torch.zeros(per * Tz * Tz, dtype=torch.float32, device="cuda"),
+                         "pback": torch.zeros(per * Tz * Tz, dtype=torch.float32, device="cuda"),
+                         "grid_stride": Tz * Tz, "grid_ld": Tz}
+        if extra is not None:
+            extra["grid_slot"] = (sr["roi_ind"] - 1).contiguous()
+        t = time.perf_counter()
+        psf_kw = {}
+        if sampled_psf is not None:
+            stack = np.asarray(sampled_psf, np.float32)
+            psf_kw["sampled_psf"] = stack
+            if stack.ndim == 5:
+                if stack.shape[0] != per:
+                    raise ValueError("one sampled PSF per sub-region position is needed")
+                psf_kw["psf_slot"] = (sr["roi_ind"] - 1).to(torch.int32).contiguous()
+        res = mapfit.analyze(dev, rj, seed=seed + f0, proposal=proposal, pos_len=pos_len, grids=extra, **psf_kw)
+        _sync()
+        timing["sampler_map_refine"] += time.perf_counter() - t
+        rec = res["refined"]
+        ci = global_emitters(rec, sr["roi_ind"].cpu().numpy(), sr["xsize"].cpu().numpy(),
+                             sr["ysize"].cpu().numpy(), sr["frame_num"].cpu().numpy() + f0, sr["Xsub"], sr["Ysub"],
+                             box, overlap)
+        ci["ROInum"] = ci["ROInum"] + (n_total - n)
+        cis.append(ci)
+        map_ns.append(res["map_n"])
+        del dev_frames, sr, dev, res
+    out = {"n_subregions": n_total, "timing": timing}
     t = time.perf_counter()
     if grids:
         # one grid per sub-region position, summed over frames; frame 1's ROI_Struct rows describe them
-        xs, ys = sr["xsize"][:per].contiguous(), sr["ysize"][:per].contiguous()
-        ri = sr["roi_ind"][:per].contiguous()
+        per = geom["per"]
         for key, name in (("pgrid", "PImage"), ("pback", "PBg")):
             g = extra[key]
-            tiles.remove_overlapping_device(g, per, Tz, xs, ys, ri, sr["Xsub"], sr["Ysub"], overlap, Zm)
-            img, bad = tiles.stitch_rois_device(g, per, Tz, xs, ys, sr["frame_num"][:per].contiguous(), ri,
-                                                (Y, X, 1), box, overlap, Zm)
+            tiles.remove_overlapping_device(g, per, Tz, geom["xsize"], geom["ysize"], geom["roi_ind"],
+                                            geom["Xsub"], geom["Ysub"], overlap, Zm)
+            img, bad = tiles.stitch_rois_device(g, per, Tz, geom["xsize"], geom["ysize"], geom["frame_num"],
+                                                geom["roi_ind"], (Y, X, 1), box, overlap, Zm)
             out[name] = img.view(Zm * X, Zm * Y).t()
     _sync()
     timing["stitch"] = time.perf_counter() - t
-    rec = res["refined"]
-    ci = global_emitters(rec, sr["roi_ind"].cpu().numpy(), sr["xsize"].cpu().numpy(), sr["ysize"].cpu().numpy(),
-                         sr["frame_num"].cpu().numpy(), sr["Xsub"], sr["Ysub"], box, overlap)
-    out["ClustInfo"] = ci
-    out["map_n"] = res["map_n"]
+    out["ClustInfo"] = {k: np.concatenate([c[k] for c in cis]) for k in cis[0]}
+    out["map_n"] = map_ns[0] if len(map_ns) == 1 else _cat(map_ns)
     timing["total"] = sum(timing.values())
     return out
+
+
+def _cat(parts):
+    import torch
+    if isinstance(parts[0], torch.Tensor):
+        return torch.cat(parts)
+    return np.concatenate(parts)
 
 
 def localisation_stats(ci: dict, truth, radius: float = 1.0) -> dict:

@@ -14,8 +14,10 @@ value     ROIs/s with inputs resident in HBM (device entry point)
 e2e       ROIs/s through bamf_rjmcmc_batch_host with host buffers (H2D/D2H inside)
 roofline  the sampler kernel against the measured MUFU log2 rate: one log2 per
           ROI pixel per scored proposal (the likelihood-ratio pass)
-cpu_baseline  the CPU restatement of the reference sampler (glibc math, bit-
-          identical to the reference build) on the host cores, on a sample
+cpu_baseline  the reference sampler (source/c/LibRJMCMC.cpp compiled unmodified,
+          glibc math; the C restatement where that build is absent, and
+          beside it where present) on all host cores, on a sample with the
+          same number of ROIs of every size class
 plain_exact  (rank 0, outside the timed region) the plain-RJMCMC
           configuration (200 ROIs 16x16, 3000+3000 jumps) in exact
           arithmetic, whose chains equal the reference sampler's bit for bit:
@@ -27,13 +29,14 @@ frontend  (rank 0, outside the timed region) FindROI + gaussMLE on the
           measured HBM bandwidth (one 4-byte read per pixel), fits/s, and an
           end-to-end frames/s with the stack copied from pinned host memory
 dense_e2e (rank 0, outside the timed region) the dense end-to-end frame
-          analysis (bamf_gb300.pipeline) on 20 of its frames: frames/s,
-          stage times, localisation RMSE / recall / precision
+          analysis (bamf_gb300.pipeline) on 500 of its frames, 100 per pass:
+          frames/s, stage times, localisation RMSE / recall / precision
 learned_proposal  (rank 0, outside the timed region) the learned-vs-uniform
-          birth-proposal evaluation on 16x16 ROIs (bamf_gb300.learned_eval):
-          network training rate, per-arm ROIs/s, ESS/s of the emitter count
-          and of the mean-X functional, MAP count accuracy, RMSE, and the
-          throughput at equal MAP accuracy
+          proposal evaluation on 16x16 ROIs (bamf_gb300.learned_eval), 4
+          dispersed chains per ROI: network training rate, per-arm chains/s,
+          multi-chain bulk ESS/s and R-hat of the emitter count and of the
+          mean-X functional, MAP count accuracy, RMSE, and the throughput at
+          equal MAP accuracy with RMSE within 5%
 
 Under torchrun (N > 1) every rank runs its own 100,000 ROIs (weak scaling,
 no data-path collective); value = all ROIs / max rank time.
@@ -78,18 +81,20 @@ def parse():
                     help="skip the plain-RJMCMC exact-arithmetic measurement (200 ROIs 16x16)")
     ap.add_argument("--frontend-frames", type=int, default=2000)
     ap.add_argument("--no-dense", action="store_true", help="skip the dense end-to-end frame analysis")
-    ap.add_argument("--dense-frames", type=int, default=20)
+    ap.add_argument("--dense-frames", type=int, default=500)
+    ap.add_argument("--dense-chunk", type=int, default=100, help="frames per pipeline pass of the dense analysis")
     return ap.parse_args()
 
 
-def dense_bench(n_frames: int) -> dict:
+def dense_bench(n_frames: int, chunk: int = 100) -> dict:
     """The dense end-to-end stress workload on n_frames of its 10,000
     frames (256x256, 100 nm pixels, U[1,10] emitters/um^2, sigma 1.3,
     LogN(ln 800, 0.5), background U[50,200]): priors from the front end,
     16x16 sub-regions (BoxSize 10, Overlap 3), batched sampler with learned
     births (network trained on the generator with this workload's
-    statistics), MAP + refinement, stitched posterior image; frames/s of a
-    warmed second run, localisation against the truth."""
+    statistics), MAP + refinement, stitched posterior image; the stack is
+    analysed `chunk` frames per pass (the posterior grids accumulate over
+    all passes); frames/s of a warmed run, localisation against the truth."""
     from bamf_gb300 import learned, pipeline, priors, rjstruct, synth
     frames, truth, _ = synth.frames_dense(n_frames, seed=5)
     rj = rjstruct.c0_rjstruct()
@@ -108,11 +113,12 @@ def dense_bench(n_frames: int) -> dict:
               bg=50.0, bg_max=200.0)
     t_train = time.perf_counter() - t0
     pipeline.analyze_frames(frames[:, :, :2], rj, proposal="learned", net=net, seed=2)  # warm-up
-    out = pipeline.analyze_frames(frames, rj, proposal="learned", net=net, seed=2)
+    out = pipeline.analyze_frames(frames, rj, proposal="learned", net=net, seed=2, chunk_frames=chunk)
     st = pipeline.localisation_stats(out["ClustInfo"], truth)
     t = out["timing"]
     return {"workload": f"dense end to end: {n_frames} frames 256x256, U[1,10] emitters/um^2, 16x16 sub-regions "
-                        f"(BoxSize 10, Overlap 3), learned births, 3000+3000 jumps + 1000+1000 refinement",
+                        f"(BoxSize 10, Overlap 3), learned births, 3000+3000 jumps + 1000+1000 refinement, "
+                        f"{chunk} frames per pass",
             "frames_per_s": n_frames / t["total"], "subregions": out["n_subregions"],
             "subregions_per_s": out["n_subregions"] / t["total"],
             "stage_seconds": {k: round(v, 4) for k, v in t.items()},
@@ -165,8 +171,10 @@ def plain_exact_bench(n_large: int = 4864) -> dict:
     torch.cuda.synchronize()
     out["rois_per_s_large"] = n_large / (e0.elapsed_time(e1) * 1e-3)
     threads = os.cpu_count() or 1
-    rate, secs = cpu_sample_rate(b, rj, p, bg0, 200, threads)
+    kind = cpu_kind()
+    rate, secs, _ = cpu_sample_rate(b, rj, p, bg0, 200, threads, kind)
     out["cpu_rois_per_s_200"] = rate
+    out["cpu_kind"] = CPU_DESC[kind][0]
     out["cpu_cores"] = threads
     out["cpu_seconds_200"] = secs
     return out
@@ -240,6 +248,43 @@ def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3) -> dict:
     }
 
 
+def noalloc_bench(s, dev, outs, p, rj, bg0, n, stream) -> dict:
+    """One call each of the workspace entry point and the allocation-free
+    one on the bench batch, without MAP counts (the MAP trace of this batch
+    is beyond the allocation-free scratch), timed with CUDA events; the
+    per-ROI outputs must agree."""
+    import ctypes as C
+
+    import torch
+
+    from bamf_gb300 import abi, sampler
+    L = sampler._declare()
+    L.bamf_rjmcmc_batch_device_noalloc.restype = C.c_int
+    L.bamf_rjmcmc_batch_device_noalloc.argtypes = [
+        C.POINTER(sampler.RoiBatch), C.POINTER(abi.McmcParams), C.POINTER(sampler.Priors),
+        C.c_uint32, C.c_int, C.POINTER(sampler.BatchResults), C.c_void_p]
+    o1 = {k: torch.zeros(n, dtype=torch.int32, device="cuda") for k in ("final_n", "status")}
+    o2 = {k: torch.zeros(n, dtype=torch.int32, device="cuda") for k in ("final_n", "status")}
+    ev = lambda: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))  # noqa: E731
+    a0, a1 = ev()
+    a0.record(stream)
+    s.run_device(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=77, arith="fast", outs=o1,
+                 stream=stream.cuda_stream, bg0=bg0)
+    a1.record(stream)
+    pr, keep, bs, rs = s._structs(dev, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, o2, bg0, "reference")
+    b0, b1 = ev()
+    b0.record(stream)
+    st = L.bamf_rjmcmc_batch_device_noalloc(C.byref(bs), C.byref(p), C.byref(pr), 77, abi.BAMF_ARITH_FAST,
+                                            C.byref(rs), C.c_void_p(stream.cuda_stream))
+    b1.record(stream)
+    torch.cuda.synchronize()
+    abi.check(st, "bamf_rjmcmc_batch_device_noalloc")
+    same = bool(torch.equal(o1["final_n"], o2["final_n"]) and torch.equal(o1["status"], o2["status"]))
+    tw, tn = a0.elapsed_time(a1) * 1e-3, b0.elapsed_time(b1) * 1e-3
+    return {"workspace_rois_per_s": n / tw, "noalloc_rois_per_s": n / tn, "same_results": same,
+            "note": "no MAP counts in either; size classes serial on one stream in the allocation-free call"}
+
+
 def workload_label(n_rois: int, jumps: int) -> str:
     return (f"batched uneven RJMCMC: {n_rois // 1000}k ROIs, sides {{8,12,16,20,24}} px, "
             f"{jumps}+{jumps} jumps")
@@ -303,21 +348,51 @@ def workload(n_rois: int, seed: int, jumps: int):
     return b, rj, rjstruct.mcmc_params(rj), rjstruct.initial_bg(rj)
 
 
-def cpu_sample_rate(b, rj, p, bg0, n_sample: int, threads: int):
-    """The CPU restatement of the reference sampler (glibc math) on the first
-    n_sample ROIs, all `threads` host threads; returns (ROIs/s, seconds)."""
+def cpu_kind() -> str:
+    """The reference sampler itself (source/c/LibRJMCMC.cpp compiled
+    unmodified, glibc math) when its build is available, else the C
+    restatement (glibc math, bit-identical outputs)."""
+    import oracle
+    oracle.build()
+    return "ref_native" if oracle.available("ref_native") else "port_native"
+
+
+def stratified(b, per_class: int, start: int = 0):
+    """The ROIs [start, start + per_class) of every size class of batch b,
+    interleaved class by class (the CPU sample covers all sides equally)."""
+    from bamf_gb300 import synth
+    sides = np.maximum(b.xsize, b.ysize)
+    cols = [np.flatnonzero(sides == sd)[start:start + per_class] for sd in np.unique(sides)]
+    idx = np.stack([c[:min(len(x) for x in cols)] for c in cols], 1).ravel()
+    return synth.RoiBatch(data=b.data, offsets=b.offsets[idx], xsize=b.xsize[idx], ysize=b.ysize[idx],
+                          sigma=b.sigma[idx], bg=b.bg[idx], true_n=b.true_n[idx], true_x=[], true_y=[],
+                          true_i=[])
+
+
+def cpu_sample_rate(b, rj, p, bg0, n_sample: int, threads: int, kind: str = "port_native", per_class=None):
+    """A CPU sampler (`kind`: the reference build "ref_native" or the C
+    restatement "port_native") on a sample of batch b, all `threads` host
+    threads: the first n_sample ROIs, or per_class ROIs of every size class;
+    returns (ROIs/s, seconds, ROIs)."""
     import oracle
     from bamf_gb300 import synth
-    sub = synth.RoiBatch(
-        data=b.data, offsets=b.offsets[:n_sample], xsize=b.xsize[:n_sample],
-        ysize=b.ysize[:n_sample], sigma=b.sigma[:n_sample], bg=b.bg[:n_sample],
-        true_n=b.true_n[:n_sample], true_x=[], true_y=[], true_i=[])
-    oracle.build(ref=False)
+    if per_class:
+        sub = stratified(b, per_class)
+    else:
+        sub = synth.RoiBatch(
+            data=b.data, offsets=b.offsets[:n_sample], xsize=b.xsize[:n_sample],
+            ysize=b.ysize[:n_sample], sigma=b.sigma[:n_sample], bg=b.bg[:n_sample],
+            true_n=b.true_n[:n_sample], true_x=[], true_y=[], true_i=[])
     t = time.perf_counter()
     oracle.run_batch(sub, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, bg0, seed=1,
-                     threads=threads, kind="port_native")
+                     threads=threads, kind=kind)
     dt = time.perf_counter() - t
-    return n_sample / dt, dt
+    return sub.n / dt, dt, sub.n
+
+
+CPU_DESC = {"ref_native": ("reference", "the reference sampler source/c/LibRJMCMC.cpp compiled unmodified "
+                                        "(glibc math) behind the project's cRJMCMC driver"),
+            "port_native": ("port", "glibc-math C restatement, bit-identical to the reference sampler build")}
 
 
 def run_reference(a, rank, world):
@@ -325,15 +400,18 @@ def run_reference(a, rank, world):
         return
     b, rj, p, bg0 = workload(a.n_rois, 2, a.jumps)
     threads = os.cpu_count() or 1
-    n = a.cpu_sample or max(threads * 24, 96)  # ~1 s per step on 16 Grace cores
+    kind = cpu_kind()
+    per_class = a.cpu_sample or max(2 * threads, 8)  # 5 classes x 2 per thread: ~2 s per step on 16 cores
     for _ in range(a.warmup):
-        cpu_sample_rate(b, rj, p, bg0, min(n, 32), threads)
+        cpu_sample_rate(b, rj, p, bg0, 0, threads, kind, per_class=max(per_class // 8, 1))
     rates, secs = [], []
+    n = 0
     for _ in range(a.steps):
-        r, s = cpu_sample_rate(b, rj, p, bg0, n, threads)
+        r, s, n = cpu_sample_rate(b, rj, p, bg0, 0, threads, kind, per_class=per_class)
         rates.append(r)
         secs.append(s)
     v = len(rates) * n / sum(secs)
+    ck, desc = CPU_DESC[kind]
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "ROIs/s", "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs),
@@ -341,9 +419,9 @@ def run_reference(a, rank, world):
         "data": "synthetic (seeded, reference forward model + Poisson noise)",
         "config": {"workload": workload_label(a.n_rois, a.jumps), "n_rois": a.n_rois,
                    "jumps": [a.jumps, a.jumps], "parallelism": "host threads", "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": v, "unit": "ROIs/s", "cores": threads, "kind": "port",
-                         "sample": f"first {n} ROIs of the workload per step (same seeds), "
-                                   f"glibc-math C restatement bit-identical to the reference build"},
+        "cpu_baseline": {"value": v, "unit": "ROIs/s", "cores": threads, "kind": ck,
+                         "sample": f"{n} ROIs per step: the first {per_class} of each size class of the "
+                                   f"workload (same seeds); {desc}"},
         "e2e": {"value": v, "unit": "ROIs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -382,6 +460,7 @@ def main():
             "final_n": torch.zeros(n, dtype=torch.int32, device="cuda"),
             "status": torch.zeros(n, dtype=torch.int32, device="cuda"),
             "llr_evals": torch.zeros(n, dtype=torch.int32, device="cuda"),
+            "overflow": torch.zeros(n, dtype=torch.int32, device="cuda"),
             "n_entries": torch.zeros(n, dtype=torch.int32, device="cuda")}
     s = sampler.Sampler()
     stream = torch.cuda.current_stream()
@@ -440,14 +519,24 @@ def main():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-        t0 = time.perf_counter()
-        host_out = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=1234,
-                              arith="fast", bg0=bg0)
-        dt = replicas.max_over_ranks(time.perf_counter() - t0, dist, "cuda")
+        calls = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            host_out = s.run_host(b, p, rj.P_Offset, rj.P_EmPhotons, rj.P_BgEmPhotons, seed=1234,
+                                  arith="fast", bg0=bg0)
+            calls.append(replicas.max_over_ranks(time.perf_counter() - t0, dist, "cuda"))
+        dt = statistics.median(calls)
         h2d = b.data.nbytes + b.offsets.nbytes + b.xsize.nbytes + b.ysize.nbytes + b.sigma.nbytes
         d2h = sum(v.nbytes for v in host_out.values())
         e2e = {"value": replicas.whole_job_rate(n, world, dt), "unit": "ROIs/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+               "d2h_bytes_per_step": int(d2h), "calls": len(calls),
+               "seconds_per_call": {"median": dt, "min": min(calls), "max": max(calls)}}
+
+    # the allocation-free entry point against the workspace one, both
+    # without MAP counts (the MAP trace of 100k ROIs is beyond the fixed scratch)
+    noalloc_block = None
+    if rank == 0:
+        noalloc_block = noalloc_bench(s, dev, outs, p, rj, bg0, n, stream)
 
     # per step: order_kernel, one sampler launch per non-empty size class, map_n_kernel
     sides = np.maximum(b.xsize, b.ysize)
@@ -464,9 +553,14 @@ def main():
             "workload": r["workload"],
             "train_rois_per_s": r["train_rois_per_s"], "infer_seconds": r["infer_seconds"],
             **{f"{k}_{f}": arms[k][f] for k in arms for f in
-               ("rois_per_s", "ess_n_per_s", "ess_x_per_s", "map_count_accuracy", "rmse_px")},
+               ("chains_per_s", "ess_n_per_chain", "ess_x_per_chain", "ess_n_per_s", "ess_x_per_s",
+                "rhat_n_median", "rhat_x_median", "rhat_n_above_1_05", "rhat_x_above_1_05",
+                "map_count_accuracy", "rmse_px")},
             "ess_n_per_s_ratio": r["ess_n_per_s_ratio"], "ess_x_per_s_ratio": r["ess_x_per_s_ratio"],
+            "ess_n_per_s_ratio_init": r["ess_n_per_s_ratio_init"],
+            "ess_x_per_s_ratio_init": r["ess_x_per_s_ratio_init"],
             "equal_accuracy": r["equal_accuracy_vs_uniform_at_full_length"],
+            "accuracy_vs_jumps": r["accuracy_vs_jumps"],
         }
 
     plain_block = None
@@ -478,16 +572,22 @@ def main():
         frontend_block = frontend_bench(a.frontend_frames)
     dense_block = None
     if rank == 0 and not a.no_dense:
-        dense_block = dense_bench(a.dense_frames)
+        dense_block = dense_bench(a.dense_frames, a.dense_chunk)
 
     cpu = None
     if rank == 0:
         threads = os.cpu_count() or 1
-        ns = a.cpu_sample or max(threads * 24, 96)  # ~20 thread-seconds of CPU work
-        rate, secs = cpu_sample_rate(b, rj, p, bg0, ns, threads)
-        cpu = {"value": rate, "unit": "ROIs/s", "cores": threads, "kind": "port",
-               "sample": f"first {ns} ROIs of the workload, {secs:.1f} s on {threads} host threads; "
-                         f"glibc-math C restatement bit-identical to the reference sampler build"}
+        per_class = a.cpu_sample or max(2 * threads, 8)  # ~30 thread-seconds of CPU work
+        kind = cpu_kind()
+        rate, secs, ns = cpu_sample_rate(b, rj, p, bg0, 0, threads, kind, per_class=per_class)
+        ck, desc = CPU_DESC[kind]
+        cpu = {"value": rate, "unit": "ROIs/s", "cores": threads, "kind": ck,
+               "sample": f"{ns} ROIs: the first {per_class} of each size class of the workload, {secs:.1f} s "
+                         f"on {threads} host threads; {desc}"}
+        if kind != "port_native":
+            prate, psecs, _ = cpu_sample_rate(b, rj, p, bg0, 0, threads, "port_native", per_class=per_class)
+            cpu["port_value"] = prate
+            cpu["port"] = CPU_DESC["port_native"][1]
 
     if rank == 0:
         line = {
@@ -512,6 +612,8 @@ def main():
             "plain_exact": plain_block,
             "frontend": frontend_block,
             "dense_e2e": dense_block,
+            "noalloc": noalloc_block,
+            "overflow_rois_frac": float((outs["overflow"] > 0).float().mean().item()),
             "map_n_mean": float(outs["map_n"].float().mean().item()),
             "true_n_mean": float(b.true_n.mean()),
         }

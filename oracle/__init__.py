@@ -22,7 +22,9 @@ import numpy as np
 from bamf_gb300 import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = os.environ.get("BAMF_REFERENCE_DIR", "/root/reference")
+# where the reference sampler sources are staged for machines without the
+# reference tree (git-ignored; `make -C oracle stage-ref`)
+STAGED_REF = os.path.join(HERE, "_ref", "src")
 PATHS = {
     "port": os.path.join(HERE, "_build", "liboracle.so"),
     "port_native": os.path.join(HERE, "_build", "liboracle_native.so"),
@@ -33,13 +35,36 @@ PREFIX = {"port": "oracle", "port_native": "oracle", "ref": "ref", "ref_native":
 _libs: dict = {}
 
 
+def _has_sampler_sources(d: str | None) -> bool:
+    return bool(d) and os.path.isfile(os.path.join(d, "source", "c", "LibRJMCMC.cpp"))
+
+
+def ref_dir() -> str | None:
+    """The reference tree named by $BAMF_REFERENCE_DIR, else the staged copy
+    of its sampler sources, else None."""
+    d = os.environ.get("BAMF_REFERENCE_DIR")
+    if _has_sampler_sources(d):
+        return d
+    return STAGED_REF if _has_sampler_sources(STAGED_REF) else None
+
+
 def build(ref: bool | None = None) -> None:
-    """Compile the port (always) and the reference oracle (when its sources exist)."""
+    """Compile the port (always) and the reference sampler oracle (when its
+    sources can be found; with the full reference tree also stage them for
+    machines that lack it)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
+    d = ref_dir()
+    if d and d != STAGED_REF:
+        subprocess.run(["make", "-s", "-C", HERE, "stage-ref", f"REF_DIR={d}"], check=True)
+        # the reference's CUDA front-end kernels as sm_103a cubins (nvcc
+        # cross-compiles them here; the cubins travel to the GPU host)
+        subprocess.run(["make", "-s", "-C", HERE, "ref-cubin", f"REF_DIR={d}"], check=True)
     if ref is None:
-        ref = os.path.isfile(os.path.join(REF_DIR, "source", "c", "LibRJMCMC.cpp"))
+        ref = d is not None
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={REF_DIR}"], check=True)
+        if d is None:
+            raise FileNotFoundError("reference sampler sources not found: set BAMF_REFERENCE_DIR")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_DIR={d}"], check=True)
 
 
 def available(kind: str) -> bool:
@@ -70,11 +95,11 @@ def load(kind: str = "port") -> C.CDLL:
     getattr(L, f"{p}_result_grids").argtypes = [C.c_void_p, pf, pf]
     getattr(L, f"{p}_result_counters").argtypes = [C.c_void_p, C.POINTER(abi.Counters)]
     getattr(L, f"{p}_result_free").argtypes = [C.c_void_p]
+    pi = C.POINTER(C.c_int32)
+    getattr(L, f"{p}_rjmcmc_batch").argtypes = [
+        pf, C.POINTER(C.c_int64), pi, pi, pf, C.c_int, C.POINTER(abi.McmcParams),
+        pf, C.c_int, pf, C.c_int, pf, C.c_int, C.c_float, C.c_uint32, C.c_int, pi, pi, pi]
     if kind.startswith("port"):
-        pi = C.POINTER(C.c_int32)
-        L.oracle_rjmcmc_batch.argtypes = [
-            pf, C.POINTER(C.c_int64), pi, pi, pf, C.c_int, C.POINTER(abi.McmcParams),
-            pf, C.c_int, pf, C.c_int, pf, C.c_int, C.c_float, C.c_uint32, C.c_int, pi, pi, pi]
         L.oracle_findroi_filter.argtypes = [pf, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                             C.c_int, C.c_float, pf, C.c_int]
         L.oracle_gaussmle_xynb.argtypes = [pf, C.c_int, C.c_int, C.c_float, C.c_int, pf, pf, pf,
@@ -147,8 +172,11 @@ def run_chain(kind: str, roi: np.ndarray, params: abi.McmcParams, off: np.ndarra
 
 def run_batch(batch, params: abi.McmcParams, off, sig, back, bg0: float, seed: int,
               threads: int = 1, kind: str = "port_native") -> dict:
-    """Per-ROI summaries (final N, MAP N, accepted moves) on host threads."""
+    """Per-ROI summaries (final N, MAP N, accepted moves) on host threads;
+    kind "port"/"port_native" (the restatement) or "ref"/"ref_native" (the
+    reference sampler build)."""
     L = load(kind)
+    batch_fn = getattr(L, f"{PREFIX[kind]}_rjmcmc_batch")
     n = batch.n
     fn = np.zeros(n, np.int32)
     mn = np.zeros(n, np.int32)
@@ -157,7 +185,7 @@ def run_batch(batch, params: abi.McmcParams, off, sig, back, bg0: float, seed: i
     sig = np.ascontiguousarray(sig, np.float32)
     back = np.ascontiguousarray(back, np.float32)
     pi = C.POINTER(C.c_int32)
-    abi.check(L.oracle_rjmcmc_batch(
+    abi.check(batch_fn(
         abi.fptr(batch.data), batch.offsets.ctypes.data_as(C.POINTER(C.c_int64)),
         batch.xsize.ctypes.data_as(pi), batch.ysize.ctypes.data_as(pi),
         abi.fptr(np.ascontiguousarray(batch.sigma, np.float32)), n, C.byref(params),

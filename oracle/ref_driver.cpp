@@ -20,6 +20,11 @@
  * defined here from the Philox stream (include/bamf_philox.h).  State is
  * thread-local so that tests may run several ROIs on host threads.
  */
+/* standard headers the batch runner needs, before the reference header
+ * defines its min/max/pi macros */
+#include <atomic>
+#include <thread>
+
 #include "LibRJMCMCreturn.hpp"
 
 #include <cstdarg>
@@ -250,3 +255,77 @@ extern "C" int ref_result_counters(void *h, bamf_counters *c)
 }
 
 extern "C" void ref_result_free(void *h) { delete static_cast<RefResult *>(h); }
+
+/* A batch of ROIs through the reference sampler on host threads, the way the
+ * @RJ pipeline runs them (one cRJMCMC call per ROI, RJ.m:217-244 parfor over
+ * workers): ROI k with the empty start of rjmcmc.m:43-47 (BG = bg0), its own
+ * PSF sigma, uniform stream (seed, k, 0).  Per ROI: final emitter count, MAP
+ * count (mode of the Signal==1 count over entries round(L/2)..L of the
+ * accepted chain without its last entry, findMap.m:29-45) and accepted
+ * moves.  Same interface as the port's oracle_rjmcmc_batch. */
+static int ref_map_n(const RefResult &r)
+{
+    const std::vector<int> &N = r.N[0];
+    const int entries = (int)N.size();
+    const int iter = entries - 1;
+    if (iter < 1) return 0;
+    const int start = (iter + 1) / 2 < 1 ? 1 : (iter + 1) / 2;
+    std::vector<int> nsig(entries, 0);
+    size_t rec = 0;
+    for (int e = 0; e < entries; ++e) {
+        const int n = N[e] < 1 ? 1 : N[e];
+        int s = 0;
+        for (int k = 0; k < n && rec + k < r.Signal[0].size(); ++k) s += r.Signal[0][rec + k] == 1;
+        nsig[e] = N[e] < 1 ? 0 : s;
+        rec += (size_t)n;
+    }
+    std::vector<int> hist(BAMF_NMAX * 4 + 2, 0);
+    int maxn = 0;
+    for (int k = start; k <= iter; ++k) {
+        int v = nsig[k - 1];
+        if (v > BAMF_NMAX * 4) v = BAMF_NMAX * 4;
+        hist[v]++;
+        if (v > maxn) maxn = v;
+    }
+    int best = 0;
+    for (int v = 1; v <= maxn; ++v)
+        if (hist[v] > hist[best]) best = v;
+    return best;
+}
+
+extern "C" int ref_rjmcmc_batch(const float *data, const int64_t *offsets, const int32_t *xs, const int32_t *ys,
+                                const float *sigma, int n_rois, const bamf_mcmc_params *p, const float *off,
+                                int loff, const float *sig, int lsig, const float *back, int lback, float bg0,
+                                uint32_t seed, int threads, int32_t *final_n, int32_t *map_n, int32_t *n_accepted)
+{
+    if (!data || !offsets || !xs || !ys || n_rois < 0 || !p || !final_n || !map_n || !n_accepted)
+        return BAMF_ERR_INVALID_ARG;
+    std::atomic<int> next(0);
+    auto worker = [&]() {
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n_rois) break;
+            bamf_emitters e0 = {0, nullptr, nullptr, nullptr, bg0};
+            bamf_rng rng = {seed, (uint32_t)i, 0u};
+            bamf_mcmc_params pk = *p;
+            if (sigma) pk.PSFsigma = sigma[i];
+            RefResult *r = static_cast<RefResult *>(ref_rjmcmc_run_model(
+                data + offsets[i], xs[i], ys[i], &e0, &pk, off, loff, sig, lsig, back, lback, nullptr, nullptr, 0,
+                &rng));
+            if (!r) {
+                final_n[i] = map_n[i] = n_accepted[i] = -1;
+                continue;
+            }
+            final_n[i] = r->N[0].empty() ? 0 : r->N[0].back();
+            map_n[i] = ref_map_n(*r);
+            const bamf_counters &c = r->counters;
+            n_accepted[i] = c.A_jump + c.A_split + c.A_merge + c.A_birth + c.A_death;
+            delete r;
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> th;
+    for (int t = 0; t < threads; ++t) th.emplace_back(worker);
+    for (auto &t : th) t.join();
+    return BAMF_OK;
+}

@@ -34,4 +34,7 @@ def main(ref: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BAMF_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_circle_fixture.py <reference tree>  (or set BAMF_REFERENCE_DIR)")
+    main(ref)
