@@ -1247,6 +1247,24 @@ struct ChainWarp {
             float aIn = A_I(nn), aXn = A_X(nn), aYn = A_Y(nn);
             int aSn = A_S(nn);
             float nI, nX, nY;
+            if (!EXACT && K->proposal == BAMF_PROPOSAL_LEARNED && urand() < 0.25f) {
+                /* LEARNED relocation (no reference counterpart): an
+                 * independence proposal of the emitter's position from the
+                 * birth mixture q = 1/2 learned + 1/2 uniform on the extended
+                 * box, intensity kept; Hastings factor q(old) / q(new) =
+                 * birth_q_ratio(new) / birth_q_ratio(old), position prior
+                 * uniform on the box, so the target is unchanged for any q */
+                cinc(aSn == 1 ? C_N_jumpFg : C_N_jumpBg);
+                birth_position(&nX, &nY);
+                setT(nn, aIn, nX, nY);
+                if (!EXACT) a_dirty |= 1u << nn;
+                pk_move = MV_JUMP;
+                pk_type = type;
+                pk_f0 = birth_q_ratio(nX, nY) / birth_q_ratio(aXn, aYn);
+                pk_c1 = C_A_jump;
+                pk_c2 = aSn == 1 ? C_A_jumpFg : C_A_jumpBg;
+                return testT() ? ACT_EVAL : ACT_REJECT;
+            }
             if (aSn == 1) {
                 cinc(C_N_jumpFg);
                 nI = aIn + p.I_stdFg * randn();

@@ -293,11 +293,15 @@ typedef struct bamf_roi_batch {
      *                            rejected), which the reference's ratio omits
      *   BAMF_PROPOSAL_LEARNED    UNIFORM, with the birth position drawn half of
      *                            the time from a per-ROI density over 4x4
-     *                            sub-cells of each pixel, and half of the
+     *                            sub-cells of each pixel, half of the
      *                            splits placing the first emitter from that
      *                            density (intensity fraction triangular on
-     *                            [0.3, 0.7]); the exact mixture densities enter
-     *                            the birth, death, split and merge ratios
+     *                            [0.3, 0.7]), and a quarter of the
+     *                            single-emitter jumps relocating the emitter
+     *                            to a position drawn from the birth mixture
+     *                            (intensity kept); the exact mixture densities
+     *                            enter the birth, death, split, merge and
+     *                            relocation ratios
      * Anything but REFERENCE needs BAMF_ARITH_FAST.  LEARNED reads
      *   birth_cdf   [pixel] running sum of the pixel probabilities, laid out
      *               like data (ROI k at offsets[k], y fastest)
