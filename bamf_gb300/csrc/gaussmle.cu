@@ -3,8 +3,7 @@
  * (gaussMLE 'Basic'/'CCD': kernel_MLEFit_XYNB_, cuda_gaussMLEv2.cu:16-141,
  * with GPUgaussLib.cuh:14-258 and MatInvLib.h:15-75) for sm_103a.
  *
- * One thread per fit, ROIs staged through shared memory with coalesced
- * loads (the reference reads each ROI per thread, uncoalesced).  The model
+ * A group of 8 lanes per fit (one thread per fit in the reference).  The model
  * is separable: the integrated PSF along x depends only on the column ii
  * and along y only on the row jj, and so do the x/y derivative factors up to
  * the final multiply by the other axis's PSF.  Those per-axis terms are
@@ -19,18 +18,9 @@
 
 #include "bamf.h"
 
-/* a failed CUDA runtime call: clear its error so that a later call on this
- * thread does not report it again */
-static inline bamf_status clear_cuda_error()
-{
-    cudaGetLastError();
-    return BAMF_ERR_CUDA;
-}
-
 namespace {
 
 constexpr int MAXSZ = 21;        /* IMSZBIG of definitions.h: largest fit window */
-constexpr int FITS_PER_BLOCK = 64;
 #define MLE_PI 3.141592f         /* definitions.h:13 */
 
 /* kernel_IntGauss1D (GPUgaussLib.cuh:14-24) */
@@ -50,90 +40,145 @@ __device__ __forceinline__ void dgauss_axis(int ii, float x, float sigma, float 
     *d2 = -N / sqrtf(2.0f * MLE_PI) / (sigma * sigma * sigma) * ((ii + 1.0f - x) * a - (ii - x) * b);
 }
 
-__global__ void __launch_bounds__(FITS_PER_BLOCK) mle_xynb_kernel(
+/* One fit per group of GL lanes (GL = 8: four fits per warp), ROIs staged
+ * through shared memory with coalesced loads (the reference reads each ROI
+ * per thread, uncoalesced).  Lane l of a group owns pixels l, l + GL, ...;
+ * the centre of mass,
+ * the start-up filter's positions, the Newton sums and the Fisher
+ * information are lane partial sums (or maxima / minima) combined by
+ * butterfly shuffles within the group, so every lane of the group holds
+ * the same totals and the same theta.  The per-axis PSF and derivative
+ * terms of an iteration are computed one value per lane into the group's
+ * shared-memory rows.  The group's first lane inverts the 4 x 4 Fisher
+ * matrix (MatInvLib.h:15-75) and writes the fit.  The reference's formulas
+ * throughout; only the order of the pixel sums differs from its serial
+ * loops. */
+constexpr int GL = 8;
+constexpr int GROUP_FITS_PER_BLOCK = 16; /* 128 threads */
+
+__device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = GL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(GL * GROUP_FITS_PER_BLOCK) mle_xynb_group_kernel(
     const float *__restrict__ data, float sigma, int sz, int iterations,
     float *__restrict__ P, float *__restrict__ CRLB, float *__restrict__ LL, int nfits)
 {
     extern __shared__ float sm[];
     const int npx = sz * sz;
-    const int64_t first = (int64_t)blockIdx.x * FITS_PER_BLOCK;
-    const int nblk = (int)min((int64_t)FITS_PER_BLOCK, (int64_t)nfits - first);
-    /* coalesced staging of this block's ROIs */
+    const int64_t first = (int64_t)blockIdx.x * GROUP_FITS_PER_BLOCK;
+    const int nblk = (int)min((int64_t)GROUP_FITS_PER_BLOCK, (int64_t)nfits - first);
+    /* coalesced staging of this block's ROIs; per fit 6 axis rows and the
+     * start-up filter's weight table behind them */
+    float *axis_all = sm + GROUP_FITS_PER_BLOCK * npx;
+    /* pixel p -> (ii, jj) as ii << 8 | jj, once per block (no division in the
+     * pixel loops) */
+    int *pix = (int *)(axis_all + GROUP_FITS_PER_BLOCK * 8 * MAXSZ);
     for (int i = threadIdx.x; i < nblk * npx; i += blockDim.x) sm[i] = data[first * npx + i];
+    for (int q = threadIdx.x; q < npx; q += blockDim.x) pix[q] = (q / sz) << 8 | (q % sz);
     __syncthreads();
-    if ((int)threadIdx.x >= nblk) return;
-    const float *d = sm + threadIdx.x * npx;
-    const int64_t fit = first + threadIdx.x;
+    const int g = threadIdx.x / GL, l = threadIdx.x % GL;
+    /* a group past the batch's end fits the block's first ROI again (its
+     * lanes take part in the warp's shuffles) and writes nothing */
+    const bool active = g < nblk;
+    const float *d = sm + (active ? g : 0) * npx;
+    float *px = axis_all + g * 6 * MAXSZ, *py = px + MAXSZ, *dx1 = py + MAXSZ, *dx2 = dx1 + MAXSZ,
+          *dy1 = dx2 + MAXSZ, *dy2 = dy1 + MAXSZ;
+    const int64_t fit = first + g;
 
     float theta[4];
     const float maxjump[4] = {1e0f, 1e0f, 1e2f, 2e0f};
     /* kernel_CenterofMass2D (GPUgaussLib.cuh:207-227) */
     float tx = 0.0f, ty = 0.0f, ts = 0.0f;
-    for (int ii = 0; ii < sz; ii++)
-        for (int jj = 0; jj < sz; jj++) {
-            float v = d[sz * jj + ii];
-            tx += v * ii;
-            ty += v * jj;
-            ts += v;
-        }
+    for (int p = l; p < npx; p += GL) {
+        const int ii = pix[p] >> 8, jj = pix[p] & 255; /* pixel d[sz*jj + ii] */
+        const float v = d[sz * jj + ii];
+        tx += v * ii;
+        ty += v * jj;
+        ts += v;
+    }
+    tx = group_sum(tx);
+    ty = group_sum(ty);
+    ts = group_sum(ts);
     theta[0] = tx / ts;
     theta[1] = ty / ts;
-    /* kernel_GaussFMaxMin2D (:230-258) with the distinct weights tabulated */
-    float w[2 * MAXSZ - 1];
+    /* kernel_GaussFMaxMin2D (:230-258): each lane filters its positions,
+     * with the group's table of the 2 sz - 1 distinct Gaussian weights */
+    float *w = axis_all + GROUP_FITS_PER_BLOCK * 6 * MAXSZ + g * (2 * MAXSZ);
     {
         const float norm = 1.0f / 2.0f / sigma / sigma;
-        for (int q = -(sz - 1); q <= sz - 1; ++q) w[q + sz - 1] = expf(-(float)(q * q) * norm);
+        for (int q = l - (sz - 1); q <= sz - 1; q += GL) w[q + sz - 1] = expf(-(float)(q * q) * norm);
     }
+    __syncwarp();
     float Nmax = 0.0f, MinBG = 10e10f;
-    for (int kk = 0; kk < sz; kk++)
-        for (int ll = 0; ll < sz; ll++) {
-            float fp = 0.0f, sum = 0.0f;
-            for (int ii = 0; ii < sz; ii++)
-                for (int jj = 0; jj < sz; jj++) {
-                    float ww = w[ii - kk + sz - 1] * w[ll - jj + sz - 1];
-                    fp += ww * d[ii * sz + jj];
-                    sum += ww;
-                }
-            fp /= sum;
-            Nmax = fmaxf(Nmax, fp);
-            MinBG = fminf(MinBG, fp);
-        }
+    for (int pos = l; pos < npx; pos += GL) {
+        const int kk = pix[pos] >> 8, ll = pix[pos] & 255;
+        float fp = 0.0f, sum = 0.0f;
+        for (int ii = 0; ii < sz; ii++)
+            for (int jj = 0; jj < sz; jj++) {
+                const float ww = w[ii - kk + sz - 1] * w[ll - jj + sz - 1];
+                fp += ww * d[ii * sz + jj];
+                sum += ww;
+            }
+        fp /= sum;
+        Nmax = fmaxf(Nmax, fp);
+        MinBG = fminf(MinBG, fp);
+    }
+#pragma unroll
+    for (int o = GL / 2; o > 0; o >>= 1) {
+        Nmax = fmaxf(Nmax, __shfl_xor_sync(0xffffffffu, Nmax, o));
+        MinBG = fminf(MinBG, __shfl_xor_sync(0xffffffffu, MinBG, o));
+    }
     theta[3] = MinBG;
     theta[2] = fmaxf(0.0f, (Nmax - theta[3]) * 2 * 2 * MLE_PI * sigma * sigma);
 
-    float px[MAXSZ], py[MAXSZ], dx1[MAXSZ], dx2[MAXSZ], dy1[MAXSZ], dy2[MAXSZ];
-    for (int kk = 0; kk < iterations; kk++) {
-        float num[4] = {0.0f, 0.0f, 0.0f, 0.0f}, den[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        for (int q = 0; q < sz; ++q) {
+    for (int kk = 0; kk <= iterations; kk++) {
+        /* the axis terms of theta (after the last iteration: for the Fisher
+         * information) */
+        for (int q = l; q < sz; q += GL) {
             px[q] = int_gauss(q, theta[0], sigma);
             py[q] = int_gauss(q, theta[1], sigma);
             dgauss_axis(q, theta[0], sigma, theta[2], &dx1[q], &dx2[q]);
             dgauss_axis(q, theta[1], sigma, theta[2], &dy1[q], &dy2[q]);
         }
-        for (int ii = 0; ii < sz; ii++)
-            for (int jj = 0; jj < sz; jj++) {
-                float PSFx = px[ii], PSFy = py[jj];
-                float model = theta[3] + theta[2] * PSFx * PSFy;
-                float data_v = d[sz * jj + ii];
-                float dudt[4], d2udt2[4];
-                dudt[0] = dx1[ii] * PSFy;
-                d2udt2[0] = dx2[ii] * PSFy;
-                dudt[1] = dy1[jj] * PSFx;
-                d2udt2[1] = dy2[jj] * PSFx;
-                dudt[2] = PSFx * PSFy;
-                d2udt2[2] = 0.0f;
-                dudt[3] = 1.0f;
-                d2udt2[3] = 0.0f;
-                float cf = 0.0f, df = 0.0f;
-                if (model > 10e-3f) cf = data_v / model - 1;
-                if (model > 10e-3f) df = data_v / (model * model);
-                cf = fminf(cf, 10e4f);
-                df = fminf(df, 10e4f);
-                for (int l = 0; l < 4; l++) {
-                    num[l] += dudt[l] * cf;
-                    den[l] += d2udt2[l] * cf - (dudt[l] * dudt[l]) * df;
-                }
+        __syncwarp();
+        if (kk == iterations) break;
+        float num[4] = {0.0f, 0.0f, 0.0f, 0.0f}, den[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int p = l; p < npx; p += GL) {
+            const int ii = pix[p] >> 8, jj = pix[p] & 255;
+            const float PSFx = px[ii], PSFy = py[jj];
+            const float model = theta[3] + theta[2] * PSFx * PSFy;
+            const float data_v = d[sz * jj + ii];
+            float dudt[4], d2udt2[4];
+            dudt[0] = dx1[ii] * PSFy;
+            d2udt2[0] = dx2[ii] * PSFy;
+            dudt[1] = dy1[jj] * PSFx;
+            d2udt2[1] = dy2[jj] * PSFx;
+            dudt[2] = PSFx * PSFy;
+            d2udt2[2] = 0.0f;
+            dudt[3] = 1.0f;
+            d2udt2[3] = 0.0f;
+            float cf = 0.0f, df = 0.0f;
+            if (model > 10e-3f) {
+                const float r = __frcp_rn(model); /* data/model, data/model^2 as products */
+                cf = data_v * r - 1;
+                df = data_v * r * r;
             }
+            cf = fminf(cf, 10e4f);
+            df = fminf(df, 10e4f);
+            for (int q = 0; q < 4; q++) {
+                num[q] += dudt[q] * cf;
+                den[q] += d2udt2[q] * cf - (dudt[q] * dudt[q]) * df;
+            }
+        }
+        for (int q = 0; q < 4; q++) {
+            num[q] = group_sum(num[q]);
+            den[q] = group_sum(den[q]);
+        }
+        __syncwarp(); /* every lane has read the axis rows before they change */
         theta[0] -= fminf(fmaxf(num[0] / den[0], -maxjump[0]), maxjump[0]);
         theta[1] -= fminf(fmaxf(num[1] / den[1], -maxjump[1]), maxjump[1]);
         theta[2] -= fminf(fmaxf(num[2] / den[2], -theta[2]), theta[2]);
@@ -142,34 +187,40 @@ __global__ void __launch_bounds__(FITS_PER_BLOCK) mle_xynb_kernel(
         theta[3] = fmaxf(theta[3], 0.01f);
     }
 
-    /* Fisher information, log-likelihood (cuda_gaussMLEv2.cu:104-130) */
-    float M[16];
-    for (int q = 0; q < 16; ++q) M[q] = 0.0f;
+    /* Fisher information (10 distinct entries) and log-likelihood
+     * (cuda_gaussMLEv2.cu:104-130) */
+    float F[10] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     float Div = 0.0f;
-    for (int q = 0; q < sz; ++q) {
-        px[q] = int_gauss(q, theta[0], sigma);
-        py[q] = int_gauss(q, theta[1], sigma);
-        dgauss_axis(q, theta[0], sigma, theta[2], &dx1[q], &dx2[q]);
-        dgauss_axis(q, theta[1], sigma, theta[2], &dy1[q], &dy2[q]);
-    }
-    for (int ii = 0; ii < sz; ii++)
-        for (int jj = 0; jj < sz; jj++) {
-            float PSFx = px[ii], PSFy = py[jj];
-            float model = theta[3] + theta[2] * PSFx * PSFy;
-            float data_v = d[sz * jj + ii];
-            float dudt[4] = {dx1[ii] * PSFy, dy1[jj] * PSFx, PSFx * PSFy, 1.0f};
-            for (int a = 0; a < 4; a++)
-                for (int b = a; b < 4; b++) {
-                    M[a * 4 + b] += dudt[b] * dudt[a] / model;
-                    M[b * 4 + a] = M[a * 4 + b];
-                }
-            if (model > 0) {
-                if (data_v > 0)
-                    Div += data_v * logf(model) - model - data_v * logf(data_v) + data_v;
-                else
-                    Div += -model;
-            }
+    for (int p = l; p < npx; p += GL) {
+        const int ii = pix[p] >> 8, jj = pix[p] & 255;
+        const float PSFx = px[ii], PSFy = py[jj];
+        const float model = theta[3] + theta[2] * PSFx * PSFy;
+        const float data_v = d[sz * jj + ii];
+        const float dudt[4] = {dx1[ii] * PSFy, dy1[jj] * PSFx, PSFx * PSFy, 1.0f};
+        const float rm = __frcp_rn(model);
+        int e = 0;
+        for (int a = 0; a < 4; a++)
+            for (int b = a; b < 4; b++) F[e++] += dudt[b] * dudt[a] * rm;
+        if (model > 0) {
+            if (data_v > 0)
+                Div += data_v * logf(model) - model - data_v * logf(data_v) + data_v;
+            else
+                Div += -model;
         }
+    }
+    for (int e = 0; e < 10; ++e) F[e] = group_sum(F[e]);
+    Div = group_sum(Div);
+    if (l != 0 || !active) return;
+    float M[16];
+    {
+        int e = 0;
+        for (int a = 0; a < 4; a++)
+            for (int b = a; b < 4; b++) {
+                M[a * 4 + b] = F[e];
+                M[b * 4 + a] = F[e];
+                ++e;
+            }
+    }
     /* kernel_MatInvN (MatInvLib.h:15-75): LU without pivoting, diagonal of
      * the inverse */
     const int n = 4;
@@ -222,13 +273,10 @@ extern "C" bamf_status bamf_gauss_mle_device(const float *rois, int sz, int nfit
         return BAMF_ERR_INVALID_ARG;
     if (sz > MAXSZ) return BAMF_ERR_TOO_LARGE;
     if (nfits == 0) return BAMF_OK;
-    size_t smem = (size_t)FITS_PER_BLOCK * sz * sz * sizeof(float);
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(mle_xynb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-        return clear_cuda_error();
-    int blocks = (nfits + FITS_PER_BLOCK - 1) / FITS_PER_BLOCK;
-    mle_xynb_kernel<<<blocks, FITS_PER_BLOCK, smem, (cudaStream_t)stream>>>(
+    /* a group of GL lanes per fit: 16 fits per CTA of 128 threads */
+    size_t smem = ((size_t)GROUP_FITS_PER_BLOCK * (sz * sz + 8 * MAXSZ) + (size_t)sz * sz) * sizeof(float);
+    int blocks = (nfits + GROUP_FITS_PER_BLOCK - 1) / GROUP_FITS_PER_BLOCK;
+    mle_xynb_group_kernel<<<blocks, GL * GROUP_FITS_PER_BLOCK, smem, (cudaStream_t)stream>>>(
         rois, psf_sigma, sz, iterations, params, crlb, loglik, nfits);
     return cudaGetLastError() == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;
 }

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "bamf.h"
+#include "bamf_parity_math.h"
 
 /* a failed CUDA runtime call: clear its error so that a later call on this
  * thread does not report it again */
@@ -82,4 +83,34 @@ extern "C" bamf_status bamf_probe_peaks(double *fp32_flops, double *mufu_ops)
     cudaEventDestroy(e1);
     cudaFree(out);
     return err == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;
+}
+
+/* The parity math of the exact sampler (include/bamf_parity_math.h) on the
+ * device: out[i] = f(x[i]) for f = erf (0), log (1), exp (2); a host caller
+ * compares with the same header compiled for the CPU. */
+__global__ void parity_math_kernel(const float *__restrict__ x, int n, int fn, float *__restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float v = x[i];
+    out[i] = fn == 0 ? bamf_pm_erff(v) : (fn == 1 ? bamf_pm_logf(v) : bamf_pm_expf(v));
+}
+
+extern "C" bamf_status bamf_parity_math_device(int fn, const float *x, int n, float *out)
+{
+    if (!x || !out || n < 0 || fn < 0 || fn > 2) return BAMF_ERR_INVALID_ARG;
+    if (n == 0) return BAMF_OK;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    float *d = nullptr;
+    if (cudaMalloc(&d, 2 * (size_t)n * sizeof(float)) != cudaSuccess) return clear_cuda_error();
+    bamf_status st = BAMF_OK;
+    if (cudaMemcpy(d, x, (size_t)n * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) st = BAMF_ERR_CUDA;
+    if (!st) {
+        parity_math_kernel<<<(n + 255) / 256, 256>>>(d, n, fn, d + n);
+        if (cudaMemcpy(out, d + n, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = BAMF_ERR_CUDA;
+    }
+    if (st) cudaGetLastError();
+    cudaFree(d);
+    return st;
 }

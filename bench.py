@@ -180,7 +180,18 @@ def plain_exact_bench(n_large: int = 4864) -> dict:
     return out
 
 
-def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3) -> dict:
+def gaussmle_flops_per_fit(sz: int, iterations: int) -> int:
+    """Algorithmic FP32 operations of one 'Basic' fit (an FMA counted as 2,
+    a transcendental or a reciprocal as 1): the start-up filter (sz^2
+    positions x sz^2 weighted pixels, 3 each, plus the division), every
+    Newton iteration (per pixel 25: model 3, derivatives 5, the Poisson
+    factors 5, the four num/den sums 12; per axis value 2 erf + 2 exp + 16)
+    and the Fisher information (per pixel 30) plus the 4 x 4 inversion."""
+    px = sz * sz
+    return px * px * 3 + px + iterations * (px * 25 + 2 * sz * 20) + px * 30 + 100
+
+
+def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3, fp32_peak: float | None = None) -> dict:
     """FindROI + gaussMLE on n_frames 256x256 frames (Poisson(50) emitters
     per frame, sigma 1.3, I ~ LogN(ln 1500, 0.3), bg 20; Boxsize 7, Minval
     from findROI.m:74, 10 Newton iterations).  The stack (524 MB at 2000
@@ -243,6 +254,12 @@ def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3) -> dict:
                              "algorithmic_bytes": alg},
         "maxima": count, "gaussmle_ms": tm * 1e3, "gaussmle_fits_per_s": count / tm,
         "gaussmle_achieved_gbs": count * (49 + 9) * 4.0 / tm / 1e9,
+        "gaussmle_roofline": None if not fp32_peak else {
+            "bound": "fp32 issue", "achieved": count * gaussmle_flops_per_fit(7, 10) / tm / 1e12,
+            "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+            "frac": count * gaussmle_flops_per_fit(7, 10) / tm / fp32_peak,
+            "flops_per_fit": gaussmle_flops_per_fit(7, 10),
+            "peak_source": "FP32 FMA rate measured in-process by bamf_probe_peaks"},
         "e2e": {"value": n_frames / statistics.median(e2e[1:]), "unit": "frames/s",
                 "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(d2h)},
     }
@@ -569,7 +586,7 @@ def main():
 
     frontend_block = None
     if rank == 0 and not a.no_frontend:
-        frontend_block = frontend_bench(a.frontend_frames)
+        frontend_block = frontend_bench(a.frontend_frames, fp32_peak=fp32.value)
     dense_block = None
     if rank == 0 and not a.no_dense:
         dense_block = dense_bench(a.dense_frames, a.dense_chunk)

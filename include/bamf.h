@@ -634,6 +634,13 @@ bamf_status bamf_gauss_mle_fit_host(const float *rois, int sz, int nfits, int fi
  * roofline denominators of the sampler.  Not used by any sampler path. */
 bamf_status bamf_probe_peaks(double *fp32_flops, double *mufu_ops);
 
+/* The erf (fn 0), log (1) and exp (2) of the exact sampler
+ * (include/bamf_parity_math.h) evaluated on the device for n host inputs
+ * x into host out: the same header compiled for the CPU must give the same
+ * bits (the exact sampler's parity with the reference build rests on it).
+ * Synchronous. */
+bamf_status bamf_parity_math_device(int fn, const float *x, int n, float *out);
+
 /* Known-answer check of the 5th-generation tensor-core path (tcgen05 MMA
  * from shared-memory descriptors into TMEM, read back with tcgen05.ld): a
  * 128 x 32 x 16 BF16 product of small integers.  *max_abs_err = the largest

@@ -11,23 +11,39 @@
  * sampler both call the functions below instead, so the two agree exactly;
  * the native-math flip rate is measured separately.
  *
- * Method (all in IEEE double, rounded once to float at the end):
+ * Arithmetic: single-precision operations only, carried as unevaluated sums
+ * of two floats ("double-float", T. J. Dekker, "A floating-point technique
+ * for extending the available precision", Numer. Math. 18, 1971): a product
+ * is split exactly by one fused multiply-add, a sum by Knuth's two-sum, so
+ * every intermediate holds about 46 significant bits, and the result is
+ * rounded once to float at the end.  Single-precision operations because
+ * the GPU's FP64 rate is a small fraction of its FP32 rate; 46 bits because
+ * then the float result is the correctly rounded one except in rare
+ * near-midpoint cases, as a double evaluation would give.
+ *
+ * Methods (in double-float):
  *   log : x = m * 2^e with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s),
- *         s = (m-1)/(m+1), atanh series s (1 + s^2/3 + s^4/5 + ...)
- *         (Abramowitz & Stegun 4.1.27).
- *   exp : Cody-Waite range reduction x = k ln2 + r, |r| <= ln2/2, with ln2
- *         split into float(ln2) + remainder; Taylor series of e^r to r^14.
+ *         s = (m-1)/(m+1), atanh series s (1 + s^2/3 + s^4/5 + ... + s^22/23)
+ *         (Abramowitz & Stegun 4.1.27); log x = e ln 2 + log m.
+ *   exp : Cody-Waite range reduction y = k ln2 + r, |r| <= ln2/2, with ln 2
+ *         carried in three floats (the first with 16 significant bits, so
+ *         k times it is exact); Taylor series of e^r to r^12; times 2^k.
  *   erf : A&S 7.1.6, erf a = 2/sqrt(pi) e^{-a^2} sum_n 2^n a^{2n+1}/(2n+1)!!,
- *         a series of positive terms (no cancellation), for |a| < 4;
+ *         a series of positive terms (no cancellation), for |a| < 4, with
+ *         a^2 split exactly into two floats for e^{-a^2};
  *         erf = +-1 in float for |a| >= 4 since erfc(4) < 2^-25.
  *   pow : integer exponents only (the reference's two uses), by repeated
- *         double multiplication.
- * Accuracy: the double result is within a few 1e-15 relative of the true
- * value, so the float result is the correctly rounded one except in rare
- * near-midpoint cases.  Determinism: every operation is an explicit IEEE
- * double operation (device: __dadd_rn etc., so nvcc cannot contract them;
- * host: build with -ffp-contract=off), and no table or library call differs
- * between the two sides.
+ *         double-float multiplication.
+ * Determinism: every operation is an explicit IEEE single operation (device:
+ * __fadd_rn, __fmul_rn, __fmaf_rn, __fdiv_rn, so nvcc cannot contract or
+ * reorder them; host: build with -ffp-contract=off, fmaf from libm, which is
+ * the exact fused operation on x86-64 and aarch64), the constants are
+ * double literals rounded by the compiler (IEEE round-to-nearest on both
+ * sides), and no table or library call differs between the two sides.
+ *
+ * bamf_pm_pow_fi (pow of a float to an int, as C++ promotes it to double)
+ * stays in double: the reference computes it in double, and the distances it
+ * feeds are compared in double (LibRJMCMC.cpp:534-654).
  */
 #ifndef BAMF_PARITY_MATH_H
 #define BAMF_PARITY_MATH_H
@@ -45,24 +61,25 @@
 #endif
 
 #if defined(__CUDA_ARCH__)
-#define PM_DADD(a, b) __dadd_rn((a), (b))
-#define PM_DSUB(a, b) __dsub_rn((a), (b))
+#define PM_FADD(a, b) __fadd_rn((a), (b))
+#define PM_FSUB(a, b) __fsub_rn((a), (b))
+#define PM_FMUL(a, b) __fmul_rn((a), (b))
+#define PM_FDIV(a, b) __fdiv_rn((a), (b))
+#define PM_FFMA(a, b, c) __fmaf_rn((a), (b), (c))
 #define PM_DMUL(a, b) __dmul_rn((a), (b))
-#define PM_DDIV(a, b) __ddiv_rn((a), (b))
-#define PM_D2F(a) __double2float_rn(a)
 #else
-#define PM_DADD(a, b) ((a) + (b))
-#define PM_DSUB(a, b) ((a) - (b))
+#define PM_FADD(a, b) ((float)(a) + (float)(b))
+#define PM_FSUB(a, b) ((float)(a) - (float)(b))
+#define PM_FMUL(a, b) ((float)(a) * (float)(b))
+#define PM_FDIV(a, b) ((float)(a) / (float)(b))
+#define PM_FFMA(a, b, c) fmaf((a), (b), (c))
 #define PM_DMUL(a, b) ((a) * (b))
-#define PM_DDIV(a, b) ((a) / (b))
-#define PM_D2F(a) ((float)(a))
 #endif
 
-#define BAMF_PM_LN2 0.6931471805599453           /* ln 2 rounded to double      */
-#define BAMF_PM_LN2_HI 0.693147182464599609375   /* float(ln 2), 24 bits        */
-#define BAMF_PM_LN2_LO (-1.904654299957768e-09)  /* ln 2 - LN2_HI               */
-#define BAMF_PM_INV_LN2 1.4426950408889634       /* 1 / ln 2                    */
-#define BAMF_PM_2_SQRTPI 1.1283791670955126      /* 2 / sqrt(pi)                */
+/* a double constant as two floats: hi = the nearest float, lo = the
+ * nearest float to the remainder */
+#define BAMF_PM_HI(c) ((float)(c))
+#define BAMF_PM_LO(c) ((float)((c) - (double)(float)(c)))
 
 BAMF_PM_HD uint32_t bamf_pm_f2u(float f)
 {
@@ -86,60 +103,145 @@ BAMF_PM_HD float bamf_pm_u2f(uint32_t u)
 #endif
 }
 
-BAMF_PM_HD double bamf_pm_u2d(uint64_t u)
+/* ------------------------------------------------------------ double-float */
+typedef struct bamf_pm_df {
+    float hi, lo;
+} bamf_pm_df;
+
+BAMF_PM_HD bamf_pm_df bamf_pm_df_make(float hi, float lo)
 {
-#if defined(__CUDA_ARCH__)
-    return __longlong_as_double((long long)u);
-#else
-    double d;
-    memcpy(&d, &u, 8);
-    return d;
-#endif
+    bamf_pm_df r;
+    r.hi = hi;
+    r.lo = lo;
+    return r;
 }
 
-BAMF_PM_HD double bamf_pm_floor_d(double x)
+/* |a| >= |b| (or a == 0): s + e = a + b exactly */
+BAMF_PM_HD bamf_pm_df bamf_pm_fast_two_sum(float a, float b)
 {
-#if defined(__CUDA_ARCH__)
-    return floor(x);
-#else
-    return floor(x);
-#endif
+    const float s = PM_FADD(a, b);
+    return bamf_pm_df_make(s, PM_FSUB(b, PM_FSUB(s, a)));
 }
 
-/* e^y for y in [-200, 200], in double. */
-BAMF_PM_HD double bamf_pm_exp_d(double y)
+/* s + e = a + b exactly, any order (Knuth) */
+BAMF_PM_HD bamf_pm_df bamf_pm_two_sum(float a, float b)
 {
-    double kd = bamf_pm_floor_d(PM_DADD(PM_DMUL(y, BAMF_PM_INV_LN2), 0.5));
-    double r = PM_DSUB(y, PM_DMUL(kd, BAMF_PM_LN2_HI));
-    r = PM_DSUB(r, PM_DMUL(kd, BAMF_PM_LN2_LO));
-    /* Taylor coefficients 1/n!, n = 14 .. 1; n! is exact in double here. */
-    double p = 1.0 / 87178291200.0;
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 6227020800.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 479001600.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 39916800.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 3628800.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 362880.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 40320.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 5040.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 720.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 120.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 24.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0 / 6.0);
-    p = PM_DADD(PM_DMUL(p, r), 0.5);
-    p = PM_DADD(PM_DMUL(p, r), 1.0);
-    p = PM_DADD(PM_DMUL(p, r), 1.0);
-    int k = (int)kd;
-    double scale = bamf_pm_u2d((uint64_t)(int64_t)(k + 1023) << 52);
-    return PM_DMUL(p, scale);
+    const float s = PM_FADD(a, b);
+    const float bb = PM_FSUB(s, a);
+    return bamf_pm_df_make(s, PM_FADD(PM_FSUB(a, PM_FSUB(s, bb)), PM_FSUB(b, bb)));
 }
 
-/* expf replacement. */
+BAMF_PM_HD bamf_pm_df bamf_pm_df_add(bamf_pm_df x, bamf_pm_df y)
+{
+    const bamf_pm_df s = bamf_pm_two_sum(x.hi, y.hi);
+    const float e = PM_FADD(s.lo, PM_FADD(x.lo, y.lo));
+    return bamf_pm_fast_two_sum(s.hi, e);
+}
+
+BAMF_PM_HD bamf_pm_df bamf_pm_df_mul(bamf_pm_df x, bamf_pm_df y)
+{
+    const float p = PM_FMUL(x.hi, y.hi);
+    float e = PM_FFMA(x.hi, y.hi, -p); /* exact low part of the product */
+    e = PM_FFMA(x.hi, y.lo, e);
+    e = PM_FFMA(x.lo, y.hi, e);
+    return bamf_pm_fast_two_sum(p, e);
+}
+
+BAMF_PM_HD bamf_pm_df bamf_pm_df_mul_f(bamf_pm_df x, float f)
+{
+    const float p = PM_FMUL(x.hi, f);
+    float e = PM_FFMA(x.hi, f, -p);
+    e = PM_FFMA(x.lo, f, e);
+    return bamf_pm_fast_two_sum(p, e);
+}
+
+BAMF_PM_HD bamf_pm_df bamf_pm_df_div(bamf_pm_df x, bamf_pm_df y)
+{
+    const float q1 = PM_FDIV(x.hi, y.hi);
+    const bamf_pm_df r = bamf_pm_df_add(x, bamf_pm_df_mul_f(bamf_pm_df_make(-y.hi, -y.lo), q1));
+    const float q2 = PM_FDIV(r.hi, y.hi);
+    return bamf_pm_fast_two_sum(q1, q2);
+}
+
+BAMF_PM_HD float bamf_pm_df_round(bamf_pm_df x) { return PM_FADD(x.hi, x.lo); }
+
+/* a double constant c as a double-float */
+#define BAMF_PM_DF(c) bamf_pm_df_make(BAMF_PM_HI(c), BAMF_PM_LO(c))
+
+/* ln 2 in three floats: LN2_A has 16 significant bits (k * LN2_A is exact
+ * for |k| < 2^8), LN2_B and LN2_C the rest */
+#define BAMF_PM_LN2 0.69314718055994530941723212145818
+#define BAMF_PM_LN2_A 0.693145751953125f
+#define BAMF_PM_LN2_B ((float)(BAMF_PM_LN2 - 0.693145751953125))
+#define BAMF_PM_LN2_C ((float)(BAMF_PM_LN2 - 0.693145751953125 - (double)BAMF_PM_LN2_B))
+#define BAMF_PM_INV_LN2 1.4426950408889634f
+#define BAMF_PM_2_SQRTPI 1.1283791670955125738961589031215
+
+/* e^r with r = y - k ln 2 (returned) and k (in *kout) for a double-float
+ * y with |y| <= 104: e^y = e^r * 2^k, e^r in [0.7, 1.42] */
+BAMF_PM_HD bamf_pm_df bamf_pm_exp_reduced(bamf_pm_df y, int *kout)
+{
+    const float kf = floorf(PM_FFMA(y.hi, BAMF_PM_INV_LN2, 0.5f));
+    /* r = y - k ln 2: k * LN2_A exact, the subtraction exact near y.hi */
+    bamf_pm_df r = bamf_pm_two_sum(PM_FFMA(-kf, BAMF_PM_LN2_A, y.hi), y.lo);
+    const float pb = PM_FMUL(-kf, BAMF_PM_LN2_B); /* -k LN2_B = pb + eb exactly */
+    const float eb = PM_FFMA(-kf, BAMF_PM_LN2_B, -pb);
+    r = bamf_pm_df_add(r, bamf_pm_df_make(pb, eb));
+    r = bamf_pm_df_add(r, bamf_pm_df_make(PM_FMUL(-kf, BAMF_PM_LN2_C), 0.0f));
+    /* Taylor coefficients 1/n!, n = 12 .. 2 */
+    bamf_pm_df p = BAMF_PM_DF(1.0 / 479001600.0);
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 39916800.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 3628800.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 362880.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 40320.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 5040.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 720.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 120.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 24.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), BAMF_PM_DF(1.0 / 6.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), bamf_pm_df_make(0.5f, 0.0f));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), bamf_pm_df_make(1.0f, 0.0f));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, r), bamf_pm_df_make(1.0f, 0.0f));
+    *kout = (int)kf;
+    return p;
+}
+
+/* f * 2^k in two steps (2^k alone can leave the float range); exact while
+ * the result is a normal float */
+BAMF_PM_HD float bamf_pm_scale(float f, int k)
+{
+    const int k1 = k / 2, k2 = k - k1;
+    return PM_FMUL(PM_FMUL(f, bamf_pm_u2f((uint32_t)(k1 + 127) << 23)), bamf_pm_u2f((uint32_t)(k2 + 127) << 23));
+}
+
+/* e^y as a double-float for |y| <= 16 (the erf series' e^{-a^2}) */
+BAMF_PM_HD bamf_pm_df bamf_pm_exp_df(bamf_pm_df y)
+{
+    int k;
+    const bamf_pm_df p = bamf_pm_exp_reduced(y, &k);
+    return bamf_pm_df_make(bamf_pm_scale(p.hi, k), bamf_pm_scale(p.lo, k));
+}
+
+/* expf replacement: e^r rounded to float, then scaled by 2^k (exact for a
+ * normal result).  A subnormal result (below about -87.3) is rounded
+ * directly to a multiple of 2^-149: t = e^r 2^(k+149) is formed exactly,
+ * its nearest integer n (ties to even) taken from t.hi and the sign of t.lo,
+ * and n 2^-149 returned. */
 BAMF_PM_HD float bamf_pm_expf(float x)
 {
     if (x != x) return x;
-    if (x > 100.0f) return bamf_pm_u2f(0x7f800000u);
-    if (x < -120.0f) return 0.0f;
-    return PM_D2F(bamf_pm_exp_d((double)x));
+    if (x > 89.0f) return bamf_pm_u2f(0x7f800000u);
+    if (x < -104.0f) return 0.0f;
+    int k;
+    const bamf_pm_df p = bamf_pm_exp_reduced(bamf_pm_df_make(x, 0.0f), &k);
+    const float f = bamf_pm_scale(bamf_pm_df_round(p), k);
+    if (f >= 1.17549435e-38f) return f;
+    const float th = bamf_pm_scale(p.hi, k + 149), tl = bamf_pm_scale(p.lo, k + 149);
+    float n = rintf(th);
+    const float fr = PM_FSUB(th, n); /* exact, in [-1/2, 1/2] */
+    if (fr == 0.5f && tl > 0.0f) n = PM_FADD(n, 1.0f);
+    else if (fr == -0.5f && tl < 0.0f) n = PM_FSUB(n, 1.0f);
+    return bamf_pm_scale(n, -149);
 }
 
 /* logf replacement. */
@@ -152,7 +254,7 @@ BAMF_PM_HD float bamf_pm_logf(float x)
     if (u & 0x80000000u) return bamf_pm_u2f(0x7fc00000u); /* x < 0 -> NaN  */
     int e = 0;
     if ((u & 0x7f800000u) == 0) {                      /* subnormal       */
-        x = x * 8388608.0f;                            /* * 2^23, exact   */
+        x = PM_FMUL(x, 8388608.0f);                    /* * 2^23, exact   */
         u = bamf_pm_f2u(x);
         e = -23;
     }
@@ -162,66 +264,76 @@ BAMF_PM_HD float bamf_pm_logf(float x)
         mu -= 0x00800000u;                             /* m / 2           */
         e += 1;
     }
-    double m = (double)bamf_pm_u2f(mu);
-    double s = PM_DDIV(PM_DSUB(m, 1.0), PM_DADD(m, 1.0));
-    double z = PM_DMUL(s, s);
-    double p = 1.0 / 23.0;
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 21.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 19.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 17.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 15.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 13.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 11.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 9.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 7.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 5.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0 / 3.0);
-    p = PM_DADD(PM_DMUL(p, z), 1.0);
-    double r = PM_DMUL(PM_DADD(s, s), p);
-    return PM_D2F(PM_DADD(PM_DMUL((double)e, BAMF_PM_LN2), r));
+    const float m = bamf_pm_u2f(mu);
+    const float f = PM_FSUB(m, 1.0f);                  /* exact (Sterbenz) */
+    const bamf_pm_df s = bamf_pm_df_div(bamf_pm_df_make(f, 0.0f), bamf_pm_two_sum(m, 1.0f));
+    const bamf_pm_df z = bamf_pm_df_mul(s, s);
+    bamf_pm_df p = BAMF_PM_DF(1.0 / 23.0);
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 21.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 19.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 17.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 15.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 13.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 11.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 9.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 7.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 5.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), BAMF_PM_DF(1.0 / 3.0));
+    p = bamf_pm_df_add(bamf_pm_df_mul(p, z), bamf_pm_df_make(1.0f, 0.0f));
+    const bamf_pm_df lm = bamf_pm_df_mul(bamf_pm_df_make(PM_FADD(s.hi, s.hi), PM_FADD(s.lo, s.lo)), p);
+    /* e ln 2 as a double-float: e * LN2_A exact, e * (LN2_B + LN2_C) */
+    const float ef = (float)e;
+    const float pb = PM_FMUL(ef, BAMF_PM_LN2_B); /* e LN2_B = pb + eb exactly */
+    const float eb = PM_FFMA(ef, BAMF_PM_LN2_B, -pb);
+    bamf_pm_df el = bamf_pm_two_sum(PM_FMUL(ef, BAMF_PM_LN2_A), pb);
+    el = bamf_pm_df_add(el, bamf_pm_df_make(eb, PM_FMUL(ef, BAMF_PM_LN2_C)));
+    return bamf_pm_df_round(bamf_pm_df_add(el, lm));
 }
 
-/* Reciprocals 1/(2n+3) used by the erf series; constant-folded, so the
- * host and device tables hold the same doubles. */
+/* 1/(2n+3), n = 0..95, as double-floats for the erf series: constant-folded
+ * by the compiler from double literals, so host and device hold the same
+ * floats. */
 #define BAMF_PM_ERF_NTERMS 96
 #define BAMF_PM_R(n) (1.0 / (2.0 * (n) + 3.0))
-#define BAMF_PM_R8(n) BAMF_PM_R(n), BAMF_PM_R(n + 1), BAMF_PM_R(n + 2), BAMF_PM_R(n + 3), \
-                      BAMF_PM_R(n + 4), BAMF_PM_R(n + 5), BAMF_PM_R(n + 6), BAMF_PM_R(n + 7)
-#define BAMF_PM_ERF_RECIP_INIT { BAMF_PM_R8(0), BAMF_PM_R8(8), BAMF_PM_R8(16), BAMF_PM_R8(24), \
-    BAMF_PM_R8(32), BAMF_PM_R8(40), BAMF_PM_R8(48), BAMF_PM_R8(56), BAMF_PM_R8(64),          \
-    BAMF_PM_R8(72), BAMF_PM_R8(80), BAMF_PM_R8(88) }
-
+#define BAMF_PM_R8(F, n) F(BAMF_PM_R(n)), F(BAMF_PM_R(n + 1)), F(BAMF_PM_R(n + 2)), F(BAMF_PM_R(n + 3)), \
+                         F(BAMF_PM_R(n + 4)), F(BAMF_PM_R(n + 5)), F(BAMF_PM_R(n + 6)), F(BAMF_PM_R(n + 7))
+#define BAMF_PM_RTAB(F) { BAMF_PM_R8(F, 0), BAMF_PM_R8(F, 8), BAMF_PM_R8(F, 16), BAMF_PM_R8(F, 24),  \
+    BAMF_PM_R8(F, 32), BAMF_PM_R8(F, 40), BAMF_PM_R8(F, 48), BAMF_PM_R8(F, 56), BAMF_PM_R8(F, 64), \
+    BAMF_PM_R8(F, 72), BAMF_PM_R8(F, 80), BAMF_PM_R8(F, 88) }
 #if defined(__CUDACC__)
-__device__ static const double bamf_pm_erf_recip_dev[BAMF_PM_ERF_NTERMS] = BAMF_PM_ERF_RECIP_INIT;
+__device__ static const float bamf_pm_rec_hi_dev[BAMF_PM_ERF_NTERMS] = BAMF_PM_RTAB(BAMF_PM_HI);
+__device__ static const float bamf_pm_rec_lo_dev[BAMF_PM_ERF_NTERMS] = BAMF_PM_RTAB(BAMF_PM_LO);
 #endif
-static const double bamf_pm_erf_recip_host[BAMF_PM_ERF_NTERMS] = BAMF_PM_ERF_RECIP_INIT;
+static const float bamf_pm_rec_hi_host[BAMF_PM_ERF_NTERMS] = BAMF_PM_RTAB(BAMF_PM_HI);
+static const float bamf_pm_rec_lo_host[BAMF_PM_ERF_NTERMS] = BAMF_PM_RTAB(BAMF_PM_LO);
 
 /* erff replacement. */
 BAMF_PM_HD float bamf_pm_erff(float x)
 {
     if (x != x) return x;
-    uint32_t sign = bamf_pm_f2u(x) & 0x80000000u;
-    float a = bamf_pm_u2f(bamf_pm_f2u(x) & 0x7fffffffu);
+    const uint32_t sign = bamf_pm_f2u(x) & 0x80000000u;
+    const float a = bamf_pm_u2f(bamf_pm_f2u(x) & 0x7fffffffu);
     float r;
     if (a >= 4.0f) {
         r = 1.0f;
     } else {
+        const float a2h = PM_FMUL(a, a);
+        const bamf_pm_df a2 = bamf_pm_df_make(a2h, PM_FFMA(a, a, -a2h)); /* a^2 exactly */
+        const bamf_pm_df two_a2 = bamf_pm_df_make(PM_FADD(a2.hi, a2.hi), PM_FADD(a2.lo, a2.lo));
 #if defined(__CUDA_ARCH__)
-        const double *rec = bamf_pm_erf_recip_dev;
+        const float *rh = bamf_pm_rec_hi_dev, *rl = bamf_pm_rec_lo_dev;
 #else
-        const double *rec = bamf_pm_erf_recip_host;
+        const float *rh = bamf_pm_rec_hi_host, *rl = bamf_pm_rec_lo_host;
 #endif
-        double ad = (double)a;
-        double a2 = PM_DMUL(ad, ad);          /* exact: 48 significant bits */
-        double two_a2 = PM_DADD(a2, a2);
-        double term = ad, sum = ad;
+        bamf_pm_df term = bamf_pm_df_make(a, 0.0f), sum = term;
         for (int n = 0; n < BAMF_PM_ERF_NTERMS; ++n) {
-            term = PM_DMUL(PM_DMUL(term, two_a2), rec[n]);
-            sum = PM_DADD(sum, term);
-            if (term <= PM_DMUL(sum, 1e-17)) break;
+            /* term *= 2 a^2 / (2n + 3) */
+            term = bamf_pm_df_mul(bamf_pm_df_mul(term, two_a2), bamf_pm_df_make(rh[n], rl[n]));
+            sum = bamf_pm_df_add(sum, term);
+            if (term.hi <= PM_FMUL(sum.hi, 7e-15f)) break;
         }
-        double e = bamf_pm_exp_d(-a2);
-        r = PM_D2F(PM_DMUL(PM_DMUL(BAMF_PM_2_SQRTPI, e), sum));
+        const bamf_pm_df e = bamf_pm_exp_df(bamf_pm_df_make(-a2.hi, -a2.lo));
+        r = bamf_pm_df_round(bamf_pm_df_mul(bamf_pm_df_mul(BAMF_PM_DF(BAMF_PM_2_SQRTPI), e), sum));
     }
     return bamf_pm_u2f(bamf_pm_f2u(r) | sign);
 }
@@ -232,11 +344,11 @@ BAMF_PM_HD float bamf_pm_erff(float x)
 BAMF_PM_HD float bamf_pm_powf(float x, float y)
 {
     if (y != y || x != x) return bamf_pm_u2f(0x7fc00000u);
-    int n = (int)y;
+    const int n = (int)y;
     if ((float)n != y || n < 0 || n > 64) return bamf_pm_u2f(0x7fc00000u);
-    double xd = (double)x, r = 1.0;
-    for (int i = 0; i < n; ++i) r = PM_DMUL(r, xd);
-    return PM_D2F(r);
+    bamf_pm_df r = bamf_pm_df_make(1.0f, 0.0f);
+    for (int i = 0; i < n; ++i) r = bamf_pm_df_mul_f(r, x);
+    return bamf_pm_df_round(r);
 }
 
 /* pow(float, int) as C++ evaluates it (promoted to double); only n == 2

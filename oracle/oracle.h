@@ -61,6 +61,9 @@ int oracle_gaussmle_xynb_f64(const float *rois, int sz, int nfits, double psf_si
                              int iterations, double *params, double *crlb, double *loglik,
                              int threads);
 
+/* the parity math (include/bamf_parity_math.h) on the host: 0 erf, 1 log, 2 exp */
+int oracle_parity_math(int fn, const float *x, int n, float *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1365,3 +1365,13 @@ int oracle_rjmcmc_batch(const float *data, const int64_t *offsets, const int32_t
     free(th);
     return BAMF_OK;
 }
+
+/* The parity math on the host, for the device comparison (fn: 0 erf,
+ * 1 log, 2 exp). */
+int oracle_parity_math(int fn, const float *x, int n, float *out)
+{
+    if (!x || !out || n < 0 || fn < 0 || fn > 2) return BAMF_ERR_INVALID_ARG;
+    for (int i = 0; i < n; ++i)
+        out[i] = fn == 0 ? bamf_pm_erff(x[i]) : (fn == 1 ? bamf_pm_logf(x[i]) : bamf_pm_expf(x[i]));
+    return BAMF_OK;
+}
