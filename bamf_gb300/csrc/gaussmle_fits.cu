@@ -6,8 +6,13 @@
  * GPUgaussLib.cuh:14-258 and MatInvLib.h:15-75).  CCD 'Basic' has its own
  * optimised kernel (gaussmle.cu).
  *
- * One thread per fit, the block's ROIs staged through shared memory with
- * coalesced loads.  Parameters theta: 0 = position along the contiguous
+ * One group of 8 lanes per fit (four fits per warp), the block's ROIs staged
+ * through shared memory with coalesced loads; lane l of a group evaluates
+ * pixels l, l + 8, ..., and the group's partial sums (centre of mass,
+ * Newton numerators and denominators, Fisher information, log-likelihood)
+ * and the start-up filter's maximum and minimum are combined by butterfly
+ * shuffles, so all lanes of a group carry the same parameters.  Parameters
+ * theta: 0 = position along the contiguous
  * ROI axis (MATLAB rows: Results.Y), 1 = the other axis (Results.X),
  * 2 = photons, 3 = background, then
  *   Sigma:   4 = sigma of a symmetric PSF
@@ -19,8 +24,9 @@
  * ROI's box corner) enters as cf = (data - model)/(model + g),
  * df = (data + g)/(model + g)^2.  The reference's CRLB / log-likelihood pass
  * does not re-read g per pixel: it uses the value left from the last pixel
- * of the last Newton iteration, and so does this code (0 when there are no
- * iterations, where the reference reads an uninitialised value).
+ * of the last Newton iteration, (sz-1, sz-1), and so does this code (0 when
+ * there are no iterations, where the reference reads an uninitialised
+ * value).
  */
 #include <cuda_runtime.h>
 
@@ -29,7 +35,7 @@
 namespace {
 
 constexpr int MAXSZ = 21;
-constexpr int FITS_PER_BLOCK = 64;
+constexpr int FITS_PER_BLOCK = 16; /* fits per CTA, 8 lanes each */
 #define MLE_PI 3.141592f
 
 struct ZPar {
@@ -137,8 +143,17 @@ __device__ __forceinline__ void pixel(int ii, int jj, const float *th, float sig
     }
 }
 
+constexpr int GL = 8; /* lanes per fit: four fits per warp */
+
+__device__ __forceinline__ float group_sum(float v)
+{
+#pragma unroll
+    for (int o = GL / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 template <int FIT, bool SCMOS>
-__global__ void __launch_bounds__(FITS_PER_BLOCK) mle_fit_kernel(
+__global__ void __launch_bounds__(GL * FITS_PER_BLOCK) mle_fit_kernel(
     const float *__restrict__ data, float sigma, ZPar zp, const float *__restrict__ coords,
     const float *__restrict__ gmap, int mapsz, int sz, int iterations, float *__restrict__ P,
     float *__restrict__ CRLB, float *__restrict__ LL, int nfits)
@@ -148,11 +163,19 @@ __global__ void __launch_bounds__(FITS_PER_BLOCK) mle_fit_kernel(
     const int npx = sz * sz;
     const int64_t first = (int64_t)blockIdx.x * FITS_PER_BLOCK;
     const int nblk = (int)min((int64_t)FITS_PER_BLOCK, (int64_t)nfits - first);
+    /* staged ROIs, then per fit the start-up filter's weight table, then the
+     * pixel -> (ii, jj) table (ii << 8 | jj) */
+    float *wt = sm + FITS_PER_BLOCK * npx;
+    int *pix = (int *)(wt + FITS_PER_BLOCK * (2 * MAXSZ));
     for (int i = threadIdx.x; i < nblk * npx; i += blockDim.x) sm[i] = data[first * npx + i];
+    for (int q = threadIdx.x; q < npx; q += blockDim.x) pix[q] = (q / sz) << 8 | (q % sz);
     __syncthreads();
-    if ((int)threadIdx.x >= nblk) return;
-    const float *d = sm + threadIdx.x * npx;
-    const int64_t fit = first + threadIdx.x;
+    const int g = threadIdx.x / GL, l = threadIdx.x % GL;
+    /* a group past the batch's end fits the block's first ROI again (its
+     * lanes take part in the warp's shuffles) and writes nothing */
+    const bool active = g < nblk;
+    const float *d = sm + (active ? g : 0) * npx;
+    const int64_t fit = first + (active ? g : 0);
     float c0 = 0.0f, c1 = 0.0f;
     if (SCMOS) {
         c0 = coords[2 * fit];
@@ -161,38 +184,45 @@ __global__ void __launch_bounds__(FITS_PER_BLOCK) mle_fit_kernel(
 
     float th[6];
     float maxjump[6] = {1e0f, 1e0f, 1e2f, 2e0f, FIT == BAMF_FIT_SIGMA ? 5e-1f : 1e-1f, 1e-1f};
-    /* kernel_CenterofMass2D (GPUgaussLib.cuh:207-227) */
+    /* kernel_CenterofMass2D (GPUgaussLib.cuh:207-227): lane partial sums */
     float tx = 0.0f, ty = 0.0f, ts = 0.0f;
-    for (int ii = 0; ii < sz; ii++)
-        for (int jj = 0; jj < sz; jj++) {
-            float v = d[sz * jj + ii];
-            tx += v * ii;
-            ty += v * jj;
-            ts += v;
-        }
-    th[0] = tx / ts;
-    th[1] = ty / ts;
-    /* kernel_GaussFMaxMin2D (:230-258), distinct weights tabulated */
+    for (int p = l; p < npx; p += GL) {
+        const int ii = pix[p] >> 8, jj = pix[p] & 255;
+        const float v = d[sz * jj + ii];
+        tx += v * ii;
+        ty += v * jj;
+        ts += v;
+    }
+    th[0] = group_sum(tx) / group_sum(ts);
+    th[1] = group_sum(ty) / group_sum(ts);
+    /* kernel_GaussFMaxMin2D (:230-258): each lane filters its positions with
+     * the group's table of the distinct weights */
     const float s_init = FIT == BAMF_FIT_Z ? zp.sx : sigma;
-    float w[2 * MAXSZ - 1];
+    float *w = wt + g * (2 * MAXSZ);
     {
         const float norm = 1.0f / 2.0f / s_init / s_init;
-        for (int q = -(sz - 1); q <= sz - 1; ++q) w[q + sz - 1] = expf(-(float)(q * q) * norm);
+        for (int q = l - (sz - 1); q <= sz - 1; q += GL) w[q + sz - 1] = expf(-(float)(q * q) * norm);
     }
+    __syncwarp();
     float Nmax = 0.0f, MinBG = 10e10f;
-    for (int kk = 0; kk < sz; kk++)
-        for (int ll = 0; ll < sz; ll++) {
-            float fp = 0.0f, sum = 0.0f;
-            for (int ii = 0; ii < sz; ii++)
-                for (int jj = 0; jj < sz; jj++) {
-                    float ww = w[ii - kk + sz - 1] * w[ll - jj + sz - 1];
-                    fp += ww * d[ii * sz + jj];
-                    sum += ww;
-                }
-            fp /= sum;
-            Nmax = fmaxf(Nmax, fp);
-            MinBG = fminf(MinBG, fp);
-        }
+    for (int pos = l; pos < npx; pos += GL) {
+        const int kk = pix[pos] >> 8, ll = pix[pos] & 255;
+        float fp = 0.0f, sum = 0.0f;
+        for (int ii = 0; ii < sz; ii++)
+            for (int jj = 0; jj < sz; jj++) {
+                float ww = w[ii - kk + sz - 1] * w[ll - jj + sz - 1];
+                fp += ww * d[ii * sz + jj];
+                sum += ww;
+            }
+        fp /= sum;
+        Nmax = fmaxf(Nmax, fp);
+        MinBG = fminf(MinBG, fp);
+    }
+#pragma unroll
+    for (int o = GL / 2; o > 0; o >>= 1) {
+        Nmax = fmaxf(Nmax, __shfl_xor_sync(0xffffffffu, Nmax, o));
+        MinBG = fminf(MinBG, __shfl_xor_sync(0xffffffffu, MinBG, o));
+    }
     th[3] = MinBG;
     if (FIT == BAMF_FIT_Z) {
         th[2] = fmaxf(0.0f, (Nmax - th[3]) * 2 * MLE_PI * zp.sx * zp.sy * sqrtf(2.0f));
@@ -203,33 +233,36 @@ __global__ void __launch_bounds__(FITS_PER_BLOCK) mle_fit_kernel(
         th[5] = sigma;
     }
 
-    float gR = 0.0f; /* variance-gain ratio of the last pixel visited */
     for (int kk = 0; kk < iterations; kk++) {
         float num[6] = {0, 0, 0, 0, 0, 0}, den[6] = {0, 0, 0, 0, 0, 0};
-        for (int ii = 0; ii < sz; ii++)
-            for (int jj = 0; jj < sz; jj++) {
-                float PSFx, PSFy, du[6], d2u[6];
-                pixel<FIT>(ii, jj, th, sigma, zp, &PSFx, &PSFy, du, d2u);
-                float model = th[3] + th[2] * PSFx * PSFy;
-                float dv = d[sz * jj + ii];
-                float cf = 0.0f, df = 0.0f;
-                if (SCMOS) {
-                    int gi = (int)((c1 + jj) * mapsz + c0 + ii);
-                    gi = min(max(gi, 0), mapsz * mapsz - 1); /* corners outside the map: edge value */
-                    gR = gmap[gi];
-                    if (model > 10e-3f) cf = (dv - model) / (model + gR);
-                    if (model > 10e-3f) df = (dv + gR) / ((model + gR) * (model + gR));
-                } else {
-                    if (model > 10e-3f) cf = dv / model - 1;
-                    if (model > 10e-3f) df = dv / (model * model);
-                }
-                cf = fminf(cf, 10e4f);
-                df = fminf(df, 10e4f);
-                for (int l = 0; l < NV; l++) {
-                    num[l] += du[l] * cf;
-                    den[l] += d2u[l] * cf - (du[l] * du[l]) * df;
-                }
+        for (int p = l; p < npx; p += GL) {
+            const int ii = pix[p] >> 8, jj = pix[p] & 255;
+            float PSFx, PSFy, du[6], d2u[6];
+            pixel<FIT>(ii, jj, th, sigma, zp, &PSFx, &PSFy, du, d2u);
+            float model = th[3] + th[2] * PSFx * PSFy;
+            float dv = d[sz * jj + ii];
+            float cf = 0.0f, df = 0.0f;
+            if (SCMOS) {
+                int gi = (int)((c1 + jj) * mapsz + c0 + ii);
+                gi = min(max(gi, 0), mapsz * mapsz - 1); /* corners outside the map: edge value */
+                const float gRp = gmap[gi];
+                if (model > 10e-3f) cf = (dv - model) / (model + gRp);
+                if (model > 10e-3f) df = (dv + gRp) / ((model + gRp) * (model + gRp));
+            } else {
+                if (model > 10e-3f) cf = dv / model - 1;
+                if (model > 10e-3f) df = dv / (model * model);
             }
+            cf = fminf(cf, 10e4f);
+            df = fminf(df, 10e4f);
+            for (int q = 0; q < NV; q++) {
+                num[q] += du[q] * cf;
+                den[q] += d2u[q] * cf - (du[q] * du[q]) * df;
+            }
+        }
+        for (int q = 0; q < NV; q++) {
+            num[q] = group_sum(num[q]);
+            den[q] = group_sum(den[q]);
+        }
         th[0] -= fminf(fmaxf(num[0] / den[0], -maxjump[0]), maxjump[0]);
         th[1] -= fminf(fmaxf(num[1] / den[1], -maxjump[1]), maxjump[1]);
         th[2] -= fminf(fmaxf(num[2] / den[2], -th[2]), th[2]);
@@ -248,37 +281,57 @@ __global__ void __launch_bounds__(FITS_PER_BLOCK) mle_fit_kernel(
             th[5] = fminf(th[5], sz / 2.0f);
         }
     }
+    /* the reference's CRLB / log-likelihood pass uses the variance-gain
+     * ratio left from the last pixel of the last iteration, (sz-1, sz-1) */
+    float gR = 0.0f;
+    if (SCMOS && iterations > 0) {
+        int gi = (int)((c1 + (sz - 1)) * mapsz + c0 + (sz - 1));
+        gR = gmap[min(max(gi, 0), mapsz * mapsz - 1)];
+    }
 
-    /* Fisher information and log-likelihood */
-    float M[NV * NV];
-    for (int q = 0; q < NV * NV; ++q) M[q] = 0.0f;
+    /* Fisher information (distinct entries, lane partial sums) and
+     * log-likelihood */
+    constexpr int NF = NV * (NV + 1) / 2;
+    float F[NF];
+    for (int q = 0; q < NF; ++q) F[q] = 0.0f;
     float Div = 0.0f;
-    for (int ii = 0; ii < sz; ii++)
-        for (int jj = 0; jj < sz; jj++) {
-            float PSFx, PSFy, du[6];
-            pixel<FIT>(ii, jj, th, sigma, zp, &PSFx, &PSFy, du, nullptr);
-            float model = th[3] + th[2] * PSFx * PSFy;
-            float dv = d[sz * jj + ii];
-            float den = SCMOS ? model + gR : model;
-            for (int a = 0; a < NV; a++)
-                for (int b = a; b < NV; b++) {
-                    M[a * NV + b] += du[b] * du[a] / den;
-                    M[b * NV + a] = M[a * NV + b];
-                }
-            if (SCMOS) {
-                if (model + gR > 0) {
-                    if (dv + gR > 0)
-                        Div += (dv + gR) * logf(model + gR) - model - (dv + gR) * logf(dv + gR) + dv;
-                    else
-                        Div += -model - gR;
-                }
-            } else if (model > 0) {
-                if (dv > 0)
-                    Div += dv * logf(model) - model - dv * logf(dv) + dv;
+    for (int p = l; p < npx; p += GL) {
+        const int ii = pix[p] >> 8, jj = pix[p] & 255;
+        float PSFx, PSFy, du[6];
+        pixel<FIT>(ii, jj, th, sigma, zp, &PSFx, &PSFy, du, nullptr);
+        float model = th[3] + th[2] * PSFx * PSFy;
+        float dv = d[sz * jj + ii];
+        float den = SCMOS ? model + gR : model;
+        int e = 0;
+        for (int a = 0; a < NV; a++)
+            for (int b = a; b < NV; b++) F[e++] += du[b] * du[a] / den;
+        if (SCMOS) {
+            if (model + gR > 0) {
+                if (dv + gR > 0)
+                    Div += (dv + gR) * logf(model + gR) - model - (dv + gR) * logf(dv + gR) + dv;
                 else
-                    Div += -model;
+                    Div += -model - gR;
             }
+        } else if (model > 0) {
+            if (dv > 0)
+                Div += dv * logf(model) - model - dv * logf(dv) + dv;
+            else
+                Div += -model;
         }
+    }
+    for (int q = 0; q < NF; ++q) F[q] = group_sum(F[q]);
+    Div = group_sum(Div);
+    if (l != 0 || !active) return;
+    float M[NV * NV];
+    {
+        int e = 0;
+        for (int a = 0; a < NV; a++)
+            for (int b = a; b < NV; b++) {
+                M[a * NV + b] = F[e];
+                M[b * NV + a] = F[e];
+                ++e;
+            }
+    }
     /* inverse by LU without pivoting (the order of MatInvLib.h:15-75),
      * diagonal only */
     float Minv[NV * NV], yy[NV], tmp1 = 0.0f;
@@ -324,15 +377,15 @@ template <int FIT, bool SCMOS>
 cudaError_t launch(const float *rois, int sz, int nfits, float sigma, const ZPar &zp, const float *coords,
                    const float *gmap, int mapsz, int iterations, float *P, float *C, float *L, cudaStream_t s)
 {
-    size_t smem = (size_t)FITS_PER_BLOCK * sz * sz * sizeof(float);
+    size_t smem = ((size_t)FITS_PER_BLOCK * (sz * sz + 2 * MAXSZ) + (size_t)sz * sz) * sizeof(float);
     if (smem > 48 * 1024) {
         cudaError_t e =
             cudaFuncSetAttribute(mle_fit_kernel<FIT, SCMOS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     int blocks = (nfits + FITS_PER_BLOCK - 1) / FITS_PER_BLOCK;
-    mle_fit_kernel<FIT, SCMOS><<<blocks, FITS_PER_BLOCK, smem, s>>>(rois, sigma, zp, coords, gmap, mapsz, sz,
-                                                                    iterations, P, C, L, nfits);
+    mle_fit_kernel<FIT, SCMOS><<<blocks, GL * FITS_PER_BLOCK, smem, s>>>(rois, sigma, zp, coords, gmap, mapsz, sz,
+                                                                         iterations, P, C, L, nfits);
     return cudaGetLastError();
 }
 
