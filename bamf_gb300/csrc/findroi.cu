@@ -29,17 +29,71 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
+#include <mutex>
+#include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "bamf.h"
 
 namespace {
 
+/* rb0 = RN(1/b0); the fused filter divides by b0 through rb0 (div_fast)
+ * for |q| in [lo, hi], and with IEEE division elsewhere (lo = +inf: never
+ * through rb0). */
 struct Coef {
-    float b0, b1, b2, b3, B;
+    float b0, b1, b2, b3, B, rb0, lo, hi;
 };
+
+/* Division by the constant b0 with one multiply and two FMAs (Markstein,
+ * "Computation of elementary functions on the IBM RISC System/6000
+ * processor", IBM J. Res. Dev. 34(1), 1990): q0 = RN(q*rb0), the residual
+ * b0*q0 - q in one FMA, the corrected quotient RN(q0 - residual*rb0); a zero
+ * q keeps its sign.  The sequence is invariant under scaling q by a power of
+ * two while no intermediate leaves the normal range, which holds for |q| in
+ * [2^-100, 2^100] and b0 in [2^-20, 2^20]; so it equals RN(q/b0) on that whole
+ * range iff it does for the 2^23 significands of [1, 2), which
+ * fast_division_exact checks on the host, once per divisor. */
+__host__ __device__ __forceinline__ float div_fast(float q, float b0, float rb0)
+{
+#ifdef __CUDA_ARCH__
+    const float q0 = __fmul_rn(q, rb0);
+    return __fmaf_rn(-__fmaf_rn(b0, q0, -q), rb0, q0);
+#else
+    const float q0 = q * rb0;
+    return std::fma(-std::fma(b0, q0, -q), rb0, q0);
+#endif
+}
+
+bool fast_division_exact(float b0, float rb0)
+{
+    if (!(std::fabs(b0) >= 0x1p-20f && std::fabs(b0) <= 0x1p20f)) return false;
+    static std::mutex mu;
+    static std::vector<std::pair<float, bool>> seen;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto &s : seen)
+        if (std::memcmp(&s.first, &b0, sizeof b0) == 0) return s.second;
+    constexpr int NT = 8;
+    std::atomic<bool> ok{true};
+    std::vector<std::thread> th;
+    for (int k = 0; k < NT; ++k)
+        th.emplace_back([&, k] {
+            for (uint32_t m = (uint32_t)k; m < (1u << 23) && ok.load(std::memory_order_relaxed); m += NT) {
+                const uint32_t bits = 0x3f800000u | m;
+                float q;
+                std::memcpy(&q, &bits, sizeof q);
+                const float want = q / b0, got = div_fast(q, b0, rb0);
+                if (std::memcmp(&want, &got, sizeof got) != 0) ok = false;
+            }
+        });
+    for (auto &t : th) t.join();
+    seen.emplace_back(b0, ok.load());
+    return ok.load();
+}
 
 /* findROI.m:169-182 in double; the kernel receives singles. */
 Coef iir_coef(double Sigma)
@@ -55,13 +109,23 @@ Coef iir_coef(double Sigma)
     double B2 = -1.4281 * Qq - 1.26661 * Qqq;
     double B3 = 0.422205 * Qqq;
     double B = 1 - (B1 + B2 + B3) / B0;
-    return Coef{(float)B0, (float)B1, (float)B2, (float)B3, (float)B};
+    Coef c{(float)B0, (float)B1, (float)B2, (float)B3, (float)B, 0.0f, INFINITY, 0.0f};
+    c.rb0 = 1.0f / c.b0;
+    if (fast_division_exact(c.b0, c.rb0)) {
+        c.lo = 0x1p-100f;
+        c.hi = 0x1p100f;
+    }
+    return c;
+}
+
+__device__ __forceinline__ float iir_q(float w1, float w2, float w3, const Coef &c)
+{
+    return __fmaf_rn(c.b3, w3, __fmaf_rn(c.b1, w1, __fmul_rn(c.b2, w2)));
 }
 
 __device__ __forceinline__ float iir_step(float w0, float w1, float w2, float w3, const Coef &c)
 {
-    float q = __fmaf_rn(c.b3, w3, __fmaf_rn(c.b1, w1, __fmul_rn(c.b2, w2)));
-    return __fmaf_rn(w0, c.B, __fdiv_rn(q, c.b0));
+    return __fmaf_rn(w0, c.B, __fdiv_rn(iir_q(w1, w2, w3, c), c.b0));
 }
 
 /* Pass 1: one thread per (frame, row) runs the row's recurrence for both
@@ -224,83 +288,498 @@ __global__ void __launch_bounds__(128) cols_kernel(float *__restrict__ a, float 
     }
 }
 
+/* Passes 1 and 2 fused, for whole frames (frames of up to FF_MAX_SLOT
+ * pixels per intermediate image; larger frames take rows_kernel +
+ * cols_kernel).  One CTA owns one frame at a time, persistent over the
+ * stack, and keeps the frame's two intermediate images in its own slot of
+ * `scratch`: column-major, pixel (r, j) at j*YP + r with YP = Y rounded up to
+ * 32, 2*X*YP floats.  The grid's slots together stay within L2, so only the
+ * frames are read from DRAM and only the DoG is written.  The recurrences
+ * run exactly as in rows_kernel / cols_kernel (bit-identical results):
+ *   rows, forward:  thread r walks its row through shared-memory chunks of
+ *                   FF_CW columns (cp.async, double-buffered) and writes each
+ *                   output to the slot (consecutive r: coalesced)
+ *   rows, backward: the slot's chunks come back through shared memory, last
+ *                   first; outputs overwrite the forward ones in place
+ *   cols, forward:  tiles of FF_CW rows x FF_T columns, [column][FF_TS]:
+ *                   thread c walks column c in float4 steps (conflict-free),
+ *                   results go back into the tile and the tile to the slot
+ *   cols, backward: the same, last tile first, the DoG written to `dog` in
+ *                   frame layout (consecutive c: coalesced) */
+constexpr int FF_T = 256;   /* threads: rows of a row group / columns of a column group */
+constexpr int FF_CW = 32;   /* columns per row-pass chunk, rows per column-pass tile */
+constexpr int FF_TS = 36;   /* tile row stride in floats: 16-byte rows, float4 reads conflict-free */
+constexpr size_t FF_MAX_SLOT = 80 * 1024; /* pixels per image in a slot (X * YP) */
+constexpr int FF_SMEM_FLOATS = 2 * 2 * FF_T * FF_TS; /* the largest phase: column tiles */
+
+/* L2 eviction priorities: the frames and the DoG stream through L2 once
+ * (evict first); the slots are reused all the time (evict last) and are
+ * discarded at the end of each frame instead of being written back. */
+__device__ __forceinline__ uint64_t l2_evict_first()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ uint64_t l2_evict_last()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ void cp_async16(float *smem, const float *gmem, uint64_t pol)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "l"(pol)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(float *smem, const float *gmem, uint64_t pol)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "l"(pol)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+/* all but the most recent group landed */
+__device__ __forceinline__ void cp_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+__device__ __forceinline__ void st_hint(float *g, float v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(g), "f"(v), "l"(pol));
+}
+
+__device__ __forceinline__ void st4_hint(float *g, float4 v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(g), "f"(v.x), "f"(v.y),
+                 "f"(v.z), "f"(v.w), "l"(pol));
+}
+
+__device__ __forceinline__ void discard_line(const float *g)
+{
+    asm volatile("discard.global.L2 [%0], 128;" ::"l"(g) : "memory");
+}
+
+struct IirState {
+    float w1, w2, w3;
+    __device__ __forceinline__ void init(float v) { w1 = w2 = w3 = v; }
+    __device__ __forceinline__ void push(float o)
+    {
+        w3 = w2;
+        w2 = w1;
+        w1 = o;
+    }
+    /* one step, IEEE division */
+    __device__ __forceinline__ float step(float w0, const Coef &c)
+    {
+        const float o = iir_step(w0, w1, w2, w3, c);
+        push(o);
+        return o;
+    }
+    /* one step, division through rb0; `slow` records a q outside [lo, hi] */
+    __device__ __forceinline__ float step_fast(float w0, const Coef &c, bool &slow)
+    {
+        const float q = iir_q(w1, w2, w3, c);
+        slow |= !(fabsf(q) >= c.lo && fabsf(q) <= c.hi);
+        const float o = __fmaf_rn(w0, c.B, div_fast(q, c.b0, c.rb0));
+        push(o);
+        return o;
+    }
+};
+
+/* Four steps of both recurrences, inputs xa / xb to outputs ya / yb in
+ * processing order.  A block in which any q left [lo, hi] is redone from
+ * its saved state with IEEE division, so every output is the one iir_step
+ * gives. */
+__device__ __forceinline__ void steps4(IirState &a, IirState &b, const Coef &ca, const Coef &cb,
+                                       const float (&xa)[4], const float (&xb)[4], float (&ya)[4], float (&yb)[4])
+{
+    const IirState a0 = a, b0 = b;
+    bool slow = false;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        ya[u] = a.step_fast(xa[u], ca, slow);
+        yb[u] = b.step_fast(xb[u], cb, slow);
+    }
+    if (slow) {
+        a = a0;
+        b = b0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            ya[u] = a.step(xa[u], ca);
+            yb[u] = b.step(xb[u], cb);
+        }
+    }
+}
+
+template <bool VEC>
+__global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict__ in, float *__restrict__ dog,
+                                                         float *__restrict__ scratch, int X, int Y, int Z, int YP,
+                                                         Coef ca, Coef cb)
+{
+    extern __shared__ __align__(16) float fsm[];
+    const int t = threadIdx.x;
+    const uint64_t pf = l2_evict_first(), pl = l2_evict_last();
+    const size_t img = (size_t)X * YP;
+    float *FA = scratch + (size_t)blockIdx.x * 2 * img, *FB = FA + img;
+    const int nch = (X + FF_CW - 1) / FF_CW, nq = (Y + FF_CW - 1) / FF_CW;
+    for (int z = blockIdx.x; z < Z; z += gridDim.x) {
+        const float *fin = in + (size_t)z * X * Y;
+        for (int rg = 0; rg < Y; rg += FF_T) {
+            const int nr = min(FF_T, Y - rg), r = rg + t;
+            const bool mine = t < nr;
+            IirState a, b;
+            /* ---- rows, forward: input chunk [row][FF_TS] */
+            auto stage_in = [&](int c, float *buf) {
+                const int c0 = c * FF_CW, w = min(FF_CW, X - c0);
+                if (VEC) {
+                    const int p = t & 7;
+                    if (4 * p < w)
+                        for (int i = t >> 3; i < nr; i += FF_T / 8)
+                            cp_async16(buf + i * FF_TS + 4 * p, fin + (size_t)(rg + i) * X + c0 + 4 * p, pf);
+                } else {
+                    const int p = t & 31;
+                    if (p < w)
+                        for (int i = t >> 5; i < nr; i += FF_T / 32)
+                            cp_async4(buf + i * FF_TS + p, fin + (size_t)(rg + i) * X + c0 + p, pf);
+                }
+            };
+            stage_in(0, fsm);
+            cp_commit();
+            for (int c = 0; c < nch; ++c) {
+                if (c + 1 < nch) stage_in(c + 1, fsm + ((c + 1) & 1) * FF_T * FF_TS);
+                cp_commit();
+                cp_wait_prev();
+                __syncthreads();
+                const float *ti = fsm + (c & 1) * FF_T * FF_TS + t * FF_TS;
+                const int c0 = c * FF_CW, w = min(FF_CW, X - c0);
+                if (mine) {
+                    if (c == 0) {
+                        a.init(ti[0]);
+                        b.init(ti[0]);
+                    }
+                    float *pa = FA + (size_t)c0 * YP + r, *pb = FB + (size_t)c0 * YP + r;
+                    if (w == FF_CW) {
+#pragma unroll 1
+                        for (int j4 = 0; j4 < FF_CW; j4 += 4) {
+                            const float4 v = *reinterpret_cast<const float4 *>(ti + j4);
+                            const float x[4] = {v.x, v.y, v.z, v.w};
+                            float ya[4], yb[4];
+                            steps4(a, b, ca, cb, x, x, ya, yb);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                st_hint(pa + (size_t)(j4 + u) * YP, ya[u], pl);
+                                st_hint(pb + (size_t)(j4 + u) * YP, yb[u], pl);
+                            }
+                        }
+                    } else {
+                        for (int j = 0; j < w; ++j) {
+                            st_hint(pa + (size_t)j * YP, a.step(ti[j], ca), pl);
+                            st_hint(pb + (size_t)j * YP, b.step(ti[j], cb), pl);
+                        }
+                    }
+                }
+                __syncthreads(); /* buffer c & 1 is restaged for chunk c + 2 */
+            }
+            /* ---- rows, backward: slot chunks [sigma][column][row] */
+            constexpr int BUF = 2 * FF_CW * FF_T;
+            auto stage_f = [&](int c, float *buf) {
+                const int c0 = c * FF_CW, w = min(FF_CW, X - c0), n4 = (nr + 3) >> 2;
+                const int q4 = t & 63;
+                if (q4 < n4)
+                    for (int j = t >> 6; j < w; j += FF_T / 64) {
+                        cp_async16(buf + j * FF_T + 4 * q4, FA + (size_t)(c0 + j) * YP + rg + 4 * q4, pl);
+                        cp_async16(buf + (FF_CW + j) * FF_T + 4 * q4, FB + (size_t)(c0 + j) * YP + rg + 4 * q4, pl);
+                    }
+            };
+            stage_f(nch - 1, fsm);
+            cp_commit();
+            for (int ci = 0; ci < nch; ++ci) {
+                const int c = nch - 1 - ci;
+                if (c > 0) stage_f(c - 1, fsm + ((ci + 1) & 1) * BUF);
+                cp_commit();
+                cp_wait_prev();
+                __syncthreads();
+                const float *fa = fsm + (ci & 1) * BUF + t, *fb = fa + FF_CW * FF_T;
+                const int c0 = c * FF_CW, w = min(FF_CW, X - c0);
+                if (mine) {
+                    if (ci == 0) {
+                        a.init(fa[(w - 1) * FF_T]);
+                        b.init(fb[(w - 1) * FF_T]);
+                    }
+                    float *pa = FA + (size_t)c0 * YP + r, *pb = FB + (size_t)c0 * YP + r;
+                    if (w == FF_CW) {
+#pragma unroll 1
+                        for (int j4 = FF_CW - 4; j4 >= 0; j4 -= 4) {
+                            const float xa[4] = {fa[(j4 + 3) * FF_T], fa[(j4 + 2) * FF_T], fa[(j4 + 1) * FF_T],
+                                                 fa[j4 * FF_T]};
+                            const float xb[4] = {fb[(j4 + 3) * FF_T], fb[(j4 + 2) * FF_T], fb[(j4 + 1) * FF_T],
+                                                 fb[j4 * FF_T]};
+                            float ya[4], yb[4];
+                            steps4(a, b, ca, cb, xa, xb, ya, yb);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                st_hint(pa + (size_t)(j4 + 3 - u) * YP, ya[u], pl);
+                                st_hint(pb + (size_t)(j4 + 3 - u) * YP, yb[u], pl);
+                            }
+                        }
+                    } else {
+                        for (int j = w - 1; j >= 0; --j) {
+                            st_hint(pa + (size_t)j * YP, a.step(fa[j * FF_T], ca), pl);
+                            st_hint(pb + (size_t)j * YP, b.step(fb[j * FF_T], cb), pl);
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        /* ---- columns: tiles [sigma][column][FF_TS] of FF_CW rows */
+        constexpr int TBUF = 2 * FF_T * FF_TS;
+        for (int cg = 0; cg < X; cg += FF_T) {
+            const int nc = min(FF_T, X - cg), col = cg + t;
+            const bool mine = t < nc;
+            auto stage_t = [&](int q, float *buf) {
+                const int p = t & 7;
+                for (int c = t >> 3; c < nc; c += FF_T / 8) {
+                    const size_t g = (size_t)(cg + c) * YP + q * FF_CW + 4 * p;
+                    cp_async16(buf + c * FF_TS + 4 * p, FA + g, pl);
+                    cp_async16(buf + (FF_T + c) * FF_TS + 4 * p, FB + g, pl);
+                }
+            };
+            IirState a, b;
+            /* forward */
+            stage_t(0, fsm);
+            cp_commit();
+            for (int q = 0; q < nq; ++q) {
+                if (q + 1 < nq) stage_t(q + 1, fsm + ((q + 1) & 1) * TBUF);
+                cp_commit();
+                cp_wait_prev();
+                __syncthreads();
+                float *buf = fsm + (q & 1) * TBUF;
+                float *ta = buf + t * FF_TS, *tb = ta + FF_T * FF_TS;
+                const int nr = min(FF_CW, Y - q * FF_CW);
+                if (mine) {
+                    if (q == 0) {
+                        a.init(ta[0]);
+                        b.init(tb[0]);
+                    }
+                    if (nr == FF_CW) {
+#pragma unroll 1
+                        for (int i4 = 0; i4 < FF_CW; i4 += 4) {
+                            const float4 va = *reinterpret_cast<const float4 *>(ta + i4);
+                            const float4 vb = *reinterpret_cast<const float4 *>(tb + i4);
+                            const float xa[4] = {va.x, va.y, va.z, va.w}, xb[4] = {vb.x, vb.y, vb.z, vb.w};
+                            float ya[4], yb[4];
+                            steps4(a, b, ca, cb, xa, xb, ya, yb);
+                            *reinterpret_cast<float4 *>(ta + i4) = make_float4(ya[0], ya[1], ya[2], ya[3]);
+                            *reinterpret_cast<float4 *>(tb + i4) = make_float4(yb[0], yb[1], yb[2], yb[3]);
+                        }
+                    } else {
+                        for (int i = 0; i < nr; ++i) {
+                            ta[i] = a.step(ta[i], ca);
+                            tb[i] = b.step(tb[i], cb);
+                        }
+                    }
+                }
+                __syncthreads();
+                {
+                    const int p = t & 7;
+                    for (int c = t >> 3; c < nc; c += FF_T / 8) {
+                        const size_t g = (size_t)(cg + c) * YP + q * FF_CW + 4 * p;
+                        st4_hint(FA + g, *reinterpret_cast<const float4 *>(buf + c * FF_TS + 4 * p), pl);
+                        st4_hint(FB + g, *reinterpret_cast<const float4 *>(buf + (FF_T + c) * FF_TS + 4 * p), pl);
+                    }
+                }
+                __syncthreads(); /* buffer q & 1 is restaged for tile q + 2 */
+            }
+            /* backward, DoG out */
+            stage_t(nq - 1, fsm);
+            cp_commit();
+            for (int qi = 0; qi < nq; ++qi) {
+                const int q = nq - 1 - qi;
+                if (q > 0) stage_t(q - 1, fsm + ((qi + 1) & 1) * TBUF);
+                cp_commit();
+                cp_wait_prev();
+                __syncthreads();
+                const float *ta = fsm + (qi & 1) * TBUF + t * FF_TS, *tb = ta + FF_T * FF_TS;
+                const int nr = min(FF_CW, Y - q * FF_CW);
+                if (mine) {
+                    if (qi == 0) {
+                        a.init(ta[nr - 1]);
+                        b.init(tb[nr - 1]);
+                    }
+                    float *pd = dog + ((size_t)z * Y + (size_t)q * FF_CW) * X + col;
+                    if (nr == FF_CW) {
+#pragma unroll 1
+                        for (int i4 = FF_CW - 4; i4 >= 0; i4 -= 4) {
+                            const float4 va = *reinterpret_cast<const float4 *>(ta + i4);
+                            const float4 vb = *reinterpret_cast<const float4 *>(tb + i4);
+                            const float xa[4] = {va.w, va.z, va.y, va.x}, xb[4] = {vb.w, vb.z, vb.y, vb.x};
+                            float ya[4], yb[4];
+                            steps4(a, b, ca, cb, xa, xb, ya, yb);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                st_hint(pd + (size_t)(i4 + 3 - u) * X, __fsub_rn(ya[u], yb[u]), pf);
+                        }
+                    } else {
+                        for (int i = nr - 1; i >= 0; --i)
+                            st_hint(pd + (size_t)i * X, __fsub_rn(a.step(ta[i], ca), b.step(tb[i], cb)), pf);
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        /* the frame's slot is dead: drop its lines without writing them back */
+        for (size_t off = (size_t)t * 32; off < 2 * img; off += (size_t)FF_T * 32) discard_line(FA + off);
+        __syncthreads();
+    }
+}
+
+
 /* Passes 3 and 4, fused: kernel_maxX (window max along rows with floor
  * minval, +max / -max) then kernel_maxY (window max of |.| along columns,
  * flag where it equals the pixel within 1e-6), cuda_FindROI.cu:94-147.
- * One CTA per (32-column strip, MAX_TH-row tile, frame): every row-max value
- * the tile's column windows need (its rows and k above and below, clamped to
- * the frame) is formed from a linear chunk of the DoG stack staged in shared
- * memory, with the window bounds formed in float over the stack's linear
- * index exactly as the reference does ((int)((fmaxf(0, c-k) + (float)(X*row))
- * + (float)(X*Y*frame))); a window that leaves the staged chunk (only where
- * the float spacing of the linear index exceeds the halo, stacks beyond
- * ~2^28 pixels) reads global memory.  An index past the stack's end (only in
- * the very last row) is left out of the max (the reference reads beyond its
- * buffer there).  The column maxima then run over the staged row maxima. */
-constexpr int MAX_TW = 32, MAX_TH = 128, MAX_WARPS = 8, MAX_HALO_EXTRA = 32;
+ * One CTA per (32-column strip, MAX_TH-row tile, frame).
+ * Row maxima: every row-max value the tile's column windows need (its rows
+ * and k above and below, clamped to the frame) is formed by a warp from a
+ * linear chunk of the DoG stack staged in shared memory, the strip and H =
+ * k + hr values either side of it, where hr bounds how far the reference's
+ * float-rounded window bounds stray from the nominal ones (0 while the
+ * stack has at most 2^24 pixels; the host derives it from the float spacing
+ * near n).  The bounds are formed in float over the stack's linear index
+ * exactly as the reference does ((int)((fmaxf(0, c-k) + (float)(X*row)) +
+ * (float)(X*Y*frame))); a window that leaves the chunk anyway (a stack past
+ * 2^32 pixels, whose 32-bit frame offset wraps as the reference's does)
+ * reads global memory.  An index past the stack's end (only in the very
+ * last row) is left out of the max (the reference reads beyond its buffer
+ * there).  The window max walks the chunk's quad maxima (max of 4
+ * consecutive values) in steps of 4 and closes with the quad, pair or value
+ * that ends the window (overlaps are harmless: max is idempotent).
+ * Column maxima: van Herk / Gil-Werman over the tile's rows of |row max|,
+ * blocks of W = 2k+1 rows from the tile's first row: g (max from the block
+ * start) and h (max to the block end) per (block, column) task; a window
+ * [s, e] of at most W rows is max(h[s], g[e]) across two blocks, g[e] when
+ * it starts a block and h[s] when it ends one (only windows clamped to the
+ * frame are shorter than W: they start at row 0 or end at the frame's last
+ * row, the tile's last).  Both maxima are exact, so the flags are the
+ * reference's. */
+constexpr int MAX_TW = 32, MAX_TH = 128, MAX_WARPS = 8, MAX_BOXSIZE = 128;
 
-__host__ __device__ inline int maxima_smem_floats(int k)
+__host__ __device__ inline int maxima_cwp(int k, int hr) { return (MAX_TW + 2 * (k + hr) + 31) / 32 * 32; }
+
+/* shared memory of maxima_kernel in 4-byte words: per warp two chunks
+ * (double-buffered) and the pair and quad maxima, then the rm, g and h tiles
+ * [MAX_TH + 2k][MAX_TW] and the row -> block table */
+__host__ __device__ inline int maxima_smem_floats(int k, int hr)
 {
-    return MAX_WARPS * (MAX_TW + 2 * (k + MAX_HALO_EXTRA)) + (MAX_TH + 2 * k) * MAX_TW;
+    return MAX_WARPS * 4 * maxima_cwp(k, hr) + 3 * (MAX_TH + 2 * k) * MAX_TW + (MAX_TH + 2 * k);
 }
 
+template <bool IDX64>
 __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__restrict__ dog,
                                                                 uint8_t *__restrict__ flags, int X, int Y,
-                                                                int Z, int k, float minval, float eps_hi)
+                                                                int Z, int k, float minval, float eps_hi, int hr)
 {
+    using Idx = typename std::conditional<IDX64, int64_t, int>::type;
     extern __shared__ float sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int H = k + MAX_HALO_EXTRA, CW = MAX_TW + 2 * H;
-    float *chunk = sm + warp * CW;
-    float *rmT = sm + MAX_WARPS * CW; /* [MAX_TH + 2k][MAX_TW] */
-    const int64_t n = (int64_t)X * Y * Z;
+    const int H = k + hr, CW = MAX_TW + 2 * H, CWP = maxima_cwp(k, hr), NR = MAX_TH + 2 * k;
+    float *ch0 = sm + warp * 4 * CWP, *p1 = ch0 + 2 * CWP, *p2 = p1 + CWP;
+    float *rmT = sm + MAX_WARPS * 4 * CWP, *gT = rmT + NR * MAX_TW, *hT = gT + NR * MAX_TW;
+    int *bdiv = reinterpret_cast<int *>(hT + NR * MAX_TW); /* i / W for the tile's rows */
+    const Idx n = (Idx)((int64_t)X * Y * Z);
     const int c0 = blockIdx.x * MAX_TW, r0 = blockIdx.y * MAX_TH, c = c0 + lane;
-    const int rlo = max(0, r0 - k), rhi = min(Y - 1, r0 + MAX_TH - 1 + k);
+    const int r1 = min(Y, r0 + MAX_TH) - 1;
+    const int rlo = max(0, r0 - k), rhi = min(Y - 1, r1 + k), nrows = rhi - rlo + 1;
+    const int W = 2 * k + 1, nblk = (nrows + W - 1) / W;
+    for (int i = threadIdx.x; i < NR; i += blockDim.x) bdiv[i] = i / W;
+    const float lo = fmaxf(0.0f, (float)(c - k));
+    const float hi = fminf((float)(X - 1), (float)(c + k));
+    /* the chunk of row r: [cbeg, cbeg + CW) of the stack, zero outside it */
+    auto stage = [&](int z, int r, float *buf) {
+        const Idx cbeg = ((Idx)z * Y + r) * X + c0 - H;
+        for (int i = lane; i < CW; i += 32) {
+            const Idx g = cbeg + i;
+            const bool in = g >= 0 && g < n;
+            const unsigned d = (unsigned)__cvta_generic_to_shared(buf + i);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(in ? dog + g : dog),
+                         "r"(in ? 4 : 0)
+                         : "memory");
+        }
+    };
     for (int z = blockIdx.z; z < Z; z += gridDim.z) {
-        __syncthreads(); /* rmT of the previous frame is consumed */
-        for (int r = rlo + warp; r <= rhi; r += MAX_WARPS) {
-            const int64_t base = ((int64_t)z * Y + r) * X + c0, cbeg = base - H;
-            for (int i = lane; i < CW; i += 32) {
-                const int64_t g = cbeg + i;
-                chunk[i] = (g >= 0 && g < n) ? __ldg(&dog[g]) : 0.0f; /* never inside a window */
-            }
+        __syncthreads(); /* the tiles of the previous frame are consumed */
+        const float zb = __uint2float_rn((unsigned)X * (unsigned)Y * (unsigned)z);
+        int j = 0;
+        if (rlo + warp <= rhi) stage(z, rlo + warp, ch0);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        for (int r = rlo + warp; r <= rhi; r += MAX_WARPS, ++j) {
+            float *ch = ch0 + (j & 1) * CWP;
+            if (r + MAX_WARPS <= rhi) stage(z, r + MAX_WARPS, ch0 + ((j + 1) & 1) * CWP);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+            __syncwarp();
+            for (int i = lane; i < CW - 1; i += 32) p1[i] = fmaxf(ch[i], ch[i + 1]);
+            __syncwarp();
+            for (int i = lane; i < CW - 3; i += 32) p2[i] = fmaxf(p1[i], p1[i + 2]);
             __syncwarp();
             float rmv = 0.0f;
             if (c < X) {
-                const float lo = fmaxf(0.0f, (float)(c - k));
-                const float hi = fminf((float)(X - 1), (float)(c + k));
+                const Idx cbeg = ((Idx)z * Y + r) * X + c0 - H;
                 const float rb = __uint2float_rn((unsigned)X * (unsigned)r);
-                const float zb = __uint2float_rn((unsigned)X * (unsigned)Y * (unsigned)z);
-                const int64_t start = (int64_t)__fadd_rn(__fadd_rn(lo, rb), zb);
-                int64_t end = (int64_t)__fadd_rn(__fadd_rn(hi, rb), zb);
+                const Idx start = (Idx)__fadd_rn(__fadd_rn(lo, rb), zb);
+                Idx end = (Idx)__fadd_rn(__fadd_rn(hi, rb), zb);
                 if (end > n - 1) end = n - 1;
                 float maxval = minval;
-                if (start >= cbeg && end < cbeg + CW) {
-                    const int s0 = (int)(start - cbeg), s1 = (int)(end - cbeg);
-#pragma unroll 4
-                    for (int i = s0; i <= s1; ++i) maxval = fmaxf(maxval, chunk[i]);
+                const Idx s = start - cbeg, e = end - cbeg;
+                if (s >= 0 && e < CW) {
+                    const int si = (int)s, ei = (int)e;
+                    int i = si;
+                    for (; i + 3 <= ei; i += 4) maxval = fmaxf(maxval, p2[i]);
+                    if (i <= ei)
+                        maxval = fmaxf(maxval, ei - 3 >= si ? p2[ei - 3] : (ei > si ? fmaxf(p1[si], p1[ei - 1]) : ch[si]));
                 } else {
-                    for (int64_t i = start; i <= end; ++i) maxval = fmaxf(maxval, __ldg(&dog[i]));
+                    for (Idx i = start; i <= end; ++i) maxval = fmaxf(maxval, __ldg(&dog[i]));
                 }
-                const float inpixel = chunk[lane + H];
+                const float inpixel = ch[lane + H];
                 rmv = maxval > inpixel ? -maxval : (maxval == inpixel ? maxval : 0.0f);
             }
             rmT[(r - rlo) * MAX_TW + lane] = rmv;
-            __syncwarp(); /* the chunk is restaged for the warp's next row */
+            __syncwarp(); /* p1, p2 and this chunk are rewritten for the warp's next rows */
+        }
+        __syncthreads();
+        for (int task = threadIdx.x; task < nblk * MAX_TW; task += blockDim.x) {
+            const int col = task & (MAX_TW - 1), i0 = (task / MAX_TW) * W, i1 = min(nrows, i0 + W) - 1;
+            float m = fabsf(rmT[i0 * MAX_TW + col]);
+            gT[i0 * MAX_TW + col] = m;
+            for (int i = i0 + 1; i <= i1; ++i) {
+                m = fmaxf(m, fabsf(rmT[i * MAX_TW + col]));
+                gT[i * MAX_TW + col] = m;
+            }
+            m = fabsf(rmT[i1 * MAX_TW + col]);
+            hT[i1 * MAX_TW + col] = m;
+            for (int i = i1 - 1; i >= i0; --i) {
+                m = fmaxf(m, fabsf(rmT[i * MAX_TW + col]));
+                hT[i * MAX_TW + col] = m;
+            }
         }
         __syncthreads();
         if (c < X) {
-            for (int r = r0 + warp; r < min(Y, r0 + MAX_TH); r += MAX_WARPS) {
-                const int start = (int)fmaxf(0.0f, (float)(r - k));
-                const int end = (int)fminf((float)(Y - 1), (float)(r + k));
-                float maxval = minval;
-                const float *col = rmT + (start - rlo) * MAX_TW + lane;
-#pragma unroll 4
-                for (int i = 0; i <= end - start; ++i) maxval = fmaxf(maxval, fabsf(col[i * MAX_TW]));
+            uint8_t *fl = flags + ((int64_t)z * Y) * X + c;
+            for (int r = r0 + warp; r <= r1; r += MAX_WARPS) {
+                const int s = max(0, r - k) - rlo, e = min(Y - 1, r + k) - rlo;
+                const int bs = bdiv[s];
+                const float m = bs != bdiv[e] ? fmaxf(hT[s * MAX_TW + lane], gT[e * MAX_TW + lane])
+                                              : (s == bs * W ? gT[e * MAX_TW + lane] : hT[s * MAX_TW + lane]);
+                const float maxval = fmaxf(minval, m);
                 const float inpixel = rmT[(r - rlo) * MAX_TW + lane];
                 /* (double)d < 1e-6 for a float d is d < eps_hi, the float
                  * just above the double 1e-6 */
-                flags[((int64_t)z * Y + r) * X + c] = fabsf(__fsub_rn(maxval, inpixel)) < eps_hi ? 1 : 0;
+                fl[(int64_t)r * X] = fabsf(__fsub_rn(maxval, inpixel)) < eps_hi ? 1 : 0;
             }
         }
     }
@@ -521,41 +1000,34 @@ extern "C" void bamf_findroi_workspace_destroy(bamf_findroi_ws *ws) { delete ws;
 
 namespace {
 
-/* Passes 1-5 on `frames` (device).  With host_frames, the frames are first
- * copied from there in chunks of chunk_frames on the workspace's copy
- * stream, and each chunk's row and column filters start on `s` as soon as
+/* Passes 1-2 (the DoG) of `frames` (device) into `dog`.  With host_frames,
+ * the frames are first copied from there in chunks of chunk_frames on the
+ * workspace's copy stream, and each chunk's filters start on `s` as soon as
  * its copy has landed (the filters are frame-local, so a chunk is filtered
- * exactly as inside the whole stack); the window maxima and everything after
- * them run on the whole stack once every chunk is filtered. */
-bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_frames, const float *frames,
-                     int ysize, int xsize, int zsize, double sigma1, double sigma2, int boxsize, float minval,
-                     int64_t capacity, int32_t *coords, int32_t *corners, float *roi_stack, int64_t *count,
-                     uint8_t *flags_out, cudaStream_t s)
+ * exactly as inside the whole stack).  Frames whose two intermediate images
+ * fit a slot take the fused filter (one slot per CTA, one CTA per SM, the
+ * slots in ws->b); larger frames take rows_kernel + cols_kernel (the second
+ * image in ws->b). */
+bamf_status run_filter(bamf_findroi_ws *ws, const float *host_frames, int chunk_frames, const float *frames,
+                       int KX, int KY, int zsize, double sigma1, double sigma2, float *dog, cudaStream_t s)
 {
-    if (!ws || !frames || !coords || !count || ysize < 1 || xsize < 1 || zsize < 1 || boxsize < 1 ||
-        capacity < 0)
-        return BAMF_ERR_INVALID_ARG;
-    if ((roi_stack != nullptr) && corners == nullptr) return BAMF_ERR_INVALID_ARG;
-    if (xsize > ysize * 64 || ysize > xsize * 64) return BAMF_ERR_INVALID_ARG;
-    if (boxsize > 256) return BAMF_ERR_TOO_LARGE; /* the maxima tiles stage 2 boxsize + 96 rows */
-    const int64_t n = (int64_t)xsize * ysize * zsize;
-    /* kernel view (as the reference launches it): each frame is KY = Ysize
-     * runs of KX = Xsize contiguous floats (size(Image,2), findROI.m:186-189) */
-    const int KX = xsize, KY = ysize;
-    Coef ca = iir_coef(sigma1), cb = iir_coef(sigma2);
-    if (!ws->a.ensure(n * sizeof(float)) || !ws->b.ensure(n * sizeof(float))) return BAMF_ERR_CUDA;
-    uint8_t *flags = flags_out;
-    if (!flags) {
-        if (!ws->flags.ensure(n)) return BAMF_ERR_CUDA;
-        flags = (uint8_t *)ws->flags.p;
-    }
-    int64_t nchunks = (n + CHUNK - 1) / CHUNK;
-    if (!ws->chunks.ensure(nchunks * sizeof(int32_t)) || !ws->total.ensure(sizeof(int64_t)))
-        return BAMF_ERR_CUDA;
-    float *A = (float *)ws->a.p, *Bb = (float *)ws->b.p;
+    const Coef ca = iir_coef(sigma1), cb = iir_coef(sigma2);
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int step = host_frames ? std::max(1, chunk_frames) : zsize;
+    const int64_t plane = (int64_t)KX * KY, n = plane * zsize;
+    const int YP = (KY + FF_CW - 1) / FF_CW * FF_CW;
+    const bool fused = (size_t)KX * YP <= FF_MAX_SLOT;
+    const int ff_grid = std::min(step, sms);
+    const size_t b_bytes = fused ? (size_t)ff_grid * 2 * KX * YP * sizeof(float) : n * sizeof(float);
+    if (!ws->b.ensure(b_bytes)) return BAMF_ERR_CUDA;
+    float *Bb = (float *)ws->b.p;
+    const bool vec = KX % 4 == 0 && (reinterpret_cast<uintptr_t>(frames) & 15) == 0;
+    const size_t ff_smem = (size_t)FF_SMEM_FLOATS * sizeof(float);
+    if (fused && cudaFuncSetAttribute(vec ? filter_kernel<true> : filter_kernel<false>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff_smem) != cudaSuccess)
+        return cuda_fail();
     if (host_frames) {
         if (!ws->copy && cudaStreamCreateWithFlags(&ws->copy, cudaStreamNonBlocking) != cudaSuccess)
             return cuda_fail();
@@ -565,8 +1037,6 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
         if (cudaEventRecord(ws->landed, s) != cudaSuccess || cudaStreamWaitEvent(ws->copy, ws->landed, 0) != cudaSuccess)
             return cuda_fail();
     }
-    const int step = host_frames ? std::max(1, chunk_frames) : zsize;
-    const int64_t plane = (int64_t)KX * KY;
     for (int z0 = 0; z0 < zsize; z0 += step) {
         const int zc = std::min(step, zsize - z0);
         const int64_t off = z0 * plane;
@@ -577,24 +1047,76 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
                 cudaStreamWaitEvent(s, ws->landed, 0) != cudaSuccess)
                 return cuda_fail();
         }
+        if (fused) {
+            const unsigned grid = (unsigned)std::min(zc, ff_grid);
+            if (vec)
+                filter_kernel<true><<<grid, FF_T, ff_smem, s>>>(frames + off, dog + off, Bb, KX, KY, zc, YP, ca, cb);
+            else
+                filter_kernel<false><<<grid, FF_T, ff_smem, s>>>(frames + off, dog + off, Bb, KX, KY, zc, YP, ca, cb);
+            continue;
+        }
         const int64_t nrows = (int64_t)KY * zc, ncols = (int64_t)KX * zc;
         const int64_t groups = (nrows + 31) / 32;
         const unsigned grid = (unsigned)std::max<int64_t>(
             1, std::min<int64_t>((groups + ROWS_WARPS - 1) / ROWS_WARPS, (int64_t)sms * ROWS_CTAS_PER_SM));
-        rows_kernel<<<grid, 32 * ROWS_WARPS, 0, s>>>(frames + off, A + off, Bb + off, KX, KY, zc, ca, cb);
-        cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(A + off, Bb + off, KX, KY, zc, ca, cb);
+        rows_kernel<<<grid, 32 * ROWS_WARPS, 0, s>>>(frames + off, dog + off, Bb + off, KX, KY, zc, ca, cb);
+        cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(dog + off, Bb + off, KX, KY, zc, ca, cb);
     }
+    return launch_err();
+}
+
+/* Passes 1-5 on `frames` (device), copied first from host_frames when given
+ * (run_filter); the window maxima and everything after them run on the
+ * whole stack once every chunk is filtered. */
+bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_frames, const float *frames,
+                     int ysize, int xsize, int zsize, double sigma1, double sigma2, int boxsize, float minval,
+                     int64_t capacity, int32_t *coords, int32_t *corners, float *roi_stack, int64_t *count,
+                     uint8_t *flags_out, cudaStream_t s)
+{
+    if (!ws || !frames || !coords || !count || ysize < 1 || xsize < 1 || zsize < 1 || boxsize < 1 ||
+        capacity < 0)
+        return BAMF_ERR_INVALID_ARG;
+    if ((roi_stack != nullptr) && corners == nullptr) return BAMF_ERR_INVALID_ARG;
+    if (xsize > ysize * 64 || ysize > xsize * 64) return BAMF_ERR_INVALID_ARG;
+    /* the maxima tiles hold 2 boxsize + 128 rows: boxsize up to 128 */
+    if (boxsize > MAX_BOXSIZE) return BAMF_ERR_TOO_LARGE;
+    const int64_t n = (int64_t)xsize * ysize * zsize;
+    /* kernel view (as the reference launches it): each frame is KY = Ysize
+     * runs of KX = Xsize contiguous floats (size(Image,2), findROI.m:186-189) */
+    const int KX = xsize, KY = ysize;
+    if (!ws->a.ensure(n * sizeof(float))) return BAMF_ERR_CUDA;
+    uint8_t *flags = flags_out;
+    if (!flags) {
+        if (!ws->flags.ensure(n)) return BAMF_ERR_CUDA;
+        flags = (uint8_t *)ws->flags.p;
+    }
+    int64_t nchunks = (n + CHUNK - 1) / CHUNK;
+    if (!ws->chunks.ensure(nchunks * sizeof(int32_t)) || !ws->total.ensure(sizeof(int64_t)))
+        return BAMF_ERR_CUDA;
+    float *A = (float *)ws->a.p;
+    bamf_status st = run_filter(ws, host_frames, chunk_frames, frames, KX, KY, zsize, sigma1, sigma2, A, s);
+    if (st) return st;
     {
-        const size_t smem = (size_t)maxima_smem_floats(boxsize) * sizeof(float);
-        if (smem > 48 * 1024 &&
-            cudaFuncSetAttribute(maxima_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return cuda_fail();
-        dim3 grid((unsigned)((KX + MAX_TW - 1) / MAX_TW), (unsigned)((KY + MAX_TH - 1) / MAX_TH),
-                  (unsigned)std::min(zsize, 65535));
         /* the smallest float above the double 1e-6 */
         float eps_hi = (float)1e-6;
         if ((double)eps_hi <= 1e-6) eps_hi = std::nextafter(eps_hi, 1.0f);
-        maxima_kernel<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, boxsize, minval, eps_hi);
+        /* how far the float-rounded window bounds can stray from the
+         * nominal ones: exact up to 2^24 stack pixels; above, each of the
+         * reference's two float additions and its float frame offset moves
+         * a bound by at most half the float spacing near n (halved while the
+         * tiles would not fit shared memory: windows that stray further read
+         * global memory) */
+        int hr = 0;
+        if (n > (int64_t(1) << 24)) hr = 2 * (1 << std::min(7, std::max(0, std::ilogb((float)n) - 23)));
+        while (hr > 0 && (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float) > 220 * 1024) hr /= 2;
+        const size_t smem = (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float);
+        auto kern = n > (int64_t(1) << 31) - 4096 ? maxima_kernel<true> : maxima_kernel<false>;
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return cuda_fail();
+        dim3 grid((unsigned)((KX + MAX_TW - 1) / MAX_TW), (unsigned)((KY + MAX_TH - 1) / MAX_TH),
+                  (unsigned)std::min(zsize, 65535));
+        kern<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, boxsize, minval, eps_hi, hr);
     }
     count_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
     scan_kernel<<<1, 1024, 0, s>>>((int32_t *)ws->chunks.p, nchunks, (int64_t *)ws->total.p);
@@ -612,7 +1134,63 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
     return launch_err();
 }
 
+/* Every float q run through div_fast and __fdiv_rn by one b0: differing
+ * results with |q| in [lo, hi] (the range the filter sends through
+ * div_fast) and in all (NaN results compare equal). */
+__global__ void division_check_kernel(Coef c, unsigned long long *bad_in_range, unsigned long long *bad)
+{
+    unsigned long long n_in = 0, n_all = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (1ull << 32); i += stride) {
+        const float q = __uint_as_float((unsigned)i);
+        const float want = __fdiv_rn(q, c.b0), got = div_fast(q, c.b0, c.rb0);
+        if (__float_as_uint(want) != __float_as_uint(got) && !(isnan(want) && isnan(got))) {
+            ++n_all;
+            if (fabsf(q) >= c.lo && fabsf(q) <= c.hi) ++n_in;
+        }
+    }
+    if (n_all) atomicAdd(bad, n_all);
+    if (n_in) atomicAdd(bad_in_range, n_in);
+}
+
 }  // namespace
+
+extern "C" bamf_status bamf_find_roi_dog_device(bamf_findroi_ws *ws, const float *frames, int ysize, int xsize,
+                                                int zsize, double sigma1, double sigma2, float *dog, void *stream)
+{
+    if (!ws || !frames || !dog || ysize < 1 || xsize < 1 || zsize < 1) return BAMF_ERR_INVALID_ARG;
+    if (xsize > ysize * 64 || ysize > xsize * 64) return BAMF_ERR_INVALID_ARG;
+    return run_filter(ws, nullptr, 0, frames, xsize, ysize, zsize, sigma1, sigma2, dog, (cudaStream_t)stream);
+}
+
+extern "C" bamf_status bamf_findroi_division_check(double sigma, int *host_exact,
+                                                   unsigned long long *dev_mismatch_in_range,
+                                                   unsigned long long *dev_mismatch)
+{
+    if (!host_exact) return BAMF_ERR_INVALID_ARG;
+    const Coef c = iir_coef(sigma);
+    *host_exact = c.lo <= c.hi;
+    if (!dev_mismatch_in_range && !dev_mismatch) return BAMF_OK;
+    if (!dev_mismatch_in_range || !dev_mismatch) return BAMF_ERR_INVALID_ARG;
+    if (bamf_device_count() < 1) return BAMF_ERR_NO_DEVICE;
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 2 * sizeof *d) != cudaSuccess) return cuda_fail();
+    bamf_status st = BAMF_OK;
+    unsigned long long h[2] = {0, 0};
+    if (cudaMemset(d, 0, 2 * sizeof *d) != cudaSuccess) st = BAMF_ERR_CUDA;
+    if (!st) {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        division_check_kernel<<<sms * 8, 256>>>(c, d, d + 1);
+        if (cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess) st = BAMF_ERR_CUDA;
+    }
+    if (st) cudaGetLastError();
+    cudaFree(d);
+    *dev_mismatch_in_range = h[0];
+    *dev_mismatch = h[1];
+    return st;
+}
 
 extern "C" bamf_status bamf_find_roi_device(bamf_findroi_ws *ws, const float *frames, int ysize,
                                             int xsize, int zsize, double sigma1, double sigma2,

@@ -32,6 +32,12 @@ def _declare():
     L.bamf_find_roi_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
                                        C.c_double, C.c_int, C.c_float, C.c_int64, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.bamf_find_roi_dog_device.restype = C.c_int
+    L.bamf_find_roi_dog_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_double,
+                                           C.c_double, C.c_void_p, C.c_void_p]
+    L.bamf_findroi_division_check.restype = C.c_int
+    L.bamf_findroi_division_check.argtypes = [C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_ulonglong),
+                                              C.POINTER(C.c_ulonglong)]
     L.bamf_find_roi_pinned.restype = C.c_int
     L.bamf_find_roi_pinned.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.c_double, C.c_double, C.c_int, C.c_float, C.c_int64, C.c_void_p,
@@ -159,6 +165,23 @@ def gaussMLE(Data, FitType: str = "Basic", CameraType: str = "CCD", Sigma=1.3, *
     return out
 
 
+def division_check(sigma: float, device: bool = False) -> dict:
+    """The filters' fast division by the recurrence constant b0 of width
+    `sigma` (bamf_findroi_division_check): host_exact, and with device=True
+    the device counts of results differing from IEEE division over all 2^32
+    floats (in the fast range / in all)."""
+    L = _declare()
+    ok = C.c_int()
+    if not device:
+        abi.check(L.bamf_findroi_division_check(float(sigma), C.byref(ok), None, None),
+                  "bamf_findroi_division_check")
+        return {"host_exact": bool(ok.value)}
+    a, b = C.c_ulonglong(), C.c_ulonglong()
+    abi.check(L.bamf_findroi_division_check(float(sigma), C.byref(ok), C.byref(a), C.byref(b)),
+              "bamf_findroi_division_check")
+    return {"host_exact": bool(ok.value), "dev_mismatch_in_range": int(a.value), "dev_mismatch": int(b.value)}
+
+
 class FindRoiDevice:
     """findROI on device-resident stacks (torch CUDA tensors)."""
 
@@ -202,6 +225,18 @@ class FindRoiDevice:
             out["stack"].data_ptr() if want_stack else None, out["count"].data_ptr(),
             out["flags"].data_ptr() if want_flags else None, C.c_void_p(stream) if stream else None)
         abi.check(st, "bamf_find_roi_device")
+        return out
+
+    def dog(self, frames, ysize, xsize, zsize, sigma1=1.3, sigma2=2.6, stream=None):
+        """The difference-of-Gaussians image the maxima run on, a CUDA
+        tensor of ysize*xsize*zsize floats in the frames' layout.  Enqueued
+        on `stream`."""
+        import torch
+        out = torch.empty(ysize * xsize * zsize, dtype=torch.float32, device="cuda")
+        abi.check(self._L.bamf_find_roi_dog_device(self._ws, frames.data_ptr(), ysize, xsize, zsize, float(sigma1),
+                                                   float(sigma2), out.data_ptr(),
+                                                   C.c_void_p(stream) if stream else None),
+                  "bamf_find_roi_dog_device")
         return out
 
     def run_pinned(self, host_frames, ysize, xsize, zsize, sigma1=1.3, sigma2=2.6, boxsize=7, minval=None,

@@ -524,8 +524,9 @@ bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *rois,
 /* Front end: findROI                                                   */
 /* ------------------------------------------------------------------ */
 
-/* Device scratch of the ROI finder (two float images and one byte of flags
- * per pixel of the stack, chunk counts); grows on demand. */
+/* Device scratch of the ROI finder (the DoG image and one byte of flags per
+ * pixel of the stack, the filters' per-SM frame slots or, for frames of more
+ * than about 80k pixels, a second image; chunk counts); grows on demand. */
 typedef struct bamf_findroi_ws bamf_findroi_ws;
 bamf_status bamf_findroi_workspace_create(bamf_findroi_ws **ws);
 void bamf_findroi_workspace_destroy(bamf_findroi_ws *ws);
@@ -536,7 +537,8 @@ void bamf_findroi_workspace_destroy(bamf_findroi_ws *ws);
  * maxima of a frame stack.
  *   frames       ysize*xsize*zsize floats, y fastest (MATLAB Y x X x Z)
  *   sigma1/2     the two recursive-Gaussian widths (findROI.m Sigma1/Sigma2)
- *   boxsize      maximum-window half width and ROI side (Boxsize)
+ *   boxsize      maximum-window half width and ROI side (Boxsize), at most
+ *                128 (BAMF_ERR_TOO_LARGE beyond)
  *   minval       floor of the maxima (Minval), as the single the kernel gets
  *   capacity     rows available in coords/corners/roi_stack
  *   coords       [capacity][3] 1-based (row, col, frame) of each maximum in
@@ -574,6 +576,28 @@ bamf_status bamf_find_roi_pinned(bamf_findroi_ws *ws, const float *host_frames, 
                                  double sigma2, int boxsize, float minval, int64_t capacity,
                                  int32_t *coords, int32_t *corners, float *roi_stack,
                                  int64_t *count, uint8_t *flags_out, void *stream);
+
+/* The difference-of-Gaussians image findROI's maxima run on
+ * (cuda_FindROI.cu kernel_gaussX / kernel_gaussY for sigma1 and sigma2, then
+ * kernel_subtract): dog = G(sigma1) - G(sigma2) of each frame, in the frames'
+ * layout (ysize*xsize*zsize floats, device).  Enqueued on stream. */
+bamf_status bamf_find_roi_dog_device(bamf_findroi_ws *ws, const float *frames, int ysize, int xsize,
+                                     int zsize, double sigma1, double sigma2, float *dog, void *stream);
+
+/* The filters divide by the recurrence constant b0 with one multiply and
+ * two FMAs through RN(1/b0) (Markstein's method) where |q| lies in
+ * [2^-100, 2^100], after the host has checked, once per b0, that this equals
+ * IEEE division over the 2^23 significands of [1, 2) (the method is
+ * scale-invariant on that range); elsewhere, and for a b0 that fails the
+ * check, they use IEEE division.  For the b0 of filter width `sigma`:
+ * *host_exact = 1 when the host check passed.  With both counters given,
+ * every one of the 2^32 float bit patterns q is also divided on the device
+ * both ways: *dev_mismatch_in_range counts differing results with |q| in
+ * the fast range (0 expected when *host_exact), *dev_mismatch all differing
+ * results (NaN results compare equal).  Synchronous. */
+bamf_status bamf_findroi_division_check(double sigma, int *host_exact,
+                                        unsigned long long *dev_mismatch_in_range,
+                                        unsigned long long *dev_mismatch);
 
 /* ------------------------------------------------------------------ */
 /* Front end: gaussMLE                                                  */

@@ -102,6 +102,7 @@ def load(kind: str = "port") -> C.CDLL:
     if kind.startswith("port"):
         L.oracle_findroi_filter.argtypes = [pf, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                             C.c_int, C.c_float, pf, C.c_int]
+        L.oracle_findroi_dog.argtypes = [pf, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, pf]
         L.oracle_gaussmle_xynb.argtypes = [pf, C.c_int, C.c_int, C.c_float, C.c_int, pf, pf, pf,
                                            C.c_int]
         pd = C.POINTER(C.c_double)
@@ -193,6 +194,22 @@ def run_batch(batch, params: abi.McmcParams, off, sig, back, bg0: float, seed: i
         float(bg0), int(seed), int(threads), fn.ctypes.data_as(pi), mn.ctypes.data_as(pi),
         na.ctypes.data_as(pi)), "oracle_rjmcmc_batch")
     return {"final_n": fn, "map_n": mn, "n_accepted": na}
+
+
+def findroi_dog(stack: np.ndarray, sigma1: float = 1.3, sigma2: float = 2.6) -> np.ndarray:
+    """The difference-of-Gaussians image of findROI's kernels (gaussX /
+    gaussY per sigma, subtract) for a (Y, X, Z) stack; returned flat in the
+    stack's memory order (y fastest)."""
+    L = load("port")
+    st = np.asarray(stack, np.float32)
+    if st.ndim == 2:
+        st = st[:, :, None]
+    ys, xs, zs = st.shape
+    flat = np.ascontiguousarray(st.ravel(order="F"))
+    dog = np.zeros_like(flat)
+    abi.check(L.oracle_findroi_dog(abi.fptr(flat), ys, xs, zs, float(sigma1), float(sigma2), abi.fptr(dog)),
+              "oracle_findroi_dog")
+    return dog
 
 
 def findroi(stack: np.ndarray, sigma1: float = 1.3, sigma2: float = 2.6, boxsize: int = 7,

@@ -165,6 +165,34 @@ static void *findroi_worker(void *arg)
     return NULL;
 }
 
+/* The difference of Gaussians alone (cuda_FindROI.cu kernel_gaussX,
+ * kernel_gaussY for each sigma, kernel_subtract: the first half of
+ * findroi_frame) into dog, frame by frame. */
+int oracle_findroi_dog(const float *frames, int ysize, int xsize, int zsize, double sigma1, double sigma2,
+                       float *dog)
+{
+    if (!frames || !dog || ysize < 1 || xsize < 1 || zsize < 1) return BAMF_ERR_INVALID_ARG;
+    const int X = xsize, Y = ysize;
+    const size_t fs = (size_t)X * Y;
+    float cA[5], cB[5];
+    iir_coeffs(sigma1, cA);
+    iir_coeffs(sigma2, cB);
+    float *Bf = (float *)malloc(fs * sizeof(float));
+    if (!Bf) return BAMF_ERR_INVALID_ARG;
+    for (int z = 0; z < zsize; ++z) {
+        float *A = dog + z * fs;
+        memcpy(A, frames + z * fs, fs * sizeof(float));
+        memcpy(Bf, frames + z * fs, fs * sizeof(float));
+        for (int r = 0; r < Y; ++r) iir_line(A + (size_t)r * X, X, 1, cA);
+        for (int c = 0; c < X; ++c) iir_line(A + c, Y, X, cA);
+        for (int r = 0; r < Y; ++r) iir_line(Bf + (size_t)r * X, X, 1, cB);
+        for (int c = 0; c < X; ++c) iir_line(Bf + c, Y, X, cB);
+        for (size_t i = 0; i < fs; ++i) A[i] = A[i] - Bf[i];
+    }
+    free(Bf);
+    return 0;
+}
+
 /* flags: zsize*ysize*xsize floats (1 = local maximum), memory order of the
  * input stack.  The window of kernel_maxX may cross into the next frame's
  * first DoG value when its float bounds round up (frames >= 256 at

@@ -55,6 +55,8 @@ int oracle_rjmcmc_batch(const float *data, const int64_t *offsets, const int32_t
 /* ---- front end -------------------------------------------------------- */
 int oracle_findroi_filter(float *frames, int ysize, int xsize, int zsize, double sigma1,
                           double sigma2, int boxsize, float minval, float *flags, int threads);
+int oracle_findroi_dog(const float *frames, int ysize, int xsize, int zsize, double sigma1, double sigma2,
+                       float *dog);
 int oracle_gaussmle_xynb(const float *rois, int sz, int nfits, float psf_sigma, int iterations,
                          float *params, float *crlb, float *loglik, int threads);
 int oracle_gaussmle_xynb_f64(const float *rois, int sz, int nfits, double psf_sigma,

@@ -64,6 +64,23 @@ def test_findroi_small_and_edge_frames(cuda_lib):
     assert len(coords) >= 3
 
 
+@pytest.mark.parametrize("shape", [(320, 320), (250, 96), (96, 250), (33, 47)])
+def test_findroi_frame_shapes_on_both_filter_paths(cuda_lib, shape):
+    """Frames whose intermediate images do not fit the fused filter's slot
+    (320 x 320) take the row / column kernels; the others, with rows and
+    columns not multiples of the tile sizes and unaligned row lengths, take
+    the fused filter.  Both are bit-exact against the oracle."""
+    ys, xs = shape
+    st, _ = synth.frames(3, size=max(ys, xs), seed=6)
+    st = np.asfortranarray(st[:ys, :xs, :])
+    ref = oracle.findroi(st, 1.3, 2.6, 7)
+    SMD, rois, coords = frontend.findROI(st, 1.3, 2.6, 7)
+    assert len(coords) > 3
+    np.testing.assert_array_equal(coords, ref["coords"])
+    np.testing.assert_array_equal(SMD["XBoxCorner"], ref["XBoxCorner"])
+    np.testing.assert_array_equal(rois, ref["ROIStack"])
+
+
 def test_gaussmle_matches_float_restatement_and_fp64(cuda_lib, frames):
     st, _ = frames
     _, rois, _ = frontend.findROI(st, 1.3, 2.6, 7)
