@@ -43,8 +43,8 @@ static inline bamf_status clear_cuda_error()
 /* defined in api_sampler.cu */
 bamf_status check_proposal_and_traces(const bamf_roi_batch *rois, const bamf_mcmc_params *p, int arith,
                                       const bamf_batch_results *out);
-__global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__restrict__ ys, int n,
-                             int32_t *__restrict__ order, int32_t *__restrict__ class_range);
+bamf_status launch_batch_order(const bamf_roi_batch *rois, int n, void *order_scratch, int32_t *class_range,
+                               cudaStream_t s);
 __global__ void map_n_kernel(const uint8_t *__restrict__ trace, int trace_cap,
                              const int32_t *__restrict__ n_entries, int n_rois,
                              int32_t *__restrict__ map_n);
@@ -178,7 +178,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
         used = align256(used + (size_t)4 * L[k] * sizeof(float));
     }
     size_t off_order = used;
-    used = align256(used + (size_t)n * sizeof(int32_t));
+    used = align256(used + BAMF_ORDER_SCRATCH(n));
     size_t off_entries = used;
     bool own_entries = want_map && out->n_entries == nullptr;
     if (own_entries) used = align256(used + (size_t)n * sizeof(int32_t));
@@ -253,7 +253,7 @@ extern "C" bamf_status bamf_rjmcmc_batch_device_noalloc(const bamf_roi_batch *ro
     B.model_drift = arith == BAMF_ARITH_FAST ? out->model_drift : nullptr;
     B.order = (int32_t *)(S + off_order);
     B.class_range = (int32_t *)(S + 256);
-    order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)B.order, (int32_t *)B.class_range);
+    if ((r = launch_batch_order(rois, n, S + off_order, (int32_t *)B.class_range, s))) return r;
     int32_t *entries = out->n_entries;
     if (own_entries) entries = (int32_t *)(S + off_entries);
     B.n_entries = entries;

@@ -358,59 +358,125 @@ __global__ void map_n_kernel(const uint8_t *__restrict__ trace, int trace_cap,
     }
 }
 
-/* Stable counting sort of ROI ids by size class, largest class first (one
- * block of up to 1024 threads), and the [begin, end) range of every class in
- * the sorted order.  Within a class the ROIs keep their input order, so the
- * order (and with it which chains share a CTA) is the same on every call. */
-__global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__restrict__ ys,
-                             int n, int32_t *__restrict__ order, int32_t *__restrict__ class_range)
+/* Photon estimate of each ROI, one warp per ROI: the pixels above a
+ * background (the mean of the pixels below the ROI's mean), summed; its
+ * bucket in half octaves (0..BAMF_N_BUCKETS-1) is the secondary key of the
+ * batch order.  Warp sums in a fixed order: the same bucket on every call. */
+constexpr int BAMF_N_BUCKETS = 32;
+
+__global__ void photon_bucket_kernel(const float *__restrict__ data, const int64_t *__restrict__ offsets,
+                                     const int32_t *__restrict__ xs, const int32_t *__restrict__ ys, int n,
+                                     uint8_t *__restrict__ bucket)
 {
-    __shared__ int cnt[BAMF_N_CLASSES];
-    __shared__ int pos[BAMF_N_CLASSES];
-    __shared__ int wbase[32][BAMF_N_CLASSES];
+    const int lane = threadIdx.x & 31;
+    const int i = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (i >= n) return;
+    const int npix = max(xs[i], 0) * max(ys[i], 0);
+    const float *d = data + offsets[i];
+    auto wsum = [](float v) {
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return v;
+    };
+    float s = 0.0f;
+    for (int p = lane; p < npix; p += 32) s += d[p];
+    const float mean = wsum(s) / (float)max(npix, 1);
+    float sb = 0.0f, cb = 0.0f;
+    for (int p = lane; p < npix; p += 32)
+        if (d[p] < mean) {
+            sb += d[p];
+            cb += 1.0f;
+        }
+    sb = wsum(sb);
+    cb = wsum(cb);
+    const float bg = cb > 0.0f ? sb / cb : mean;
+    float e = 0.0f;
+    for (int p = lane; p < npix; p += 32) e += fmaxf(d[p] - bg, 0.0f);
+    e = wsum(e);
+    if (lane == 0) bucket[i] = (uint8_t)min(BAMF_N_BUCKETS - 1, max(0, (int)(2.0f * log2f(1.0f + e))));
+}
+
+/* One block: stable counting sort of the ids in[0..n) (0..n-1 when in is
+ * null) by key(id) in [0, K), largest key first; out gets the ids and, when
+ * range is given, range[2k], range[2k+1] the [begin, end) of key k.  Ranks
+ * within a warp by ballot, warp offsets by a per-key scan over the warps, in
+ * id order: the same order on every call. */
+template <int K, class KeyF>
+__device__ void block_count_sort(int n, const int32_t *__restrict__ in, int32_t *__restrict__ out,
+                                 int32_t *__restrict__ range, KeyF key)
+{
+    __shared__ int cnt[K], pos[K];
+    __shared__ int wbase[32][K];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (threadIdx.x < BAMF_N_CLASSES) cnt[threadIdx.x] = 0;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) cnt[k] = 0;
     __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        int c = side_class(min(max(max(xs[i], ys[i]), 1), BAMF_MAX_ROI_SIDE));
-        atomicAdd(&cnt[c], 1);
-    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&cnt[key(in ? in[i] : i)], 1);
     __syncthreads();
     if (threadIdx.x == 0) {
         int acc = 0;
-        for (int c = BAMF_N_CLASSES - 1; c >= 0; --c) {
+        for (int c = K - 1; c >= 0; --c) {
             pos[c] = acc;
-            class_range[2 * c] = acc;
+            if (range) range[2 * c] = acc;
             acc += cnt[c];
-            class_range[2 * c + 1] = acc;
+            if (range) range[2 * c + 1] = acc;
         }
     }
     __syncthreads();
-    /* chunks of blockDim.x ids: rank within the warp by ballot, warp offsets
-     * by a per-class scan over the warps, in id order */
     for (int base = 0; base < n; base += blockDim.x) {
-        int i = base + threadIdx.x;
-        int c = i < n ? side_class(min(max(max(xs[i], ys[i]), 1), BAMF_MAX_ROI_SIDE)) : -1;
+        const int i = base + threadIdx.x;
+        const int id = i < n ? (in ? in[i] : i) : -1;
+        const int c = i < n ? key(id) : -1;
         int rank = 0;
-        for (int k = 0; k < BAMF_N_CLASSES; ++k) {
-            unsigned m = __ballot_sync(0xffffffffu, c == k);
+        for (int k = 0; k < K; ++k) {
+            const unsigned m = __ballot_sync(0xffffffffu, c == k);
             if (c == k) rank = __popc(m & ((1u << lane) - 1u));
             if (lane == 0) wbase[wid][k] = __popc(m);
         }
         __syncthreads();
-        if (threadIdx.x < BAMF_N_CLASSES) {
-            int k = threadIdx.x, acc = pos[k];
+        for (int k = threadIdx.x; k < K; k += blockDim.x) {
+            int acc = pos[k];
             for (int w = 0; w < nw; ++w) {
-                int t = wbase[w][k];
+                const int t = wbase[w][k];
                 wbase[w][k] = acc;
                 acc += t;
             }
             pos[k] = acc;
         }
         __syncthreads();
-        if (c >= 0) order[wbase[wid][c] + rank] = i;
+        if (c >= 0) out[wbase[wid][c] + rank] = id;
         __syncthreads();
     }
+}
+
+/* The batch order: ROI ids by size class, largest class first, and within a
+ * class by photon bucket, brightest first (two stable passes: bucket, then
+ * class), plus the [begin, end) of every class.  The chains of a
+ * move-synchronous CTA then carry similar emitter counts (they wait less
+ * for each other at the per-jump barrier) and the costliest chains of a
+ * class start first. */
+__global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__restrict__ ys,
+                             const uint8_t *__restrict__ bucket, int n, int32_t *__restrict__ tmp,
+                             int32_t *__restrict__ order, int32_t *__restrict__ class_range)
+{
+    block_count_sort<BAMF_N_BUCKETS>(n, nullptr, tmp, nullptr, [&](int id) { return (int)bucket[id]; });
+    __syncthreads();
+    block_count_sort<BAMF_N_CLASSES>(n, tmp, order, class_range, [&](int id) {
+        return side_class(min(max(max(xs[id], ys[id]), 1), BAMF_MAX_ROI_SIDE));
+    });
+}
+
+/* Enqueues the batch order on s: `order_scratch` holds BAMF_ORDER_SCRATCH(n)
+ * bytes (the order first, then the buckets and the first pass's ids). */
+bamf_status launch_batch_order(const bamf_roi_batch *rois, int n, void *order_scratch, int32_t *class_range,
+                               cudaStream_t s)
+{
+    int32_t *order = (int32_t *)order_scratch;
+    int32_t *tmp = order + n;
+    uint8_t *bucket = (uint8_t *)(tmp + n);
+    photon_bucket_kernel<<<(unsigned)(((int64_t)n * 32 + 255) / 256), 256, 0, s>>>(rois->data, rois->offsets,
+                                                                                   rois->xsize, rois->ysize, n,
+                                                                                   bucket);
+    order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, bucket, n, tmp, order, class_range);
+    return cudaGetLastError() == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;
 }
 
 /* Checks of the proposal fields of a batch and of the trace outputs, shared
@@ -518,11 +584,10 @@ extern "C" bamf_status bamf_rjmcmc_batch_device(bamf_workspace *ws, const bamf_r
         B.x_trace = out->x_trace;
         B.x_cap = out->trace_len;
     }
-    if ((r = ws->order.ensure((size_t)n * sizeof(int32_t) + 256))) return r;
+    if ((r = ws->order.ensure(BAMF_ORDER_SCRATCH(n) + 256))) return r;
     B.order = (int32_t *)((char *)ws->order.p + 256);
     int32_t *class_range = (int32_t *)ws->order.p; /* 2 * BAMF_N_CLASSES ints */
-    order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)B.order, class_range);
-    CU(cudaGetLastError());
+    if ((r = launch_batch_order(rois, n, (char *)ws->order.p + 256, class_range, s))) return r;
     B.class_range = class_range;
     if (out->n_trace) {
         B.nsig_trace = out->n_trace;
@@ -646,13 +711,12 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
     B.sampled_psf = rois->opt_model == 1 ? rois->sampled_psf : nullptr;
     B.psf_slot = rois->opt_model == 1 ? rois->psf_slot : nullptr;
     B.n_psf = std::max(rois->n_psf, 1);
-    if ((r = ws->order.ensure((size_t)n * sizeof(int32_t) + 256))) return r;
+    if ((r = ws->order.ensure(BAMF_ORDER_SCRATCH(n) + 256))) return r;
     if ((r = ws->tune_range.ensure(sizeof(int32_t) * 2 * BAMF_N_CLASSES))) return r;
     if ((r = ws->queue.ensure(sizeof(int32_t) * BAMF_N_CLASSES))) return r;
     B.order = (int32_t *)((char *)ws->order.p + 256);
     int32_t *class_range = (int32_t *)ws->order.p;
-    order_kernel<<<1, 1024, 0, s>>>(rois->xsize, rois->ysize, n, (int32_t *)B.order, class_range);
-    CU(cudaGetLastError());
+    if ((r = launch_batch_order(rois, n, (char *)ws->order.p + 256, class_range, s))) return r;
     int32_t cr[2 * BAMF_N_CLASSES];
     CU(cudaMemcpyAsync(cr, class_range, sizeof cr, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));

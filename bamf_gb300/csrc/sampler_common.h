@@ -95,6 +95,9 @@ struct SamplerBatch {
  * the move-synchronous fast kernel; a CTA holds at most this many chains. */
 #define BAMF_SYNC_GROUP 8
 #define BAMF_N_CLASSES 7
+/* device bytes of the batch order of n ROIs: the order, the ids of its
+ * first pass (4 bytes each) and the photon buckets (1 byte each) */
+#define BAMF_ORDER_SCRATCH(n) ((size_t)(n) * 9 + 16)
 __host__ __device__ inline int side_class(int side)
 {
     return side <= 8 ? 0 : (side <= 12 ? 1 : (side <= 16 ? 2 : (side <= 20 ? 3 : (side <= 24 ? 4 : (side <= 28 ? 5 : 6)))));

@@ -487,7 +487,7 @@ bamf_status bamf_autotune_shapes(const bamf_workspace *ws, int arith, int32_t *c
  * the library: every GPU that loads the library holds it until the process
  * exits, and every call shares it.  A call needs
  *   512 + sum over the 3 priors of 16*len (each rounded up to 256)
- *   + 4*n_rois (rounded up to 256)
+ *   + 9*n_rois + 16 (the batch order; rounded up to 256)
  *   + [map_n wanted] n_rois*(N_Burnin+N_Trials) (+ 4*n_rois if n_entries is NULL)
  * bytes; a call needing more returns BAMF_ERR_TOO_LARGE before any GPU work
  * (split the batch).
