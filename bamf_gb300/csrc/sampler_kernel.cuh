@@ -1123,8 +1123,11 @@ struct ChainWarp {
         if (is_burnin || !B->pgrid) return;
         int Z = K->p.Grid_Zoom;
         if (lane < an) {
-            int x = (int)floor(dadd((double)((float)Z * (aX + K->p.DriftX)), 0.5));
-            int y = (int)floor(dadd((double)((float)Z * (aY + K->p.DriftY)), 0.5));
+            /* the float sum with 0.5 is exact for |coordinate| < 2^22: fast
+             * mode rounds as the reference's double sum does */
+            const float gx = (float)Z * (aX + K->p.DriftX), gy = (float)Z * (aY + K->p.DriftY);
+            int x = EXACT ? (int)floor(dadd((double)gx, 0.5)) : (int)floorf(gx + 0.5f);
+            int y = EXACT ? (int)floor(dadd((double)gy, 0.5)) : (int)floorf(gy + 0.5f);
             float *gb = aS == 1 ? B->pgrid : B->pback;
             if (gb && x >= 0 && x < X * Z && y >= 0 && y < Y * Z && aI > K->p.Icutoff) {
                 /* grid slot (ROIs sharing one accumulate) and column stride */
