@@ -464,6 +464,17 @@ __global__ void order_kernel(const int32_t *__restrict__ xs, const int32_t *__re
     });
 }
 
+/* The autotuner's sample of a class: slots [lo, lo + m) of pick get m of
+ * the class's ROIs [lo, hi) of order, evenly strided, so that the sample
+ * spans the class's whole photon range (the order puts the brightest first)
+ * and neighbouring slots stay neighbours in brightness. */
+__global__ void strided_pick_kernel(const int32_t *__restrict__ order, int lo, int hi, int m,
+                                    int32_t *__restrict__ pick)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) pick[lo + j] = order[lo + (int)((int64_t)j * (hi - lo) / m)];
+}
+
 /* Enqueues the batch order on s: `order_scratch` holds BAMF_ORDER_SCRATCH(n)
  * bytes (the order first, then the buckets and the first pass's ids). */
 bamf_status launch_batch_order(const bamf_roi_batch *rois, int n, void *order_scratch, int32_t *class_range,
@@ -717,6 +728,9 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
     B.order = (int32_t *)((char *)ws->order.p + 256);
     int32_t *class_range = (int32_t *)ws->order.p;
     if ((r = launch_batch_order(rois, n, (char *)ws->order.p + 256, class_range, s))) return r;
+    /* the order's first-pass ids (dead once the order is built) hold the
+     * tuning samples */
+    int32_t *tune_order = (int32_t *)B.order + n;
     int32_t cr[2 * BAMF_N_CLASSES];
     CU(cudaMemcpyAsync(cr, class_range, sizeof cr, cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
@@ -735,22 +749,29 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
         if (hi <= lo) continue;
         SamplerBatch Bc = B;
         Bc.class_range = (const int32_t *)ws->tune_range.p;
+        Bc.order = tune_order;
         Bc.cls = c;
         Bc.queue = (int32_t *)ws->queue.p + c;
         Bc.side_max = std::min(class_side(c), side_max);
         float best_ms = 0.0f;
         int best = 0, best_mc = 0;
+        /* every shape runs the same ROIs: at least `sample`, and at least
+         * three rounds of the largest shape's resident chains, so that the
+         * wait for the last chains of a round weighs on every shape alike
+         * (at most the class) */
+        int max_resident = 0;
+        for (int k = 0; k < ncand; ++k) {
+            const int wpb = cand[k][0], mc = cand[k][1];
+            const int per = exact ? blocks_per_sm_exact(Bc.side_max, wpb, K.opt_model)
+                                  : blocks_per_sm_fast(Bc.side_max, wpb, mc, K.opt_model);
+            max_resident = std::max(max_resident, per * sms * wpb);
+        }
+        const int m = std::min(hi - lo, std::max(sample, 3 * max_resident));
         for (int k = 0; k < ncand && !res; ++k) {
             const int wpb = cand[k][0], mc = cand[k][1];
             int per = exact ? blocks_per_sm_exact(Bc.side_max, wpb, K.opt_model)
                             : blocks_per_sm_fast(Bc.side_max, wpb, mc, K.opt_model);
             if (per < 1) continue;
-            /* a whole number of rounds of this shape's resident chains (at
-             * least one), so that no shape is timed with a partial last
-             * round; compared per ROI */
-            const int resident = per * sms * wpb;
-            int m = std::max(resident, (sample / resident) * resident);
-            m = std::min(m, hi - lo);
             int32_t clip[2 * BAMF_N_CLASSES] = {};
             clip[2 * c] = lo;
             clip[2 * c + 1] = lo + m;
@@ -758,6 +779,7 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
                 res = BAMF_ERR_CUDA;
                 break;
             }
+            strided_pick_kernel<<<(m + 255) / 256, 256, 0, s>>>(B.order, lo, hi, m, tune_order);
             int blocks = std::min((m + wpb - 1) / wpb, per * sms);
             for (int rep = 0; rep < 2 && !res; ++rep) { /* the first launch warms up */
                 if (cudaMemsetAsync(Bc.queue, 0, sizeof(int32_t), s) != cudaSuccess ||

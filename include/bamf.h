@@ -456,10 +456,12 @@ void bamf_rjmcmc_batch_graph_destroy(bamf_batch_graph *graph);
 /* Autotuner (no reference counterpart): for every ROI size class present
  * in the (device) batch, times each CTA shape - 8, 4, 2 or 1 chains per CTA
  * in fast arithmetic, each with the kernel build whose registers are sized
- * for 2 or for 3 CTAs per SM; 4, 2 or 1 in exact - on about `sample` ROIs
- * of the class (a whole number of rounds of the shape's resident chains,
- * at least one, at most the class) with chains of `jumps` burn-in jumps,
- * and keeps the shape with the least time per ROI in the workspace; later bamf_rjmcmc_batch_device calls on that workspace launch
+ * for 2 or for 3 CTAs per SM; 4, 2 or 1 in exact - on the same ROIs of the
+ * class for every shape (at least `sample` and at least three rounds of
+ * the largest shape's resident chains, at most the class; evenly strided
+ * through the class in the batch order, so that they span its whole photon
+ * range) with chains of `jumps` burn-in jumps, and keeps the fastest shape
+ * in the workspace; later bamf_rjmcmc_batch_device calls on that workspace launch
  * each class with its tuned shape.  Results of a batch do not depend on
  * the shape.  Synchronises `stream`. */
 bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *rois, const bamf_mcmc_params *p,
