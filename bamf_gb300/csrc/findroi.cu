@@ -1108,9 +1108,10 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
          * global memory) */
         int hr = 0;
         if (n > (int64_t(1) << 24)) hr = 2 * (1 << std::min(7, std::max(0, std::ilogb((float)n) - 23)));
+        const bool idx64 = n > (int64_t(1) << 31) - 4096;
         while (hr > 0 && (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float) > 220 * 1024) hr /= 2;
         const size_t smem = (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float);
-        auto kern = n > (int64_t(1) << 31) - 4096 ? maxima_kernel<true> : maxima_kernel<false>;
+        auto kern = idx64 ? maxima_kernel<true> : maxima_kernel<false>;
         if (smem > 48 * 1024 &&
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return cuda_fail();
