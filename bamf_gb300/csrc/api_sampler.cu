@@ -739,10 +739,10 @@ extern "C" bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *r
     CU(cudaEventCreate(&e1));
     const int sms = sm_count();
     /* (chains per CTA, register budget in CTAs per SM) */
-    const int cand_f[8][2] = {{8, 2}, {4, 2}, {2, 2}, {1, 2}, {8, 3}, {4, 3}, {2, 3}, {1, 3}};
+    const int cand_f[9][2] = {{8, 2}, {4, 2}, {2, 2}, {1, 2}, {8, 3}, {4, 3}, {2, 3}, {1, 3}, {BAMF_SYNC_GROUP, 1}};
     const int cand_e[3][2] = {{4, 0}, {2, 0}, {1, 0}};
     const int(*cand)[2] = exact ? cand_e : cand_f;
-    const int ncand = exact ? 3 : 8;
+    const int ncand = exact ? 3 : 9;
     bamf_status res = BAMF_OK;
     for (int c = 0; c < BAMF_N_CLASSES && !res; ++c) {
         int lo = cr[2 * c], hi = cr[2 * c + 1];

@@ -93,7 +93,7 @@ struct SamplerBatch {
 /* Size classes by ROI side: (0,8] (8,12] (12,16] (16,20] (20,24] (24,28] (28,32]. */
 /* ROIs (consecutive slots of a size class) that share one move-type stream in
  * the move-synchronous fast kernel; a CTA holds at most this many chains. */
-#define BAMF_SYNC_GROUP 8
+#define BAMF_SYNC_GROUP 24
 #define BAMF_N_CLASSES 7
 /* device bytes of the batch order of n ROIs: the order, the ids of its
  * first pass (4 bytes each) and the photon buckets (1 byte each) */

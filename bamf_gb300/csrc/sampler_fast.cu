@@ -16,12 +16,14 @@ namespace bamf {
 cudaError_t launch_fast_gauss(const SamplerConsts &K, const SamplerBatch &B, size_t smem, int blocks, int threads,
                               int min_ctas, cudaStream_t stream)
 {
+    if (min_ctas == 1) return launch_kernel(rjmcmc_kernel_sync<false, 1>, K, B, smem, blocks, threads, stream);
     return min_ctas == 3 ? launch_kernel(rjmcmc_kernel_sync<false, 3>, K, B, smem, blocks, threads, stream)
                          : launch_kernel(rjmcmc_kernel_sync<false, 2>, K, B, smem, blocks, threads, stream);
 }
 
 int occupancy_fast_gauss(size_t smem, int threads, int min_ctas)
 {
+    if (min_ctas == 1) return resident_ctas(rjmcmc_kernel_sync<false, 1>, smem, threads);
     return min_ctas == 3 ? resident_ctas(rjmcmc_kernel_sync<false, 3>, smem, threads)
                          : resident_ctas(rjmcmc_kernel_sync<false, 2>, smem, threads);
 }
@@ -30,7 +32,7 @@ cudaError_t launch_rjmcmc_fast(const SamplerConsts &K, const SamplerBatch &B, in
                                int warps_per_block, int min_ctas, cudaStream_t stream)
 {
     if (warps_per_block < 1 || BAMF_SYNC_GROUP % warps_per_block != 0) return cudaErrorInvalidValue;
-    if (min_ctas != 2 && min_ctas != 3) return cudaErrorInvalidValue;
+    if (min_ctas < 1 || min_ctas > 3) return cudaErrorInvalidValue;
     size_t smem = (size_t)warp_smem_floats(side_max, false) * sizeof(float) * warps_per_block;
     (void)K.sync_moves; /* always move-synchronous in fast arithmetic */
     return K.opt_model == 1 ? launch_fast_num(K, B, smem, blocks, 32 * warps_per_block, min_ctas, stream)

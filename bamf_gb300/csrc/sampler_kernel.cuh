@@ -2175,7 +2175,7 @@ __global__ void __launch_bounds__(128, 4) rjmcmc_kernel(const __grid_constant__ 
  * barrier per jump, with the move type and jump sub-branch shared across the
  * CTA (run_chain_sync). */
 template <bool NUM, int MIN_CTAS>
-__global__ void __launch_bounds__(32 * BAMF_SYNC_GROUP, MIN_CTAS) rjmcmc_kernel_sync(const __grid_constant__ SamplerConsts Kc,
+__global__ void __launch_bounds__(MIN_CTAS == 1 ? 32 * BAMF_SYNC_GROUP : 256, MIN_CTAS) rjmcmc_kernel_sync(const __grid_constant__ SamplerConsts Kc,
                                                           const __grid_constant__ SamplerBatch Bc)
 {
     extern __shared__ float smem_raw[];
@@ -2209,7 +2209,7 @@ __global__ void __launch_bounds__(32 * BAMF_SYNC_GROUP, MIN_CTAS) rjmcmc_kernel_
         /* the shared move stream is keyed by the slot group of BAMF_SYNC_GROUP
          * ROIs, not by the CTA, so a chain's moves (and its result) do not
          * depend on the launch's warps per block (any divisor of the group) */
-        w.run_chain_sync(active, (uint32_t)(q_begin + ((base - q_begin) & ~(BAMF_SYNC_GROUP - 1))));
+        w.run_chain_sync(active, (uint32_t)(q_begin + (base - q_begin) / BAMF_SYNC_GROUP * BAMF_SYNC_GROUP));
         if (active) end_roi(w, Bt);
     }
 }

@@ -456,7 +456,8 @@ void bamf_rjmcmc_batch_graph_destroy(bamf_batch_graph *graph);
 /* Autotuner (no reference counterpart): for every ROI size class present
  * in the (device) batch, times each CTA shape - 8, 4, 2 or 1 chains per CTA
  * in fast arithmetic, each with the kernel build whose registers are sized
- * for 2 or for 3 CTAs per SM; 4, 2 or 1 in exact - on the same ROIs of the
+ * for 2 or for 3 CTAs per SM, and (Gaussian PSF) one CTA of 24 chains per
+ * SM, whose chains all follow one move stream; 4, 2 or 1 in exact - on the same ROIs of the
  * class for every shape (at least `sample` and at least three rounds of
  * the largest shape's resident chains, at most the class; evenly strided
  * through the class in the batch order, so that they span its whole photon
@@ -471,7 +472,7 @@ bamf_status bamf_autotune(bamf_workspace *ws, const bamf_roi_batch *rois, const 
 bamf_status bamf_autotune_result(const bamf_workspace *ws, int arith, int32_t *chains_per_cta);
 /* The tuned shapes with the fast kernel's register budget: chains_per_cta
  * as bamf_autotune_result, ctas_per_sm_budget[c] the CTAs per SM the chosen
- * build's registers are sized for (fast: 2 or 3; exact: 4; 0 untuned). */
+ * build's registers are sized for (fast: 1, 2 or 3; exact: 4; 0 untuned). */
 bamf_status bamf_autotune_shapes(const bamf_workspace *ws, int arith, int32_t *chains_per_cta,
                                  int32_t *ctas_per_sm_budget);
 
