@@ -60,6 +60,17 @@ int best_fast_shape(int side_max, int opt_model, int *warps_per_block, int *min_
                 best_per = per;
             }
         }
+    /* up to side 12, one CTA of a whole move-stream group per SM (all of
+     * the SM's warps on one instruction stream) measured faster than three
+     * CTAs of 8 chains, when it keeps as many chains resident */
+    if (side_max <= 12 && opt_model != 1) {
+        const int per = blocks_per_sm_fast(side_max, BAMF_SYNC_GROUP, 1, opt_model);
+        if (per * BAMF_SYNC_GROUP >= best_w) {
+            best_wpb = BAMF_SYNC_GROUP;
+            best_mc = 1;
+            best_per = per;
+        }
+    }
     *warps_per_block = best_wpb;
     *min_ctas = best_mc;
     return best_per;

@@ -23,7 +23,8 @@ cudaError_t launch_rjmcmc_exact(const SamplerConsts &K, const SamplerBatch &B, i
 int blocks_per_sm_exact(int side_max, int warps_per_block, int opt_model);
 
 /* the CTA shape with the most resident chains per SM for a fast launch
- * (ties: the larger register budget per thread, then more chains per CTA) */
+ * (ties: the larger register budget per thread, then more chains per CTA;
+ * up to side 12, a whole move-stream group per CTA when it keeps as many) */
 int best_fast_shape(int side_max, int opt_model, int *warps_per_block, int *min_ctas);
 
 /* per translation unit */
