@@ -656,7 +656,7 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
  * 2^32 pixels, whose 32-bit frame offset wraps as the reference's does)
  * reads global memory.  An index past the stack's end (only in the very
  * last row) is left out of the max (the reference reads beyond its buffer
- * there).  The window max walks the chunk's quad maxima (max of 4
+ * there).  The window max takes the chunk's quad maxima (max of 4
  * consecutive values) in steps of 4 and closes with the quad, pair or value
  * that ends the window (overlaps are harmless: max is idempotent).
  * Column maxima: van Herk / Gil-Werman over the tile's rows of |row max|,
@@ -738,7 +738,13 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
                 const Idx s = start - cbeg, e = end - cbeg;
                 if (s >= 0 && e < CW) {
                     const int si = (int)s, ei = (int)e;
-                    int i = si;
+                    /* the first six quads unrolled and predicated (windows
+                     * of up to 2k+1+2*(float spacing/2): 23 values at 2000
+                     * frames of 256x256, k = 7), then any further quads */
+#pragma unroll
+                    for (int q = 0; q < 6; ++q)
+                        if (si + 4 * q + 3 <= ei) maxval = fmaxf(maxval, p2[si + 4 * q]);
+                    int i = si + 4 * min(6, (ei - si + 1) >> 2);
                     for (; i + 3 <= ei; i += 4) maxval = fmaxf(maxval, p2[i]);
                     if (i <= ei)
                         maxval = fmaxf(maxval, ei - 3 >= si ? p2[ei - 3] : (ei > si ? fmaxf(p1[si], p1[ei - 1]) : ch[si]));
