@@ -929,22 +929,28 @@ __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ f
     }
 }
 
-/* ROI crop (findROI.m:157-160): ROIStack(:,:,b) = Image(rows, cols, Kk). */
+/* ROI crop (findROI.m:157-160): ROIStack(:,:,b) = Image(rows, cols, Kk).
+ * A warp per ROI, grid-stride over the ROIs found (the count is read on
+ * the device): the box's pixels in stack order, each column's run of box
+ * pixels contiguous in the frame; stores coalesced. */
 __global__ void crop_kernel(const float *__restrict__ frames, int Ysz, int Xsz,
                             const int32_t *__restrict__ coords, const int32_t *__restrict__ corners,
                             const int64_t *__restrict__ count, int box, float *__restrict__ stack,
                             int64_t capacity)
 {
-    int64_t nroi = *count < capacity ? *count : capacity;
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    int64_t per = (int64_t)box * box;
-    if (t >= nroi * per) return;
-    int64_t b = t / per;
-    int p = (int)(t - b * per);
-    int col = p / box, row = p - col * box;
-    int sr = corners[2 * b], sc = corners[2 * b + 1], kk = coords[3 * b + 2];
-    int64_t src = (int64_t)(sr - 1 + row) + (int64_t)(sc - 1 + col) * Ysz + (int64_t)(kk - 1) * Ysz * Xsz;
-    stack[t] = frames[src];
+    const int64_t nroi = *count < capacity ? *count : capacity;
+    const int lane = threadIdx.x & 31, per = box * box;
+    const int64_t plane = (int64_t)Ysz * Xsz;
+    for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nroi;
+         b += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int sr = corners[2 * b], sc = corners[2 * b + 1], kk = coords[3 * b + 2];
+        const float *src = frames + (int64_t)(kk - 1) * plane + (int64_t)(sc - 1) * Ysz + (sr - 1);
+        float *dst = stack + b * per;
+        for (int q = lane; q < per; q += 32) {
+            const int col = q / box, row = q - col * box;
+            dst[q] = src[(int64_t)col * Ysz + row];
+        }
+    }
 }
 
 struct Scratch {
@@ -1131,12 +1137,14 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
                                                   boxsize, capacity, coords, corners);
     if (cudaMemcpyAsync(count, ws->total.p, sizeof(int64_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return cuda_fail();
-    if (roi_stack) {
-        int64_t work = capacity * boxsize * boxsize;
-        if (work > 0)
-            crop_kernel<<<(unsigned)((work + 255) / 256), 256, 0, s>>>(frames, ysize, xsize, coords, corners,
-                                                                      (int64_t *)ws->total.p, boxsize,
-                                                                      roi_stack, capacity);
+    if (roi_stack && capacity > 0) {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int64_t warps = std::min<int64_t>(capacity, (int64_t)sms * 64);
+        crop_kernel<<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(frames, ysize, xsize, coords, corners,
+                                                                (int64_t *)ws->total.p, boxsize, roi_stack,
+                                                                capacity);
     }
     return launch_err();
 }
