@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <type_traits>
@@ -643,7 +644,8 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
 /* Passes 3 and 4, fused: kernel_maxX (window max along rows with floor
  * minval, +max / -max) then kernel_maxY (window max of |.| along columns,
  * flag where it equals the pixel within 1e-6), cuda_FindROI.cu:94-147.
- * One CTA per (32-column strip, MAX_TH-row tile, frame).
+ * One CTA per (32-column strip, MAX_TH-row tile, frame), over the frames
+ * [z0, z1) of the Z-frame stack.
  * Row maxima: every row-max value the tile's column windows need (its rows
  * and k above and below, clamped to the frame) is formed by a warp from a
  * linear chunk of the DoG stack staged in shared memory, the strip and H =
@@ -682,7 +684,8 @@ __host__ __device__ inline int maxima_smem_floats(int k, int hr)
 template <bool IDX64>
 __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__restrict__ dog,
                                                                 uint8_t *__restrict__ flags, int X, int Y,
-                                                                int Z, int k, float minval, float eps_hi, int hr)
+                                                                int Z, int z0, int z1, int k, float minval,
+                                                                float eps_hi, int hr)
 {
     using Idx = typename std::conditional<IDX64, int64_t, int>::type;
     extern __shared__ float sm[];
@@ -711,7 +714,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
                          : "memory");
         }
     };
-    for (int z = blockIdx.z; z < Z; z += gridDim.z) {
+    for (int z = z0 + blockIdx.z; z < z1; z += gridDim.z) {
         __syncthreads(); /* the tiles of the previous frame are consumed */
         const float zb = __uint2float_rn((unsigned)X * (unsigned)Y * (unsigned)z);
         int j = 0;
@@ -1019,9 +1022,11 @@ namespace {
  * exactly as inside the whole stack).  Frames whose two intermediate images
  * fit a slot take the fused filter (one slot per CTA, one CTA per SM, the
  * slots in ws->b); larger frames take rows_kernel + cols_kernel (the second
- * image in ws->b). */
+ * image in ws->b).  after_chunk, when given, is called with the number of
+ * frames filtered so far after each chunk's launches. */
 bamf_status run_filter(bamf_findroi_ws *ws, const float *host_frames, int chunk_frames, const float *frames,
-                       int KX, int KY, int zsize, double sigma1, double sigma2, float *dog, cudaStream_t s)
+                       int KX, int KY, int zsize, double sigma1, double sigma2, float *dog, cudaStream_t s,
+                       const std::function<bamf_status(int)> *after_chunk = nullptr)
 {
     const Coef ca = iir_coef(sigma1), cb = iir_coef(sigma2);
     int dev = 0, sms = 1;
@@ -1065,14 +1070,18 @@ bamf_status run_filter(bamf_findroi_ws *ws, const float *host_frames, int chunk_
                 filter_kernel<true><<<grid, FF_T, ff_smem, s>>>(frames + off, dog + off, Bb, KX, KY, zc, YP, ca, cb);
             else
                 filter_kernel<false><<<grid, FF_T, ff_smem, s>>>(frames + off, dog + off, Bb, KX, KY, zc, YP, ca, cb);
-            continue;
+        } else {
+            const int64_t nrows = (int64_t)KY * zc, ncols = (int64_t)KX * zc;
+            const int64_t groups = (nrows + 31) / 32;
+            const unsigned grid = (unsigned)std::max<int64_t>(
+                1, std::min<int64_t>((groups + ROWS_WARPS - 1) / ROWS_WARPS, (int64_t)sms * ROWS_CTAS_PER_SM));
+            rows_kernel<<<grid, 32 * ROWS_WARPS, 0, s>>>(frames + off, dog + off, Bb + off, KX, KY, zc, ca, cb);
+            cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(dog + off, Bb + off, KX, KY, zc, ca, cb);
         }
-        const int64_t nrows = (int64_t)KY * zc, ncols = (int64_t)KX * zc;
-        const int64_t groups = (nrows + 31) / 32;
-        const unsigned grid = (unsigned)std::max<int64_t>(
-            1, std::min<int64_t>((groups + ROWS_WARPS - 1) / ROWS_WARPS, (int64_t)sms * ROWS_CTAS_PER_SM));
-        rows_kernel<<<grid, 32 * ROWS_WARPS, 0, s>>>(frames + off, dog + off, Bb + off, KX, KY, zc, ca, cb);
-        cols_kernel<<<(unsigned)((ncols + 127) / 128), 128, 0, s>>>(dog + off, Bb + off, KX, KY, zc, ca, cb);
+        if (after_chunk) {
+            const bamf_status r = (*after_chunk)(z0 + zc);
+            if (r) return r;
+        }
     }
     return launch_err();
 }
@@ -1106,31 +1115,46 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
     if (!ws->chunks.ensure(nchunks * sizeof(int32_t)) || !ws->total.ensure(sizeof(int64_t)))
         return BAMF_ERR_CUDA;
     float *A = (float *)ws->a.p;
-    bamf_status st = run_filter(ws, host_frames, chunk_frames, frames, KX, KY, zsize, sigma1, sigma2, A, s);
-    if (st) return st;
-    {
-        /* the smallest float above the double 1e-6 */
-        float eps_hi = (float)1e-6;
-        if ((double)eps_hi <= 1e-6) eps_hi = std::nextafter(eps_hi, 1.0f);
-        /* how far the float-rounded window bounds can stray from the
-         * nominal ones: exact up to 2^24 stack pixels; above, each of the
-         * reference's two float additions and its float frame offset moves
-         * a bound by at most half the float spacing near n (halved while the
-         * tiles would not fit shared memory: windows that stray further read
-         * global memory) */
-        int hr = 0;
-        if (n > (int64_t(1) << 24)) hr = 2 * (1 << std::min(7, std::max(0, std::ilogb((float)n) - 23)));
-        const bool idx64 = n > (int64_t(1) << 31) - 4096;
-        while (hr > 0 && (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float) > 220 * 1024) hr /= 2;
-        const size_t smem = (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float);
-        auto kern = idx64 ? maxima_kernel<true> : maxima_kernel<false>;
-        if (smem > 48 * 1024 &&
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return cuda_fail();
+    /* the smallest float above the double 1e-6 */
+    float eps_hi = (float)1e-6;
+    if ((double)eps_hi <= 1e-6) eps_hi = std::nextafter(eps_hi, 1.0f);
+    /* how far the float-rounded window bounds can stray from the nominal
+     * ones: exact up to 2^24 stack pixels; above, each of the reference's two
+     * float additions and its float frame offset moves a bound by at most
+     * half the float spacing near n (halved while the tiles would not fit
+     * shared memory: windows that stray further read global memory) */
+    int hr = 0;
+    if (n > (int64_t(1) << 24)) hr = 2 * (1 << std::min(7, std::max(0, std::ilogb((float)n) - 23)));
+    const bool idx64 = n > (int64_t(1) << 31) - 4096;
+    while (hr > 0 && (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float) > 220 * 1024) hr /= 2;
+    const size_t smem = (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float);
+    auto kern = idx64 ? maxima_kernel<true> : maxima_kernel<false>;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return cuda_fail();
+    auto maxima = [&](int z0, int z1) {
+        if (z1 <= z0) return BAMF_OK;
         dim3 grid((unsigned)((KX + MAX_TW - 1) / MAX_TW), (unsigned)((KY + MAX_TH - 1) / MAX_TH),
-                  (unsigned)std::min(zsize, 65535));
-        kern<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, boxsize, minval, eps_hi, hr);
-    }
+                  (unsigned)std::min(z1 - z0, 65535));
+        kern<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, z0, z1, boxsize, minval, eps_hi, hr);
+        return launch_err();
+    };
+    /* frames in host memory: the maxima of a chunk's frames start once the
+     * chunk is filtered, while later chunks are still being copied, except
+     * the frames whose windows may reach into frames not filtered yet (the
+     * float-rounded bounds reach at most k + hr stack pixels past a frame) */
+    const int reach = 1 + (int)((int64_t)(boxsize + hr) / ((int64_t)KX * KY));
+    int done = 0;
+    const std::function<bamf_status(int)> after = [&](int filtered) {
+        const int upto = filtered >= zsize ? zsize : filtered - reach;
+        const bamf_status r = maxima(done, upto);
+        if (upto > done) done = upto;
+        return r;
+    };
+    bamf_status st = run_filter(ws, host_frames, chunk_frames, frames, KX, KY, zsize, sigma1, sigma2, A, s,
+                                host_frames ? &after : nullptr);
+    if (st) return st;
+    if ((st = maxima(done, zsize))) return st;
     count_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
     scan_kernel<<<1, 1024, 0, s>>>((int32_t *)ws->chunks.p, nchunks, (int64_t *)ws->total.p);
     emit_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p, ysize, xsize,
