@@ -13,7 +13,10 @@ followed by the MAP emitter-count reduction.
 value     ROIs/s with inputs resident in HBM (device entry point)
 e2e       ROIs/s through bamf_rjmcmc_batch_host with host buffers (H2D/D2H inside)
 roofline  the sampler kernel against the measured MUFU log2 rate: one log2 per
-          ROI pixel per scored proposal (the likelihood-ratio pass)
+          ROI pixel per scored proposal (the likelihood-ratio pass); traffic =
+          the DRAM bytes (read + write) of the step's sampler launches measured
+          by ncu on this workload (dram__bytes_read.sum + dram__bytes_write.sum),
+          given only for that configuration
 cpu_baseline  the reference sampler (source/c/LibRJMCMC.cpp compiled unmodified,
           glibc math; the C restatement where that build is absent, and
           beside it where present) on all host cores, on a sample with the
@@ -56,6 +59,16 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) measured by ncu,
+# one pass, on GB300:
+#   the five sampler launches of one step of the default workload (100k ROIs,
+#   3000+3000 jumps): 159.1 MB read + 294.0 MB written (mostly the per-jump
+#   count trace of the MAP summary);
+#   the FindROI kernels of one whole-stack call on 600 frames of 256x256
+#   (filter, maxima, count, scan, emit, crop): 764.1 MB, scaled by frames.
+SAMPLER_STEP_DRAM_BYTES = {(100_000, 3000): 453.1e6}
+FINDROI_DRAM_BYTES_PER_FRAME = 764.1e6 / 600
 
 METRIC = "RJMCMC ROIs/s (batched sampler, 3000+3000 jumps per ROI)"
 
@@ -250,7 +263,9 @@ def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3, fp32_peak: fl
         "workload": f"FindROI + gaussMLE: {n_frames} frames 256x256, Boxsize 7, 10 iterations",
         "findroi_ms": tf * 1e3, "findroi_frames_per_s": n_frames / tf,
         "findroi_roofline": {"bound": "hbm", "achieved": alg / tf / 1e9, "peak": peak, "unit": "GB/s",
-                             "frac": alg / tf / 1e9 / peak, "traffic": None, "peak_source": src,
+                             "frac": alg / tf / 1e9 / peak, "traffic": FINDROI_DRAM_BYTES_PER_FRAME * n_frames,
+                             "traffic_note": "DRAM bytes of a 600-frame call measured by ncu, scaled by frames",
+                             "peak_source": src,
                              "algorithmic_bytes": alg},
         "maxima": count, "gaussmle_ms": tm * 1e3, "gaussmle_fits_per_s": count / tm,
         "gaussmle_achieved_gbs": count * (49 + 9) * 4.0 / tm / 1e9,
@@ -619,7 +634,8 @@ def main():
                        "ctas_per_sm_register_budget_by_size_class": budget},
             "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": mufu.value / 1e9,
                          "unit": "Gop/s (MUFU log2)", "frac": achieved / mufu.value,
-                         "traffic": None,
+                         "traffic": SAMPLER_STEP_DRAM_BYTES.get((a.n_rois, a.jumps)),
+                         "traffic_unit": "bytes per step (all sampler launches)",
                          "peak_source": "measured in-process by bamf_probe_peaks (MUFU lg2 probe)",
                          "fp32_peak_tflops_measured": fp32.value / 1e12},
             "cpu_baseline": cpu, "e2e": e2e,
