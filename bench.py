@@ -570,11 +570,12 @@ def main():
     if rank == 0:
         noalloc_block = noalloc_bench(s, dev, outs, p, rj, bg0, n, stream)
 
-    # per step: order_kernel, one sampler launch per non-empty size class, map_n_kernel
+    # per step: photon_bucket_kernel and order_kernel (the batch order), one sampler launch per
+    # non-empty size class, map_n_kernel
     sides = np.maximum(b.xsize, b.ysize)
     bounds = [8, 12, 16, 20, 24, 28, 32]
     classes = {next(i for i, hi in enumerate(bounds) if sd <= hi) for sd in np.unique(sides)}
-    launches_per_step = 2 + len(classes)
+    launches_per_step = 3 + len(classes)
 
     learned_block = None
     if rank == 0 and not a.no_learned:
