@@ -570,9 +570,10 @@ bamf_status bamf_find_roi_host(const float *frames, int ysize, int xsize, int zs
  * host_frames (pinned, for the copies to overlap) into dev_frames (the
  * same size, device) in chunks of chunk_frames frames on a stream of the
  * workspace, and starts each chunk's row and column filters on `stream`
- * as soon as its copy has landed; the window maxima and the rest run on
- * the whole stack afterwards.  Outputs identical to bamf_find_roi_device
- * on the same frames (the filters are frame-local).  Enqueued on stream;
+ * as soon as its copy has landed, then the window maxima of the chunk's
+ * frames (those whose windows cannot reach a frame not yet filtered); the
+ * compaction and crops run on the whole stack afterwards.  Outputs
+ * identical to bamf_find_roi_device on the same frames.  Enqueued on stream;
  * host_frames must stay valid until the stream reaches this call's end. */
 bamf_status bamf_find_roi_pinned(bamf_findroi_ws *ws, const float *host_frames, float *dev_frames,
                                  int chunk_frames, int ysize, int xsize, int zsize, double sigma1,
