@@ -794,6 +794,248 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
     }
 }
 
+/* Passes 3 and 4 for rows of a multiple of 4 floats, Boxsize up to 12 and
+ * stacks indexed in 32 bits (maxima_kernel takes the others): the same
+ * flags from a CTA per (WIDE_TW-column strip, TH-row tile, frame) in which
+ * a lane owns 4 adjacent columns.
+ * Row maxima: a warp stages the strip's chunk of a row and H = k + hr values
+ * either side of it (16-byte copies from the multiple of 4 at or below the
+ * chunk's start), then a sparse table over it: level L holds, from each
+ * index, the maximum of the 2^L values starting there; levels 1 to 3 come
+ * from one pass over three staged quads in registers, higher ones from the
+ * level below, up to the longest window among the warp's columns.  A window
+ * [s, e], its bounds formed in float over the stack's linear index as the
+ * reference forms them, is max(T_L[s], T_L[e + 1 - 2^L]) with
+ * 2^L <= e - s + 1 < 2^(L+1): two overlapping halves, exact because max is
+ * idempotent.  A window outside the chunk, or longer than the levels built,
+ * reads global memory.
+ * Column maxima: van Herk / Gil-Werman in registers, a thread per (column,
+ * half of the tile's windows), blocks of W = 2k+1 rows from the half's first
+ * window start: the window starting at offset j of a block is the block's
+ * maximum for j = 0 and else max(h_j, g_(j-1)), h the maximum from offset j
+ * to the block's end (kept from the previous block) and g the maximum from
+ * the next block's start (accumulated while it is read).  Windows clamped to
+ * the frame's first or last row are scanned directly.
+ * KT > 0 fixes k = KT at compile time; KT = 0 takes k up to 12 at run time. */
+constexpr int WIDE_TW = 128, WIDE_WARPS = 8, WIDE_TH = 128;
+
+/* 16-byte units staged per row: the chunk [start - H, start + WIDE_TW + H)
+ * from the multiple of 4 at or below its first index */
+__host__ __device__ inline int wide_units(int H) { return (((-H) & 3) + WIDE_TW + 2 * H + 3) >> 2; }
+/* words per staged row or table level (level builds read up to 8 words
+ * past the staged ones) */
+__host__ __device__ inline int wide_cwp(int H) { return 4 * wide_units(H) + 8; }
+/* per warp: two staged rows (slots 0 and 1, level 0) and level L in slot
+ * L + 1 for L = 1..max(LV, 3) */
+__host__ __device__ inline int wide_slots(int LV) { return (LV > 3 ? LV : 3) + 2; }
+/* shared memory of maxima_wide_kernel in 4-byte words: the warps' slots,
+ * then the row-max tile [TH + 2k][WIDE_TW] */
+__host__ __device__ inline int wide_smem_floats(int k, int H, int LV, int TH)
+{
+    return WIDE_WARPS * wide_slots(LV) * wide_cwp(H) + (TH + 2 * k) * WIDE_TW;
+}
+
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, float a, float b, float c, float d)
+{
+    *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
+}
+
+template <int KT>
+__global__ void __launch_bounds__(32 * WIDE_WARPS, 2)
+    maxima_wide_kernel(const float *__restrict__ dog, uint8_t *__restrict__ flags, int X, int Y, int Z, int z0,
+                       int z1, int k_arg, float minval, float eps_hi, int H, int LV, int TH)
+{
+    constexpr int WMAX = KT > 0 ? 2 * KT + 1 : 25;
+    const int k = KT > 0 ? KT : k_arg, W = KT > 0 ? WMAX : 2 * k + 1;
+    extern __shared__ __align__(16) float sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int sh = (-H) & 3, units = wide_units(H), CWP = wide_cwp(H), staged = 4 * units;
+    float *wb = sm + warp * wide_slots(LV) * CWP;
+    float *rmT = sm + WIDE_WARPS * wide_slots(LV) * CWP;
+    const int n = X * Y * Z;
+    const int c0 = blockIdx.x * WIDE_TW, r0 = blockIdx.y * TH;
+    const int r1 = min(Y, r0 + TH) - 1;
+    const int rlo = max(0, r0 - k), rhi = min(Y - 1, r1 + k);
+    float lo[4], hi[4];
+    bool on[4];
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+        const int c = c0 + 4 * lane + jj;
+        on[jj] = c < X;
+        lo[jj] = fmaxf(0.0f, (float)(c - k));
+        hi[jj] = fminf((float)(X - 1), (float)(c + k));
+    }
+    /* row r's chunk from index cb4 = its strip start - H - sh (a multiple of
+     * 4, as is n: a unit lies wholly inside or outside the stack) */
+    auto stage = [&](int z, int r, float *buf) {
+        const int cb4 = (z * Y + r) * X + c0 - H - sh;
+        for (int u = lane; u < units; u += 32) {
+            const int g = cb4 + 4 * u;
+            const bool in = g >= 0 && g < n;
+            const unsigned d = (unsigned)__cvta_generic_to_shared(buf + 4 * u);
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(in ? dog + g : dog),
+                         "r"(in ? 16 : 0)
+                         : "memory");
+        }
+    };
+    for (int z = z0 + blockIdx.z; z < z1; z += gridDim.z) {
+        __syncthreads(); /* the tile of the previous frame is consumed */
+        const float zb = __uint2float_rn((unsigned)X * (unsigned)Y * (unsigned)z);
+        int j = 0;
+        if (rlo + warp <= rhi) stage(z, rlo + warp, wb);
+        cp_commit();
+        for (int r = rlo + warp; r <= rhi; r += WIDE_WARPS, ++j) {
+            float *ch = wb + (j & 1) * CWP;
+            if (r + WIDE_WARPS <= rhi) stage(z, r + WIDE_WARPS, wb + ((j + 1) & 1) * CWP);
+            cp_commit();
+            cp_wait_prev();
+            __syncwarp();
+            const int cb4 = (z * Y + r) * X + c0 - H - sh;
+            const float rb = __uint2float_rn((unsigned)X * (unsigned)r);
+            int s[4], e[4];
+            int lmax = 1;
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) {
+                const int start = (int)__fadd_rn(__fadd_rn(lo[jj], rb), zb);
+                const int end = min((int)__fadd_rn(__fadd_rn(hi[jj], rb), zb), n - 1);
+                s[jj] = start - cb4;
+                e[jj] = end - cb4;
+                if (on[jj]) lmax = max(lmax, e[jj] - s[jj] + 1);
+            }
+            lmax = __reduce_max_sync(0xffffffffu, lmax);
+            const int nl = min(LV, 31 - __clz(lmax));
+            if (nl >= 1) {
+                float *t1 = wb + 2 * CWP, *t2 = wb + 3 * CWP, *t3 = wb + 4 * CWP;
+                for (int q = lane; q < units; q += 32) {
+                    const float4 a = ld4(ch + 4 * q), b = ld4(ch + 4 * q + 4), c = ld4(ch + 4 * q + 8);
+                    const float x[11] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z};
+                    float p[10], f[8];
+#pragma unroll
+                    for (int i = 0; i < 10; ++i) p[i] = fmaxf(x[i], x[i + 1]);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) f[i] = fmaxf(p[i], p[i + 2]);
+                    st4(t1 + 4 * q, p[0], p[1], p[2], p[3]);
+                    st4(t2 + 4 * q, f[0], f[1], f[2], f[3]);
+                    st4(t3 + 4 * q, fmaxf(f[0], f[4]), fmaxf(f[1], f[5]), fmaxf(f[2], f[6]), fmaxf(f[3], f[7]));
+                }
+                __syncwarp();
+                for (int L = 4; L <= nl; ++L) {
+                    const float *prev = wb + L * CWP;
+                    float *cur = wb + (L + 1) * CWP;
+                    const int d = 1 << (L - 1), nq = (staged - (1 << L) + 4) >> 2;
+                    for (int q = lane; q < nq; q += 32) {
+                        const float4 a = ld4(prev + 4 * q), b = ld4(prev + 4 * q + d);
+                        st4(cur + 4 * q, fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z), fmaxf(a.w, b.w));
+                    }
+                    __syncwarp();
+                }
+            }
+            /* the maximum of chunk values [a, b], 1 <= b - a + 1 < 2^(nl+1) */
+            auto window = [&](int a, int b) {
+                const int L = 31 - __clz(b - a + 1);
+                const float *t = L == 0 ? ch : wb + (L + 1) * CWP;
+                return fmaxf(t[a], t[b + 1 - (1 << L)]);
+            };
+            /* a lane's 4 columns are all inside the frame or all outside it
+             * (X and c0 are multiples of 4), and their bounds grow with the
+             * column: every window of the warp lies in the chunk, is not
+             * empty and has its level built, or the per-column path runs */
+            const bool fast =
+                __all_sync(0xffffffffu, !on[0] || (s[0] >= 0 && e[3] < staged &&
+                                                   min(min(e[0] - s[0], e[1] - s[1]), min(e[2] - s[2], e[3] - s[3])) >= 0)) &&
+                lmax < (2 << nl);
+            const float4 px = ld4(ch + 4 * lane + H + sh);
+            const float pix[4] = {px.x, px.y, px.z, px.w};
+            float rm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (on[0]) {
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj) {
+                    const int a = s[jj], b = e[jj], len = b - a + 1;
+                    float m = -INFINITY;
+                    if (fast) {
+                        m = window(a, b);
+                    } else if (len > 0) {
+                        if (a >= 0 && b < staged && len < (2 << nl))
+                            m = window(a, b);
+                        else
+                            for (int i = cb4 + a; i <= cb4 + b; ++i) m = fmaxf(m, __ldg(&dog[i]));
+                    }
+                    const float maxval = fmaxf(minval, m);
+                    rm[jj] = maxval > pix[jj] ? -maxval : (maxval == pix[jj] ? maxval : 0.0f);
+                }
+            }
+            st4(rmT + (r - rlo) * WIDE_TW + 4 * lane, rm[0], rm[1], rm[2], rm[3]);
+            __syncwarp(); /* this buffer and the levels are rewritten for the warp's next rows */
+        }
+        __syncthreads();
+        const int cl = threadIdx.x & (WIDE_TW - 1), part = threadIdx.x / WIDE_TW;
+        const int c = c0 + cl;
+        if (c < X) {
+            uint8_t *fl = flags + (int64_t)z * Y * X + c;
+            const float *col = rmT + cl;
+            /* (double)d < 1e-6 for a float d is d < eps_hi, the float just
+             * above the double 1e-6 */
+            auto flag = [&](uint8_t *p, int i, float m) {
+                *p = fabsf(__fsub_rn(fmaxf(minval, m), col[i * WIDE_TW])) < eps_hi ? 1 : 0;
+            };
+            /* rows whose window [r - k, r + k] lies in the frame; window
+             * starts (tile rows) [s_lo, s_lo + cnt), split in two halves */
+            const int ia = max(r0, k), ib = min(r1, Y - 1 - k);
+            if (ib >= ia) {
+                const int s_lo = ia - k - rlo, cnt = ib - ia + 1, half = (cnt + 1) >> 1;
+                const int sb = s_lo + part * half, se = min(s_lo + cnt - 1, sb + half - 1), emax = se + 2 * k;
+                if (sb <= se) {
+                    /* rows past emax are read as emax: they reach only g
+                     * values and blocks that no emitted window uses */
+                    float v[WMAX], hp[WMAX];
+#pragma unroll
+                    for (int q = 0; q < WMAX; ++q)
+                        if (q < W) v[q] = fabsf(col[min(sb + q, emax) * WIDE_TW]);
+                    float m = -INFINITY;
+#pragma unroll
+                    for (int q = WMAX - 1; q >= 0; --q)
+                        if (q < W) {
+                            m = fmaxf(m, v[q]);
+                            hp[q] = m;
+                        }
+                    for (int base = sb + W; base - W <= se; base += W) {
+#pragma unroll
+                        for (int q = 0; q < WMAX; ++q)
+                            if (q < W) v[q] = fabsf(col[min(base + q, emax) * WIDE_TW]);
+                        float g = -INFINITY;
+                        uint8_t *fp = fl + (int64_t)(base - W + k + rlo) * X;
+#pragma unroll
+                        for (int q = 0; q < WMAX; ++q)
+                            if (q < W) {
+                                if (base - W + q <= se) flag(fp, base - W + q + k, fmaxf(hp[q], g));
+                                g = fmaxf(g, v[q]);
+                                fp += X;
+                            }
+                        m = -INFINITY;
+#pragma unroll
+                        for (int q = WMAX - 1; q >= 0; --q)
+                            if (q < W) {
+                                m = fmaxf(m, v[q]);
+                                hp[q] = m;
+                            }
+                    }
+                }
+            }
+            /* windows clamped to the frame: rows above k, then rows within
+             * k of the last one (and not above k) */
+            auto direct = [&](int r) {
+                const int s = max(0, r - k) - rlo, e = min(Y - 1, r + k) - rlo;
+                float m = -INFINITY;
+                for (int i = s; i <= e; ++i) m = fmaxf(m, fabsf(col[i * WIDE_TW]));
+                flag(fl + (int64_t)r * X, r - rlo, m);
+            };
+            for (int r = r0 + part; r <= min(r1, k - 1); r += 2) direct(r);
+            for (int r = max(max(r0, Y - k), k) + part; r <= r1; r += 2) direct(r);
+        }
+    }
+}
+
 /* Compaction: chunks of CHUNK pixels, one block of 256 threads each, a
  * thread owning 32 consecutive pixels (two 16-byte loads of flags where the
  * 32 lie inside the stack and are 16-byte aligned). */
@@ -1125,25 +1367,54 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
      * shared memory: windows that stray further read global memory) */
     int hr = 0;
     if (n > (int64_t(1) << 24)) hr = 2 * (1 << std::min(7, std::max(0, std::ilogb((float)n) - 23)));
+    const int hr_bound = hr;
     const bool idx64 = n > (int64_t(1) << 31) - 4096;
-    while (hr > 0 && (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float) > 220 * 1024) hr /= 2;
-    const size_t smem = (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float);
+    /* maxima_wide_kernel where it applies: row-max tiles of WIDE_TH rows or
+     * fewer and table levels for windows up to 2k + 1 + hr, within two CTAs
+     * per SM (hr halved last) */
+    bool wide = KX % 4 == 0 && boxsize <= 12 && !idx64 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+    int wth = WIDE_TH, wlv = 0;
+    size_t wsmem = 0;
+    if (wide) {
+        constexpr size_t limit = 112 * 1024;
+        auto size_for = [&](int th, int h) {
+            wlv = 0;
+            while ((2 << wlv) <= 2 * boxsize + 1 + h) ++wlv;
+            return (size_t)wide_smem_floats(boxsize, boxsize + h, wlv, th) * sizeof(float);
+        };
+        while (wth > 32 && size_for(wth, hr) > limit) wth /= 2;
+        while (hr > 0 && size_for(wth, hr) > limit) hr /= 2;
+        wsmem = size_for(wth, hr);
+        wide = wsmem <= limit;
+    }
+    if (!wide)
+        while (hr > 0 && (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float) > 220 * 1024) hr /= 2;
+    const size_t smem = wide ? wsmem : (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float);
     auto kern = idx64 ? maxima_kernel<true> : maxima_kernel<false>;
-    if (smem > 48 * 1024 &&
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    auto wkern = boxsize == 7 ? maxima_wide_kernel<7> : boxsize == 8 ? maxima_wide_kernel<8> : maxima_wide_kernel<0>;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(wide ? (const void *)wkern : (const void *)kern,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return cuda_fail();
     auto maxima = [&](int z0, int z1) {
         if (z1 <= z0) return BAMF_OK;
-        dim3 grid((unsigned)((KX + MAX_TW - 1) / MAX_TW), (unsigned)((KY + MAX_TH - 1) / MAX_TH),
-                  (unsigned)std::min(z1 - z0, 65535));
-        kern<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, z0, z1, boxsize, minval, eps_hi, hr);
+        if (wide) {
+            dim3 grid((unsigned)((KX + WIDE_TW - 1) / WIDE_TW), (unsigned)((KY + wth - 1) / wth),
+                      (unsigned)std::min(z1 - z0, 65535));
+            wkern<<<grid, 32 * WIDE_WARPS, smem, s>>>(A, flags, KX, KY, zsize, z0, z1, boxsize, minval, eps_hi,
+                                                      boxsize + hr, wlv, wth);
+        } else {
+            dim3 grid((unsigned)((KX + MAX_TW - 1) / MAX_TW), (unsigned)((KY + MAX_TH - 1) / MAX_TH),
+                      (unsigned)std::min(z1 - z0, 65535));
+            kern<<<grid, 32 * MAX_WARPS, smem, s>>>(A, flags, KX, KY, zsize, z0, z1, boxsize, minval, eps_hi, hr);
+        }
         return launch_err();
     };
     /* frames in host memory: the maxima of a chunk's frames start once the
      * chunk is filtered, while later chunks are still being copied, except
      * the frames whose windows may reach into frames not filtered yet (the
-     * float-rounded bounds reach at most k + hr stack pixels past a frame) */
-    const int reach = 1 + (int)((int64_t)(boxsize + hr) / ((int64_t)KX * KY));
+     * float-rounded bounds reach at most k + hr_bound stack pixels past a
+     * frame) */
+    const int reach = 1 + (int)((int64_t)(boxsize + hr_bound) / ((int64_t)KX * KY));
     int done = 0;
     const std::function<bamf_status(int)> after = [&](int filtered) {
         const int upto = filtered >= zsize ? zsize : filtered - reach;

@@ -64,6 +64,20 @@ def test_findroi_small_and_edge_frames(cuda_lib):
     assert len(coords) >= 3
 
 
+@pytest.mark.parametrize("boxsize", [3, 12, 13])
+def test_findroi_boxsizes_on_both_maxima_kernels(cuda_lib, boxsize):
+    """Boxsize 3 and 12 take the wide maxima kernel with k chosen at run time
+    (7 and 8 have their own instantiations), 13 the 32-column kernel: the
+    same coordinates and crops as the oracle."""
+    st, _ = synth.frames(6, seed=11)
+    ref = oracle.findroi(st, 1.3, 2.6, boxsize)
+    SMD, rois, coords = frontend.findROI(st, 1.3, 2.6, boxsize)
+    assert len(coords) > 3
+    np.testing.assert_array_equal(coords, ref["coords"])
+    np.testing.assert_array_equal(SMD["XBoxCorner"], ref["XBoxCorner"])
+    np.testing.assert_array_equal(rois, ref["ROIStack"])
+
+
 @pytest.mark.parametrize("shape", [(320, 320), (250, 96), (96, 250), (33, 47)])
 def test_findroi_frame_shapes_on_both_filter_paths(cuda_lib, shape):
     """Frames whose intermediate images do not fit the fused filter's slot

@@ -13,7 +13,8 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.skipif(not refgpu.available("findroi"), reason="reference FindROI cubin not built")
 @pytest.mark.parametrize("nframes,box,minval", [(12, 7, None), (6, 8, 1500 / (4 * np.pi * 1.3 ** 2) / 4),
-                                                (300, 7, None), (1100, 7, None)])
+                                                (300, 7, None), (1100, 7, None), (300, 12, None),
+                                                (300, 3, None), (40, 13, None)])
 def test_findroi_flags_identical_to_reference_kernels(cuda_lib, nframes, box, minval):
     import torch
     from bamf_gb300 import frontend, synth
