@@ -311,7 +311,9 @@ constexpr int FF_T = 256;   /* threads: rows of a row group / columns of a colum
 constexpr int FF_CW = 32;   /* columns per row-pass chunk, rows per column-pass tile */
 constexpr int FF_TS = 36;   /* tile row stride in floats: 16-byte rows, float4 reads conflict-free */
 constexpr size_t FF_MAX_SLOT = 80 * 1024; /* pixels per image in a slot (X * YP) */
-constexpr int FF_SMEM_FLOATS = 2 * 2 * FF_T * FF_TS; /* the largest phase: column tiles */
+/* per warp: the largest phase, two buffers of column tiles [sigma][32 columns][FF_TS] */
+constexpr int FF_WARP_FLOATS = 2 * 2 * 32 * FF_TS;
+constexpr int FF_SMEM_FLOATS = (FF_T / 32) * FF_WARP_FLOATS;
 
 /* L2 eviction priorities: the frames and the DoG stream through L2 once
  * (evict first); the slots are reused all the time (evict last) and are
@@ -423,40 +425,40 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
                                                          Coef ca, Coef cb)
 {
     extern __shared__ __align__(16) float fsm[];
-    const int t = threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t pf = l2_evict_first(), pl = l2_evict_last();
     const size_t img = (size_t)X * YP;
     float *FA = scratch + (size_t)blockIdx.x * 2 * img, *FB = FA + img;
+    float *wsm = fsm + warp * FF_WARP_FLOATS; /* this warp's chunks and tiles */
     const int nch = (X + FF_CW - 1) / FF_CW, nq = (Y + FF_CW - 1) / FF_CW;
     for (int z = blockIdx.x; z < Z; z += gridDim.x) {
         const float *fin = in + (size_t)z * X * Y;
-        for (int rg = 0; rg < Y; rg += FF_T) {
-            const int nr = min(FF_T, Y - rg), r = rg + t;
-            const bool mine = t < nr;
+        /* rows: the warp's 32 rows of each group of FF_T */
+        for (int rg = 32 * warp; rg < Y; rg += FF_T) {
+            const int nr = min(32, Y - rg), r = rg + lane;
+            const bool mine = lane < nr;
             IirState a, b;
             /* ---- rows, forward: input chunk [row][FF_TS] */
             auto stage_in = [&](int c, float *buf) {
                 const int c0 = c * FF_CW, w = min(FF_CW, X - c0);
                 if (VEC) {
-                    const int p = t & 7;
+                    const int p = lane & 7;
                     if (4 * p < w)
-                        for (int i = t >> 3; i < nr; i += FF_T / 8)
+                        for (int i = lane >> 3; i < nr; i += 4)
                             cp_async16(buf + i * FF_TS + 4 * p, fin + (size_t)(rg + i) * X + c0 + 4 * p, pf);
-                } else {
-                    const int p = t & 31;
-                    if (p < w)
-                        for (int i = t >> 5; i < nr; i += FF_T / 32)
-                            cp_async4(buf + i * FF_TS + p, fin + (size_t)(rg + i) * X + c0 + p, pf);
+                } else if (lane < w) {
+                    for (int i = 0; i < nr; ++i)
+                        cp_async4(buf + i * FF_TS + lane, fin + (size_t)(rg + i) * X + c0 + lane, pf);
                 }
             };
-            stage_in(0, fsm);
+            stage_in(0, wsm);
             cp_commit();
             for (int c = 0; c < nch; ++c) {
-                if (c + 1 < nch) stage_in(c + 1, fsm + ((c + 1) & 1) * FF_T * FF_TS);
+                if (c + 1 < nch) stage_in(c + 1, wsm + ((c + 1) & 1) * 32 * FF_TS);
                 cp_commit();
                 cp_wait_prev();
-                __syncthreads();
-                const float *ti = fsm + (c & 1) * FF_T * FF_TS + t * FF_TS;
+                __syncwarp();
+                const float *ti = wsm + (c & 1) * 32 * FF_TS + lane * FF_TS;
                 const int c0 = c * FF_CW, w = min(FF_CW, X - c0);
                 if (mine) {
                     if (c == 0) {
@@ -484,42 +486,43 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
                         }
                     }
                 }
-                __syncthreads(); /* buffer c & 1 is restaged for chunk c + 2 */
+                __syncwarp(); /* buffer c & 1 is restaged for chunk c + 2; the slot stores are seen */
             }
-            /* ---- rows, backward: slot chunks [sigma][column][row] */
-            constexpr int BUF = 2 * FF_CW * FF_T;
+            /* ---- rows, backward: the warp's rows of the slot's chunks,
+             * [sigma][column][32 rows] */
+            constexpr int BUF = 2 * FF_CW * 32;
             auto stage_f = [&](int c, float *buf) {
                 const int c0 = c * FF_CW, w = min(FF_CW, X - c0), n4 = (nr + 3) >> 2;
-                const int q4 = t & 63;
+                const int q4 = lane & 7;
                 if (q4 < n4)
-                    for (int j = t >> 6; j < w; j += FF_T / 64) {
-                        cp_async16(buf + j * FF_T + 4 * q4, FA + (size_t)(c0 + j) * YP + rg + 4 * q4, pl);
-                        cp_async16(buf + (FF_CW + j) * FF_T + 4 * q4, FB + (size_t)(c0 + j) * YP + rg + 4 * q4, pl);
+                    for (int j = lane >> 3; j < w; j += 4) {
+                        cp_async16(buf + j * 32 + 4 * q4, FA + (size_t)(c0 + j) * YP + rg + 4 * q4, pl);
+                        cp_async16(buf + (FF_CW + j) * 32 + 4 * q4, FB + (size_t)(c0 + j) * YP + rg + 4 * q4, pl);
                     }
             };
-            stage_f(nch - 1, fsm);
+            stage_f(nch - 1, wsm);
             cp_commit();
             for (int ci = 0; ci < nch; ++ci) {
                 const int c = nch - 1 - ci;
-                if (c > 0) stage_f(c - 1, fsm + ((ci + 1) & 1) * BUF);
+                if (c > 0) stage_f(c - 1, wsm + ((ci + 1) & 1) * BUF);
                 cp_commit();
                 cp_wait_prev();
-                __syncthreads();
-                const float *fa = fsm + (ci & 1) * BUF + t, *fb = fa + FF_CW * FF_T;
+                __syncwarp();
+                const float *fa = wsm + (ci & 1) * BUF + lane, *fb = fa + FF_CW * 32;
                 const int c0 = c * FF_CW, w = min(FF_CW, X - c0);
                 if (mine) {
                     if (ci == 0) {
-                        a.init(fa[(w - 1) * FF_T]);
-                        b.init(fb[(w - 1) * FF_T]);
+                        a.init(fa[(w - 1) * 32]);
+                        b.init(fb[(w - 1) * 32]);
                     }
                     float *pa = FA + (size_t)c0 * YP + r, *pb = FB + (size_t)c0 * YP + r;
                     if (w == FF_CW) {
 #pragma unroll 1
                         for (int j4 = FF_CW - 4; j4 >= 0; j4 -= 4) {
-                            const float xa[4] = {fa[(j4 + 3) * FF_T], fa[(j4 + 2) * FF_T], fa[(j4 + 1) * FF_T],
-                                                 fa[j4 * FF_T]};
-                            const float xb[4] = {fb[(j4 + 3) * FF_T], fb[(j4 + 2) * FF_T], fb[(j4 + 1) * FF_T],
-                                                 fb[j4 * FF_T]};
+                            const float xa[4] = {fa[(j4 + 3) * 32], fa[(j4 + 2) * 32], fa[(j4 + 1) * 32],
+                                                 fa[j4 * 32]};
+                            const float xb[4] = {fb[(j4 + 3) * 32], fb[(j4 + 2) * 32], fb[(j4 + 1) * 32],
+                                                 fb[j4 * 32]};
                             float ya[4], yb[4];
                             steps4(a, b, ca, cb, xa, xb, ya, yb);
 #pragma unroll
@@ -530,38 +533,40 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
                         }
                     } else {
                         for (int j = w - 1; j >= 0; --j) {
-                            st_hint(pa + (size_t)j * YP, a.step(fa[j * FF_T], ca), pl);
-                            st_hint(pb + (size_t)j * YP, b.step(fb[j * FF_T], cb), pl);
+                            st_hint(pa + (size_t)j * YP, a.step(fa[j * 32], ca), pl);
+                            st_hint(pb + (size_t)j * YP, b.step(fb[j * 32], cb), pl);
                         }
                     }
                 }
-                __syncthreads();
+                __syncwarp();
             }
         }
-        /* ---- columns: tiles [sigma][column][FF_TS] of FF_CW rows */
-        constexpr int TBUF = 2 * FF_T * FF_TS;
-        for (int cg = 0; cg < X; cg += FF_T) {
-            const int nc = min(FF_T, X - cg), col = cg + t;
-            const bool mine = t < nc;
+        __syncthreads(); /* every row of the frame is in the slot */
+        /* columns: the warp's 32 columns of each group of FF_T, tiles
+         * [sigma][column][FF_TS] of FF_CW rows */
+        constexpr int TBUF = 2 * 32 * FF_TS;
+        for (int cg = 32 * warp; cg < X; cg += FF_T) {
+            const int nc = min(32, X - cg), col = cg + lane;
+            const bool mine = lane < nc;
             auto stage_t = [&](int q, float *buf) {
-                const int p = t & 7;
-                for (int c = t >> 3; c < nc; c += FF_T / 8) {
+                const int p = lane & 7;
+                for (int c = lane >> 3; c < nc; c += 4) {
                     const size_t g = (size_t)(cg + c) * YP + q * FF_CW + 4 * p;
                     cp_async16(buf + c * FF_TS + 4 * p, FA + g, pl);
-                    cp_async16(buf + (FF_T + c) * FF_TS + 4 * p, FB + g, pl);
+                    cp_async16(buf + (32 + c) * FF_TS + 4 * p, FB + g, pl);
                 }
             };
             IirState a, b;
-            /* forward */
-            stage_t(0, fsm);
+            /* ---- columns, forward */
+            stage_t(0, wsm);
             cp_commit();
             for (int q = 0; q < nq; ++q) {
-                if (q + 1 < nq) stage_t(q + 1, fsm + ((q + 1) & 1) * TBUF);
+                if (q + 1 < nq) stage_t(q + 1, wsm + ((q + 1) & 1) * TBUF);
                 cp_commit();
                 cp_wait_prev();
-                __syncthreads();
-                float *buf = fsm + (q & 1) * TBUF;
-                float *ta = buf + t * FF_TS, *tb = ta + FF_T * FF_TS;
+                __syncwarp();
+                float *buf = wsm + (q & 1) * TBUF;
+                float *ta = buf + lane * FF_TS, *tb = ta + 32 * FF_TS;
                 const int nr = min(FF_CW, Y - q * FF_CW);
                 if (mine) {
                     if (q == 0) {
@@ -586,27 +591,27 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
                         }
                     }
                 }
-                __syncthreads();
+                __syncwarp();
                 {
-                    const int p = t & 7;
-                    for (int c = t >> 3; c < nc; c += FF_T / 8) {
+                    const int p = lane & 7;
+                    for (int c = lane >> 3; c < nc; c += 4) {
                         const size_t g = (size_t)(cg + c) * YP + q * FF_CW + 4 * p;
                         st4_hint(FA + g, *reinterpret_cast<const float4 *>(buf + c * FF_TS + 4 * p), pl);
-                        st4_hint(FB + g, *reinterpret_cast<const float4 *>(buf + (FF_T + c) * FF_TS + 4 * p), pl);
+                        st4_hint(FB + g, *reinterpret_cast<const float4 *>(buf + (32 + c) * FF_TS + 4 * p), pl);
                     }
                 }
-                __syncthreads(); /* buffer q & 1 is restaged for tile q + 2 */
+                __syncwarp(); /* buffer q & 1 is restaged for tile q + 2; the slot stores are seen */
             }
-            /* backward, DoG out */
-            stage_t(nq - 1, fsm);
+            /* ---- columns, backward, DoG out */
+            stage_t(nq - 1, wsm);
             cp_commit();
             for (int qi = 0; qi < nq; ++qi) {
                 const int q = nq - 1 - qi;
-                if (q > 0) stage_t(q - 1, fsm + ((qi + 1) & 1) * TBUF);
+                if (q > 0) stage_t(q - 1, wsm + ((qi + 1) & 1) * TBUF);
                 cp_commit();
                 cp_wait_prev();
-                __syncthreads();
-                const float *ta = fsm + (qi & 1) * TBUF + t * FF_TS, *tb = ta + FF_T * FF_TS;
+                __syncwarp();
+                const float *ta = wsm + (qi & 1) * TBUF + lane * FF_TS, *tb = ta + 32 * FF_TS;
                 const int nr = min(FF_CW, Y - q * FF_CW);
                 if (mine) {
                     if (qi == 0) {
@@ -631,11 +636,12 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
                             st_hint(pd + (size_t)i * X, __fsub_rn(a.step(ta[i], ca), b.step(tb[i], cb)), pf);
                     }
                 }
-                __syncthreads();
+                __syncwarp();
             }
         }
+        __syncthreads(); /* every read of the slot is done */
         /* the frame's slot is dead: drop its lines without writing them back */
-        for (size_t off = (size_t)t * 32; off < 2 * img; off += (size_t)FF_T * 32) discard_line(FA + off);
+        for (size_t off = (size_t)threadIdx.x * 32; off < 2 * img; off += (size_t)FF_T * 32) discard_line(FA + off);
         __syncthreads();
     }
 }
