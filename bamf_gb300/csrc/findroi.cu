@@ -356,6 +356,31 @@ __device__ __forceinline__ void st_hint(float *g, float v, uint64_t pol)
     asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(g), "f"(v), "l"(pol));
 }
 
+/* st_hint at g + OFF bytes, the offset folded into the address */
+template <int OFF>
+__device__ __forceinline__ void st_hint_at(float *g, float v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.f32 [%0+%3], %1, %2;" ::"l"(g), "f"(v), "l"(pol), "n"(OFF));
+}
+
+/* v0..v3 to g[0], g[stride], g[2 stride], g[3 stride]; with the stride
+ * known at compile time (S > 0) the offsets are immediates */
+template <int S>
+__device__ __forceinline__ void st_hint_4(float *g, int stride, float v0, float v1, float v2, float v3, uint64_t pol)
+{
+    if (S > 0) {
+        st_hint_at<0>(g, v0, pol);
+        st_hint_at<4 * S>(g, v1, pol);
+        st_hint_at<8 * S>(g, v2, pol);
+        st_hint_at<12 * S>(g, v3, pol);
+    } else {
+        st_hint(g, v0, pol);
+        st_hint(g + stride, v1, pol);
+        st_hint(g + 2 * (size_t)stride, v2, pol);
+        st_hint(g + 3 * (size_t)stride, v3, pol);
+    }
+}
+
 __device__ __forceinline__ void st4_hint(float *g, float4 v, uint64_t pol)
 {
     asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(g), "f"(v.x), "f"(v.y),
@@ -419,11 +444,13 @@ __device__ __forceinline__ void steps4(IirState &a, IirState &b, const Coef &ca,
     }
 }
 
-template <bool VEC>
+/* F > 0: frames of F x F pixels (YP = F), the strides compile-time */
+template <bool VEC, int F>
 __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict__ in, float *__restrict__ dog,
-                                                         float *__restrict__ scratch, int X, int Y, int Z, int YP,
+                                                         float *__restrict__ scratch, int X_, int Y_, int Z, int YP_,
                                                          Coef ca, Coef cb)
 {
+    const int X = F > 0 ? F : X_, Y = F > 0 ? F : Y_, YP = F > 0 ? F : YP_;
     extern __shared__ __align__(16) float fsm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t pf = l2_evict_first(), pl = l2_evict_last();
@@ -473,11 +500,8 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
                             const float x[4] = {v.x, v.y, v.z, v.w};
                             float ya[4], yb[4];
                             steps4(a, b, ca, cb, x, x, ya, yb);
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                st_hint(pa + (size_t)(j4 + u) * YP, ya[u], pl);
-                                st_hint(pb + (size_t)(j4 + u) * YP, yb[u], pl);
-                            }
+                            st_hint_4<F>(pa + (size_t)j4 * YP, YP, ya[0], ya[1], ya[2], ya[3], pl);
+                            st_hint_4<F>(pb + (size_t)j4 * YP, YP, yb[0], yb[1], yb[2], yb[3], pl);
                         }
                     } else {
                         for (int j = 0; j < w; ++j) {
@@ -525,11 +549,8 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
                                                  fb[j4 * 32]};
                             float ya[4], yb[4];
                             steps4(a, b, ca, cb, xa, xb, ya, yb);
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                st_hint(pa + (size_t)(j4 + 3 - u) * YP, ya[u], pl);
-                                st_hint(pb + (size_t)(j4 + 3 - u) * YP, yb[u], pl);
-                            }
+                            st_hint_4<F>(pa + (size_t)j4 * YP, YP, ya[3], ya[2], ya[1], ya[0], pl);
+                            st_hint_4<F>(pb + (size_t)j4 * YP, YP, yb[3], yb[2], yb[1], yb[0], pl);
                         }
                     } else {
                         for (int j = w - 1; j >= 0; --j) {
@@ -627,9 +648,8 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
                             const float xa[4] = {va.w, va.z, va.y, va.x}, xb[4] = {vb.w, vb.z, vb.y, vb.x};
                             float ya[4], yb[4];
                             steps4(a, b, ca, cb, xa, xb, ya, yb);
-#pragma unroll
-                            for (int u = 0; u < 4; ++u)
-                                st_hint(pd + (size_t)(i4 + 3 - u) * X, __fsub_rn(ya[u], yb[u]), pf);
+                            st_hint_4<F>(pd + (size_t)i4 * X, X, __fsub_rn(ya[3], yb[3]), __fsub_rn(ya[2], yb[2]),
+                                         __fsub_rn(ya[1], yb[1]), __fsub_rn(ya[0], yb[0]), pf);
                         }
                     } else {
                         for (int i = nr - 1; i >= 0; --i)
@@ -822,7 +842,8 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
  * to the block's end (kept from the previous block) and g the maximum from
  * the next block's start (accumulated while it is read).  Windows clamped to
  * the frame's first or last row are scanned directly.
- * KT > 0 fixes k = KT at compile time; KT = 0 takes k up to 12 at run time. */
+ * KT > 0 fixes k = KT at compile time; KT = 0 takes k up to 12 at run time.
+ * F > 0 fixes X = Y = F. */
 constexpr int WIDE_TW = 128, WIDE_WARPS = 8, WIDE_TH = 128;
 
 /* 16-byte units staged per row: the chunk [start - H, start + WIDE_TW + H)
@@ -847,11 +868,12 @@ __device__ __forceinline__ void st4(float *p, float a, float b, float c, float d
     *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
 }
 
-template <int KT>
+template <int KT, int F>
 __global__ void __launch_bounds__(32 * WIDE_WARPS, 2)
-    maxima_wide_kernel(const float *__restrict__ dog, uint8_t *__restrict__ flags, int X, int Y, int Z, int z0,
+    maxima_wide_kernel(const float *__restrict__ dog, uint8_t *__restrict__ flags, int X_, int Y_, int Z, int z0,
                        int z1, int k_arg, float minval, float eps_hi, int H, int LV, int TH)
 {
+    const int X = F > 0 ? F : X_, Y = F > 0 ? F : Y_;
     constexpr int WMAX = KT > 0 ? 2 * KT + 1 : 25;
     const int k = KT > 0 ? KT : k_arg, W = KT > 0 ? WMAX : 2 * k + 1;
     extern __shared__ __align__(16) float sm[];
@@ -1290,8 +1312,10 @@ bamf_status run_filter(bamf_findroi_ws *ws, const float *host_frames, int chunk_
     float *Bb = (float *)ws->b.p;
     const bool vec = KX % 4 == 0 && (reinterpret_cast<uintptr_t>(frames) & 15) == 0;
     const size_t ff_smem = (size_t)FF_SMEM_FLOATS * sizeof(float);
-    if (fused && cudaFuncSetAttribute(vec ? filter_kernel<true> : filter_kernel<false>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff_smem) != cudaSuccess)
+    /* 256 x 256 frames (the common camera region) have their own build */
+    auto ff = vec ? (KX == 256 && KY == 256 ? filter_kernel<true, 256> : filter_kernel<true, 0>)
+                  : filter_kernel<false, 0>;
+    if (fused && cudaFuncSetAttribute(ff, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ff_smem) != cudaSuccess)
         return cuda_fail();
     if (host_frames) {
         if (!ws->copy && cudaStreamCreateWithFlags(&ws->copy, cudaStreamNonBlocking) != cudaSuccess)
@@ -1314,10 +1338,7 @@ bamf_status run_filter(bamf_findroi_ws *ws, const float *host_frames, int chunk_
         }
         if (fused) {
             const unsigned grid = (unsigned)std::min(zc, ff_grid);
-            if (vec)
-                filter_kernel<true><<<grid, FF_T, ff_smem, s>>>(frames + off, dog + off, Bb, KX, KY, zc, YP, ca, cb);
-            else
-                filter_kernel<false><<<grid, FF_T, ff_smem, s>>>(frames + off, dog + off, Bb, KX, KY, zc, YP, ca, cb);
+            ff<<<grid, FF_T, ff_smem, s>>>(frames + off, dog + off, Bb, KX, KY, zc, YP, ca, cb);
         } else {
             const int64_t nrows = (int64_t)KY * zc, ncols = (int64_t)KX * zc;
             const int64_t groups = (nrows + 31) / 32;
@@ -1397,7 +1418,10 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
         while (hr > 0 && (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float) > 220 * 1024) hr /= 2;
     const size_t smem = wide ? wsmem : (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float);
     auto kern = idx64 ? maxima_kernel<true> : maxima_kernel<false>;
-    auto wkern = boxsize == 7 ? maxima_wide_kernel<7> : boxsize == 8 ? maxima_wide_kernel<8> : maxima_wide_kernel<0>;
+    const bool f256 = KX == 256 && KY == 256;
+    auto wkern = boxsize == 7   ? (f256 ? maxima_wide_kernel<7, 256> : maxima_wide_kernel<7, 0>)
+                 : boxsize == 8 ? (f256 ? maxima_wide_kernel<8, 256> : maxima_wide_kernel<8, 0>)
+                                : maxima_wide_kernel<0, 0>;
     if (smem > 48 * 1024 && cudaFuncSetAttribute(wide ? (const void *)wkern : (const void *)kern,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return cuda_fail();
