@@ -707,7 +707,7 @@ __host__ __device__ inline int maxima_smem_floats(int k, int hr)
     return MAX_WARPS * 4 * maxima_cwp(k, hr) + 3 * (MAX_TH + 2 * k) * MAX_TW + (MAX_TH + 2 * k);
 }
 
-template <bool IDX64>
+template <bool IDX64, bool WORDS>
 __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__restrict__ dog,
                                                                 uint8_t *__restrict__ flags, int X, int Y,
                                                                 int Z, int z0, int z1, int k, float minval,
@@ -803,7 +803,7 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
             }
         }
         __syncthreads();
-        if (c < X) {
+        if (c < X) { /* the whole warp or none of it where WORDS */
             uint8_t *fl = flags + ((int64_t)z * Y) * X + c;
             for (int r = r0 + warp; r <= r1; r += MAX_WARPS) {
                 const int s = max(0, r - k) - rlo, e = min(Y - 1, r + k) - rlo;
@@ -814,7 +814,14 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
                 const float inpixel = rmT[(r - rlo) * MAX_TW + lane];
                 /* (double)d < 1e-6 for a float d is d < eps_hi, the float
                  * just above the double 1e-6 */
-                fl[(int64_t)r * X] = fabsf(__fsub_rn(maxval, inpixel)) < eps_hi ? 1 : 0;
+                const bool f = fabsf(__fsub_rn(maxval, inpixel)) < eps_hi;
+                if (WORDS) {
+                    const unsigned b = __ballot_sync(0xffffffffu, f);
+                    if (lane == 0)
+                        reinterpret_cast<uint32_t *>(flags)[(((int64_t)z * Y + r) * X + c0) >> 5] = b;
+                } else {
+                    fl[(int64_t)r * X] = f ? 1 : 0;
+                }
             }
         }
     }
@@ -843,7 +850,9 @@ __global__ void __launch_bounds__(32 * MAX_WARPS) maxima_kernel(const float *__r
  * the next block's start (accumulated while it is read).  Windows clamped to
  * the frame's first or last row are scanned directly.
  * KT > 0 fixes k = KT at compile time; KT = 0 takes k up to 12 at run time.
- * F > 0 fixes X = Y = F. */
+ * F > 0 fixes X = Y = F.  WORDS (X a multiple of 32): the flags as a bit
+ * mask in memory order, bit p % 32 of word p / 32 for pixel p, a warp's 32
+ * columns of a row being one word; else one byte per pixel. */
 constexpr int WIDE_TW = 128, WIDE_WARPS = 8, WIDE_TH = 128;
 
 /* 16-byte units staged per row: the chunk [start - H, start + WIDE_TW + H)
@@ -868,7 +877,7 @@ __device__ __forceinline__ void st4(float *p, float a, float b, float c, float d
     *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
 }
 
-template <int KT, int F>
+template <int KT, int F, bool WORDS>
 __global__ void __launch_bounds__(32 * WIDE_WARPS, 2)
     maxima_wide_kernel(const float *__restrict__ dog, uint8_t *__restrict__ flags, int X_, int Y_, int Z, int z0,
                        int z1, int k_arg, float minval, float eps_hi, int H, int LV, int TH)
@@ -999,13 +1008,19 @@ __global__ void __launch_bounds__(32 * WIDE_WARPS, 2)
         __syncthreads();
         const int cl = threadIdx.x & (WIDE_TW - 1), part = threadIdx.x / WIDE_TW;
         const int c = c0 + cl;
-        if (c < X) {
-            uint8_t *fl = flags + (int64_t)z * Y * X + c;
+        if (c < X) { /* the whole warp or none of it where WORDS */
+            const int64_t fl = (int64_t)z * Y * X + c; /* pixel (z, 0, c) */
             const float *col = rmT + cl;
             /* (double)d < 1e-6 for a float d is d < eps_hi, the float just
              * above the double 1e-6 */
-            auto flag = [&](uint8_t *p, int i, float m) {
-                *p = fabsf(__fsub_rn(fmaxf(minval, m), col[i * WIDE_TW])) < eps_hi ? 1 : 0;
+            auto flag = [&](int64_t px, int i, float m) {
+                const bool f = fabsf(__fsub_rn(fmaxf(minval, m), col[i * WIDE_TW])) < eps_hi;
+                if (WORDS) {
+                    const unsigned b = __ballot_sync(0xffffffffu, f);
+                    if (lane == 0) reinterpret_cast<uint32_t *>(flags)[px >> 5] = b;
+                } else {
+                    flags[px] = f ? 1 : 0;
+                }
             };
             /* rows whose window [r - k, r + k] lies in the frame; window
              * starts (tile rows) [s_lo, s_lo + cnt), split in two halves */
@@ -1032,13 +1047,26 @@ __global__ void __launch_bounds__(32 * WIDE_WARPS, 2)
                         for (int q = 0; q < WMAX; ++q)
                             if (q < W) v[q] = fabsf(col[min(base + q, emax) * WIDE_TW]);
                         float g = -INFINITY;
-                        uint8_t *fp = fl + (int64_t)(base - W + k + rlo) * X;
+                        /* this block's first output row: its byte, or the
+                         * word of the warp's 32 columns, rows X apart */
+                        const int64_t px0 = fl + (int64_t)(base - W + k + rlo) * X;
+                        uint8_t *fb = flags + px0;
+                        uint32_t *fw = reinterpret_cast<uint32_t *>(flags) + (px0 >> 5);
+                        const float *ctr = col + (base - W + k) * WIDE_TW;
 #pragma unroll
                         for (int q = 0; q < WMAX; ++q)
                             if (q < W) {
-                                if (base - W + q <= se) flag(fp, base - W + q + k, fmaxf(hp[q], g));
+                                if (base - W + q <= se) {
+                                    const bool f =
+                                        fabsf(__fsub_rn(fmaxf(minval, fmaxf(hp[q], g)), ctr[q * WIDE_TW])) < eps_hi;
+                                    if (WORDS) {
+                                        const unsigned b = __ballot_sync(0xffffffffu, f);
+                                        if (lane == 0) fw[q * (X >> 5)] = b;
+                                    } else {
+                                        fb[q * X] = f ? 1 : 0;
+                                    }
+                                }
                                 g = fmaxf(g, v[q]);
-                                fp += X;
                             }
                         m = -INFINITY;
 #pragma unroll
@@ -1065,8 +1093,9 @@ __global__ void __launch_bounds__(32 * WIDE_WARPS, 2)
 }
 
 /* Compaction: chunks of CHUNK pixels, one block of 256 threads each, a
- * thread owning 32 consecutive pixels (two 16-byte loads of flags where the
- * 32 lie inside the stack and are 16-byte aligned). */
+ * thread owning 32 consecutive pixels: one word of the bit mask (WORDS; n a
+ * multiple of 32), or two 16-byte loads of byte flags where the 32 lie inside
+ * the stack and are 16-byte aligned. */
 constexpr int CHUNK = 256 * 32;
 
 /* the flags of pixels [j0, j0 + 32) as a bit mask, bit q = pixel j0 + q
@@ -1091,13 +1120,21 @@ __device__ __forceinline__ uint32_t flag_bits(const uint8_t *__restrict__ flags,
     return m;
 }
 
+template <bool WORDS>
+__device__ __forceinline__ uint32_t flag_word(const uint8_t *__restrict__ flags, int64_t n, int64_t j0)
+{
+    if (WORDS) return j0 < n ? reinterpret_cast<const uint32_t *>(flags)[j0 >> 5] : 0u;
+    return flag_bits(flags, n, j0);
+}
+
 /* phase 1: flags per chunk. */
+template <bool WORDS>
 __global__ void __launch_bounds__(256) count_kernel(const uint8_t *__restrict__ flags, int64_t n,
                                                     int32_t *__restrict__ counts)
 {
     __shared__ int wsum[8];
     const int64_t j0 = (int64_t)blockIdx.x * CHUNK + (int64_t)threadIdx.x * 32;
-    int local = __popc(flag_bits(flags, n, j0));
+    int local = __popc(flag_word<WORDS>(flags, n, j0));
     for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
     if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = local;
     __syncthreads();
@@ -1148,6 +1185,7 @@ __global__ void scan_kernel(int32_t *__restrict__ counts, int64_t nchunks,
 /* phase 3: write the flagged pixels of each chunk in memory order as MATLAB
  * 1-based (row, col, frame) = ind2sub([Ysize Xsize Zsize], m+1), plus the
  * clamped box corners of findROI.m:130-148. */
+template <bool WORDS>
 __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ flags, int64_t n,
                                                    const int32_t *__restrict__ offs, int Ysz,
                                                    int Xsz, int box, int64_t capacity,
@@ -1158,7 +1196,7 @@ __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ f
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     /* each thread owns 32 consecutive pixels: keeps memory order */
     const int64_t j0 = (int64_t)blockIdx.x * CHUNK + (int64_t)threadIdx.x * 32;
-    uint32_t bits = flag_bits(flags, n, j0);
+    uint32_t bits = flag_word<WORDS>(flags, n, j0);
     const int cnt = __popc(bits);
     int x = cnt;
     for (int o = 1; o < 32; o <<= 1) {
@@ -1376,8 +1414,11 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
     const int KX = xsize, KY = ysize;
     if (!ws->a.ensure(n * sizeof(float))) return BAMF_ERR_CUDA;
     uint8_t *flags = flags_out;
+    /* without byte flags asked for, rows of a multiple of 32 pixels keep the
+     * flags as a bit mask (a warp's 32 columns of a row are one word) */
+    const bool words = !flags_out && KX % 32 == 0;
     if (!flags) {
-        if (!ws->flags.ensure(n)) return BAMF_ERR_CUDA;
+        if (!ws->flags.ensure(words ? (size_t)(n / 8) : (size_t)n)) return BAMF_ERR_CUDA;
         flags = (uint8_t *)ws->flags.p;
     }
     int64_t nchunks = (n + CHUNK - 1) / CHUNK;
@@ -1417,11 +1458,18 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
     if (!wide)
         while (hr > 0 && (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float) > 220 * 1024) hr /= 2;
     const size_t smem = wide ? wsmem : (size_t)maxima_smem_floats(boxsize, hr) * sizeof(float);
-    auto kern = idx64 ? maxima_kernel<true> : maxima_kernel<false>;
+    auto kern = idx64 ? (words ? maxima_kernel<true, true> : maxima_kernel<true, false>)
+                      : (words ? maxima_kernel<false, true> : maxima_kernel<false, false>);
     const bool f256 = KX == 256 && KY == 256;
-    auto wkern = boxsize == 7   ? (f256 ? maxima_wide_kernel<7, 256> : maxima_wide_kernel<7, 0>)
-                 : boxsize == 8 ? (f256 ? maxima_wide_kernel<8, 256> : maxima_wide_kernel<8, 0>)
-                                : maxima_wide_kernel<0, 0>;
+    /* the 256 x 256 builds write the bit mask; byte flags asked for take the
+     * run-time build */
+    auto wkern = boxsize == 7
+                     ? (words ? (f256 ? maxima_wide_kernel<7, 256, true> : maxima_wide_kernel<7, 0, true>)
+                              : maxima_wide_kernel<7, 0, false>)
+                 : boxsize == 8
+                     ? (words ? (f256 ? maxima_wide_kernel<8, 256, true> : maxima_wide_kernel<8, 0, true>)
+                              : maxima_wide_kernel<8, 0, false>)
+                     : (words ? maxima_wide_kernel<0, 0, true> : maxima_wide_kernel<0, 0, false>);
     if (smem > 48 * 1024 && cudaFuncSetAttribute(wide ? (const void *)wkern : (const void *)kern,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return cuda_fail();
@@ -1456,10 +1504,13 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
                                 host_frames ? &after : nullptr);
     if (st) return st;
     if ((st = maxima(done, zsize))) return st;
-    count_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
+    if (words)
+        count_kernel<true><<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
+    else
+        count_kernel<false><<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
     scan_kernel<<<1, 1024, 0, s>>>((int32_t *)ws->chunks.p, nchunks, (int64_t *)ws->total.p);
-    emit_kernel<<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p, ysize, xsize,
-                                                  boxsize, capacity, coords, corners);
+    (words ? emit_kernel<true> : emit_kernel<false>)<<<(unsigned)nchunks, 256, 0, s>>>(
+        flags, n, (int32_t *)ws->chunks.p, ysize, xsize, boxsize, capacity, coords, corners);
     if (cudaMemcpyAsync(count, ws->total.p, sizeof(int64_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return cuda_fail();
     if (roi_stack && capacity > 0) {
