@@ -66,9 +66,9 @@ sys.path.insert(0, ROOT)
 #   3000+3000 jumps): 159.1 MB read + 294.0 MB written (mostly the per-jump
 #   count trace of the MAP summary);
 #   the FindROI kernels of one whole-stack call on 600 frames of 256x256
-#   (filter, wide maxima, count, scan, emit, crop): 771.1 MB, scaled by frames.
+#   (filter, wide maxima, count, scan, emit, crop): 671.2 MB, scaled by frames.
 SAMPLER_STEP_DRAM_BYTES = {(100_000, 3000): 453.1e6}
-FINDROI_DRAM_BYTES_PER_FRAME = 771.1e6 / 600
+FINDROI_DRAM_BYTES_PER_FRAME = 671.2e6 / 600
 
 METRIC = "RJMCMC ROIs/s (batched sampler, 3000+3000 jumps per ROI)"
 
