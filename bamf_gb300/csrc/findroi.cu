@@ -40,6 +40,7 @@
 #include <vector>
 
 #include "bamf.h"
+#include "frontend_launch.h"
 
 namespace {
 
@@ -1127,13 +1128,14 @@ __device__ __forceinline__ uint32_t flag_word(const uint8_t *__restrict__ flags,
     return flag_bits(flags, n, j0);
 }
 
-/* phase 1: flags per chunk. */
+/* phase 1: flags per chunk, chunks chunk0 + blockIdx.x. */
 template <bool WORDS>
 __global__ void __launch_bounds__(256) count_kernel(const uint8_t *__restrict__ flags, int64_t n,
-                                                    int32_t *__restrict__ counts)
+                                                    int32_t *__restrict__ counts, int64_t chunk0)
 {
     __shared__ int wsum[8];
-    const int64_t j0 = (int64_t)blockIdx.x * CHUNK + (int64_t)threadIdx.x * 32;
+    const int64_t c = chunk0 + blockIdx.x;
+    const int64_t j0 = c * CHUNK + (int64_t)threadIdx.x * 32;
     int local = __popc(flag_word<WORDS>(flags, n, j0));
     for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
     if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = local;
@@ -1141,17 +1143,23 @@ __global__ void __launch_bounds__(256) count_kernel(const uint8_t *__restrict__ 
     if (threadIdx.x == 0) {
         int s = 0;
         for (int k = 0; k < 8; ++k) s += wsum[k];
-        counts[blockIdx.x] = s;
+        counts[c] = s;
     }
 }
 
-/* phase 2: exclusive scan of the chunk counts (one block, serial tiles). */
-__global__ void scan_kernel(int32_t *__restrict__ counts, int64_t nchunks,
-                            int64_t *__restrict__ total)
+/* phase 2: exclusive scan of the chunk counts (one block, serial tiles),
+ * from *total on (accumulate) or from 0; *total becomes the sum, and range,
+ * when given, the [first, end) of the maxima these chunks hold. */
+__global__ void scan_kernel(int32_t *__restrict__ counts, int64_t nchunks, int64_t *__restrict__ total,
+                            bool accumulate, int64_t *__restrict__ range)
 {
     __shared__ int64_t carry;
     __shared__ int64_t warp_sums[32];
-    if (threadIdx.x == 0) carry = 0;
+    int64_t start = 0;
+    if (threadIdx.x == 0) {
+        start = accumulate ? *total : 0;
+        carry = start;
+    }
     __syncthreads();
     for (int64_t b0 = 0; b0 < nchunks; b0 += blockDim.x) {
         int64_t i = b0 + threadIdx.x;
@@ -1179,7 +1187,13 @@ __global__ void scan_kernel(int32_t *__restrict__ counts, int64_t nchunks,
         if (threadIdx.x == blockDim.x - 1) carry = incl;
         __syncthreads();
     }
-    if (threadIdx.x == 0) *total = carry;
+    if (threadIdx.x == 0) {
+        *total = carry;
+        if (range) {
+            range[0] = start;
+            range[1] = carry;
+        }
+    }
 }
 
 /* phase 3: write the flagged pixels of each chunk in memory order as MATLAB
@@ -1187,7 +1201,7 @@ __global__ void scan_kernel(int32_t *__restrict__ counts, int64_t nchunks,
  * clamped box corners of findROI.m:130-148. */
 template <bool WORDS>
 __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ flags, int64_t n,
-                                                   const int32_t *__restrict__ offs, int Ysz,
+                                                   const int32_t *__restrict__ offs, int64_t chunk0, int Ysz,
                                                    int Xsz, int box, int64_t capacity,
                                                    int32_t *__restrict__ coords,
                                                    int32_t *__restrict__ corners)
@@ -1195,7 +1209,8 @@ __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ f
     __shared__ int wsum[8];
     int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     /* each thread owns 32 consecutive pixels: keeps memory order */
-    const int64_t j0 = (int64_t)blockIdx.x * CHUNK + (int64_t)threadIdx.x * 32;
+    const int64_t c = chunk0 + blockIdx.x;
+    const int64_t j0 = c * CHUNK + (int64_t)threadIdx.x * 32;
     uint32_t bits = flag_word<WORDS>(flags, n, j0);
     const int cnt = __popc(bits);
     int x = cnt;
@@ -1207,7 +1222,7 @@ __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ f
     __syncthreads();
     int before = 0;
     for (int i = 0; i < w; ++i) before += wsum[i];
-    int64_t pos = (int64_t)offs[blockIdx.x] + before + x - cnt;
+    int64_t pos = (int64_t)offs[c] + before + x - cnt;
     const int half = (int)floor(box / 2.0 + 0.5);
     while (bits) {
         const int q = __ffs(bits) - 1;
@@ -1241,18 +1256,20 @@ __global__ void __launch_bounds__(256) emit_kernel(const uint8_t *__restrict__ f
 }
 
 /* ROI crop (findROI.m:157-160): ROIStack(:,:,b) = Image(rows, cols, Kk).
- * A warp per ROI, grid-stride over the ROIs found (the count is read on
- * the device): the box's pixels in stack order, each column's run of box
- * pixels contiguous in the frame; stores coalesced. */
+ * A warp per ROI, grid-stride over the ROIs found (the count, or the range
+ * [range[0], range[1]) when given, is read on the device): the box's pixels
+ * in stack order, each column's run of box pixels contiguous in the frame;
+ * stores coalesced. */
 __global__ void crop_kernel(const float *__restrict__ frames, int Ysz, int Xsz,
                             const int32_t *__restrict__ coords, const int32_t *__restrict__ corners,
-                            const int64_t *__restrict__ count, int box, float *__restrict__ stack,
-                            int64_t capacity)
+                            const int64_t *__restrict__ count, const int64_t *__restrict__ range, int box,
+                            float *__restrict__ stack, int64_t capacity)
 {
-    const int64_t nroi = *count < capacity ? *count : capacity;
+    const int64_t b0 = range ? range[0] : 0, b1 = range ? range[1] : *count;
+    const int64_t nroi = b1 < capacity ? b1 : capacity;
     const int lane = threadIdx.x & 31, per = box * box;
     const int64_t plane = (int64_t)Ysz * Xsz;
-    for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nroi;
+    for (int64_t b = b0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); b < nroi;
          b += ((int64_t)gridDim.x * blockDim.x) >> 5) {
         const int sr = corners[2 * b], sc = corners[2 * b + 1], kk = coords[3 * b + 2];
         const float *src = frames + (int64_t)(kk - 1) * plane + (int64_t)(sc - 1) * Ysz + (sr - 1);
@@ -1302,7 +1319,7 @@ bamf_status cuda_fail()
 }  // namespace
 
 struct bamf_findroi_ws {
-    Scratch a, b, flags, chunks, total;
+    Scratch a, b, flags, chunks, total, ranges;
     cudaStream_t copy = nullptr; /* host-to-device chunks of bamf_find_roi_pinned */
     cudaEvent_t landed = nullptr;
     ~bamf_findroi_ws()
@@ -1393,13 +1410,22 @@ bamf_status run_filter(bamf_findroi_ws *ws, const float *host_frames, int chunk_
     return launch_err();
 }
 
+/* gaussMLE of the ROIs found (bamf_find_roi_fit_pinned) */
+struct FitArgs {
+    float psf_sigma;
+    int iterations;
+    float *params, *crlb, *loglik; /* [4][capacity], [4][capacity], [capacity] */
+};
+
 /* Passes 1-5 on `frames` (device), copied first from host_frames when given
- * (run_filter); the window maxima and everything after them run on the
- * whole stack once every chunk is filtered. */
+ * (run_filter; each chunk's window maxima start once it is filtered).  The
+ * compaction and crop run on the whole stack at the end; with `fit`, the
+ * compaction, crops and fits run after each chunk's maxima on the flag
+ * chunks those complete, appended in memory order. */
 bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_frames, const float *frames,
                      int ysize, int xsize, int zsize, double sigma1, double sigma2, int boxsize, float minval,
                      int64_t capacity, int32_t *coords, int32_t *corners, float *roi_stack, int64_t *count,
-                     uint8_t *flags_out, cudaStream_t s)
+                     uint8_t *flags_out, cudaStream_t s, const FitArgs *fit = nullptr)
 {
     if (!ws || !frames || !coords || !count || ysize < 1 || xsize < 1 || zsize < 1 || boxsize < 1 ||
         capacity < 0)
@@ -1493,35 +1519,62 @@ bamf_status find_roi(bamf_findroi_ws *ws, const float *host_frames, int chunk_fr
      * float-rounded bounds reach at most k + hr_bound stack pixels past a
      * frame) */
     const int reach = 1 + (int)((int64_t)(boxsize + hr_bound) / ((int64_t)KX * KY));
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int32_t *cnt = (int32_t *)ws->chunks.p;
+    int64_t *total = (int64_t *)ws->total.p;
+    const unsigned crop_blocks = (unsigned)((std::min<int64_t>(std::max<int64_t>(capacity, 1), (int64_t)sms * 64) + 7) / 8);
+    if (fit) {
+        const int step = std::max(1, chunk_frames);
+        if (!ws->ranges.ensure((size_t)2 * ((zsize + step - 1) / step + 2) * sizeof(int64_t))) return BAMF_ERR_CUDA;
+    }
+    /* compaction of flag chunks [cdone, c1), their maxima after those of the
+     * chunks before; with `fit`, the crops and fits of those maxima */
+    int64_t cdone = 0;
+    int seg = 0;
+    auto compact = [&](int64_t c1) -> bamf_status {
+        if (c1 <= cdone) return BAMF_OK;
+        const unsigned nb = (unsigned)(c1 - cdone);
+        int64_t *range = fit ? (int64_t *)ws->ranges.p + 2 * seg : nullptr;
+        if (words)
+            count_kernel<true><<<nb, 256, 0, s>>>(flags, n, cnt, cdone);
+        else
+            count_kernel<false><<<nb, 256, 0, s>>>(flags, n, cnt, cdone);
+        scan_kernel<<<1, 1024, 0, s>>>(cnt + cdone, c1 - cdone, total, cdone > 0, range);
+        (words ? emit_kernel<true> : emit_kernel<false>)<<<nb, 256, 0, s>>>(
+            flags, n, cnt, cdone, ysize, xsize, boxsize, capacity, coords, corners);
+        if (fit) {
+            crop_kernel<<<crop_blocks, 256, 0, s>>>(frames, ysize, xsize, coords, corners, total, range, boxsize,
+                                                    roi_stack, capacity);
+            const bamf_status r = launch_gauss_mle_range(roi_stack, boxsize, fit->psf_sigma, fit->iterations,
+                                                         fit->params, fit->crlb, fit->loglik, capacity, range,
+                                                         capacity, sms * 8, s);
+            if (r) return r;
+        }
+        cdone = c1;
+        ++seg;
+        return launch_err();
+    };
     int done = 0;
     const std::function<bamf_status(int)> after = [&](int filtered) {
         const int upto = filtered >= zsize ? zsize : filtered - reach;
-        const bamf_status r = maxima(done, upto);
+        bamf_status r = maxima(done, upto);
         if (upto > done) done = upto;
+        /* the flag chunks wholly inside frames [0, upto) */
+        if (!r && fit) r = compact(upto >= zsize ? nchunks : (int64_t)upto * KX * KY / CHUNK);
         return r;
     };
     bamf_status st = run_filter(ws, host_frames, chunk_frames, frames, KX, KY, zsize, sigma1, sigma2, A, s,
                                 host_frames ? &after : nullptr);
     if (st) return st;
     if ((st = maxima(done, zsize))) return st;
-    if (words)
-        count_kernel<true><<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
-    else
-        count_kernel<false><<<(unsigned)nchunks, 256, 0, s>>>(flags, n, (int32_t *)ws->chunks.p);
-    scan_kernel<<<1, 1024, 0, s>>>((int32_t *)ws->chunks.p, nchunks, (int64_t *)ws->total.p);
-    (words ? emit_kernel<true> : emit_kernel<false>)<<<(unsigned)nchunks, 256, 0, s>>>(
-        flags, n, (int32_t *)ws->chunks.p, ysize, xsize, boxsize, capacity, coords, corners);
-    if (cudaMemcpyAsync(count, ws->total.p, sizeof(int64_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    if ((st = compact(nchunks))) return st;
+    if (cudaMemcpyAsync(count, total, sizeof(int64_t), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
         return cuda_fail();
-    if (roi_stack && capacity > 0) {
-        int dev = 0, sms = 1;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int64_t warps = std::min<int64_t>(capacity, (int64_t)sms * 64);
-        crop_kernel<<<(unsigned)((warps + 7) / 8), 256, 0, s>>>(frames, ysize, xsize, coords, corners,
-                                                                (int64_t *)ws->total.p, boxsize, roi_stack,
-                                                                capacity);
-    }
+    if (!fit && roi_stack && capacity > 0)
+        crop_kernel<<<crop_blocks, 256, 0, s>>>(frames, ysize, xsize, coords, corners, total, nullptr, boxsize,
+                                                roi_stack, capacity);
     return launch_err();
 }
 
@@ -1602,6 +1655,22 @@ extern "C" bamf_status bamf_find_roi_pinned(bamf_findroi_ws *ws, const float *ho
     if (!host_frames || chunk_frames < 1) return BAMF_ERR_INVALID_ARG;
     return find_roi(ws, host_frames, chunk_frames, dev_frames, ysize, xsize, zsize, sigma1, sigma2, boxsize,
                     minval, capacity, coords, corners, roi_stack, count, flags_out, (cudaStream_t)stream);
+}
+
+extern "C" bamf_status bamf_find_roi_fit_pinned(bamf_findroi_ws *ws, const float *host_frames, float *dev_frames,
+                                                int chunk_frames, int ysize, int xsize, int zsize, double sigma1,
+                                                double sigma2, int boxsize, float minval, int64_t capacity,
+                                                float psf_sigma, int iterations, int32_t *coords,
+                                                int32_t *corners, float *roi_stack, int64_t *count,
+                                                float *params, float *crlb, float *loglik, void *stream)
+{
+    if (!host_frames || chunk_frames < 1 || !corners || !roi_stack || !params || !crlb || !loglik ||
+        capacity < 1 || iterations < 0 || !(psf_sigma > 0.0f))
+        return BAMF_ERR_INVALID_ARG;
+    if (boxsize > GAUSS_MLE_MAX_SIZE) return BAMF_ERR_TOO_LARGE;
+    const FitArgs fit{psf_sigma, iterations, params, crlb, loglik};
+    return find_roi(ws, host_frames, chunk_frames, dev_frames, ysize, xsize, zsize, sigma1, sigma2, boxsize,
+                    minval, capacity, coords, corners, roi_stack, count, nullptr, (cudaStream_t)stream, &fit);
 }
 
 extern "C" bamf_status bamf_find_roi_host(const float *frames, int ysize, int xsize, int zsize,

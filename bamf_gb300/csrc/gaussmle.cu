@@ -17,10 +17,11 @@
 #include <cuda_runtime.h>
 
 #include "bamf.h"
+#include "frontend_launch.h"
 
 namespace {
 
-constexpr int MAXSZ = 21;        /* IMSZBIG of definitions.h: largest fit window */
+constexpr int MAXSZ = GAUSS_MLE_MAX_SIZE; /* IMSZBIG of definitions.h: largest fit window */
 #define MLE_PI 3.141592f         /* definitions.h:13 */
 
 /* kernel_IntGauss1D (GPUgaussLib.cuh:14-24) */
@@ -63,14 +64,16 @@ __device__ __forceinline__ float group_sum(float v)
     return v;
 }
 
-__global__ void __launch_bounds__(GL * GROUP_FITS_PER_BLOCK) mle_xynb_group_kernel(
-    const float *__restrict__ data, float sigma, int sz, int iterations,
-    float *__restrict__ P, float *__restrict__ CRLB, float *__restrict__ LL, int nfits)
+/* The nblk (<= GROUP_FITS_PER_BLOCK) fits from ROI `first` of `data`, by
+ * the whole CTA; parameter k of fit i to P[stride * k + i] and CRLB alike,
+ * the log-likelihood to LL[i].  Every thread returns here (lanes other than
+ * a group's first return early). */
+__device__ __forceinline__ void mle_xynb_block(const float *__restrict__ data, float sigma, int sz, int iterations,
+                                               float *__restrict__ P, float *__restrict__ CRLB,
+                                               float *__restrict__ LL, int64_t stride, int64_t first, int nblk)
 {
     extern __shared__ float sm[];
     const int npx = sz * sz;
-    const int64_t first = (int64_t)blockIdx.x * GROUP_FITS_PER_BLOCK;
-    const int nblk = (int)min((int64_t)GROUP_FITS_PER_BLOCK, (int64_t)nfits - first);
     /* coalesced staging of this block's ROIs; per fit 6 axis rows and the
      * start-up filter's weight table behind them */
     float *axis_all = sm + GROUP_FITS_PER_BLOCK * npx;
@@ -257,13 +260,54 @@ __global__ void __launch_bounds__(GL * GROUP_FITS_PER_BLOCK) mle_xynb_group_kern
         }
     }
     for (int k = 0; k < 4; k++) {
-        P[(int64_t)nfits * k + fit] = theta[k];
-        CRLB[(int64_t)nfits * k + fit] = Minv[k * n + k];
+        P[stride * k + fit] = theta[k];
+        CRLB[stride * k + fit] = Minv[k * n + k];
     }
     LL[fit] = Div;
 }
 
+__global__ void __launch_bounds__(GL * GROUP_FITS_PER_BLOCK) mle_xynb_group_kernel(
+    const float *__restrict__ data, float sigma, int sz, int iterations,
+    float *__restrict__ P, float *__restrict__ CRLB, float *__restrict__ LL, int nfits)
+{
+    const int64_t first = (int64_t)blockIdx.x * GROUP_FITS_PER_BLOCK;
+    mle_xynb_block(data, sigma, sz, iterations, P, CRLB, LL, nfits, first,
+                   (int)min((int64_t)GROUP_FITS_PER_BLOCK, (int64_t)nfits - first));
+}
+
+/* The fits of ROIs [range[0], min(range[1], capacity)) of a stack whose
+ * range is known only on the device: blocks of GROUP_FITS_PER_BLOCK fits,
+ * grid-stride. */
+__global__ void __launch_bounds__(GL * GROUP_FITS_PER_BLOCK) mle_xynb_range_kernel(
+    const float *__restrict__ data, float sigma, int sz, int iterations, float *__restrict__ P,
+    float *__restrict__ CRLB, float *__restrict__ LL, int64_t stride, const int64_t *__restrict__ range,
+    int64_t capacity)
+{
+    const int64_t f0 = range[0], f1 = min(range[1], capacity);
+    for (int64_t first = f0 + (int64_t)blockIdx.x * GROUP_FITS_PER_BLOCK; first < f1;
+         first += (int64_t)gridDim.x * GROUP_FITS_PER_BLOCK) {
+        mle_xynb_block(data, sigma, sz, iterations, P, CRLB, LL, stride, first,
+                       (int)min((int64_t)GROUP_FITS_PER_BLOCK, f1 - first));
+        __syncthreads(); /* the staged ROIs and axis rows are rewritten for the next fits */
+    }
+}
+
 }  // namespace
+
+static size_t gauss_mle_smem_bytes(int sz)
+{
+    return ((size_t)GROUP_FITS_PER_BLOCK * (sz * sz + 8 * MAXSZ) + (size_t)sz * sz) * sizeof(float);
+}
+
+bamf_status launch_gauss_mle_range(const float *rois, int sz, float psf_sigma, int iterations, float *params,
+                                   float *crlb, float *loglik, int64_t stride, const int64_t *range,
+                                   int64_t capacity, int blocks, cudaStream_t stream)
+{
+    if (sz < 1 || sz > MAXSZ || iterations < 0 || blocks < 1) return BAMF_ERR_INVALID_ARG;
+    mle_xynb_range_kernel<<<blocks, GL * GROUP_FITS_PER_BLOCK, gauss_mle_smem_bytes(sz), stream>>>(
+        rois, psf_sigma, sz, iterations, params, crlb, loglik, stride, range, capacity);
+    return cudaGetLastError() == cudaSuccess ? BAMF_OK : BAMF_ERR_CUDA;
+}
 
 extern "C" bamf_status bamf_gauss_mle_device(const float *rois, int sz, int nfits, float psf_sigma,
                                              int iterations, float *params, float *crlb,
@@ -274,7 +318,7 @@ extern "C" bamf_status bamf_gauss_mle_device(const float *rois, int sz, int nfit
     if (sz > MAXSZ) return BAMF_ERR_TOO_LARGE;
     if (nfits == 0) return BAMF_OK;
     /* a group of GL lanes per fit: 16 fits per CTA of 128 threads */
-    size_t smem = ((size_t)GROUP_FITS_PER_BLOCK * (sz * sz + 8 * MAXSZ) + (size_t)sz * sz) * sizeof(float);
+    size_t smem = gauss_mle_smem_bytes(sz);
     int blocks = (nfits + GROUP_FITS_PER_BLOCK - 1) / GROUP_FITS_PER_BLOCK;
     mle_xynb_group_kernel<<<blocks, GL * GROUP_FITS_PER_BLOCK, smem, (cudaStream_t)stream>>>(
         rois, psf_sigma, sz, iterations, params, crlb, loglik, nfits);

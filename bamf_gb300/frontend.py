@@ -42,6 +42,11 @@ def _declare():
     L.bamf_find_roi_pinned.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.c_double, C.c_double, C.c_int, C.c_float, C.c_int64, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.bamf_find_roi_fit_pinned.restype = C.c_int
+    L.bamf_find_roi_fit_pinned.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.c_double, C.c_double, C.c_int, C.c_float, C.c_int64, C.c_float,
+                                           C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p, C.c_void_p]
     L.bamf_gauss_mle_device.restype = C.c_int
     L.bamf_gauss_mle_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_int, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_void_p]
@@ -268,6 +273,41 @@ class FindRoiDevice:
             out["corners"].data_ptr(), out["stack"].data_ptr(), out["count"].data_ptr(), None,
             C.c_void_p(stream) if stream else None)
         abi.check(st, "bamf_find_roi_pinned")
+        return out
+
+    def run_fit_pinned(self, host_frames, ysize, xsize, zsize, sigma1=1.3, sigma2=2.6, boxsize=7, minval=None,
+                       psf_sigma=1.3, iterations=10, capacity=None, stream=None, chunk_frames=250,
+                       dev_frames=None):
+        """`run_pinned` followed by gaussMLE (XYNB, CCD) of the ROIs found,
+        chunk by chunk (bamf_find_roi_fit_pinned): the dict of run_pinned
+        plus P and CR ([4, capacity], parameter-major, the first count
+        columns written) and LL ([capacity]).  Enqueued on `stream`."""
+        import torch
+        if minval is None:
+            minval = default_minval()
+        n = ysize * xsize * zsize
+        if host_frames.device.type != "cpu" or host_frames.dtype != torch.float32 or host_frames.numel() != n:
+            raise ValueError("host_frames: a CPU float32 tensor of ysize*xsize*zsize values")
+        host_frames = host_frames.contiguous()
+        cap = capacity if capacity is not None else max(1024, n // 64)
+        if dev_frames is None:
+            dev_frames = torch.empty(n, dtype=torch.float32, device="cuda")
+        out = {"coords": torch.empty((cap, 3), dtype=torch.int32, device="cuda"),
+               "corners": torch.empty((cap, 2), dtype=torch.int32, device="cuda"),
+               "count": torch.zeros(1, dtype=torch.int64, device="cuda"),
+               "stack": torch.empty((cap, boxsize * boxsize), dtype=torch.float32, device="cuda"),
+               "P": torch.empty((4, cap), dtype=torch.float32, device="cuda"),
+               "CR": torch.empty((4, cap), dtype=torch.float32, device="cuda"),
+               "LL": torch.empty(cap, dtype=torch.float32, device="cuda"),
+               "frames": dev_frames,
+               "host_frames": host_frames}  # the copies read it until the stream gets there
+        st = self._L.bamf_find_roi_fit_pinned(
+            self._ws, host_frames.data_ptr(), dev_frames.data_ptr(), int(chunk_frames), ysize, xsize, zsize,
+            float(sigma1), float(sigma2), int(boxsize), float(np.float32(minval)), cap, float(psf_sigma),
+            int(iterations), out["coords"].data_ptr(), out["corners"].data_ptr(), out["stack"].data_ptr(),
+            out["count"].data_ptr(), out["P"].data_ptr(), out["CR"].data_ptr(), out["LL"].data_ptr(),
+            C.c_void_p(stream) if stream else None)
+        abi.check(st, "bamf_find_roi_fit_pinned")
         return out
 
 

@@ -31,6 +31,7 @@ frontend  (rank 0, outside the timed region) FindROI + gaussMLE on the
           2000-frame 256x256 front-end workload: frames/s, FindROI against the
           measured HBM bandwidth (one 4-byte read per pixel), fits/s, and an
           end-to-end frames/s with the stack copied from pinned host memory
+          and the fits read back (bamf_find_roi_fit_pinned)
 dense_e2e (rank 0, outside the timed region) the dense end-to-end frame
           analysis (bamf_gb300.pipeline) on 500 of its frames, 100 per pass:
           frames/s, stage times, localisation RMSE / recall / precision
@@ -244,16 +245,17 @@ def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3, fp32_peak: fl
         torch.cuda.synchronize()
         t_mle.append(e0.elapsed_time(e1) * 1e-3)
     # end to end through the API for host frames: pinned frames in (copied
-    # in chunks whose filters start as each lands), fits out
+    # in chunks; each chunk's filters start as it lands, and its maxima are
+    # compacted, cropped and fitted while later chunks are copied), fits out
     e2e = []
     dframes = torch.empty_like(dev)
     for _ in range(steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        o = fr.run_pinned(host, 256, 256, n_frames, boxsize=7, minval=mv, dev_frames=dframes)
+        o = fr.run_fit_pinned(host, 256, 256, n_frames, boxsize=7, minval=mv, psf_sigma=1.3, iterations=10,
+                              capacity=max(1024, n // 256), dev_frames=dframes)
         c = int(o["count"].item())
-        P, CR, LL = frontend.gauss_mle_device(o["stack"][:c].contiguous(), 7, c, 1.3, 10)
-        res = (o["coords"][:c].cpu(), P.cpu(), CR.cpu(), LL.cpu())
+        res = (o["coords"][:c].cpu(), o["P"][:, :c].cpu(), o["CR"][:, :c].cpu(), o["LL"][:c].cpu())
         e2e.append(time.perf_counter() - t0)
     d2h = sum(r.numel() * r.element_size() for r in res)
     tf, tm = statistics.median(t_find), statistics.median(t_mle)

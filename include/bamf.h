@@ -581,6 +581,27 @@ bamf_status bamf_find_roi_pinned(bamf_findroi_ws *ws, const float *host_frames, 
                                  int32_t *coords, int32_t *corners, float *roi_stack,
                                  int64_t *count, uint8_t *flags_out, void *stream);
 
+/* bamf_find_roi_pinned followed by gaussMLE (XYNB, CCD; gaussMLE.m:92-205
+ * with the ROI stack findROI.m:157-160 crops), chunk by chunk: after each
+ * chunk's window maxima, the maxima of the flag chunks those complete are
+ * appended to the coordinates in memory order, cropped and fitted while
+ * later chunks are still being copied, so the work after the last copy is
+ * the last chunk's.  coords, corners, roi_stack and count are
+ * bamf_find_roi_pinned's (identical values); params and crlb are
+ * [4][capacity]: bamf_gauss_mle_device's parameters (MATLAB Y, X, photons,
+ * background) with the stride capacity, parameter k of ROI i at
+ * k * capacity + i; loglik [capacity]; only the first min(count, capacity)
+ * ROIs are written.
+ * Device outputs, enqueued on stream; host_frames must stay valid until
+ * the stream reaches this call's end.  boxsize up to 21 (the gaussMLE
+ * window limit). */
+bamf_status bamf_find_roi_fit_pinned(bamf_findroi_ws *ws, const float *host_frames, float *dev_frames,
+                                     int chunk_frames, int ysize, int xsize, int zsize, double sigma1,
+                                     double sigma2, int boxsize, float minval, int64_t capacity,
+                                     float psf_sigma, int iterations, int32_t *coords,
+                                     int32_t *corners, float *roi_stack, int64_t *count,
+                                     float *params, float *crlb, float *loglik, void *stream);
+
 /* The difference-of-Gaussians image findROI's maxima run on
  * (cuda_FindROI.cu kernel_gaussX / kernel_gaussY for sigma1 and sigma2, then
  * kernel_subtract): dog = G(sigma1) - G(sigma2) of each frame, in the frames'

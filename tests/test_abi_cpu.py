@@ -122,6 +122,42 @@ def test_find_roi_pinned_rejects_bad_arguments_before_touching_the_device():
     fr.close()
 
 
+def test_find_roi_fit_pinned_rejects_bad_arguments_before_touching_the_device():
+    """bamf_find_roi_fit_pinned: missing crops or fit outputs, no capacity,
+    a non-positive PSF sigma or negative iterations are
+    BAMF_ERR_INVALID_ARG, a box beyond gaussMLE's 21 pixels
+    BAMF_ERR_TOO_LARGE (checked on the host, no CUDA call)."""
+    import numpy as np
+
+    from bamf_gb300 import abi, frontend
+    fr = frontend.FindRoiDevice()
+    L = fr._L
+    buf = np.zeros(16, np.float32)
+    i32 = np.zeros(64, np.int32)
+    f32 = np.zeros(64, np.float32)
+    cnt = np.zeros(1, np.int64)
+
+    def call(host=buf.ctypes.data, chunk=8, box=7, cap=4, psf=1.3, it=10, corners=i32.ctypes.data,
+             stack=f32.ctypes.data, params=f32.ctypes.data, crlb=f32.ctypes.data, ll=f32.ctypes.data):
+        return L.bamf_find_roi_fit_pinned(fr._ws, host, buf.ctypes.data, chunk, 4, 4, 1, 1.3, 2.6, box, 1.0, cap,
+                                          psf, it, i32.ctypes.data, corners, stack, cnt.ctypes.data, params,
+                                          crlb, ll, None)
+
+    bad = abi.BAMF_ERR_INVALID_ARG
+    assert call(host=None) == bad
+    assert call(chunk=0) == bad
+    assert call(cap=0) == bad
+    assert call(psf=0.0) == bad
+    assert call(it=-1) == bad
+    assert call(corners=None) == bad
+    assert call(stack=None) == bad
+    assert call(params=None) == bad
+    assert call(crlb=None) == bad
+    assert call(ll=None) == bad
+    assert call(box=22) == abi.BAMF_ERR_TOO_LARGE
+    fr.close()
+
+
 def test_crjmcmc_mirror_checks_the_model_option_on_the_host():
     """sampler.cRJMCMC (the MEX call, cRJMCMC.cpp:74): OptModel 0 or 1 only,
     and OptModel 1 needs a SampledPSF; both refused before any GPU call."""

@@ -132,3 +132,34 @@ def test_findroi_from_pinned_host_in_chunks_matches_the_device_call(cuda_lib, ch
     assert torch.equal(a["corners"][:c], b["corners"][:c])
     assert torch.equal(a["stack"][:c], b["stack"][:c])
     assert torch.equal(b["frames"], host.cuda())
+
+
+@pytest.mark.parametrize("chunk,cap_less", [(64, 0), (37, 25)])
+def test_findroi_fit_pinned_equals_the_separate_calls(cuda_lib, chunk, cap_less):
+    """bamf_find_roi_fit_pinned (each chunk's maxima compacted, cropped and
+    fitted once its frames are done) gives the coordinates, corners, crops
+    and count of bamf_find_roi_pinned and the fits of gaussMLE on that ROI
+    stack, bit for bit, on a 300-frame stack whose row-max window bounds
+    round; with a capacity below the count only the first `capacity` ROIs
+    are written and fitted."""
+    import torch
+    st, _ = synth.frames(300, seed=5)
+    host = torch.from_numpy(np.asfortranarray(st).ravel(order="F")).pin_memory()
+    fr = frontend.FindRoiDevice()
+    a = fr.run_pinned(host, 256, 256, 300, boxsize=7, chunk_frames=chunk)
+    torch.cuda.synchronize()
+    c = int(a["count"].item())
+    assert c > 100
+    cap = c - cap_less
+    b = fr.run_fit_pinned(host, 256, 256, 300, boxsize=7, psf_sigma=1.3, iterations=10, chunk_frames=chunk,
+                          capacity=cap)
+    torch.cuda.synchronize()
+    assert int(b["count"].item()) == c
+    assert torch.equal(a["coords"][:cap], b["coords"][:cap])
+    assert torch.equal(a["corners"][:cap], b["corners"][:cap])
+    assert torch.equal(a["stack"][:cap], b["stack"][:cap])
+    P, CR, LL = frontend.gauss_mle_device(a["stack"][:cap].contiguous(), 7, cap, 1.3, 10)
+    torch.cuda.synchronize()
+    assert torch.equal(P.view(4, cap), b["P"][:, :cap])
+    assert torch.equal(CR.view(4, cap), b["CR"][:, :cap])
+    assert torch.equal(LL, b["LL"][:cap])
