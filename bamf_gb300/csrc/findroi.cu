@@ -695,7 +695,9 @@ __global__ void __launch_bounds__(FF_T, 1) filter_kernel(const float *__restrict
  * it starts a block and h[s] when it ends one (only windows clamped to the
  * frame are shorter than W: they start at row 0 or end at the frame's last
  * row, the tile's last).  Both maxima are exact, so the flags are the
- * reference's. */
+ * reference's.  WORDS (X a multiple of 32): the flags as a bit mask in
+ * memory order, a warp's 32 columns of a row one word; else one byte per
+ * pixel. */
 constexpr int MAX_TW = 32, MAX_TH = 128, MAX_WARPS = 8, MAX_BOXSIZE = 128;
 
 __host__ __device__ inline int maxima_cwp(int k, int hr) { return (MAX_TW + 2 * (k + hr) + 31) / 32 * 32; }

@@ -155,6 +155,9 @@ def test_find_roi_fit_pinned_rejects_bad_arguments_before_touching_the_device():
     assert call(crlb=None) == bad
     assert call(ll=None) == bad
     assert call(box=22) == abi.BAMF_ERR_TOO_LARGE
+    import torch
+    with pytest.raises(ValueError):
+        fr.run_fit_pinned(torch.zeros(10), 4, 4, 1)
     fr.close()
 
 
