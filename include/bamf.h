@@ -496,10 +496,10 @@ bamf_status bamf_autotune_shapes(const bamf_workspace *ws, int arith, int32_t *c
  * (split the batch).
  *
  * Set-up: the first call on each device looks up the array's device address
- * with that device current and keeps it for the life of the process; make
- * that first call before any stream capture begins.  The address belongs to
- * the device's context: after cudaDeviceReset of a device, this entry point
- * must not be called on that device again in the same process.
+ * with that device current and keeps it for the life of the process.  The
+ * address belongs to the device's context: after cudaDeviceReset of a
+ * device, this entry point must not be called on that device again in the
+ * same process.
  *
  * Priors: the three prior PDF arrays (priors->*_pdf) are host memory that
  * the call copies into the scratch with copies enqueued on `stream`.  From
