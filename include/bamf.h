@@ -7,6 +7,8 @@
  *                                    source/cuda/cuda_FindROI/cuda_FindROI.cu)
  *   - the single-emitter MLE fitter (gaussMLE, @RJ/gaussMLE.m:64-211 driving
  *                                    kernel_MLEFit_XYNB_, cuda_gaussMLEv2.cu:16-141)
+ * (bamf_find_roi_fit_pinned runs the last two as one pipelined call on
+ * frames in pinned host memory.)
  *
  * Conventions: plain C types only; every function returns a bamf_status;
  * images are column-major with y (MATLAB rows) fastest, exactly as MATLAB
