@@ -278,7 +278,10 @@ def frontend_bench(n_frames: int, steps: int = 5, warmup: int = 3, fp32_peak: fl
             "flops_per_fit": gaussmle_flops_per_fit(7, 10),
             "peak_source": "FP32 FMA rate measured in-process by bamf_probe_peaks"},
         "e2e": {"value": n_frames / statistics.median(e2e[1:]), "unit": "frames/s",
-                "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(d2h)},
+                "h2d_bytes_per_step": int(host.numel() * 4), "d2h_bytes_per_step": int(d2h),
+                "calls": len(e2e) - 1,
+                "seconds_per_call": {"median": statistics.median(e2e[1:]), "min": min(e2e[1:]),
+                                     "max": max(e2e[1:])}},
     }
 
 
